@@ -1,0 +1,374 @@
+"""Benchmark: fused RK4 site-updates/s at 1024^2 on GB300 (one JSON line on rank 0).
+
+Workload (the precision-check physics at 1024^2): periodic 1024x1024 grid,
+lx = ly = 400 um, dt = 5e-4 ps, single reservoir, zero potential, continuous
+Gaussian pump (P0 = 0.02, sigma drawn per member in [8, 20] um), truncated-Wigner
+noise on (Philox seed 42 + member), complex64.  ``--members`` same-shape fields
+are stepped together (default 32: 512 MB of state, four times the 129 MB L2, so
+every step streams from HBM).  A "step" is one RK4 time step of every member.
+
+* ``value``  -- device-resident throughput: K steps between CUDA events on the
+  library stream, inputs already in HBM.
+* ``e2e``    -- the same metric through the public solver API
+  (``RK4CudaSolver.advance`` on pinned host state): each call copies psi and n_R
+  host->device, runs 64 steps in CUDA graphs and copies them back.
+* ``roofline`` -- 28 algorithmic bytes per site-update (psi r/w 16 B, n_R r/w 8 B,
+  pump 4 B) / average kernel time, against the measured HBM copy bandwidth.
+* ``cpu_baseline`` -- the FP64 NumPy oracle (a restatement of the reference's
+  rk4-fdm) on a bounded sample, on this host's cores.
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+oracle port, one worker process per member up to the host's core count) on the
+same workload and metric.  Multi-GPU runs (torchrun) step independent replicas:
+the path has no exchange step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+NX = NY = 1024
+LX = LY = 400.0
+DT = 5e-4
+P0 = 0.02
+BYTES_PER_SITE = 28  # FP32: psi 8 B read + 8 B write, n_R 4 + 4, pump envelope 4
+METRIC = "RK4 site-updates/s at 1024^2"
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(members, precision="single"):
+    """Host arrays of the benchmark workload: psi0, n0, per-member envelopes, physics."""
+    from polarism_gb300.host import make_initial_psi
+
+    dx, dy = LX / NX, LY / NY
+    x = (np.arange(NX) - (NX - 1) * 0.5) * dx
+    y = (np.arange(NY) - (NY - 1) * 0.5) * dy
+    rng = np.random.default_rng(1234)
+    sigmas = rng.uniform(8.0, 20.0, size=members)
+    cdt = np.complex64 if precision == "single" else np.complex128
+    rdt = np.float32 if precision == "single" else np.float64
+    env = np.stack([np.exp(-0.5 * (x[None, :] ** 2 + y[:, None] ** 2) / s ** 2) for s in sigmas])
+    psi = np.stack([make_initial_psi((NY, NX), 1e-3, 42 + m, cdt, rdt) for m in range(members)])
+    return dict(dx=dx, dy=dy, psi=psi[:, None], n=np.zeros((members, 1, NY, NX), rdt),
+                env=env[:, None].astype(rdt), seeds=[42 + m for m in range(members)],
+                sigmas=sigmas)
+
+
+PHYSICS = dict(hbar=0.6582119514, m_eff=0.284, g_C=0.001, g_R=0.002, g_I=0.0, R=0.02,
+               gamma_C=0.083, gamma_R=0.005)
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """Sample nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(members):
+    """DRAM bytes per launch of the RK4 kernel from the committed ncu summary, if any."""
+    path = ROOT / "profiles" / "rk4_stream_traffic.json"
+    if not path.exists():
+        return None
+    data = json.loads(path.read_text())
+    per_site = data.get("dram_bytes_per_site")
+    if per_site is None:
+        return None
+    return float(per_site) * members * NX * NY
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def _cpu_member_steps(args):
+    """Worker: FP64 oracle RK4 steps on one member (used by the CPU legs)."""
+    member, steps, precision = args
+    sys.path.insert(0, str(ROOT))
+    from oracle import gpe
+
+    w = workload(1, "double")
+    p = dict(PHYSICS)
+    env = w["env"][0, 0].astype(np.float64) * P0
+    psi, fields = w["psi"].astype(np.complex128), (w["n"].astype(np.float64),)
+    noise = gpe.Noise([42 + member], [p["gamma_C"]], [p["R"]], [1.0], DT, w["dx"] * w["dy"])
+    t0 = time.perf_counter()
+    gpe.rk4_advance(psi, fields, lambda t: env, 0.0, p, w["dx"], w["dy"], DT, 0, steps,
+                    noise=noise)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(sample_steps=8):
+    """Oracle port, one core, a bounded sample (sample_steps RK4 steps of one 1024^2 member)."""
+    _cpu_member_steps((0, 1, "double"))  # warm-up
+    elapsed = _cpu_member_steps((0, sample_steps, "double"))
+    return {"value": sample_steps * NX * NY / elapsed, "unit": "site-updates/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{sample_steps} RK4 steps of one 1024^2 member, FP64 NumPy oracle "
+                      "(restatement of the reference rk4-fdm + Wigner), 1 thread"}
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm's CPU implementation on all host cores."""
+    import multiprocessing as mp
+
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    workers = max(1, min(args.members, cores))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        pool.map(_cpu_member_steps, [(m, 1, "double") for m in range(workers)])  # warm-up
+        # Each timed step: one RK4 step of every member, members spread over the workers.
+        budget_steps = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(budget_steps):
+            pool.map(_cpu_member_steps, [(m, 1, "double") for m in range(args.members)])
+        elapsed = time.perf_counter() - t0
+    value = budget_steps * args.members * NX * NY / elapsed
+    line = {
+        "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world,
+        "steps": budget_steps, "warmup": 1, "ms_per_step": 1e3 * elapsed / budget_steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"rk4 1024^2 x {args.members} members, Wigner on", "members": args.members},
+        "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": workers, "kind": "port",
+                         "sample": f"{budget_steps} RK4 steps of {args.members} members at 1024^2, "
+                                   f"FP64 NumPy oracle port, {workers} worker processes"},
+        "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU leg
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from polarism_gb300 import build as _build
+
+    _build.build()
+    from polarism_gb300.engine import MemberPhysics, RK4Engine
+
+    members = args.members
+    w = workload(members)
+    eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**PHYSICS), "single",
+                    pump_per_member=True)
+    eng.set_pump(w["env"])
+    eng.set_noise(w["seeds"], PHYSICS["gamma_C"], PHYSICS["R"], 1.0, DT / (4 * w["dx"] * w["dy"]))
+    eng.set_state(w["psi"], w["n"])
+    stream = torch.cuda.ExternalStream(eng.stream)
+    total = args.warmup + args.steps
+    scales = np.full((total, 3, members), P0)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    eng.advance(0, args.warmup, scales[:args.warmup])
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    start.record(stream)
+    eng.advance(args.warmup, args.steps, scales[args.warmup:])
+    stop.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    launches = eng.last_launch_count
+    elapsed_ms = start.elapsed_time(stop)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    sites = members * NX * NY
+    value = world * sites * args.steps / (elapsed_ms / 1e3)
+    kernel_s = elapsed_ms / 1e3 / args.steps
+    achieved = BYTES_PER_SITE * sites / kernel_s / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = profiled_traffic(members)
+
+    # End to end through the public solver API on pinned host state.
+    e2e = run_e2e(args, w, members, torch)
+    eng.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "rk4-cuda fused step, 1024^2 periodic, lx=ly=400, dt=5e-4, "
+                               "single reservoir, Wigner noise on, complex64",
+                   "members": members, "global_members": members * world, "grid": [NY, NX],
+                   "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_site": BYTES_PER_SITE},
+        "e2e": e2e,
+        "clocks": clocks,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_sample_steps)
+    print(json.dumps(line), flush=True)
+
+
+def run_e2e(args, w, members, torch):
+    """Steps/s through RK4CudaSolver.advance with pinned host state (64-step calls)."""
+    from polarism_gb300.host import Config, build_simulation
+    from polarism_gb300.solvers import RK4CudaSolver
+
+    cfg = Config()
+    cfg.grid.nx, cfg.grid.ny, cfg.grid.lx, cfg.grid.ly = NX, NY, LX, LY
+    cfg.solver.dt, cfg.solver.precision = DT, "single"
+    cfg.noise.stochastic, cfg.noise.seed = "wigner", 42
+    cfg.laser.P0 = P0
+    member_cfgs = []
+    import copy
+
+    for m in range(members):
+        c = copy.deepcopy(cfg)
+        c.noise.seed = 42 + m
+        c.laser.sigma_space = float(w["sigmas"][m])
+        member_cfgs.append(c)
+    grid, model, state = build_simulation(cfg, member_cfgs if members > 1 else None)
+    pinned_psi = torch.empty(state.field.shape, dtype=torch.complex64, pin_memory=True).numpy()
+    pinned_psi[...] = state.field
+    state.field = pinned_psi
+    pinned_n = torch.empty(model.reservoir.nR.shape, dtype=torch.float32, pin_memory=True).numpy()
+    pinned_n[...] = model.reservoir.nR
+    model.reservoir.nR = pinned_n
+    solver = RK4CudaSolver(cfg, grid, model)
+    solver.inplace_host = True  # results land in the same pinned arrays every call
+    chunk = 64
+    solver.advance(model, state, chunk)  # warm-up: uploads pump/noise, captures graphs
+
+    calls = max(1, min(args.e2e_calls, 1 + args.steps // chunk))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        solver.advance(model, state, chunk)
+    elapsed = time.perf_counter() - t0
+    sites = members * NX * NY
+    h2d = sites * (8 + 4)
+    return {"value": sites * chunk * calls / elapsed, "unit": "site-updates/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+            "step": f"one RK4CudaSolver.advance call of {chunk} steps on pinned host state",
+            "calls": calls}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--members", type=int, default=32)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-calls", type=int, default=8)
+    ap.add_argument("--cpu-sample-steps", type=int, default=6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,122 @@
+/* polarism_gb300 -- C ABI of the GB300 (sm_103a) GPE time-stepping library.
+ *
+ * Plain C types only: pointers, sizes and status codes.  Every entry point returns
+ * PG_OK (0) on success or a PG_ERR_* code; pg_last_error() then holds a message
+ * for the calling thread.  Complex arrays are interleaved (re, im) in the
+ * reference's canonical layout (B, C, ny, nx); reservoir arrays are (B, C_res, ny, nx).
+ *
+ * A pg_solver owns its device buffers, one non-blocking CUDA stream and the CUDA
+ * graphs it captures.  Host buffers passed in are read/written synchronously
+ * before the call returns unless stated otherwise; "on_device" flags say whether
+ * a pointer is a device address (1) or host memory (0).
+ *
+ * Each solver entry point replaces the launch path of one reference solver
+ * (paths relative to the Polarism source tree):
+ *   pg_rk4_advance     <- polarism/solver/rk4_cuda_solver.py:3451-3642 (RK4CudaSolver.advance)
+ *                         and _step_gpu :3251-3350 (tiled whole-step kernel :1296-1479)
+ *   pg_philox_words    <- polarism/noise/philox.py:59-109 (philox_words kernel, test hook)
+ *   pg_set_noise       <- polarism/noise/stochastic.py:15-37 (NoiseApplier member arrays)
+ *   pg_set_pump        <- polarism/laser/pump_field.py:71-79 (separable envelope) and
+ *                         rk4_cuda_solver.py:3564-3578 (per-stage pump scales)
+ */
+#ifndef POLARISM_GB300_H
+#define POLARISM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_OK 0
+#define PG_ERR_INVALID 1     /* bad argument or unsupported configuration */
+#define PG_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define PG_ERR_UNSUPPORTED 3 /* feature not available in this build */
+#define PG_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+
+#define PG_SINGLE 0
+#define PG_DOUBLE 1
+
+#define PG_RES_NONE 0
+#define PG_RES_SINGLE 1
+
+#define PG_POT_NONE 0
+#define PG_POT_REAL 1
+#define PG_POT_COMPLEX 2
+
+/* Physics constants of one sweep member; names and meaning follow
+ * polarism/config/simulation_parameters.py:43-67 (PhysicsConstants). */
+typedef struct pg_physics {
+  double hbar, m_eff, g_C, g_R, g_I, R, gamma_C, gamma_R;
+  double kinetic_relaxation_eta;
+} pg_physics;
+
+typedef struct pg_config {
+  int32_t nx, ny;          /* periodic grid */
+  int32_t members;         /* batch size B */
+  int32_t precision;       /* PG_SINGLE (complex64) or PG_DOUBLE (complex128) */
+  int32_t reservoir;       /* PG_RES_NONE or PG_RES_SINGLE */
+  int32_t potential;       /* PG_POT_* */
+  int32_t pump_per_member; /* 0: one envelope shared by all members; 1: one per member */
+  int32_t potential_per_member;
+  double dx, dy, dt;
+} pg_config;
+
+typedef struct pg_solver pg_solver;
+
+/* Library status. */
+const char* pg_last_error(void);
+int pg_device_count(void);
+int pg_version(void);
+
+/* Lifecycle. physics points at cfg->members entries. */
+int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out);
+void pg_destroy(pg_solver* s);
+/* The solver's CUDA stream (a cudaStream_t) for event timing by the caller. */
+void* pg_stream(pg_solver* s);
+int pg_synchronize(pg_solver* s);
+
+/* State transfer: psi is B*nx*ny complex values, res is B*nx*ny reals (or NULL
+ * without a reservoir).  pg_set_state clamps nothing; the reference clamps in
+ * reservoir.set_state after each step, and so does the step kernel. */
+int pg_set_state(pg_solver* s, const void* psi, const void* res, int on_device);
+int pg_get_state(pg_solver* s, void* psi, void* res, int on_device);
+/* Device addresses of the current state buffers (valid until the next advance). */
+int pg_state_pointers(pg_solver* s, void** psi, void** res);
+
+/* Pump envelope (nx*ny reals, or B*nx*ny with pump_per_member) and potential
+ * (nx*ny reals or complex, or B*nx*ny with potential_per_member). */
+int pg_set_pump(pg_solver* s, const void* envelope, int on_device);
+int pg_set_potential(pg_solver* s, const void* potential, int on_device);
+
+/* Truncated-Wigner noise: per member seed, gamma_C, R and strength, and the common
+ * dt / (4 dV).  seeds == NULL turns the noise off. */
+int pg_set_noise(pg_solver* s, const uint64_t* seeds, const double* gamma,
+                 const double* scattering, const double* strength, double dt_over_4dv);
+
+/* Advance n_steps fused RK4 steps starting at global step index start_step.
+ * stage_scales holds 3 * members coefficients per step, laid out
+ * [step][stage (t, t+dt/2, t+dt)][member], on the host.  use_graphs captures
+ * chunks of up to 64 steps into CUDA graphs. */
+int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const double* stage_scales,
+                   int use_graphs);
+
+/* Override the RK4 launch geometry (the autotuner's knobs): tile_w useful columns per
+ * block (tile_w >= nx selects one full-width block per row strip) and strip_h output
+ * rows per block (a positive multiple of 4). */
+int pg_rk4_set_geometry(pg_solver* s, int32_t tile_w, int32_t strip_h);
+int pg_rk4_get_geometry(pg_solver* s, int32_t* tile_w, int32_t* strip_h);
+
+/* Number of kernel launches the last advance call issued (graph nodes included). */
+int64_t pg_last_launch_count(pg_solver* s);
+
+/* Philox-4x32-10 words for n counters (4 words each) under a 64-bit key, computed on
+ * the device; counters/out are host arrays of 4*n uint32. */
+int pg_philox_words(const uint32_t* counters, uint64_t key, uint32_t* out, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* POLARISM_GB300_H */

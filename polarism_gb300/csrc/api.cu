@@ -1,0 +1,525 @@
+// C ABI of libpolarism_gb300: solver lifecycle, state transfer, RK4 advance with
+// CUDA-graph chunks, and the Philox test hook.
+//
+// The advance loop mirrors polarism/solver/rk4_cuda_solver.py:3451-3642: per-stage
+// pump scales for a chunk of up to 64 steps are copied to a device array and the
+// global step base is set before the chunk runs (rk4_cuda_solver.py:3564-3586);
+// chunks of even length keep the ping-pong buffers on the same parity.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "philox.cuh"
+#include "pg_internal.h"
+
+namespace pg {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error() { return g_last_error.c_str(); }
+
+constexpr int kChunk = 64;
+constexpr int kStagingSlots = 4;
+
+namespace {
+
+__global__ void philox_words_kernel(const uint4* __restrict__ counters, uint4* __restrict__ out,
+                                    uint32_t k0, uint32_t k1, long long n) {
+  const long long j = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const uint4 c = counters[j];
+  const Words4 w = philox4x32_10(Words4{c.x, c.y, c.z, c.w}, k0, k1);
+  out[j] = make_uint4(w.a, w.b, w.c, w.d);
+}
+
+}  // namespace
+
+int philox_words_device(const uint32_t* counters, uint64_t key, uint32_t* out, int64_t n,
+                        cudaStream_t stream) {
+  if (n <= 0) return PG_OK;
+  const int threads = 256;
+  const long long blocks = (n + threads - 1) / threads;
+  philox_words_kernel<<<static_cast<unsigned>(blocks), threads, 0, stream>>>(
+      reinterpret_cast<const uint4*>(counters), reinterpret_cast<uint4*>(out),
+      static_cast<uint32_t>(key), static_cast<uint32_t>(key >> 32), n);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+}  // namespace pg
+
+struct pg_solver {
+  pg_config cfg{};
+  std::vector<pg_physics> physics;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  size_t real_size = 4;
+  long long plane = 0;     // nx * ny
+  long long sites = 0;     // members * plane
+  void* psi[2] = {nullptr, nullptr};
+  void* res[2] = {nullptr, nullptr};
+  void* pump = nullptr;
+  void* potential = nullptr;
+  void* consts = nullptr;
+  void* scales = nullptr;  // kChunk * 3 * members reals
+  unsigned long long* step_base = nullptr;
+  int cur = 0;
+  bool noise = false;
+  std::vector<uint64_t> seeds;
+  std::vector<double> noise_gamma, noise_R, noise_strength;
+  double dt_over_4dv = 0.0;
+  pg::RK4Geom geom{};
+  // Pinned staging ring for chunk scales and the step base.
+  struct Slot {
+    void* host = nullptr;
+    cudaEvent_t done = nullptr;
+  } staging[pg::kStagingSlots];
+  int next_slot = 0;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (length, parity) -> graph
+  long long last_launches = 0;
+};
+
+namespace {
+
+using pg::kChunk;
+using pg::kStagingSlots;
+
+template <typename T>
+void build_consts(const pg_solver* s, std::vector<pg::RhsConst<T>>& out) {
+  const pg_config& c = s->cfg;
+  out.resize(c.members);
+  for (int m = 0; m < c.members; ++m) {
+    const pg_physics& p = s->physics[m];
+    const double a = p.hbar / (2.0 * p.m_eff);
+    pg::RhsConst<T>& k = out[m];
+    k.ax = static_cast<T>(a / (c.dx * c.dx));
+    k.ay = static_cast<T>(a / (c.dy * c.dy));
+    k.w0 = static_cast<T>(2.0 * (a / (c.dx * c.dx) + a / (c.dy * c.dy)));
+    k.gc = static_cast<T>(p.g_C / p.hbar);
+    k.gr = static_cast<T>(p.g_R / p.hbar);
+    k.gi = static_cast<T>(p.g_I / p.hbar);
+    k.inv_hbar = static_cast<T>(1.0 / p.hbar);
+    k.half_R = static_cast<T>(0.5 * p.R);
+    k.half_gC = static_cast<T>(0.5 * p.gamma_C);
+    k.R = static_cast<T>(p.R);
+    k.gamma_R = static_cast<T>(p.gamma_R);
+    k.eta_a = static_cast<T>(p.kinetic_relaxation_eta * a);
+    k.pad_ = T(0);
+    if (s->noise) {
+      k.noise_a = static_cast<T>(s->noise_strength[m] * s->noise_gamma[m] * s->dt_over_4dv);
+      k.noise_b = static_cast<T>(s->noise_strength[m] * s->noise_R[m] * s->dt_over_4dv);
+      k.seed = s->seeds[m];
+    } else {
+      k.noise_a = k.noise_b = T(0);
+      k.seed = 0ull;
+    }
+  }
+}
+
+int upload_consts(pg_solver* s) {
+  if (s->cfg.precision == PG_DOUBLE) {
+    std::vector<pg::RhsConst<double>> v;
+    build_consts(s, v);
+    PG_CUDA(cudaMemcpyAsync(s->consts, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice,
+                            s->stream));
+  } else {
+    std::vector<pg::RhsConst<float>> v;
+    build_consts(s, v);
+    PG_CUDA(cudaMemcpyAsync(s->consts, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice,
+                            s->stream));
+  }
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+void free_graphs(pg_solver* s) {
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+}
+
+pg::RK4Features features(const pg_solver* s) {
+  pg::RK4Features f{};
+  f.potential = s->cfg.potential;
+  f.reservoir = s->cfg.reservoir;
+  f.relax = 0;
+  for (const auto& p : s->physics)
+    if (p.kinetic_relaxation_eta != 0.0) f.relax = 1;
+  return f;
+}
+
+// Launch one RK4 step reading buffers of parity `from`; step_offset indexes the chunk scales.
+cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
+  const int to = 1 - from;
+  const pg::RK4Features f = features(s);
+  pg::RK4Geom g = s->geom;
+  g.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
+  g.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
+  if (s->cfg.precision == PG_DOUBLE) {
+    return pg::launch_rk4_step<double>(
+        static_cast<const double*>(s->psi[from]), static_cast<const double*>(s->res[from]),
+        static_cast<const double*>(s->pump), static_cast<const double*>(s->potential),
+        static_cast<double*>(s->psi[to]), static_cast<double*>(s->res[to]),
+        static_cast<const pg::RhsConst<double>*>(s->consts), static_cast<const double*>(s->scales),
+        s->step_base, step_offset, s->cfg.dt, s->noise, g, f, s->stream);
+  }
+  return pg::launch_rk4_step<float>(
+      static_cast<const float*>(s->psi[from]), static_cast<const float*>(s->res[from]),
+      static_cast<const float*>(s->pump), static_cast<const float*>(s->potential),
+      static_cast<float*>(s->psi[to]), static_cast<float*>(s->res[to]),
+      static_cast<const pg::RhsConst<float>*>(s->consts), static_cast<const float*>(s->scales),
+      s->step_base, step_offset, static_cast<float>(s->cfg.dt), s->noise, g, f, s->stream);
+}
+
+// Copy a chunk's scales and its step base into the device arrays (stream ordered).
+int stage_chunk(pg_solver* s, const double* scales, int len, int64_t step) {
+  pg_solver::Slot& slot = s->staging[s->next_slot];
+  s->next_slot = (s->next_slot + 1) % kStagingSlots;
+  PG_CUDA(cudaEventSynchronize(slot.done));
+  const int m = s->cfg.members;
+  const size_t count = static_cast<size_t>(len) * 3 * m;
+  unsigned char* host = static_cast<unsigned char*>(slot.host);
+  if (s->cfg.precision == PG_DOUBLE) {
+    std::memcpy(host, scales, count * sizeof(double));
+  } else {
+    float* h = reinterpret_cast<float*>(host);
+    for (size_t i = 0; i < count; ++i) h[i] = static_cast<float>(scales[i]);
+  }
+  const size_t bytes = count * s->real_size;
+  const size_t base_off = static_cast<size_t>(kChunk) * 3 * m * 8;
+  unsigned long long b = static_cast<unsigned long long>(step);
+  std::memcpy(host + base_off, &b, sizeof(b));
+  PG_CUDA(cudaMemcpyAsync(s->scales, host, bytes, cudaMemcpyHostToDevice, s->stream));
+  PG_CUDA(cudaMemcpyAsync(s->step_base, host + base_off, sizeof(b), cudaMemcpyHostToDevice,
+                          s->stream));
+  PG_CUDA(cudaEventRecord(slot.done, s->stream));
+  return PG_OK;
+}
+
+int graph_for(pg_solver* s, int len, int parity, cudaGraphExec_t* out) {
+  auto key = std::make_pair(len, parity);
+  auto it = s->graphs.find(key);
+  if (it != s->graphs.end()) {
+    *out = it->second;
+    return PG_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  PG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t launch_err = cudaSuccess;
+  for (int k = 0; k < len && launch_err == cudaSuccess; ++k)
+    launch_err = launch_step(s, (parity + k) & 1, k);
+  cudaError_t end_err = cudaStreamEndCapture(s->stream, &graph);
+  if (launch_err != cudaSuccess || end_err != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    pg::set_error(std::string("graph capture failed: ") +
+                  cudaGetErrorString(launch_err != cudaSuccess ? launch_err : end_err));
+    return PG_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (inst != cudaSuccess) {
+    pg::set_error(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
+    return PG_ERR_CUDA;
+  }
+  s->graphs[key] = exec;
+  *out = exec;
+  return PG_OK;
+}
+
+void release(pg_solver* s) {
+  if (!s) return;
+  free_graphs(s);
+  for (auto& slot : s->staging) {
+    if (slot.host) cudaFreeHost(slot.host);
+    if (slot.done) cudaEventDestroy(slot.done);
+  }
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(s->psi[i]);
+    cudaFree(s->res[i]);
+  }
+  cudaFree(s->pump);
+  cudaFree(s->potential);
+  cudaFree(s->consts);
+  cudaFree(s->scales);
+  cudaFree(s->step_base);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pg_last_error(void) { return pg::last_error(); }
+
+int pg_version(void) { return 1; }
+
+int pg_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) {
+  PG_CHECK(cfg && physics && out, PG_ERR_INVALID, "pg_create: null argument");
+  PG_CHECK(cfg->nx >= 4 && cfg->ny >= 4, PG_ERR_INVALID, "pg_create: grid must be at least 4x4");
+  PG_CHECK(cfg->members >= 1, PG_ERR_INVALID, "pg_create: members must be >= 1");
+  PG_CHECK(cfg->precision == PG_SINGLE || cfg->precision == PG_DOUBLE, PG_ERR_INVALID,
+           "pg_create: precision must be PG_SINGLE or PG_DOUBLE");
+  PG_CHECK(cfg->reservoir == PG_RES_NONE || cfg->reservoir == PG_RES_SINGLE, PG_ERR_UNSUPPORTED,
+           "pg_create: reservoir must be PG_RES_NONE or PG_RES_SINGLE");
+  PG_CHECK(cfg->potential >= PG_POT_NONE && cfg->potential <= PG_POT_COMPLEX, PG_ERR_INVALID,
+           "pg_create: bad potential kind");
+  PG_CHECK(cfg->dx > 0 && cfg->dy > 0 && cfg->dt > 0, PG_ERR_INVALID,
+           "pg_create: dx, dy and dt must be positive");
+  PG_CHECK(static_cast<long long>(cfg->nx) * cfg->ny < (1ll << 31), PG_ERR_INVALID,
+           "pg_create: one member must hold fewer than 2^31 sites");
+  *out = nullptr;
+  pg_solver* s = new pg_solver();
+  s->cfg = *cfg;
+  s->physics.assign(physics, physics + cfg->members);
+  s->real_size = cfg->precision == PG_DOUBLE ? 8 : 4;
+  s->plane = static_cast<long long>(cfg->nx) * cfg->ny;
+  s->sites = s->plane * cfg->members;
+  int dev = 0;
+  auto fail = [&](cudaError_t e, const char* what) {
+    pg::set_error(std::string("pg_create: ") + what + ": " + cudaGetErrorString(e));
+    release(s);
+    return PG_ERR_CUDA;
+  };
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return fail(e, "device attribute");
+  e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(e, "stream");
+  const size_t field_bytes = static_cast<size_t>(s->sites) * 2 * s->real_size;
+  const size_t res_bytes = static_cast<size_t>(s->sites) * s->real_size;
+  for (int i = 0; i < 2; ++i) {
+    if ((e = cudaMalloc(&s->psi[i], field_bytes)) != cudaSuccess) return fail(e, "psi buffers");
+    if ((e = cudaMalloc(&s->res[i], res_bytes)) != cudaSuccess) return fail(e, "reservoir buffers");
+    cudaMemsetAsync(s->psi[i], 0, field_bytes, s->stream);
+    cudaMemsetAsync(s->res[i], 0, res_bytes, s->stream);
+  }
+  const size_t pump_bytes = static_cast<size_t>(cfg->pump_per_member ? s->sites : s->plane) * s->real_size;
+  if ((e = cudaMalloc(&s->pump, pump_bytes)) != cudaSuccess) return fail(e, "pump buffer");
+  cudaMemsetAsync(s->pump, 0, pump_bytes, s->stream);
+  if (cfg->potential != PG_POT_NONE) {
+    const size_t pot_bytes = static_cast<size_t>(cfg->potential_per_member ? s->sites : s->plane) *
+                             s->real_size * (cfg->potential == PG_POT_COMPLEX ? 2 : 1);
+    if ((e = cudaMalloc(&s->potential, pot_bytes)) != cudaSuccess) return fail(e, "potential buffer");
+    cudaMemsetAsync(s->potential, 0, pot_bytes, s->stream);
+  }
+  const size_t const_bytes = static_cast<size_t>(cfg->members) *
+                             (cfg->precision == PG_DOUBLE ? sizeof(pg::RhsConst<double>)
+                                                          : sizeof(pg::RhsConst<float>));
+  if ((e = cudaMalloc(&s->consts, const_bytes)) != cudaSuccess) return fail(e, "constants");
+  const size_t scale_bytes = static_cast<size_t>(kChunk) * 3 * cfg->members * s->real_size;
+  if ((e = cudaMalloc(&s->scales, scale_bytes)) != cudaSuccess) return fail(e, "scales");
+  if ((e = cudaMalloc(&s->step_base, sizeof(unsigned long long))) != cudaSuccess)
+    return fail(e, "step base");
+  cudaMemsetAsync(s->step_base, 0, sizeof(unsigned long long), s->stream);
+  const size_t staging_bytes = static_cast<size_t>(kChunk) * 3 * cfg->members * 8 + 64;
+  for (auto& slot : s->staging) {
+    if ((e = cudaMallocHost(&slot.host, staging_bytes)) != cudaSuccess) return fail(e, "staging");
+    if ((e = cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming)) != cudaSuccess)
+      return fail(e, "staging event");
+  }
+  pg::choose_rk4_geometry(cfg->nx, cfg->ny, cfg->members, cfg->precision, s->sm_count, &s->geom);
+  int rc = upload_consts(s);
+  if (rc != PG_OK) {
+    release(s);
+    return rc;
+  }
+  *out = s;
+  return PG_OK;
+}
+
+void pg_destroy(pg_solver* s) {
+  if (s && s->stream) cudaStreamSynchronize(s->stream);
+  release(s);
+}
+
+void* pg_stream(pg_solver* s) { return s ? static_cast<void*>(s->stream) : nullptr; }
+
+int pg_synchronize(pg_solver* s) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_synchronize: null solver");
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_set_state(pg_solver* s, const void* psi, const void* res, int on_device) {
+  PG_CHECK(s && psi, PG_ERR_INVALID, "pg_set_state: null argument");
+  PG_CHECK(s->cfg.reservoir == PG_RES_NONE || res, PG_ERR_INVALID,
+           "pg_set_state: reservoir array required");
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  PG_CUDA(cudaMemcpyAsync(s->psi[s->cur], psi, static_cast<size_t>(s->sites) * 2 * s->real_size,
+                          kind, s->stream));
+  if (s->cfg.reservoir != PG_RES_NONE)
+    PG_CUDA(cudaMemcpyAsync(s->res[s->cur], res, static_cast<size_t>(s->sites) * s->real_size, kind,
+                            s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_get_state(pg_solver* s, void* psi, void* res, int on_device) {
+  PG_CHECK(s && psi, PG_ERR_INVALID, "pg_get_state: null argument");
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  PG_CUDA(cudaMemcpyAsync(psi, s->psi[s->cur], static_cast<size_t>(s->sites) * 2 * s->real_size,
+                          kind, s->stream));
+  if (res && s->cfg.reservoir != PG_RES_NONE)
+    PG_CUDA(cudaMemcpyAsync(res, s->res[s->cur], static_cast<size_t>(s->sites) * s->real_size, kind,
+                            s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_state_pointers(pg_solver* s, void** psi, void** res) {
+  PG_CHECK(s && psi && res, PG_ERR_INVALID, "pg_state_pointers: null argument");
+  *psi = s->psi[s->cur];
+  *res = s->cfg.reservoir != PG_RES_NONE ? s->res[s->cur] : nullptr;
+  return PG_OK;
+}
+
+int pg_set_pump(pg_solver* s, const void* envelope, int on_device) {
+  PG_CHECK(s && envelope, PG_ERR_INVALID, "pg_set_pump: null argument");
+  const size_t bytes =
+      static_cast<size_t>(s->cfg.pump_per_member ? s->sites : s->plane) * s->real_size;
+  PG_CUDA(cudaMemcpyAsync(s->pump, envelope, bytes,
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_set_potential(pg_solver* s, const void* potential, int on_device) {
+  PG_CHECK(s && potential, PG_ERR_INVALID, "pg_set_potential: null argument");
+  PG_CHECK(s->cfg.potential != PG_POT_NONE, PG_ERR_INVALID,
+           "pg_set_potential: solver was created without a potential");
+  const size_t bytes = static_cast<size_t>(s->cfg.potential_per_member ? s->sites : s->plane) *
+                       s->real_size * (s->cfg.potential == PG_POT_COMPLEX ? 2 : 1);
+  PG_CUDA(cudaMemcpyAsync(s->potential, potential, bytes,
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  return PG_OK;
+}
+
+int pg_set_noise(pg_solver* s, const uint64_t* seeds, const double* gamma, const double* scattering,
+                 const double* strength, double dt_over_4dv) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_set_noise: null solver");
+  if (!seeds) {
+    s->noise = false;
+  } else {
+    PG_CHECK(gamma && scattering && strength, PG_ERR_INVALID, "pg_set_noise: null member arrays");
+    const int m = s->cfg.members;
+    s->seeds.assign(seeds, seeds + m);
+    s->noise_gamma.assign(gamma, gamma + m);
+    s->noise_R.assign(scattering, scattering + m);
+    s->noise_strength.assign(strength, strength + m);
+    s->dt_over_4dv = dt_over_4dv;
+    s->noise = true;
+  }
+  free_graphs(s);
+  return upload_consts(s);
+}
+
+int pg_rk4_set_geometry(pg_solver* s, int32_t tile_w, int32_t strip_h) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_rk4_set_geometry: null solver");
+  PG_CHECK(strip_h >= 4 && strip_h % 4 == 0, PG_ERR_INVALID,
+           "pg_rk4_set_geometry: strip height must be a positive multiple of 4");
+  const int max_threads = s->cfg.precision == PG_DOUBLE ? 288 : 544;
+  const int nx = s->cfg.nx;
+  if (tile_w >= nx) {
+    PG_CHECK(((nx + 31) / 32) * 32 <= max_threads, PG_ERR_INVALID,
+             "pg_rk4_set_geometry: row too wide for a full-width block");
+    s->geom.wrap = 1;
+    s->geom.tile_w = nx;
+  } else {
+    PG_CHECK(tile_w >= 8 && ((tile_w + 8 + 31) / 32) * 32 <= max_threads, PG_ERR_INVALID,
+             "pg_rk4_set_geometry: tile width out of range");
+    s->geom.wrap = 0;
+    s->geom.tile_w = tile_w;
+  }
+  s->geom.strip_h = strip_h;
+  free_graphs(s);
+  return PG_OK;
+}
+
+int pg_rk4_get_geometry(pg_solver* s, int32_t* tile_w, int32_t* strip_h) {
+  PG_CHECK(s && tile_w && strip_h, PG_ERR_INVALID, "pg_rk4_get_geometry: null argument");
+  *tile_w = s->geom.tile_w;
+  *strip_h = s->geom.strip_h;
+  return PG_OK;
+}
+
+int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const double* stage_scales,
+                   int use_graphs) {
+  PG_CHECK(s && stage_scales, PG_ERR_INVALID, "pg_rk4_advance: null argument");
+  PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_rk4_advance: negative step count");
+  s->last_launches = 0;
+  const int m = s->cfg.members;
+  int done = 0;
+  while (done < n_steps) {
+    const int remaining = n_steps - done;
+    int len = std::min(kChunk, remaining);
+    const bool graph = use_graphs && len >= 2;
+    if (graph && (len & 1)) len -= 1;
+    int rc = stage_chunk(s, stage_scales + static_cast<size_t>(done) * 3 * m, len, start_step + done);
+    if (rc != PG_OK) return rc;
+    if (graph) {
+      cudaGraphExec_t exec = nullptr;
+      rc = graph_for(s, len, s->cur, &exec);
+      if (rc != PG_OK) return rc;
+      PG_CUDA(cudaGraphLaunch(exec, s->stream));
+      s->cur = (s->cur + len) & 1;
+    } else {
+      for (int k = 0; k < len; ++k) {
+        PG_CUDA(launch_step(s, s->cur, k));
+        s->cur ^= 1;
+      }
+    }
+    s->last_launches += len;
+    done += len;
+  }
+  return PG_OK;
+}
+
+int64_t pg_last_launch_count(pg_solver* s) { return s ? s->last_launches : -1; }
+
+int pg_philox_words(const uint32_t* counters, uint64_t key, uint32_t* out, int64_t n) {
+  PG_CHECK(counters && out && n >= 0, PG_ERR_INVALID, "pg_philox_words: bad argument");
+  if (n == 0) return PG_OK;
+  void* dc = nullptr;
+  void* dout = nullptr;
+  const size_t bytes = static_cast<size_t>(n) * 16;
+  PG_CUDA(cudaMalloc(&dc, bytes));
+  cudaError_t e = cudaMalloc(&dout, bytes);
+  if (e != cudaSuccess) {
+    cudaFree(dc);
+    pg::set_error(std::string("pg_philox_words: ") + cudaGetErrorString(e));
+    return PG_ERR_CUDA;
+  }
+  int rc = PG_OK;
+  if ((e = cudaMemcpy(dc, counters, bytes, cudaMemcpyHostToDevice)) != cudaSuccess) {
+    pg::set_error(std::string("pg_philox_words: ") + cudaGetErrorString(e));
+    rc = PG_ERR_CUDA;
+  }
+  if (rc == PG_OK) rc = pg::philox_words_device(static_cast<const uint32_t*>(dc), key,
+                                                static_cast<uint32_t*>(dout), n, nullptr);
+  if (rc == PG_OK && (e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost)) != cudaSuccess) {
+    pg::set_error(std::string("pg_philox_words: ") + cudaGetErrorString(e));
+    rc = PG_ERR_CUDA;
+  }
+  cudaFree(dc);
+  cudaFree(dout);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,211 @@
+"""Thin Python owner of one ``pg_solver`` handle (device buffers, stream, graphs).
+
+Arrays cross the C ABI as raw pointers: NumPy arrays as host memory, PyTorch CUDA
+tensors (or anything exposing ``__cuda_array_interface__``) as device memory.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from polarism_gb300 import _lib
+
+
+def _pointer(array, dtype=None, writable=False):
+    """Return (address, on_device, keepalive) for a NumPy array or a CUDA tensor."""
+    if hasattr(array, "__cuda_array_interface__"):
+        iface = array.__cuda_array_interface__
+        if iface.get("strides") not in (None,):
+            # Require a dense C-contiguous device array.
+            shape, strides = iface["shape"], iface["strides"]
+            itemsize = np.dtype(iface["typestr"]).itemsize
+            expect = itemsize
+            for dim, stride in zip(reversed(shape), reversed(strides)):
+                if dim > 1 and stride != expect:
+                    raise ValueError("device arrays passed to polarism_gb300 must be contiguous")
+                expect *= dim
+        return int(iface["data"][0]), 1, array
+    arr = np.asarray(array)
+    if dtype is not None and arr.dtype != dtype:
+        if writable:
+            raise TypeError(f"expected a {np.dtype(dtype)} array, got {arr.dtype}")
+        arr = arr.astype(dtype)
+    if not arr.flags.c_contiguous:
+        if writable:
+            raise ValueError("output arrays must be C-contiguous")
+        arr = np.ascontiguousarray(arr)
+    return arr.ctypes.data, 0, arr
+
+
+@dataclass
+class MemberPhysics:
+    hbar: float = 0.6582119514
+    m_eff: float = 0.284
+    g_C: float = 0.001
+    g_R: float = 0.002
+    g_I: float = 0.0
+    R: float = 0.02
+    gamma_C: float = 0.083
+    gamma_R: float = 0.005
+    kinetic_relaxation_eta: float = 0.0
+
+    @classmethod
+    def from_object(cls, physics, index=None):
+        """Read the constants from a PhysicsConstants-like object or a BatchPhysics."""
+        values = {}
+        for name in cls.__dataclass_fields__:
+            if hasattr(physics, "get") and not isinstance(physics, dict):
+                value = physics.get(name)
+            elif isinstance(physics, dict):
+                value = physics.get(name, getattr(cls, name))
+            else:
+                value = getattr(physics, name, getattr(cls, name))
+            value = np.asarray(value, dtype=np.float64)
+            values[name] = float(value.reshape(-1)[index if (index is not None and value.size > 1) else 0])
+        return cls(**values)
+
+    def as_struct(self):
+        return _lib.PgPhysics(**self.__dict__)
+
+
+class RK4Engine:
+    """Fused RK4 stepping of ``members`` same-shape fields on the GPU."""
+
+    def __init__(self, nx, ny, members, dx, dy, dt, physics, precision="single", reservoir=True,
+                 potential=_lib.PG_POT_NONE, pump_per_member=False, potential_per_member=False):
+        self.lib = _lib.load()
+        self.nx, self.ny, self.members = int(nx), int(ny), int(members)
+        self.precision = precision
+        self.real = np.float32 if precision == "single" else np.float64
+        self.complex = np.complex64 if precision == "single" else np.complex128
+        self.reservoir = bool(reservoir)
+        self.potential_kind = int(potential)
+        cfg = _lib.PgConfig(nx=self.nx, ny=self.ny, members=self.members,
+                            precision=_lib.PG_SINGLE if precision == "single" else _lib.PG_DOUBLE,
+                            reservoir=_lib.PG_RES_SINGLE if reservoir else _lib.PG_RES_NONE,
+                            potential=self.potential_kind, pump_per_member=int(pump_per_member),
+                            potential_per_member=int(potential_per_member),
+                            dx=float(dx), dy=float(dy), dt=float(dt))
+        if isinstance(physics, (list, tuple)):
+            plist = list(physics)
+        else:
+            plist = [physics] * self.members
+        if len(plist) != self.members:
+            raise ValueError("need one physics entry per member")
+        arr = (_lib.PgPhysics * self.members)(*[p.as_struct() for p in plist])
+        handle = C.c_void_p()
+        _lib.check(self.lib.pg_create(C.byref(cfg), arr, C.byref(handle)), "pg_create")
+        self.handle = handle
+        self.dt = float(dt)
+        self.noise_on = False
+
+    # -- lifecycle ---------------------------------------------------------------
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.pg_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.pg_stream(self.handle) or 0)
+
+    def synchronize(self):
+        _lib.check(self.lib.pg_synchronize(self.handle), "pg_synchronize")
+
+    @property
+    def shape(self):
+        return (self.members, 1, self.ny, self.nx)
+
+    # -- data --------------------------------------------------------------------
+    def set_state(self, psi, res=None):
+        p, dev, keep = _pointer(psi, self.complex)
+        if self.reservoir:
+            if res is None:
+                raise ValueError("reservoir state required")
+            r, rdev, keep_r = _pointer(res, self.real)
+            if rdev != dev:
+                raise ValueError("psi and reservoir must both be host or both be device arrays")
+        else:
+            r, keep_r = None, None
+        _lib.check(self.lib.pg_set_state(self.handle, p, r, dev), "pg_set_state")
+        del keep, keep_r
+
+    def get_state(self, psi_out=None, res_out=None):
+        psi = np.empty(self.shape, dtype=self.complex) if psi_out is None else psi_out
+        res = (np.empty(self.shape, dtype=self.real) if res_out is None else res_out) if self.reservoir else None
+        p, dev, _ = _pointer(psi, self.complex, writable=True)
+        r = _pointer(res, self.real, writable=True)[0] if res is not None else None
+        _lib.check(self.lib.pg_get_state(self.handle, p, r, dev), "pg_get_state")
+        return psi, res
+
+    def state_pointers(self):
+        p, r = C.c_void_p(), C.c_void_p()
+        _lib.check(self.lib.pg_state_pointers(self.handle, C.byref(p), C.byref(r)), "pg_state_pointers")
+        return p.value, r.value
+
+    def set_pump(self, envelope):
+        p, dev, keep = _pointer(envelope, self.real)
+        _lib.check(self.lib.pg_set_pump(self.handle, p, dev), "pg_set_pump")
+
+    def set_potential(self, potential):
+        dtype = self.complex if self.potential_kind == _lib.PG_POT_COMPLEX else self.real
+        p, dev, keep = _pointer(potential, dtype)
+        _lib.check(self.lib.pg_set_potential(self.handle, p, dev), "pg_set_potential")
+
+    def set_noise(self, seeds=None, gamma=None, scattering=None, strength=None, dt_over_4dv=0.0):
+        if seeds is None:
+            _lib.check(self.lib.pg_set_noise(self.handle, None, None, None, None, 0.0), "pg_set_noise")
+            self.noise_on = False
+            return
+        m = self.members
+        s = np.ascontiguousarray(np.broadcast_to(np.asarray(seeds, dtype=np.uint64), (m,)))
+        g = np.ascontiguousarray(np.broadcast_to(np.asarray(gamma, dtype=np.float64), (m,)))
+        r = np.ascontiguousarray(np.broadcast_to(np.asarray(scattering, dtype=np.float64), (m,)))
+        st = np.ascontiguousarray(np.broadcast_to(np.asarray(strength, dtype=np.float64), (m,)))
+        _lib.check(self.lib.pg_set_noise(self.handle, s.ctypes.data, g.ctypes.data, r.ctypes.data,
+                                         st.ctypes.data, float(dt_over_4dv)), "pg_set_noise")
+        self.noise_on = True
+
+    def set_geometry(self, tile_w, strip_h):
+        _lib.check(self.lib.pg_rk4_set_geometry(self.handle, int(tile_w), int(strip_h)),
+                   "pg_rk4_set_geometry")
+
+    def geometry(self):
+        t, h = C.c_int32(), C.c_int32()
+        _lib.check(self.lib.pg_rk4_get_geometry(self.handle, C.byref(t), C.byref(h)),
+                   "pg_rk4_get_geometry")
+        return t.value, h.value
+
+    # -- stepping ----------------------------------------------------------------
+    def advance(self, start_step, n_steps, stage_scales, use_graphs=True):
+        """``stage_scales``: array (n_steps, 3, members) of pump coefficients."""
+        scales = np.ascontiguousarray(np.broadcast_to(
+            np.asarray(stage_scales, dtype=np.float64), (int(n_steps), 3, self.members)))
+        _lib.check(self.lib.pg_rk4_advance(self.handle, int(start_step), int(n_steps),
+                                           scales.ctypes.data, int(bool(use_graphs))),
+                   "pg_rk4_advance")
+
+    @property
+    def last_launch_count(self) -> int:
+        return int(self.lib.pg_last_launch_count(self.handle))
+
+
+def philox_words(counters, key: int) -> np.ndarray:
+    """Device Philox-4x32-10 words for host counters of shape (..., 4)."""
+    lib = _lib.load()
+    ctr = np.ascontiguousarray(np.asarray(counters, dtype=np.uint32))
+    if ctr.shape[-1] != 4:
+        raise ValueError("counters must have four words")
+    out = np.empty_like(ctr)
+    n = ctr.size // 4
+    _lib.check(lib.pg_philox_words(ctr.ctypes.data, C.c_uint64(int(key)), out.ctypes.data, n),
+               "pg_philox_words")
+    return out

@@ -1,0 +1,469 @@
+"""Host-side mirror of the Polarism objects the time-stepping path consumes.
+
+When the Polarism package is installed, its own ``Config``, grid, pump, reservoir,
+noise and state objects drive the solvers in :mod:`polarism_gb300.solvers`
+directly.  Without it (a bare GPU machine), the classes here provide the same
+attribute names and meaning for the part of the API the hot path touches, so the
+solvers, tests and benchmark run unchanged:
+
+* ``PhysicsConstants`` and the parameter sections -- ``polarism/config/simulation_parameters.py:30-238``
+  (same field names and defaults)
+* ``PeriodicGrid`` -- ``polarism/grid/periodic_grid.py:17-69`` (cell-centred
+  coordinates, ``k^2`` from ``fftfreq``)
+* ``ContinuousGaussian`` / ``PumpField`` -- ``polarism/laser/continuous_gaussian.py:15-46``,
+  ``polarism/laser/abstract_laser.py:74-79``, ``polarism/laser/pump_field.py:37-89``
+* ``SingleReservoir`` / ``NoReservoir`` -- ``polarism/reservoir/single_reservoir.py:22-111``
+  (non-negative clamp in ``set_state``)
+* ``NoiseParametersArrays`` -- ``polarism/noise/stochastic.py:15-37``
+* ``make_initial_psi`` -- ``polarism/noise/initial_field.py:82-90`` (NumPy
+  ``default_rng`` on the host, zero mean, RMS-normalised)
+* ``SimulationState`` -- ``polarism/simulation_state.py:20-196`` (canonical ``(B, C, ny, nx)``)
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field, fields
+from typing import Any
+
+import numpy as np
+
+
+# --------------------------------------------------------------------------- config
+@dataclass
+class GridParameters:
+    nx: int = 256
+    ny: int = 256
+    lx: float = 100.0
+    ly: float = 100.0
+    grid_type: str = "periodic"
+    ndim: int = 2
+
+
+@dataclass
+class PhysicsConstants:
+    hbar: float = 0.6582119514
+    m_eff: float = 0.284
+    gamma_R: float = 0.005
+    gamma_C: float = 0.083
+    g_C: float = 0.001
+    g_R: float = 0.002
+    g_I: float = 0.0
+    gamma_I: float = 0.001
+    gamma_A: float = 0.005
+    R: float = 0.02
+    R_IA: float = 5e-2
+    R_AI: float = 2.5e-3
+    kappa: float = 0.05
+    kinetic_relaxation_eta: float = 0.0
+    reservoir_diffusion_I: float = 0.0
+    reservoir_diffusion_A: float = 0.0
+    reservoir_diffusion_R: float = 0.0
+    dispersion: str = "parabolic"
+    spin: str = "scalar"
+    alpha_2: float = 0.0
+    zeeman: float = 0.0
+    te_tm: float = 0.0
+
+
+@dataclass
+class NoiseParameters:
+    enabled: bool = True
+    seed: int | None = None
+    initial: str = "complex_gaussian_zero_mean"
+    initial_amplitude: float = 1e-3
+    initial_k_cutoff_um: float | None = None
+    stochastic: str = "none"
+    stochastic_strength: float = 1.0
+
+
+@dataclass
+class LaserParameters:
+    laser_type: str = "continuous-gaussian"
+    P0: float = 0.4
+    x0: float = 0.0
+    y0: float = 0.0
+    sigma_space: float = 15.0
+    delay: float = 0.0
+
+
+@dataclass
+class ReservoirParameters:
+    reservoir_type: str = "single"
+    components: int | None = None
+
+
+@dataclass
+class PotentialParameters:
+    potential_type: str = "zero"
+
+
+@dataclass
+class SolverParameters:
+    total_time: float = 5.0
+    dt: float = 1e-3
+    method: str = "rk4-cuda"
+    tableau: str = "rk4"
+    precision: str = "double"
+    laplacian: str = "five-point"
+    cuda_graphs: bool = True
+    adaptive: bool = False
+    rtol: float = 1e-6
+    atol: float = 1e-8
+    dt_max: float | None = None
+
+
+@dataclass
+class StopParameters:
+    steady_state: bool = False
+    rtol: float = 1e-6
+    check_every: float = 10.0
+    min_time: float = 0.0
+
+
+@dataclass
+class Config:
+    grid: GridParameters = field(default_factory=GridParameters)
+    physics: PhysicsConstants = field(default_factory=PhysicsConstants)
+    noise: NoiseParameters = field(default_factory=NoiseParameters)
+    laser: LaserParameters = field(default_factory=LaserParameters)
+    reservoir: ReservoirParameters = field(default_factory=ReservoirParameters)
+    potential: PotentialParameters = field(default_factory=PotentialParameters)
+    solver: SolverParameters = field(default_factory=SolverParameters)
+    stop: StopParameters = field(default_factory=StopParameters)
+
+
+def physics_float_fields():
+    return [f.name for f in fields(PhysicsConstants) if f.type in (float, "float")]
+
+
+# --------------------------------------------------------------------------- grid
+class PeriodicGrid:
+    """Two-dimensional periodic grid with cell-centred coordinates."""
+
+    boundary = "periodic"
+    grid_type = "periodic"
+    ndim = 2
+
+    def __init__(self, cfg: GridParameters):
+        self.nx, self.ny = int(cfg.nx), int(cfg.ny)
+        self.lx, self.ly = float(cfg.lx), float(cfg.ly)
+        self.dx = self.lx / self.nx
+        self.dy = self.ly / self.ny
+        self.shape = (self.ny, self.nx)
+        self.spacing = (self.dy, self.dx)
+        self.lengths = (self.ly, self.lx)
+        x = (np.arange(self.nx, dtype=np.float64) - (self.nx - 1) * 0.5) * self.dx
+        y = (np.arange(self.ny, dtype=np.float64) - (self.ny - 1) * 0.5) * self.dy
+        self.X, self.Y = np.meshgrid(x, y, indexing="xy")
+        self.kx = 2 * np.pi * np.fft.fftfreq(self.nx, d=self.dx)
+        self.ky = 2 * np.pi * np.fft.fftfreq(self.ny, d=self.dy)
+        self.KX, self.KY = np.meshgrid(self.kx, self.ky, indexing="xy")
+        self.k_squared = self.KX ** 2 + self.KY ** 2
+
+
+def real_dtype(precision: str):
+    return np.float32 if precision == "single" else np.float64
+
+
+def complex_dtype(precision: str):
+    return np.complex64 if precision == "single" else np.complex128
+
+
+# --------------------------------------------------------------------------- pump
+class ContinuousGaussian:
+    """P(r, t) = coeff(t) exp(-r^2 / (2 sigma^2)), coeff = P0 for t >= delay."""
+
+    time_independent = True
+
+    def __init__(self, cfg: LaserParameters, X, Y, precision="double"):
+        self.P0, self.x0, self.y0 = float(cfg.P0), float(cfg.x0), float(cfg.y0)
+        self.delay = float(cfg.delay)
+        self.sigma_space = float(cfg.sigma_space)
+        r2 = (X - self.x0) ** 2 + (Y - self.y0) ** 2
+        self._spatial_envelope = np.exp(-0.5 * r2 / self.sigma_space ** 2).astype(
+            real_dtype(precision), copy=False)
+
+    def power_coefficient(self, t: float) -> float:
+        return 0.0 if t < self.delay else self.P0
+
+
+class PumpField:
+    """Total pump with one cached separable (envelope, coefficient) term."""
+
+    def __init__(self, lasers, grid, precision):
+        self.lasers = list(lasers)
+        self.grid = grid
+        self.precision = precision
+
+    def separable_term(self):
+        if len(self.lasers) != 1:
+            return None
+        laser = self.lasers[0]
+        return laser._spatial_envelope, laser.power_coefficient
+
+    def separable_terms(self):
+        return [(laser._spatial_envelope, laser.power_coefficient) for laser in self.lasers]
+
+    def __call__(self, t: float):
+        total = 0
+        for envelope, coefficient in self.separable_terms():
+            total = total + envelope * coefficient(t)
+        return total
+
+
+class BatchedPumpField:
+    """One laser per member: stacked envelopes and member-vector coefficients
+    (``polarism/laser/pump_field.py:92-152``)."""
+
+    def __init__(self, member_lasers, grid, precision):
+        self.member_lasers = [list(lasers) for lasers in member_lasers]
+        self.lasers = self.member_lasers[0]
+        self.grid = grid
+        self.precision = precision
+        slot = [lasers[0] for lasers in self.member_lasers]
+        envelopes = [laser._spatial_envelope for laser in slot]
+        shared = all(np.array_equal(envelopes[0], e) for e in envelopes[1:])
+        self._envelope = envelopes[0] if shared else np.stack(envelopes)[:, None]
+        self._slot = slot
+
+    def _coefficient(self, t):
+        return np.asarray([laser.power_coefficient(t) for laser in self._slot],
+                          dtype=real_dtype(self.precision))
+
+    def separable_terms(self):
+        return [(self._envelope, self._coefficient)]
+
+    def separable_term(self):
+        return None
+
+    def __call__(self, t):
+        value = self._coefficient(t).reshape(-1, 1, 1, 1)
+        return self._envelope * value
+
+
+# --------------------------------------------------------------------------- reservoir
+class SingleReservoir:
+    """dn/dt = P - (gamma_R + R |psi|^2) n with the non-negative clamp on set_state."""
+
+    state_names = ("nR",)
+
+    def __init__(self, physics: PhysicsConstants, grid, precision="double", batch_size=None):
+        self.components = 1
+        self._dtype = real_dtype(precision)
+        self.nR = np.zeros((batch_size or 1, 1, *grid.shape), dtype=self._dtype)
+        self._batched = batch_size is not None
+
+    def get_state(self):
+        return (self.nR,)
+
+    def set_state(self, state):
+        (n,) = state
+        if n.shape != self.nR.shape:
+            raise ValueError(f"reservoir state shape must be {self.nR.shape}")
+        if n is self.nR and n.dtype == self._dtype:
+            np.maximum(n, 0, out=n)
+            return
+        self.nR = np.maximum(n, 0).astype(self._dtype, copy=False)
+
+    def get_active_density(self, state):
+        return state[0]
+
+    def get_inactive_density(self, state):
+        return state[0] * 0.0
+
+
+class NoReservoir:
+    state_names = ()
+
+    def __init__(self, *args, **kwargs):
+        self.components = 1
+
+    def get_state(self):
+        return ()
+
+    def set_state(self, state):
+        if tuple(state):
+            raise ValueError("the 'none' reservoir has no state")
+
+    def get_active_density(self, state):
+        return 0.0
+
+    def get_inactive_density(self, state):
+        return 0.0
+
+
+# --------------------------------------------------------------------------- noise
+class NoiseParametersArrays:
+    """Per-member Wigner parameters: seeds, gamma_C, R, strength, dt, cell volume."""
+
+    def __init__(self, config, grid, members=None):
+        members = members or [config]
+        self.precision = config.solver.precision
+        self.spatial_n = int(np.prod(grid.shape))
+        self.volume = float(np.prod(grid.spacing))
+        self.dt = float(config.solver.dt)
+        self.seeds = np.asarray([m.noise.seed for m in members], dtype=np.uint64)
+        self.gamma = np.asarray([m.physics.gamma_C for m in members], dtype=np.float64)
+        self.scattering = np.asarray([m.physics.R for m in members], dtype=np.float64)
+        self.strength = np.asarray([m.noise.stochastic_strength for m in members], dtype=np.float64)
+        self.active = bool(config.noise.enabled and config.noise.stochastic == "wigner"
+                           and np.any(self.strength > 0.0))
+
+
+# --------------------------------------------------------------------------- state
+def make_initial_psi(shape, eps, seed, cdtype=np.complex128, rdtype=np.float64,
+                     mode="complex_gaussian_zero_mean"):
+    """Seeded complex-Gaussian field with zero mean and RMS ``eps``."""
+    if mode == "none":
+        return np.zeros(shape, dtype=cdtype)
+    if mode != "complex_gaussian_zero_mean":
+        raise ValueError(f"unsupported initial field mode {mode!r}")
+    rng = np.random.default_rng(seed)
+    re = rng.standard_normal(shape).astype(rdtype)
+    im = rng.standard_normal(shape).astype(rdtype)
+    psi = re + 1j * im
+    psi -= np.mean(psi)
+    rms = float(np.sqrt(np.mean(np.abs(psi) ** 2)))
+    if rms < 1e-30:
+        rms = 1.0
+    return ((eps / rms) * psi).astype(cdtype)
+
+
+class SimulationState:
+    """Canonical ``(B, C, ny, nx)`` field with time bookkeeping."""
+
+    def __init__(self, field, batched=False):
+        self.batch_size = field.shape[0]
+        self.components = field.shape[1]
+        self.batched = batched
+        self._field = field
+        self._field_k = None
+        self.t = 0.0
+        self.t0 = 0.0
+        self.step = 0
+
+    @property
+    def field(self):
+        if self._field is None and self._field_k is not None:
+            self._field = np.fft.ifft2(self._field_k, axes=(-2, -1))
+        return self._field
+
+    @field.setter
+    def field(self, value):
+        self._field = value
+        self._field_k = None
+
+    @property
+    def field_k(self):
+        return self._field_k
+
+    @field_k.setter
+    def field_k(self, value):
+        self._field_k = value
+
+    @property
+    def psi(self):
+        return self.field[:, 0] if self.batched else self.field[0, 0]
+
+
+class BatchPhysicsLite:
+    """``get(name)`` returns the scalar, or the ``(B, 1, 1, 1)`` array when members differ."""
+
+    def __init__(self, physics: PhysicsConstants, members=None):
+        self.physics = physics
+        self.host = {}
+        if members and len(members) > 1:
+            for name in physics_float_fields():
+                values = np.asarray([getattr(m.physics, name) for m in members], dtype=np.float64)
+                if np.any(values != values[0]):
+                    self.host[name] = values
+        self.size = len(members) if members and len(members) > 1 and self.host else None
+
+    def get(self, name):
+        if name in self.host:
+            return self.host[name].reshape(-1, 1, 1, 1)
+        return getattr(self.physics, name, 0.0)
+
+    def any_nonzero(self, name):
+        if name in self.host:
+            return bool(np.any(self.host[name]))
+        return getattr(self.physics, name, 0.0) != 0.0
+
+    def check(self, field, components=1):
+        if field.ndim != 4 or field.shape[1] != components:
+            raise ValueError(f"batch_physics requires canonical field shape; got {field.shape}")
+
+
+class _NoAbsorption:
+    after_step_is_noop = True
+
+
+class _Boundary:
+    absorption = _NoAbsorption()
+
+    @staticmethod
+    def after_step_action(psi):
+        return psi
+
+
+@dataclass
+class Model:
+    grid: Any
+    physics: Any
+    precision: str
+    potential: Any
+    pump: Any
+    reservoir: Any
+    noise: Any = None
+    components: int = 1
+    boundary: Any = field(default_factory=_Boundary)
+    terms: tuple = ()
+    drive: Any = None
+    time_dependent_potential: bool = False
+    reservoir_components: int = 1
+    member_configs: list | None = None
+
+
+def build_simulation(cfg: Config, members: list[Config] | None = None):
+    """Build (grid, model, state) for a config, or a batch of member configs that
+    share the grid -- the subset of ``SimulationController.__init__``
+    (``polarism/simulation_controller.py:163-341``) this path needs."""
+    grid = PeriodicGrid(cfg.grid)
+    precision = cfg.solver.precision
+    batched = members is not None and len(members) >= 2
+    member_cfgs = members if members else [cfg]
+    for m in member_cfgs:
+        if m.noise.seed is None:
+            m.noise.seed = cfg.noise.seed if cfg.noise.seed is not None else 0
+    lasers = [[ContinuousGaussian(m.laser, grid.X, grid.Y, precision)] for m in member_cfgs]
+    pump = BatchedPumpField(lasers, grid, precision) if batched else PumpField(lasers[0], grid, precision)
+    res_cls = {"single": SingleReservoir, "none": NoReservoir}[cfg.reservoir.reservoir_type]
+    reservoir = res_cls(cfg.physics, grid, precision, batch_size=len(member_cfgs) if batched else None)
+    fields_ = [make_initial_psi(grid.shape, m.noise.initial_amplitude if m.noise.enabled else 0.0,
+                                m.noise.seed, complex_dtype(precision), real_dtype(precision),
+                                m.noise.initial if m.noise.enabled else "none")
+               for m in member_cfgs]
+    field_ = np.stack(fields_)[:, None]
+    state = SimulationState(np.ascontiguousarray(field_), batched=batched)
+    noise = NoiseParametersArrays(cfg, grid, member_cfgs)
+    model = Model(grid=grid, physics=BatchPhysicsLite(cfg.physics, member_cfgs), precision=precision,
+                  potential=np.zeros((), dtype=real_dtype(precision)), pump=pump,
+                  reservoir=reservoir, noise=noise if noise.active else None,
+                  member_configs=member_cfgs)
+    return grid, model, state
+
+
+def threshold_pump(physics: PhysicsConstants) -> float:
+    """Uniform-pump condensation threshold P_th = gamma_R gamma_C / R
+    (``polarism/analysis/condensation.py:52-57``)."""
+    return physics.gamma_R * physics.gamma_C / physics.R
+
+
+def copy_config(cfg: Config) -> Config:
+    import copy
+
+    return copy.deepcopy(cfg)
+
+
+def isclose(a, b):
+    return math.isclose(a, b, rel_tol=1e-12, abs_tol=0.0)

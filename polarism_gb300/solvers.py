@@ -1,0 +1,204 @@
+"""Polarism solver-registry drop-ins backed by the sm_103a kernels.
+
+``RK4CudaSolver`` replaces ``polarism/solver/rk4_cuda_solver.py:2197-3919``
+(registered as ``"rk4-cuda"``).  It keeps the reference contract of
+``AbstractSolver`` (``polarism/solver/abstract_solver.py:60-101``):
+``__init__(config, grid, model)``, ``step(model, state, dt) -> StepReport`` and
+``advance(model, state, n_steps)``, with ``state.step`` advanced and
+``state.t = state.t0 + state.step * dt`` (``rk4_cuda_solver.py:3641-3642``).
+The Wigner increment is injected inside the step kernel (``injects_noise = True``).
+
+The classes accept both the reference's own objects (``Config``, grid, ``Model``,
+``SimulationState``) and the mirrors in :mod:`polarism_gb300.host`.  There is no
+CPU path: construction fails with ``RuntimeError`` when the CUDA library or a GPU
+is missing, like the reference's GPU-only solvers (``split_step_fft_cuda_solver.py:525-526``).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from polarism_gb300 import _lib
+from polarism_gb300.engine import MemberPhysics, RK4Engine
+
+try:  # Subclass the reference's contract when Polarism is installed.
+    from polarism.solver.abstract_solver import ACCEPTED, AbstractSolver, SolverCapabilities, StepReport
+except Exception:  # pragma: no cover - exercised on hosts without Polarism
+    from polarism_gb300.contract import ACCEPTED, AbstractSolver, SolverCapabilities, StepReport
+
+
+def _member_count(state) -> int:
+    return int(state.field.shape[0]) if state.field is not None else int(state.field_k.shape[0])
+
+
+def _is_device(array) -> bool:
+    return hasattr(array, "__cuda_array_interface__")
+
+
+def _host(array):
+    """Return a NumPy view/copy of a host or device array."""
+    if _is_device(array):
+        return array.detach().cpu().numpy() if hasattr(array, "detach") else np.asarray(array.get())
+    return np.asarray(array)
+
+
+class RK4CudaSolver(AbstractSolver):
+    """Fused whole-step RK4 on GB300 with in-kernel Philox Wigner noise."""
+
+    capabilities = SolverCapabilities(
+        components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
+        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
+        potential=True, kinetic_relaxation=True, dispersion=frozenset({"parabolic"}),
+        terms=False, noise=frozenset({"none", "wigner"}), adaptive=False,
+        quantitative_reservoirs=frozenset({"single", "none"}),
+        description="GB300 fused RK4 (one sm_103a kernel per step, stage-coupled reservoir, "
+                    "Philox Wigner noise in registers).")
+    injects_noise = True
+
+    def __init__(self, config, grid, model):
+        super().__init__(config, grid, model)
+        if getattr(model, "components", 1) != 1:
+            raise ValueError("rk4-cuda (GB300) supports scalar fields only")
+        if getattr(grid, "ndim", 2) != 2 or getattr(grid, "boundary", "periodic") != "periodic":
+            raise ValueError("rk4-cuda (GB300) supports two-dimensional periodic grids")
+        reservoir_type = getattr(getattr(config, "reservoir", None), "reservoir_type", "single")
+        if reservoir_type not in ("single", "none"):
+            raise ValueError(f"rk4-cuda (GB300) does not support reservoir_type={reservoir_type!r}")
+        if getattr(config.solver, "laplacian", "five-point") != "five-point":
+            raise ValueError("rk4-cuda (GB300) implements the five-point Laplacian")
+        self._reservoir_type = reservoir_type
+        self._grid = grid
+        self._precision = getattr(config.solver, "precision", "double")
+        self._dt = float(config.solver.dt)
+        self._engine = None
+        self._engine_key = None
+        self._pump_key = None
+        self._noise_key = None
+        self._potential_key = None
+        _lib.load()
+
+    # ------------------------------------------------------------------ helpers
+    def _physics_list(self, members):
+        bp = self.batch_physics
+        return [MemberPhysics.from_object(bp, m) for m in range(members)]
+
+    def _ensure_engine(self, model, members, pump_env, potential):
+        pump_per_member = np.ndim(pump_env) == 4 and pump_env.shape[0] > 1
+        pot_kind = _lib.PG_POT_NONE
+        pot_per_member = False
+        if potential is not None and np.ndim(potential) > 0 and np.any(potential != 0):
+            pot_kind = _lib.PG_POT_COMPLEX if np.iscomplexobj(potential) else _lib.PG_POT_REAL
+            pot_per_member = np.ndim(potential) == 4 and potential.shape[0] > 1
+        key = (members, pump_per_member, pot_kind, pot_per_member)
+        if self._engine is None or self._engine_key != key:
+            if self._engine is not None:
+                self._engine.close()
+            g = self._grid
+            self._engine = RK4Engine(g.nx, g.ny, members, g.dx, g.dy, self._dt,
+                                     self._physics_list(members), self._precision,
+                                     reservoir=self._reservoir_type == "single", potential=pot_kind,
+                                     pump_per_member=pump_per_member,
+                                     potential_per_member=pot_per_member)
+            self._engine_key = key
+            self._pump_key = self._noise_key = self._potential_key = None
+        return self._engine
+
+    @staticmethod
+    def _pump_term(pump):
+        terms = pump.separable_terms() if hasattr(pump, "separable_terms") else None
+        if terms is None and hasattr(pump, "separable_term"):
+            term = pump.separable_term()
+            terms = [term] if term is not None else None
+        if not terms or len(terms) != 1:
+            raise ValueError("rk4-cuda (GB300) needs a single separable pump term "
+                             "(envelope x coefficient(t))")
+        return terms[0]
+
+    def _upload_inputs(self, engine, model, envelope, potential):
+        env = _host(envelope)
+        key = (id(envelope), env.shape)
+        if self._pump_key != key:
+            engine.set_pump(np.ascontiguousarray(env, dtype=engine.real))
+            self._pump_key = key
+        if engine.potential_kind != _lib.PG_POT_NONE:
+            pkey = id(potential)
+            if self._potential_key != pkey:
+                engine.set_potential(np.ascontiguousarray(_host(potential)))
+                self._potential_key = pkey
+        noise = model.noise
+        active = bool(noise is not None and getattr(noise, "active", True))
+        nkey = (id(noise), active)
+        if self._noise_key != nkey:
+            if active:
+                engine.set_noise(noise.seeds, noise.gamma, noise.scattering, noise.strength,
+                                 noise.dt / (4.0 * noise.volume))
+            else:
+                engine.set_noise(None)
+            self._noise_key = nkey
+
+    def stage_scales(self, coefficient, t0, start_step, n_steps, members):
+        """Pump coefficients at t, t + dt/2, t + dt of each step (shape (n, 3, B))."""
+        dt = self._dt
+        out = np.empty((n_steps, 3, members), dtype=np.float64)
+        for k in range(n_steps):
+            t = t0 + (start_step + k) * dt
+            for s, time in enumerate((t, t + 0.5 * dt, t + dt)):
+                value = np.asarray(coefficient(time), dtype=np.float64).reshape(-1)
+                out[k, s] = value if value.size == members else value[0]
+        return out
+
+    #: Write results back into the caller's host arrays (for example pinned buffers)
+    #: instead of returning fresh arrays each call.
+    inplace_host = False
+
+    @staticmethod
+    def _writable(array, dtype):
+        return (isinstance(array, np.ndarray) and array.dtype == dtype
+                and array.flags.c_contiguous and array.flags.writeable)
+
+    # ------------------------------------------------------------------ contract
+    def step(self, model, state, dt):
+        self.advance(model, state, 1)
+        return ACCEPTED
+
+    def advance(self, model, state, n_steps: int) -> None:
+        if n_steps <= 0:
+            return
+        field = state.field
+        self.batch_physics.check(field, 1)
+        members = int(field.shape[0])
+        envelope, coefficient = self._pump_term(model.pump)
+        potential = getattr(model, "potential", None)
+        engine = self._ensure_engine(model, members, np.asarray(_host(envelope)),
+                                     None if potential is None else _host(potential))
+        self._upload_inputs(engine, model, envelope, potential)
+        reservoir = model.reservoir
+        res_state = reservoir.get_state()
+        device = _is_device(field)
+        if self._reservoir_type == "single":
+            res0 = res_state[0]
+            engine.set_state(field if device else np.ascontiguousarray(field, dtype=engine.complex),
+                             res0 if device else np.ascontiguousarray(res0, dtype=engine.real))
+        else:
+            engine.set_state(field if device else np.ascontiguousarray(field, dtype=engine.complex))
+        scales = self.stage_scales(coefficient, state.t0, state.step, n_steps, members)
+        engine.advance(state.step, n_steps, scales,
+                       use_graphs=bool(getattr(self.config.solver, "cuda_graphs", True)))
+        res_in = res_state[0] if self._reservoir_type == "single" else None
+        if device:
+            psi_out = field.new_empty(field.shape) if hasattr(field, "new_empty") else None
+            res_out = res_in.new_empty(res_in.shape) if res_in is not None else None
+            psi, res = engine.get_state(psi_out, res_out)
+        elif self.inplace_host and self._writable(field, engine.complex) and (
+                res_in is None or self._writable(res_in, engine.real)):
+            psi, res = engine.get_state(field, res_in)
+        else:
+            psi, res = engine.get_state()
+        state.field = psi
+        if self._reservoir_type == "single":
+            reservoir.set_state((res,))
+        state.step += n_steps
+        state.t = state.t0 + state.step * self._dt
+
+    @property
+    def engine(self):
+        return self._engine
