@@ -16,6 +16,8 @@
  *                         and _step_gpu :3251-3350 (tiled whole-step kernel :1296-1479)
  *   pg_philox_words    <- polarism/noise/philox.py:59-109 (philox_words kernel, test hook)
  *   pg_set_noise       <- polarism/noise/stochastic.py:15-37 (NoiseApplier member arrays)
+ *   pg_split_advance   <- polarism/solver/split_step_fft_solver.py:97-159 (ordering 0) and
+ *                         polarism/solver/split_step_fft_cuda_solver.py:1144-1325 (ordering 1)
  *   pg_set_pump        <- polarism/laser/pump_field.py:71-79 (separable envelope) and
  *                         rk4_cuda_solver.py:3564-3578 (per-stage pump scales)
  */
@@ -108,12 +110,39 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
 int pg_rk4_set_geometry(pg_solver* s, int32_t tile_w, int32_t strip_h);
 int pg_rk4_get_geometry(pg_solver* s, int32_t* tile_w, int32_t* strip_h);
 
+/* Advance n_steps split-step Fourier steps (nx, ny powers of two up to 4096).
+ * ordering 0: R(dt/2) K(dt/2) N(dt) K(dt/2) R(dt/2) with psi in real space before and after
+ *             (replaces polarism/solver/split_step_fft_solver.py:97-159, "split-step-fft");
+ * ordering 1: K(dt/2) [R(dt/2) N(dt) R(dt/2)] K(dt/2) with the state left as the
+ *             unnormalised 2-D spectrum (replaces polarism/solver/split_step_fft_cuda_solver.py:
+ *             1144-1325, "split-step-fft-cuda").
+ * half_scales holds 2 * members pump coefficients per step, [step][(t+dt/4, t+3dt/4)][member].
+ * The Wigner increment is drawn after N (ordering 0, with n_R after the first half step) or after
+ * the second reservoir half step (ordering 1), with counter step = start_step + k. */
+int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t n_steps,
+                     const double* half_scales, int use_graphs);
+/* Whether the state buffer holds psi(x, y) (0) or its unnormalised spectrum (1). */
+int pg_set_state_kind(pg_solver* s, int32_t spectral);
+int pg_get_state_kind(pg_solver* s, int32_t* spectral);
+
+/* Choose the RK4 kernel: 0 automatic, 1 the tiled streaming kernel (any size, FP32/FP64,
+ * potential and relaxation terms), 2 the full-width FP32 kernel (nx a multiple of 64 up to
+ * 1024, single reservoir, no potential).  pg_rk4_get_kernel reports the one in use (1 or 2). */
+int pg_rk4_set_kernel(pg_solver* s, int32_t kind);
+int pg_rk4_get_kernel(pg_solver* s, int32_t* kind);
+
 /* Number of kernel launches the last advance call issued (graph nodes included). */
 int64_t pg_last_launch_count(pg_solver* s);
 
 /* Philox-4x32-10 words for n counters (4 words each) under a 64-bit key, computed on
  * the device; counters/out are host arrays of 4*n uint32. */
 int pg_philox_words(const uint32_t* counters, uint64_t key, uint32_t* out, int64_t n);
+
+/* The two Box-Muller normals (re, im) the step kernels draw from each counter's Philox words,
+ * with unit variance; out holds 2*n floats (PG_SINGLE) or doubles (PG_DOUBLE).  Test hook for
+ * polarism/noise/philox.py:41-56 (normal_pair). */
+int pg_wigner_normals(const uint32_t* counters, uint64_t key, int32_t precision, void* out,
+                      int64_t n);
 
 #ifdef __cplusplus
 }

@@ -58,8 +58,14 @@ SIGNATURES = {
     "pg_rk4_advance": (C.c_int, [_vp, _i64, _i32, _vp, C.c_int]),
     "pg_rk4_set_geometry": (C.c_int, [_vp, _i32, _i32]),
     "pg_rk4_get_geometry": (C.c_int, [_vp, C.POINTER(_i32), C.POINTER(_i32)]),
+    "pg_split_advance": (C.c_int, [_vp, _i32, _i64, _i32, _vp, C.c_int]),
+    "pg_set_state_kind": (C.c_int, [_vp, _i32]),
+    "pg_get_state_kind": (C.c_int, [_vp, C.POINTER(_i32)]),
+    "pg_rk4_set_kernel": (C.c_int, [_vp, _i32]),
+    "pg_rk4_get_kernel": (C.c_int, [_vp, C.POINTER(_i32)]),
     "pg_last_launch_count": (_i64, [_vp]),
     "pg_philox_words": (C.c_int, [_vp, _u64, _vp, _i64]),
+    "pg_wigner_normals": (C.c_int, [_vp, _u64, _i32, _vp, _i64]),
 }
 
 _lock = threading.Lock()

@@ -16,15 +16,14 @@
 
 #include "philox.cuh"
 #include "pg_internal.h"
+#include "solver.h"
+#include "wide_internal.h"
 
 namespace pg {
 
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error() { return g_last_error.c_str(); }
-
-constexpr int kChunk = 64;
-constexpr int kStagingSlots = 4;
 
 namespace {
 
@@ -35,6 +34,19 @@ __global__ void philox_words_kernel(const uint4* __restrict__ counters, uint4* _
   const uint4 c = counters[j];
   const Words4 w = philox4x32_10(Words4{c.x, c.y, c.z, c.w}, k0, k1);
   out[j] = make_uint4(w.a, w.b, w.c, w.d);
+}
+
+template <typename T>
+__global__ void wigner_normals_kernel(const uint4* __restrict__ counters, T* __restrict__ out,
+                                      uint32_t k0, uint32_t k1, long long n) {
+  const long long j = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const uint4 c = counters[j];
+  const Words4 w = philox4x32_10(Words4{c.x, c.y, c.z, c.w}, k0, k1);
+  T re = T(0), im = T(0);
+  WignerDraw<T>::apply(w, T(1), re, im);
+  out[2 * j] = re;
+  out[2 * j + 1] = im;
 }
 
 }  // namespace
@@ -53,36 +65,35 @@ int philox_words_device(const uint32_t* counters, uint64_t key, uint32_t* out, i
 
 }  // namespace pg
 
-struct pg_solver {
-  pg_config cfg{};
-  std::vector<pg_physics> physics;
-  cudaStream_t stream = nullptr;
-  int sm_count = 0;
-  size_t real_size = 4;
-  long long plane = 0;     // nx * ny
-  long long sites = 0;     // members * plane
-  void* psi[2] = {nullptr, nullptr};
-  void* res[2] = {nullptr, nullptr};
-  void* pump = nullptr;
-  void* potential = nullptr;
-  void* consts = nullptr;
-  void* scales = nullptr;  // kChunk * 3 * members reals
-  unsigned long long* step_base = nullptr;
-  int cur = 0;
-  bool noise = false;
-  std::vector<uint64_t> seeds;
-  std::vector<double> noise_gamma, noise_R, noise_strength;
-  double dt_over_4dv = 0.0;
-  pg::RK4Geom geom{};
-  // Pinned staging ring for chunk scales and the step base.
-  struct Slot {
-    void* host = nullptr;
-    cudaEvent_t done = nullptr;
-  } staging[pg::kStagingSlots];
-  int next_slot = 0;
-  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (length, parity) -> graph
-  long long last_launches = 0;
-};
+namespace pg {
+
+// Copy a chunk's per-step coefficients and its step base into the device arrays
+// (stream ordered, through a ring of pinned staging buffers).
+int stage_coefficients(pg_solver* s, const double* coeffs, int len, int per_step, int64_t step) {
+  pg_solver::Slot& slot = s->staging[s->next_slot];
+  s->next_slot = (s->next_slot + 1) % kStagingSlots;
+  PG_CUDA(cudaEventSynchronize(slot.done));
+  const int m = s->cfg.members;
+  const size_t count = static_cast<size_t>(len) * per_step * m;
+  unsigned char* host = static_cast<unsigned char*>(slot.host);
+  if (s->cfg.precision == PG_DOUBLE) {
+    std::memcpy(host, coeffs, count * sizeof(double));
+  } else {
+    float* h = reinterpret_cast<float*>(host);
+    for (size_t i = 0; i < count; ++i) h[i] = static_cast<float>(coeffs[i]);
+  }
+  const size_t bytes = count * s->real_size;
+  const size_t base_off = static_cast<size_t>(kChunk) * 3 * m * 8;
+  unsigned long long b = static_cast<unsigned long long>(step);
+  std::memcpy(host + base_off, &b, sizeof(b));
+  if (bytes) PG_CUDA(cudaMemcpyAsync(s->scales, host, bytes, cudaMemcpyHostToDevice, s->stream));
+  PG_CUDA(cudaMemcpyAsync(s->step_base, host + base_off, sizeof(b), cudaMemcpyHostToDevice,
+                          s->stream));
+  PG_CUDA(cudaEventRecord(slot.done, s->stream));
+  return PG_OK;
+}
+
+}  // namespace pg
 
 namespace {
 
@@ -108,7 +119,7 @@ void build_consts(const pg_solver* s, std::vector<pg::RhsConst<T>>& out) {
     k.half_gC = static_cast<T>(0.5 * p.gamma_C);
     k.R = static_cast<T>(p.R);
     k.gamma_R = static_cast<T>(p.gamma_R);
-    k.eta_a = static_cast<T>(p.kinetic_relaxation_eta * a);
+    k.eta_a = static_cast<T>(p.kinetic_relaxation_eta);
     k.pad_ = T(0);
     if (s->noise) {
       k.noise_a = static_cast<T>(s->noise_strength[m] * s->noise_gamma[m] * s->dt_over_4dv);
@@ -152,10 +163,33 @@ pg::RK4Features features(const pg_solver* s) {
   return f;
 }
 
+bool use_wide(const pg_solver* s) {
+  const pg::RK4Features f = features(s);
+  const bool eligible = s->cfg.precision == PG_SINGLE && f.potential == 0 && f.relax == 0 &&
+                        f.reservoir == 1 && pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny);
+  if (s->rk4_kernel == 1) return false;
+  return eligible;
+}
+
 // Launch one RK4 step reading buffers of parity `from`; step_offset indexes the chunk scales.
 cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
   const int to = 1 - from;
   const pg::RK4Features f = features(s);
+  if (use_wide(s)) {
+    pg::WideGeom w{};
+    w.nx = s->cfg.nx;
+    w.ny = s->cfg.ny;
+    w.members = s->cfg.members;
+    w.blocks = s->wide_blocks;
+    w.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
+    return pg::launch_rk4_wide(static_cast<const float*>(s->psi[from]),
+                               static_cast<const float*>(s->res[from]),
+                               static_cast<const float*>(s->pump), static_cast<float*>(s->psi[to]),
+                               static_cast<float*>(s->res[to]),
+                               static_cast<const pg::RhsConst<float>*>(s->consts),
+                               static_cast<const float*>(s->scales), s->step_base, step_offset,
+                               static_cast<float>(s->cfg.dt), s->noise, w, s->err_flag, s->stream);
+  }
   pg::RK4Geom g = s->geom;
   g.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
   g.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
@@ -173,31 +207,6 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
       static_cast<float*>(s->psi[to]), static_cast<float*>(s->res[to]),
       static_cast<const pg::RhsConst<float>*>(s->consts), static_cast<const float*>(s->scales),
       s->step_base, step_offset, static_cast<float>(s->cfg.dt), s->noise, g, f, s->stream);
-}
-
-// Copy a chunk's scales and its step base into the device arrays (stream ordered).
-int stage_chunk(pg_solver* s, const double* scales, int len, int64_t step) {
-  pg_solver::Slot& slot = s->staging[s->next_slot];
-  s->next_slot = (s->next_slot + 1) % kStagingSlots;
-  PG_CUDA(cudaEventSynchronize(slot.done));
-  const int m = s->cfg.members;
-  const size_t count = static_cast<size_t>(len) * 3 * m;
-  unsigned char* host = static_cast<unsigned char*>(slot.host);
-  if (s->cfg.precision == PG_DOUBLE) {
-    std::memcpy(host, scales, count * sizeof(double));
-  } else {
-    float* h = reinterpret_cast<float*>(host);
-    for (size_t i = 0; i < count; ++i) h[i] = static_cast<float>(scales[i]);
-  }
-  const size_t bytes = count * s->real_size;
-  const size_t base_off = static_cast<size_t>(kChunk) * 3 * m * 8;
-  unsigned long long b = static_cast<unsigned long long>(step);
-  std::memcpy(host + base_off, &b, sizeof(b));
-  PG_CUDA(cudaMemcpyAsync(s->scales, host, bytes, cudaMemcpyHostToDevice, s->stream));
-  PG_CUDA(cudaMemcpyAsync(s->step_base, host + base_off, sizeof(b), cudaMemcpyHostToDevice,
-                          s->stream));
-  PG_CUDA(cudaEventRecord(slot.done, s->stream));
-  return PG_OK;
 }
 
 int graph_for(pg_solver* s, int len, int parity, cudaGraphExec_t* out) {
@@ -234,6 +243,7 @@ int graph_for(pg_solver* s, int len, int parity, cudaGraphExec_t* out) {
 void release(pg_solver* s) {
   if (!s) return;
   free_graphs(s);
+  pg::split_release(s);
   for (auto& slot : s->staging) {
     if (slot.host) cudaFreeHost(slot.host);
     if (slot.done) cudaEventDestroy(slot.done);
@@ -247,6 +257,7 @@ void release(pg_solver* s) {
   cudaFree(s->consts);
   cudaFree(s->scales);
   cudaFree(s->step_base);
+  cudaFree(s->err_flag);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -327,6 +338,16 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   if ((e = cudaMalloc(&s->step_base, sizeof(unsigned long long))) != cudaSuccess)
     return fail(e, "step base");
   cudaMemsetAsync(s->step_base, 0, sizeof(unsigned long long), s->stream);
+  if ((e = cudaMalloc(&s->err_flag, sizeof(int))) != cudaSuccess) return fail(e, "error flag");
+  cudaMemsetAsync(s->err_flag, 0, sizeof(int), s->stream);
+  if (cfg->precision == PG_SINGLE && pg::wide_rk4_supported(cfg->nx, cfg->ny)) {
+    if ((e = pg::configure_wide_rk4()) != cudaSuccess) return fail(e, "wide kernel attributes");
+    const long long rows = static_cast<long long>(cfg->members) * cfg->ny;
+    const long long per_sm = pg::wide_rk4_blocks_per_sm(cfg->nx, true);
+    long long blocks = per_sm * s->sm_count;
+    const long long by_rows = std::max<long long>(1, rows / 16);
+    s->wide_blocks = static_cast<int>(std::min(blocks, by_rows));
+  }
   const size_t staging_bytes = static_cast<size_t>(kChunk) * 3 * cfg->members * 8 + 64;
   for (auto& slot : s->staging) {
     if ((e = cudaMallocHost(&slot.host, staging_bytes)) != cudaSuccess) return fail(e, "staging");
@@ -350,10 +371,26 @@ void pg_destroy(pg_solver* s) {
 
 void* pg_stream(pg_solver* s) { return s ? static_cast<void*>(s->stream) : nullptr; }
 
+namespace {
+// Read (and clear) the device error flag after a synchronisation point.
+int check_device_flag(pg_solver* s) {
+  int flag = 0;
+  PG_CUDA(cudaMemcpyAsync(&flag, s->err_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  if (flag) {
+    cudaMemsetAsync(s->err_flag, 0, sizeof(int), s->stream);
+    cudaStreamSynchronize(s->stream);
+    pg::set_error("a bounded device wait timed out; results of the last advance are invalid");
+    return PG_ERR_TIMEOUT;
+  }
+  return PG_OK;
+}
+}  // namespace
+
 int pg_synchronize(pg_solver* s) {
   PG_CHECK(s, PG_ERR_INVALID, "pg_synchronize: null solver");
   PG_CUDA(cudaStreamSynchronize(s->stream));
-  return PG_OK;
+  return check_device_flag(s);
 }
 
 int pg_set_state(pg_solver* s, const void* psi, const void* res, int on_device) {
@@ -379,6 +416,28 @@ int pg_get_state(pg_solver* s, void* psi, void* res, int on_device) {
     PG_CUDA(cudaMemcpyAsync(res, s->res[s->cur], static_cast<size_t>(s->sites) * s->real_size, kind,
                             s->stream));
   PG_CUDA(cudaStreamSynchronize(s->stream));
+  return check_device_flag(s);
+}
+
+int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_rk4_set_kernel: null solver");
+  PG_CHECK(kind >= 0 && kind <= 2, PG_ERR_INVALID, "pg_rk4_set_kernel: kind must be 0, 1 or 2");
+  if (kind == 2) {
+    const pg::RK4Features f = features(s);
+    PG_CHECK(s->cfg.precision == PG_SINGLE && f.potential == 0 && f.relax == 0 &&
+                 f.reservoir == 1 && pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny),
+             PG_ERR_UNSUPPORTED,
+             "pg_rk4_set_kernel: the full-width kernel needs FP32, a single reservoir, no "
+             "potential or relaxation term, and nx a multiple of 64 up to 1024");
+  }
+  s->rk4_kernel = kind;
+  free_graphs(s);
+  return PG_OK;
+}
+
+int pg_rk4_get_kernel(pg_solver* s, int32_t* kind) {
+  PG_CHECK(s && kind, PG_ERR_INVALID, "pg_rk4_get_kernel: null argument");
+  *kind = use_wide(s) ? 2 : 1;
   return PG_OK;
 }
 
@@ -427,7 +486,9 @@ int pg_set_noise(pg_solver* s, const uint64_t* seeds, const double* gamma, const
     s->noise = true;
   }
   free_graphs(s);
-  return upload_consts(s);
+  int rc = upload_consts(s);
+  if (rc != PG_OK) return rc;
+  return s->split_ready ? pg::split_refresh_consts(s) : PG_OK;
 }
 
 int pg_rk4_set_geometry(pg_solver* s, int32_t tile_w, int32_t strip_h) {
@@ -463,6 +524,8 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
                    int use_graphs) {
   PG_CHECK(s && stage_scales, PG_ERR_INVALID, "pg_rk4_advance: null argument");
   PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_rk4_advance: negative step count");
+  PG_CHECK(!s->spectral, PG_ERR_INVALID,
+           "pg_rk4_advance: the state holds a spectrum; set real-space psi first");
   s->last_launches = 0;
   const int m = s->cfg.members;
   int done = 0;
@@ -471,7 +534,8 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
     int len = std::min(kChunk, remaining);
     const bool graph = use_graphs && len >= 2;
     if (graph && (len & 1)) len -= 1;
-    int rc = stage_chunk(s, stage_scales + static_cast<size_t>(done) * 3 * m, len, start_step + done);
+    int rc = pg::stage_coefficients(s, stage_scales + static_cast<size_t>(done) * 3 * m, len, 3,
+                                    start_step + done);
     if (rc != PG_OK) return rc;
     if (graph) {
       cudaGraphExec_t exec = nullptr;
@@ -492,6 +556,41 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
 }
 
 int64_t pg_last_launch_count(pg_solver* s) { return s ? s->last_launches : -1; }
+
+int pg_wigner_normals(const uint32_t* counters, uint64_t key, int32_t precision, void* out,
+                      int64_t n) {
+  PG_CHECK(counters && out && n >= 0, PG_ERR_INVALID, "pg_wigner_normals: bad argument");
+  PG_CHECK(precision == PG_SINGLE || precision == PG_DOUBLE, PG_ERR_INVALID,
+           "pg_wigner_normals: bad precision");
+  if (n == 0) return PG_OK;
+  const size_t esize = precision == PG_DOUBLE ? 8 : 4;
+  void* dc = nullptr;
+  void* dout = nullptr;
+  PG_CUDA(cudaMalloc(&dc, static_cast<size_t>(n) * 16));
+  cudaError_t e = cudaMalloc(&dout, static_cast<size_t>(n) * 2 * esize);
+  if (e == cudaSuccess) e = cudaMemcpy(dc, counters, static_cast<size_t>(n) * 16, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    const int threads = 256;
+    const unsigned blocks = static_cast<unsigned>((n + threads - 1) / threads);
+    if (precision == PG_DOUBLE)
+      pg::wigner_normals_kernel<double><<<blocks, threads>>>(
+          static_cast<const uint4*>(dc), static_cast<double*>(dout), static_cast<uint32_t>(key),
+          static_cast<uint32_t>(key >> 32), n);
+    else
+      pg::wigner_normals_kernel<float><<<blocks, threads>>>(
+          static_cast<const uint4*>(dc), static_cast<float*>(dout), static_cast<uint32_t>(key),
+          static_cast<uint32_t>(key >> 32), n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, static_cast<size_t>(n) * 2 * esize, cudaMemcpyDeviceToHost);
+  cudaFree(dc);
+  cudaFree(dout);
+  if (e != cudaSuccess) {
+    pg::set_error(std::string("pg_wigner_normals: ") + cudaGetErrorString(e));
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
 
 int pg_philox_words(const uint32_t* counters, uint64_t key, uint32_t* out, int64_t n) {
   PG_CHECK(counters && out && n >= 0, PG_ERR_INVALID, "pg_philox_words: bad argument");

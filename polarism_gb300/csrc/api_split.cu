@@ -1,0 +1,366 @@
+// Host sequencing of the split-step orderings on top of the Stockham passes (split.cu).
+//
+// K-outer ordering (split-step-fft-cuda; polarism/solver/split_step_fft_cuda_solver.py:
+// 1144-1325): the spectrum is kept between steps; per step one column pass does
+// F_y^-1, the local step R(dt/2) N(dt) R(dt/2) with the Wigner increment, and F_y, and
+// one row pass does F_x, the full kinetic factor / N and F_x^-1.  The half kick at
+// entry and exit of an advance is folded into the first and last row passes.
+//
+// CPU ordering (split-step-fft; polarism/solver/split_step_fft_solver.py:97-159):
+// R/2 K/2 N K/2 R/2 with psi in real space at step boundaries; the reservoir half
+// steps ending one step and starting the next are fused into one column pass.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "pg_internal.h"
+#include "solver.h"
+#include "split_internal.h"
+
+namespace pg {
+namespace {
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+
+enum PropTable { PROP_HALF_N = 0, PROP_FULL_N = 1, PROP_EXIT = 2, PROP_COUNT = 3 };
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+int ilog2(int n) {
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+double fft_wavenumber(int j, int n, double d) {
+  const int k = j < (n + 1) / 2 ? j : j - n;  // numpy.fft.fftfreq ordering
+  return 2.0 * kPi * static_cast<double>(k) / (static_cast<double>(n) * d);
+}
+
+template <typename T>
+int setup_tables(pg_solver* s) {
+  const pg_config& c = s->cfg;
+  const int nx = c.nx, ny = c.ny, m = c.members;
+  const double N = static_cast<double>(nx) * ny;
+  // Twiddles w_N^k = exp(-2 pi i k / N), computed in double precision.
+  std::vector<T> twx(2 * nx), twy(2 * ny);
+  for (int k = 0; k < nx; ++k) {
+    const double a = -2.0 * kPi * k / nx;
+    twx[2 * k] = static_cast<T>(std::cos(a));
+    twx[2 * k + 1] = static_cast<T>(std::sin(a));
+  }
+  for (int k = 0; k < ny; ++k) {
+    const double a = -2.0 * kPi * k / ny;
+    twy[2 * k] = static_cast<T>(std::cos(a));
+    twy[2 * k + 1] = static_cast<T>(std::sin(a));
+  }
+  // Separable propagators exp(-i hbar k^2 tau / 2m) = px[j] py[i], scale folded into px.
+  const size_t per = static_cast<size_t>(nx + ny);
+  std::vector<T> prop(static_cast<size_t>(PROP_COUNT) * m * per * 2);
+  for (int table = 0; table < PROP_COUNT; ++table) {
+    for (int mm = 0; mm < m; ++mm) {
+      const pg_physics& p = s->physics[mm];
+      double tau = 0.0, scale = 1.0;
+      if (table == PROP_HALF_N) {
+        tau = 0.5 * c.dt;
+        scale = 1.0 / N;
+      } else if (table == PROP_FULL_N) {
+        tau = c.dt;
+        scale = 1.0 / N;
+      } else {
+        // The last row pass left F_x^-1 (Psi full / N); F_x of it is nx Psi full / N, so
+        // ny conj(half) turns it into Psi half.
+        tau = -0.5 * c.dt;
+        scale = static_cast<double>(ny);
+      }
+      const double cf = p.hbar * tau / (2.0 * p.m_eff);
+      T* base = prop.data() + ((static_cast<size_t>(table) * m + mm) * per) * 2;
+      for (int j = 0; j < nx; ++j) {
+        const double k = fft_wavenumber(j, nx, c.dx);
+        const std::complex<double> v = scale * std::exp(std::complex<double>(0.0, -cf * k * k));
+        base[2 * j] = static_cast<T>(v.real());
+        base[2 * j + 1] = static_cast<T>(v.imag());
+      }
+      for (int i = 0; i < ny; ++i) {
+        const double k = fft_wavenumber(i, ny, c.dy);
+        const std::complex<double> v = std::exp(std::complex<double>(0.0, -cf * k * k));
+        base[2 * (nx + i)] = static_cast<T>(v.real());
+        base[2 * (nx + i) + 1] = static_cast<T>(v.imag());
+      }
+    }
+  }
+  PG_CUDA(cudaMalloc(&s->tw_x, twx.size() * sizeof(T)));
+  PG_CUDA(cudaMalloc(&s->tw_y, twy.size() * sizeof(T)));
+  PG_CUDA(cudaMalloc(&s->prop, prop.size() * sizeof(T)));
+  PG_CUDA(cudaMalloc(&s->split_consts, static_cast<size_t>(m) * sizeof(SplitConst<T>)));
+  PG_CUDA(cudaMemcpy(s->tw_x, twx.data(), twx.size() * sizeof(T), cudaMemcpyHostToDevice));
+  PG_CUDA(cudaMemcpy(s->tw_y, twy.data(), twy.size() * sizeof(T), cudaMemcpyHostToDevice));
+  PG_CUDA(cudaMemcpy(s->prop, prop.data(), prop.size() * sizeof(T), cudaMemcpyHostToDevice));
+  PG_CUDA(configure_split_kernels<T>(200 * 1024));
+  return PG_OK;
+}
+
+template <typename T>
+int upload_split_consts(pg_solver* s) {
+  const int m = s->cfg.members;
+  std::vector<SplitConst<T>> v(m);
+  for (int i = 0; i < m; ++i) {
+    const pg_physics& p = s->physics[i];
+    SplitConst<T>& k = v[i];
+    k.inv_hbar = static_cast<T>(1.0 / p.hbar);
+    k.g_C = static_cast<T>(p.g_C);
+    k.g_R = static_cast<T>(p.g_R);
+    k.R = static_cast<T>(p.R);
+    k.gamma_C = static_cast<T>(p.gamma_C);
+    k.gamma_R = static_cast<T>(p.gamma_R);
+    if (s->noise) {
+      k.noise_a = static_cast<T>(s->noise_strength[i] * s->noise_gamma[i] * s->dt_over_4dv);
+      k.noise_b = static_cast<T>(s->noise_strength[i] * s->noise_R[i] * s->dt_over_4dv);
+      k.seed = s->seeds[i];
+    } else {
+      k.noise_a = k.noise_b = T(0);
+      k.seed = 0ull;
+    }
+  }
+  PG_CUDA(cudaMemcpy(s->split_consts, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice));
+  return PG_OK;
+}
+
+int ensure_split(pg_solver* s) {
+  if (s->split_ready) return PG_OK;
+  const pg_config& c = s->cfg;
+  PG_CHECK(is_pow2(c.nx) && is_pow2(c.ny) && c.nx >= 4 && c.ny >= 4 && c.nx <= 4096 &&
+               c.ny <= 4096,
+           PG_ERR_UNSUPPORTED, "split-step: nx and ny must be powers of two between 4 and 4096");
+  int rc = c.precision == PG_DOUBLE ? setup_tables<double>(s) : setup_tables<float>(s);
+  if (rc != PG_OK) return rc;
+  rc = c.precision == PG_DOUBLE ? upload_split_consts<double>(s) : upload_split_consts<float>(s);
+  if (rc != PG_OK) return rc;
+  s->split_ready = true;
+  return PG_OK;
+}
+
+struct PassPlan {
+  RowPassArgs row;
+  ColPassArgs col;
+};
+
+PassPlan plan(const pg_solver* s) {
+  const pg_config& c = s->cfg;
+  const bool dbl = c.precision == PG_DOUBLE;
+  const int mv = split_max_vals(dbl);
+  const size_t csize = dbl ? 16 : 8;
+  PassPlan p{};
+  RowPassArgs& r = p.row;
+  r.nx = c.nx;
+  r.ny = c.ny;
+  r.log2nx = ilog2(c.nx);
+  int rows = 1;
+  while (rows * 2 <= c.ny && rows * 2 * c.nx <= 4096) rows *= 2;
+  r.rows = rows;
+  r.log2rows = ilog2(rows);
+  int threads = (rows * c.nx + mv - 1) / mv;
+  threads = ((threads + 31) / 32) * 32;
+  r.threads = threads < 32 ? 32 : threads;
+  r.table_stride = c.nx + c.ny;
+  ColPassArgs& k = p.col;
+  k.nx = c.nx;
+  k.ny = c.ny;
+  k.log2ny = ilog2(c.ny);
+  int cols = 1;
+  while (cols * 2 <= c.nx && cols * 2 <= 16 && cols * 2 * c.ny * csize <= 160 * 1024 &&
+         cols * 2 * c.ny <= mv * 1024)
+    cols *= 2;
+  k.cols = cols;
+  k.log2cols = ilog2(cols);
+  threads = (cols * c.ny + mv - 1) / mv;
+  threads = ((threads + 31) / 32) * 32;
+  k.threads = threads < 32 ? 32 : threads;
+  k.members = c.members;
+  k.reservoir = c.reservoir == PG_RES_SINGLE;
+  k.potential = c.potential;
+  k.noise = s->noise ? 1 : 0;
+  k.pump_stride = c.pump_per_member ? s->plane : 0;
+  k.pot_stride = c.potential_per_member ? s->plane : 0;
+  k.dt_d = c.dt;
+  k.dt_f = static_cast<float>(c.dt);
+  return p;
+}
+
+template <typename T>
+cudaError_t row_launch(pg_solver* s, const PassPlan& p, int forward, int table, int inverse) {
+  RowPassArgs a = p.row;
+  a.forward = forward;
+  a.inverse = inverse;
+  a.multiply = table >= 0;
+  const size_t per = static_cast<size_t>(s->cfg.nx + s->cfg.ny);
+  const T* px = static_cast<const T*>(s->prop) +
+                (static_cast<size_t>(table < 0 ? 0 : table) * s->cfg.members * per) * 2;
+  const T* py = px + static_cast<size_t>(s->cfg.nx) * 2;
+  // Member m's factors start at px + m * (nx + ny) complex values (py follows its px).
+  return launch_row_pass<T>(static_cast<T*>(s->psi[s->cur]), static_cast<const T*>(s->tw_x), px,
+                            py, a, s->cfg.members, s->stream);
+}
+
+template <typename T>
+cudaError_t col_launch(pg_solver* s, const PassPlan& p, int inverse, int op, int forward,
+                       int scale_offset, int step_offset) {
+  ColPassArgs a = p.col;
+  a.inverse = inverse;
+  a.forward = forward;
+  a.op = op;
+  a.scale_offset = scale_offset;
+  a.step_offset = step_offset;
+  return launch_col_pass<T>(static_cast<T*>(s->psi[s->cur]), static_cast<T*>(s->res[s->cur]),
+                            static_cast<const T*>(s->pump), static_cast<const T*>(s->potential),
+                            static_cast<const T*>(s->tw_y),
+                            static_cast<const SplitConst<T>*>(s->split_consts),
+                            static_cast<const T*>(s->scales), s->step_base, a, s->stream);
+}
+
+// The launches of one chunk of `len` steps (scales already staged).
+template <typename T>
+cudaError_t chunk_launches(pg_solver* s, const PassPlan& p, int ordering, int len) {
+  cudaError_t e = cudaSuccess;
+  if (ordering == 1) {
+    for (int k = 0; k < len && e == cudaSuccess; ++k) {
+      e = col_launch<T>(s, p, 1, SPLIT_OP_KOUTER, 1, 2 * k, k);
+      if (e == cudaSuccess) e = row_launch<T>(s, p, 1, PROP_FULL_N, 1);
+    }
+    return e;
+  }
+  for (int k = 0; k < len && e == cudaSuccess; ++k) {
+    if (k == 0)
+      e = col_launch<T>(s, p, 0, SPLIT_OP_RES_START, 1, 0, 0);
+    else
+      e = col_launch<T>(s, p, 1, SPLIT_OP_RES_END_START, 1, 2 * k - 1, k);
+    if (e == cudaSuccess) e = row_launch<T>(s, p, 1, PROP_HALF_N, 1);
+    if (e == cudaSuccess) e = col_launch<T>(s, p, 1, SPLIT_OP_NONLINEAR, 1, 0, k);
+    if (e == cudaSuccess) e = row_launch<T>(s, p, 1, PROP_HALF_N, 1);
+  }
+  if (e == cudaSuccess) e = col_launch<T>(s, p, 1, SPLIT_OP_RES_END, 0, 2 * (len - 1) + 1, len - 1);
+  return e;
+}
+
+template <typename T>
+int split_advance_t(pg_solver* s, int ordering, int64_t start_step, int n_steps,
+                    const double* scales, int use_graphs) {
+  const PassPlan p = plan(s);
+  s->last_launches = 0;
+  if (ordering == 1) {
+    // Entry: spectrum (or FFT2 of psi) times the half kick, then F_x^-1.
+    if (!s->spectral) {
+      PG_CUDA(col_launch<T>(s, p, 0, SPLIT_OP_NONE, 1, 0, 0));
+      PG_CUDA(row_launch<T>(s, p, 1, PROP_HALF_N, 1));
+      s->last_launches += 2;
+    } else {
+      PG_CUDA(row_launch<T>(s, p, 0, PROP_HALF_N, 1));
+      s->last_launches += 1;
+    }
+    s->spectral = false;
+  } else {
+    PG_CHECK(!s->spectral, PG_ERR_INVALID,
+             "split-step-fft (R/2 K/2 N K/2 R/2) needs psi in real space; the state holds a "
+             "spectrum");
+  }
+  const int m = s->cfg.members;
+  int done = 0;
+  while (done < n_steps) {
+    const int len = std::min(kChunk, n_steps - done);
+    int rc = stage_coefficients(s, scales + static_cast<size_t>(done) * 2 * m, len, 2,
+                                start_step + done);
+    if (rc != PG_OK) return rc;
+    if (use_graphs && len >= 2) {
+      auto key = std::make_tuple(ordering, len, 0);
+      auto it = s->split_graphs.find(key);
+      cudaGraphExec_t exec = nullptr;
+      if (it == s->split_graphs.end()) {
+        cudaGraph_t graph = nullptr;
+        PG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t le = chunk_launches<T>(s, p, ordering, len);
+        cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
+        if (le != cudaSuccess || ee != cudaSuccess) {
+          if (graph) cudaGraphDestroy(graph);
+          set_error(std::string("split-step graph capture failed: ") +
+                    cudaGetErrorString(le != cudaSuccess ? le : ee));
+          return PG_ERR_CUDA;
+        }
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+          set_error(std::string("split-step graph instantiate failed: ") + cudaGetErrorString(ie));
+          return PG_ERR_CUDA;
+        }
+        s->split_graphs[key] = exec;
+      } else {
+        exec = it->second;
+      }
+      PG_CUDA(cudaGraphLaunch(exec, s->stream));
+    } else {
+      PG_CUDA(chunk_launches<T>(s, p, ordering, len));
+    }
+    s->last_launches += ordering == 1 ? 2 * len : 4 * len + 1;
+    done += len;
+  }
+  if (ordering == 1) {
+    // Exit: F_x, then ny conj(half) turns the last full kick into the closing half kick.
+    PG_CUDA(row_launch<T>(s, p, 1, PROP_EXIT, 0));
+    s->last_launches += 1;
+    s->spectral = true;
+  }
+  return PG_OK;
+}
+
+}  // namespace
+
+int split_release(pg_solver* s) {
+  for (auto& kv : s->split_graphs) cudaGraphExecDestroy(kv.second);
+  s->split_graphs.clear();
+  cudaFree(s->tw_x);
+  cudaFree(s->tw_y);
+  cudaFree(s->prop);
+  cudaFree(s->split_consts);
+  s->tw_x = s->tw_y = s->prop = s->split_consts = nullptr;
+  s->split_ready = false;
+  return PG_OK;
+}
+
+int split_refresh_consts(pg_solver* s) {
+  for (auto& kv : s->split_graphs) cudaGraphExecDestroy(kv.second);
+  s->split_graphs.clear();
+  return s->cfg.precision == PG_DOUBLE ? upload_split_consts<double>(s)
+                                       : upload_split_consts<float>(s);
+}
+
+}  // namespace pg
+
+extern "C" {
+
+int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t n_steps,
+                     const double* half_scales, int use_graphs) {
+  PG_CHECK(s && half_scales, PG_ERR_INVALID, "pg_split_advance: null argument");
+  PG_CHECK(ordering == 0 || ordering == 1, PG_ERR_INVALID,
+           "pg_split_advance: ordering must be 0 (R/2 K/2 N K/2 R/2) or 1 (K/2 [R/2 N R/2] K/2)");
+  PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_split_advance: negative step count");
+  if (n_steps == 0) return PG_OK;
+  int rc = pg::ensure_split(s);
+  if (rc != PG_OK) return rc;
+  return s->cfg.precision == PG_DOUBLE
+             ? pg::split_advance_t<double>(s, ordering, start_step, n_steps, half_scales, use_graphs)
+             : pg::split_advance_t<float>(s, ordering, start_step, n_steps, half_scales, use_graphs);
+}
+
+int pg_set_state_kind(pg_solver* s, int32_t spectral) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_set_state_kind: null solver");
+  s->spectral = spectral != 0;
+  return PG_OK;
+}
+
+int pg_get_state_kind(pg_solver* s, int32_t* spectral) {
+  PG_CHECK(s && spectral, PG_ERR_INVALID, "pg_get_state_kind: null argument");
+  *spectral = s->spectral ? 1 : 0;
+  return PG_OK;
+}
+
+}  // extern "C"

@@ -41,7 +41,7 @@ struct RhsConst {
   T inv_hbar;        // 1 / hbar (potential)
   T half_R, half_gC; // R / 2, gamma_C / 2
   T R, gamma_R;      // reservoir loss
-  T eta_a;           // kinetic relaxation eta * a
+  T eta_a;           // kinetic relaxation eta (multiplies n_A * a * Laplacian)
   T noise_a, noise_b;// sigma^2 = noise_a + noise_b * n_A  (strength (gamma_C + R n) dt / (4 dV))
   T pad_;
   unsigned long long seed;

@@ -14,22 +14,15 @@ struct Words4 {
   uint32_t a, b, c, d;
 };
 
-__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t x, uint32_t y) {
-#if defined(__CUDA_ARCH__)
-  return __umulhi(x, y);
-#else
-  return static_cast<uint32_t>((static_cast<uint64_t>(x) * y) >> 32);
-#endif
-}
-
 // Ten Philox rounds; the key schedule is bumped by the Weyl constants between rounds.
 __host__ __device__ __forceinline__ Words4 philox4x32_10(Words4 x, uint32_t k0, uint32_t k1) {
 #pragma unroll
   for (int round = 0; round < 10; ++round) {
-    const uint32_t hi0 = mulhi32(0xD2511F53u, x.a);
-    const uint32_t lo0 = 0xD2511F53u * x.a;
-    const uint32_t hi1 = mulhi32(0xCD9E8D57u, x.c);
-    const uint32_t lo1 = 0xCD9E8D57u * x.c;
+    // One wide 32x32->64 multiply per word pair yields both halves.
+    const uint64_t p0 = static_cast<uint64_t>(x.a) * 0xD2511F53ull;
+    const uint64_t p1 = static_cast<uint64_t>(x.c) * 0xCD9E8D57ull;
+    const uint32_t hi0 = static_cast<uint32_t>(p0 >> 32), lo0 = static_cast<uint32_t>(p0);
+    const uint32_t hi1 = static_cast<uint32_t>(p1 >> 32), lo1 = static_cast<uint32_t>(p1);
     x = Words4{hi1 ^ x.b ^ k0, lo1, hi0 ^ x.d ^ k1, lo0};
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
@@ -48,17 +41,31 @@ __device__ __forceinline__ Words4 wigner_words(uint32_t cell, uint64_t step, uin
 template <typename T>
 struct WignerDraw;
 
+// Single precision uses the SFU approximations: -2 ln u1 = -2 ln2 log2(u1) (absolute
+// error of log2 below 2^-22 on [0.5, 2]), sqrt(x) = x rsqrt(x), and sin/cos of the angle
+// reduced exactly to (-pi, pi] (u2 - 1 is exact for u2 > 1/2; absolute error of the SFU
+// sine/cosine about 2^-21 there).  The resulting normals stay within a few 1e-6 of the
+// correctly rounded Box-Muller transform except at radii below ~1e-3 (u1 within 2^-20
+// of 1), where the error is bounded in absolute terms by ~1e-4 * sqrt(variance).
 template <>
 struct WignerDraw<float> {
+  static __device__ __forceinline__ float radius2(uint32_t a) {
+    const float u1 = static_cast<float>((a >> 8) + 1u) * 5.9604644775390625e-08f;
+    return -1.3862943611198906f * __log2f(u1);  // -2 ln(u1)
+  }
+  static __device__ __forceinline__ void angle(uint32_t b, float* s, float* c) {
+    float u2 = static_cast<float>((b >> 8) + 1u) * 5.9604644775390625e-08f;
+    u2 = u2 > 0.5f ? u2 - 1.0f : u2;
+    __sincosf(6.283185307179586f * u2, s, c);
+  }
   static __device__ __forceinline__ void apply(const Words4& w, float variance, float& re,
                                                float& im) {
-    const float u1 = static_cast<float>((w.a >> 8) + 1u) * 5.9604644775390625e-08f;
-    const float u2 = static_cast<float>((w.b >> 8) + 1u) * 5.9604644775390625e-08f;
-    const float amp = sqrtf(variance * (-2.0f * logf(u1)));
+    const float x = variance * radius2(w.a);
+    const float amp = x > 0.0f ? x * rsqrtf(x) : 0.0f;
     float s, c;
-    sincosf(6.283185307179586f * u2, &s, &c);
-    re += amp * c;
-    im += amp * s;
+    angle(w.b, &s, &c);
+    re = fmaf(amp, c, re);
+    im = fmaf(amp, s, im);
   }
 };
 
@@ -72,7 +79,7 @@ struct WignerDraw<double> {
                        static_cast<double>(w.d >> 6) + 1.0) * 1.1102230246251565404e-16;
     const double amp = sqrt(variance * (-2.0 * log(u1)));
     double s, c;
-    sincos(6.283185307179586476925286766559 * u2, &s, &c);
+    sincospi(2.0 * u2, &s, &c);
     re += amp * c;
     im += amp * s;
   }

@@ -1,0 +1,330 @@
+// Full-width fused RK4 step for FP32 rows up to 1024 sites (the common case).
+//
+// Same mathematics and operation order as rk4.cu (polarism/model.py:89-127,
+// polarism/solver/rk4_fdm_solver.py:36-82, single_reservoir.py:70-98, Wigner
+// increment of rk4_cuda_solver.py:518-532), mapped differently onto the SM:
+//
+// * A block spans the whole periodic row (2 columns per thread, nx/2 threads), so
+//   there is no horizontal halo and 1024-wide rows use 16 balanced warps.
+// * Rows of psi0, n0 and the pump envelope stream into an 8-row shared-memory ring
+//   through 1-D bulk copies (TMA) that complete on per-slot mbarriers, three rows
+//   ahead of use.  Stage 1 reads its whole stencil straight from the ring; stages 2-4
+//   get vertical neighbours from per-thread register rings and horizontal ones from
+//   one double-buffered shared exchange per row.
+// * Complex arithmetic uses packed FP32x2 instructions (__ffma2_rn and friends).
+// * Blocks are persistent: block c advances rows [c R / G, (c+1) R / G) of the
+//   member-major row space (R = members * ny rows), restarting the 4-row pipeline
+//   fill whenever it crosses into the next member.
+#include "philox.cuh"
+#include "pg_internal.h"
+#include "tma.cuh"
+#include "wide_internal.h"
+
+namespace pg {
+namespace {
+
+constexpr int kRing = 8;          // rows resident: r-4..r plus three in flight
+constexpr int kWaitLimit = 100000;
+
+struct Pair {
+  float2 a, b;  // complex values of the thread's two columns
+};
+
+struct WideConst {
+  float2 nax, nay;      // (-ax, -ax), (-ay, -ay)
+  float w0, gc, gr, half_R, half_gC, R, gamma_R, noise_a, noise_b;
+  uint64_t seed;
+};
+
+// Right-hand side at one site: c centre, (lt, rt, up, dn) neighbours.  Writes
+// d = dpsi/dt and returns dn/dt.
+__device__ __forceinline__ float site_rhs(float2 c, float2 lt, float2 rt, float2 up, float2 dn,
+                                          float n, float sP, const WideConst& k, float2& d) {
+  const float2 sx = __fadd2_rn(lt, rt);
+  const float2 sy = __fadd2_rn(up, dn);
+  const float2 nl = __ffma2_rn(k.nay, sy, __fmul2_rn(k.nax, sx));  // -a (lap without centre)
+  const float rho = fmaf(c.x, c.x, c.y * c.y);
+  const float w = fmaf(k.gr, n, fmaf(k.gc, rho, k.w0));
+  const float gl = fmaf(k.half_R, n, -k.half_gC);
+  const float2 u = __ffma2_rn(make_float2(w, w), c, nl);  // w c - a lap_neighbours
+  d.x = fmaf(gl, c.x, u.y);
+  d.y = fmaf(gl, c.y, -u.x);
+  return fmaf(-fmaf(k.R, rho, k.gamma_R), n, sP);
+}
+
+__device__ __forceinline__ float2 axpy2(float h, float2 d, float2 y) {
+  return __ffma2_rn(make_float2(h, h), d, y);
+}
+
+template <bool NOISE>
+__global__ void __launch_bounds__(512, 1)
+    rk4_wide_kernel(const float2* __restrict__ psi_in, const float* __restrict__ n_in,
+                    const float* __restrict__ pump, float2* __restrict__ psi_out,
+                    float* __restrict__ n_out, const RhsConst<float>* __restrict__ consts,
+                    const float* __restrict__ scales,
+                    const unsigned long long* __restrict__ step_base, const int step_offset,
+                    const float dt, const WideGeom g, int* __restrict__ err_flag) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int nx = g.nx, ny = g.ny;
+  float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][nx]
+  float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * nx); // [kRing][nx]
+  float* ring_p = ring_n + kRing * nx;                             // [kRing][nx]
+  float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * nx);   // [2][3][nx/2]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * (nx / 2));
+
+  const int tid = threadIdx.x;
+  const int half = nx >> 1;
+  const bool active = tid < half;
+  const int t = active ? tid : half - 1;
+  const int col0 = 2 * t;
+  const int lcol = col0 == 0 ? nx - 1 : col0 - 1;   // left neighbour of column 2t
+  const int rcol = col0 + 2 == nx ? 0 : col0 + 2;   // right neighbour of column 2t+1
+  const int lthr = t == 0 ? half - 1 : t - 1;       // thread owning lcol
+  const int rthr = t + 1 == half ? 0 : t + 1;       // thread owning rcol
+  const long long plane = static_cast<long long>(nx) * ny;
+  const uint32_t row_bytes = static_cast<uint32_t>(nx) * 16u;
+
+  if (tid == 0) {
+    for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  const long long total_rows = static_cast<long long>(g.members) * ny;
+  const long long r_begin = total_rows * blockIdx.x / gridDim.x;
+  const long long r_end = total_rows * (blockIdx.x + 1) / gridDim.x;
+  const float hh = 0.5f * dt, h6 = dt / 6.0f, h3 = dt / 3.0f;
+  unsigned it = 0;  // ring use counter, continues across segments (mbarrier phases)
+  bool timed_out = false;
+
+  long long gr = r_begin;
+  while (gr < r_end) {
+    const int member = static_cast<int>(gr / ny);
+    const int ya = static_cast<int>(gr - static_cast<long long>(member) * ny);
+    const int yb = static_cast<int>(min(static_cast<long long>(ny), ya + (r_end - gr)));
+    gr += yb - ya;
+    const int n_iter = ((yb - ya) + 8 + 3) & ~3;
+
+    const RhsConst<float> kk = consts[member];
+    WideConst k;
+    k.nax = make_float2(-kk.ax, -kk.ax);
+    k.nay = make_float2(-kk.ay, -kk.ay);
+    k.w0 = kk.w0;
+    k.gc = kk.gc;
+    k.gr = kk.gr;
+    k.half_R = kk.half_R;
+    k.half_gC = kk.half_gC;
+    k.R = kk.R;
+    k.gamma_R = kk.gamma_R;
+    k.noise_a = kk.noise_a;
+    k.noise_b = kk.noise_b;
+    k.seed = kk.seed;
+    const float s0 = scales[(step_offset * 3 + 0) * g.members + member];
+    const float s1 = scales[(step_offset * 3 + 1) * g.members + member];
+    const float s2 = scales[(step_offset * 3 + 2) * g.members + member];
+    const unsigned long long noise_step = NOISE ? step_base[0] + step_offset : 0ull;
+    const float2* psi_m = psi_in + member * plane;
+    const float* n_m = n_in + member * plane;
+    const float* p_m = pump + member * g.pump_stride;
+    int row_first = (ya - 4) % ny;
+    if (row_first < 0) row_first += ny;
+
+    // Issue the bulk copies of iteration `i` (row ya - 4 + i) into its ring slot.
+    auto issue = [&](int i) {
+      const unsigned slot = (it + i) & (kRing - 1);
+      int row = row_first + i;
+      while (row >= ny) row -= ny;
+      const uint32_t bar = smem_u32(&mbar[slot]);
+      mbar_arrive_expect_tx(bar, row_bytes);
+      bulk_g2s(smem_u32(ring_psi + slot * nx), psi_m + static_cast<long long>(row) * nx, nx * 8u, bar);
+      bulk_g2s(smem_u32(ring_n + slot * nx), n_m + static_cast<long long>(row) * nx, nx * 4u, bar);
+      bulk_g2s(smem_u32(ring_p + slot * nx), p_m + static_cast<long long>(row) * nx, nx * 4u, bar);
+    };
+    if (tid == 0) {
+      for (int i = 0; i < 3 && i < n_iter; ++i) issue(i);
+    }
+
+    Pair q1[4], q2[4], q3[4], acc[4];
+    float2 m1[4], m2[4], m3[4], accn[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      q1[s] = q2[s] = q3[s] = acc[s] = Pair{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      m1[s] = m2[s] = m3[s] = accn[s] = make_float2(0.f, 0.f);
+    }
+    int row_out = (ya - 8) % ny;
+    if (row_out < 0) row_out += ny;
+
+    for (int i0 = 0; i0 < n_iter; i0 += 4) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int i = i0 + j;
+        const int ja = (j + 3) & 3, jb = (j + 2) & 3, jc = (j + 1) & 3, jd = j;
+        const unsigned u_i = it + i;
+        const unsigned slot0 = u_i & (kRing - 1);          // row r
+        const unsigned slot1 = (u_i - 1) & (kRing - 1);    // row r-1
+        const unsigned slot2 = (u_i - 2) & (kRing - 1);    // row r-2
+        const unsigned slot3 = (u_i - 3) & (kRing - 1);    // row r-3
+        const unsigned slot4 = (u_i - 4) & (kRing - 1);    // row r-4
+        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), (u_i / kRing) & 1u, kWaitLimit))
+          timed_out = true;
+        const float4* xin = xbuf + ((j + 1) & 1) * 3 * half;
+
+        // Stage 1 at row r-1 from the ring: k1 = f(psi0).
+        const float2* R1 = ring_psi + slot1 * nx;
+        const float4 c4 = *reinterpret_cast<const float4*>(R1 + col0);
+        const float4 u4 = *reinterpret_cast<const float4*>(ring_psi + slot2 * nx + col0);
+        const float4 d4 = *reinterpret_cast<const float4*>(ring_psi + slot0 * nx + col0);
+        const float2 lt = R1[lcol], rt = R1[rcol];
+        const float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
+        const float2 up0 = make_float2(u4.x, u4.y), up1 = make_float2(u4.z, u4.w);
+        const float2 dn0 = make_float2(d4.x, d4.y), dn1 = make_float2(d4.z, d4.w);
+        const float2 n1v = *reinterpret_cast<const float2*>(ring_n + slot1 * nx + col0);
+        const float2 P1 = *reinterpret_cast<const float2*>(ring_p + slot1 * nx + col0);
+        {
+          float2 da, db;
+          const float dna = site_rhs(c0, lt, c1, up0, dn0, n1v.x, __fmul_rn(s0, P1.x), k, da);
+          const float dnb = site_rhs(c1, c0, rt, up1, dn1, n1v.y, __fmul_rn(s0, P1.y), k, db);
+          q1[ja] = Pair{axpy2(hh, da, c0), axpy2(hh, db, c1)};
+          acc[ja] = Pair{axpy2(h6, da, c0), axpy2(h6, db, c1)};
+          m1[ja] = make_float2(fmaf(hh, dna, n1v.x), fmaf(hh, dnb, n1v.y));
+          accn[ja] = make_float2(fmaf(h6, dna, n1v.x), fmaf(h6, dnb, n1v.y));
+        }
+        // Stage 2 at row r-2: k2 = f(psi1).
+        {
+          const float4 L = xin[lthr], Rr = xin[rthr];
+          const float2 lt2 = make_float2(L.z, L.w), rt2 = make_float2(Rr.x, Rr.y);
+          const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * nx + col0);
+          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * nx + col0);
+          const Pair c = q1[jb];
+          float2 da, db;
+          const float dna = site_rhs(c.a, lt2, c.b, q1[jc].a, q1[ja].a, m1[jb].x,
+                                     __fmul_rn(s1, P2.x), k, da);
+          const float dnb = site_rhs(c.b, c.a, rt2, q1[jc].b, q1[ja].b, m1[jb].y,
+                                     __fmul_rn(s1, P2.y), k, db);
+          q2[jb] = Pair{axpy2(hh, da, up0), axpy2(hh, db, up1)};  // psi0 at row r-2
+          m2[jb] = make_float2(fmaf(hh, dna, n0.x), fmaf(hh, dnb, n0.y));
+          acc[jb] = Pair{axpy2(h3, da, acc[jb].a), axpy2(h3, db, acc[jb].b)};
+          accn[jb] = make_float2(fmaf(h3, dna, accn[jb].x), fmaf(h3, dnb, accn[jb].y));
+        }
+        // Stage 3 at row r-3: k3 = f(psi2).
+        {
+          const float4 L = xin[half + lthr], Rr = xin[half + rthr];
+          const float2 lt3 = make_float2(L.z, L.w), rt3 = make_float2(Rr.x, Rr.y);
+          const float2 P3 = *reinterpret_cast<const float2*>(ring_p + slot3 * nx + col0);
+          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * nx + col0);
+          const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * nx + col0);
+          const Pair c = q2[jc];
+          float2 da, db;
+          const float dna = site_rhs(c.a, lt3, c.b, q2[jd].a, q2[jb].a, m2[jc].x,
+                                     __fmul_rn(s1, P3.x), k, da);
+          const float dnb = site_rhs(c.b, c.a, rt3, q2[jd].b, q2[jb].b, m2[jc].y,
+                                     __fmul_rn(s1, P3.y), k, db);
+          q3[jc] = Pair{axpy2(dt, da, make_float2(p4.x, p4.y)), axpy2(dt, db, make_float2(p4.z, p4.w))};
+          m3[jc] = make_float2(fmaf(dt, dna, n0.x), fmaf(dt, dnb, n0.y));
+          acc[jc] = Pair{axpy2(h3, da, acc[jc].a), axpy2(h3, db, acc[jc].b)};
+          accn[jc] = make_float2(fmaf(h3, dna, accn[jc].x), fmaf(h3, dnb, accn[jc].y));
+        }
+        // Stage 4 at row r-4: k4 = f(psi3), final combine, clamp, Wigner increment.
+        {
+          const float4 L = xin[2 * half + lthr], Rr = xin[2 * half + rthr];
+          const float2 lt4 = make_float2(L.z, L.w), rt4 = make_float2(Rr.x, Rr.y);
+          const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * nx + col0);
+          const Pair c = q3[jd];
+          float2 da, db;
+          const float dna = site_rhs(c.a, lt4, c.b, q3[ja].a, q3[jc].a, m3[jd].x,
+                                     __fmul_rn(s2, P4.x), k, da);
+          const float dnb = site_rhs(c.b, c.a, rt4, q3[ja].b, q3[jc].b, m3[jd].y,
+                                     __fmul_rn(s2, P4.y), k, db);
+          float2 oa = axpy2(h6, da, acc[jd].a);
+          float2 ob = axpy2(h6, db, acc[jd].b);
+          float na = fmaf(h6, dna, accn[jd].x);
+          float nb = fmaf(h6, dnb, accn[jd].y);
+          na = na < 0.f ? 0.f : na;
+          nb = nb < 0.f ? 0.f : nb;
+          if (i >= 8 && i - 8 < yb - ya && active) {
+            const long long o = static_cast<long long>(row_out) * nx + col0;
+            if (NOISE) {
+              const Words4 wa = wigner_words(static_cast<uint32_t>(o), noise_step, 1u, k.seed);
+              WignerDraw<float>::apply(wa, k.noise_a + k.noise_b * na, oa.x, oa.y);
+              const Words4 wb = wigner_words(static_cast<uint32_t>(o + 1), noise_step, 1u, k.seed);
+              WignerDraw<float>::apply(wb, k.noise_a + k.noise_b * nb, ob.x, ob.y);
+            }
+            *reinterpret_cast<float4*>(psi_out + member * plane + o) = make_float4(oa.x, oa.y, ob.x, ob.y);
+            *reinterpret_cast<float2*>(n_out + member * plane + o) = make_float2(na, nb);
+          }
+        }
+        // Publish stage inputs for the horizontal neighbours.
+        {
+          float4* xo = xbuf + (j & 1) * 3 * half;
+          if (active) {
+            xo[t] = make_float4(q1[ja].a.x, q1[ja].a.y, q1[ja].b.x, q1[ja].b.y);
+            xo[half + t] = make_float4(q2[jb].a.x, q2[jb].a.y, q2[jb].b.x, q2[jb].b.y);
+            xo[2 * half + t] = make_float4(q3[jc].a.x, q3[jc].a.y, q3[jc].b.x, q3[jc].b.y);
+          }
+        }
+        row_out = row_out + 1 == ny ? 0 : row_out + 1;
+        __syncthreads();
+        // Slot of row r+3 held row r-5, last read by stage 4 of the previous iteration.
+        if (tid == 0 && i + 3 < n_iter) issue(i + 3);
+      }
+    }
+    it += n_iter;
+  }
+  if (timed_out) atomicOr(err_flag, 1);
+}
+
+}  // namespace
+
+bool wide_rk4_supported(int nx, int ny) {
+  return nx >= 64 && nx <= 1024 && (nx % 64) == 0 && ny >= 4;
+}
+
+size_t wide_rk4_smem(int nx) {
+  return static_cast<size_t>(kRing) * nx * 16 + static_cast<size_t>(6) * (nx / 2) * 16 +
+         kRing * sizeof(uint64_t);
+}
+
+cudaError_t configure_wide_rk4() {
+  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(wide_rk4_smem(1024)));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(rk4_wide_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(wide_rk4_smem(1024)));
+}
+
+int wide_rk4_blocks_per_sm(int nx, bool noise) {
+  int blocks = 0;
+  const int threads = nx / 2;
+  cudaError_t e =
+      noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, rk4_wide_kernel<true>, threads,
+                                                            wide_rk4_smem(nx))
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, rk4_wide_kernel<false>,
+                                                            threads, wide_rk4_smem(nx));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return blocks < 1 ? 1 : blocks;
+}
+
+cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float* pump,
+                            float* psi_out, float* n_out, const RhsConst<float>* consts,
+                            const float* scales, const unsigned long long* step_base,
+                            int step_offset, float dt, bool noise, const WideGeom& g,
+                            int* err_flag, cudaStream_t stream) {
+  const int threads = g.nx / 2;
+  const size_t smem = wide_rk4_smem(g.nx);
+  if (noise) {
+    rk4_wide_kernel<true><<<g.blocks, threads, smem, stream>>>(
+        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
+        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  } else {
+    rk4_wide_kernel<false><<<g.blocks, threads, smem, stream>>>(
+        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
+        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace pg

@@ -1,0 +1,64 @@
+// Definition of the opaque pg_solver handle shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "pg_internal.h"
+
+namespace pg {
+constexpr int kChunk = 64;         // steps per staged chunk / CUDA graph
+constexpr int kStagingSlots = 4;   // pinned staging ring depth
+}  // namespace pg
+
+struct pg_solver {
+  pg_config cfg{};
+  std::vector<pg_physics> physics;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  size_t real_size = 4;
+  long long plane = 0;     // nx * ny
+  long long sites = 0;     // members * plane
+  void* psi[2] = {nullptr, nullptr};
+  void* res[2] = {nullptr, nullptr};
+  void* pump = nullptr;
+  void* potential = nullptr;
+  void* consts = nullptr;
+  void* scales = nullptr;  // kChunk * 3 * members reals
+  unsigned long long* step_base = nullptr;
+  int cur = 0;
+  bool noise = false;
+  std::vector<uint64_t> seeds;
+  std::vector<double> noise_gamma, noise_R, noise_strength;
+  double dt_over_4dv = 0.0;
+  pg::RK4Geom geom{};
+  // Pinned staging ring for chunk scales and the step base.
+  struct Slot {
+    void* host = nullptr;
+    cudaEvent_t done = nullptr;
+  } staging[pg::kStagingSlots];
+  int next_slot = 0;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (length, parity) -> graph
+  int* err_flag = nullptr;   // set by kernels whose bounded waits gave up
+  int rk4_kernel = 0;        // 0 auto, 1 tiled streaming kernel, 2 full-width kernel
+  int wide_blocks = 0;       // persistent grid of the full-width kernel
+  // Split-step state.
+  bool spectral = false;      // psi holds the unnormalised 2-D spectrum instead of psi(x, y)
+  bool split_ready = false;
+  void* tw_x = nullptr;       // exp(-2 pi i k / nx), k < nx
+  void* tw_y = nullptr;
+  void* prop = nullptr;       // [table][member][nx + ny] propagator factors
+  void* split_consts = nullptr;
+  std::map<std::tuple<int, int, int>, cudaGraphExec_t> split_graphs;  // (ordering, len, parity)
+  long long last_launches = 0;
+};
+
+
+namespace pg {
+int split_release(pg_solver* s);
+int split_refresh_consts(pg_solver* s);
+// Stage a chunk's per-step coefficients (per_step * members doubles per step) and the step base.
+int stage_coefficients(pg_solver* s, const double* coeffs, int len, int per_step, int64_t step);
+}  // namespace pg

@@ -1,0 +1,380 @@
+// Split-step Fourier stepping: hand-written shared-memory Stockham FFT passes with
+// the kinetic propagator and the local (reservoir / nonlinear / Wigner) step fused in.
+//
+// A 2-D transform is split into a row pass (FFT along x of C contiguous rows) and a
+// column pass (FFT along y of a panel of C adjacent columns).  Both run in place on
+// the state array, each block owning disjoint rows / panels.
+//
+//   row pass:    [F_x] -> x (px[j] py[i])  -> [F_x^-1]        (propagator is separable:
+//                 exp(-i hbar (kx^2+ky^2) tau / 2m) = exp(-i c kx^2) exp(-i c ky^2))
+//   column pass: [F_y^-1] -> local op at each site -> [F_y]
+//
+// Orderings built from these passes (polarism/solver/split_step_fft_cuda_solver.py:
+// 106-184,1144-1325 for K(dt/2)[R(dt/2) N(dt) R(dt/2)]K(dt/2) with the spectrum kept
+// between steps; polarism/solver/split_step_fft_solver.py:97-159 for
+// R/2 K/2 N K/2 R/2) are sequenced by the host in api_split.cu.
+//
+// The Stockham passes follow the autosort recurrence
+//   y[q + s (R p + r)] = w_N^{p r s} * sum_t x[q + s (p + m t)] w_R^{r t}
+// with radix 4 (plus one radix-2 pass when log2 N is odd), executed in place with the
+// inputs of every butterfly staged in registers between two barriers.
+#include "philox.cuh"
+#include "pg_internal.h"
+#include "split_internal.h"
+
+namespace pg {
+namespace {
+
+template <typename T>
+struct C2T;
+template <>
+struct C2T<float> {
+  using type = float2;
+};
+template <>
+struct C2T<double> {
+  using type = double2;
+};
+
+template <typename C2>
+__device__ __forceinline__ C2 cmul(C2 a, C2 b) {
+  return C2{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <typename C2>
+__device__ __forceinline__ C2 cmulc(C2 a, C2 b) {  // a * conj(b)
+  return C2{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+
+// Complex values a thread stages per pass (keeps the 1024-thread blocks within 64 registers).
+template <typename T>
+struct MaxVals {
+  static constexpr int value = sizeof(T) == 4 ? 16 : 8;
+};
+
+// One in-place radix-R Stockham pass over C sequences of length N (all powers of two).
+// Element (i, c) of the shared buffer sits at buf[i * si + c * sc].  COLS selects which
+// index varies fastest across threads (c for column panels, i within a row) so shared
+// memory accesses stay contiguous.  s = stride (product of the radices already done),
+// m = N / (R s).  Requires N * C <= MaxVals<T>::value * blockDim.x.
+template <typename T, bool INVERSE, bool COLS, int R>
+__device__ __forceinline__ void stockham_pass(typename C2T<T>::type* buf,
+                                              const typename C2T<T>::type* tw, int log2n,
+                                              int log2c, int si, int sc, int log2s, int m) {
+  using C2 = typename C2T<T>::type;
+  constexpr int MAXB = MaxVals<T>::value / R;
+  constexpr int LOG2R = R == 4 ? 2 : 1;
+  const int log2per = log2n - LOG2R;  // butterflies per sequence = N / R
+  const int nb = 1 << (log2per + log2c);
+  const int s = 1 << log2s;
+  C2 v[MAXB][R];
+  int base_in[MAXB], cidx[MAXB];
+#pragma unroll
+  for (int kb = 0; kb < MAXB; ++kb) {
+    const int b = threadIdx.x + kb * blockDim.x;
+    if (b < nb) {
+      int c, rest;
+      if (COLS) {
+        c = b & ((1 << log2c) - 1);
+        rest = b >> log2c;
+      } else {
+        c = b >> log2per;
+        rest = b & ((1 << log2per) - 1);
+      }
+      const int q = rest & (s - 1);
+      const int p = rest >> log2s;
+      base_in[kb] = q + s * p;
+      cidx[kb] = c;
+#pragma unroll
+      for (int t = 0; t < R; ++t) v[kb][t] = buf[(base_in[kb] + s * m * t) * si + c * sc];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int kb = 0; kb < MAXB; ++kb) {
+    const int b = threadIdx.x + kb * blockDim.x;
+    if (b < nb) {
+      const int c = cidx[kb];
+      const int q = base_in[kb] & (s - 1);
+      const int p = base_in[kb] >> log2s;
+      C2 y[R];
+      if (R == 2) {
+        const C2 a = v[kb][0], bb = v[kb][1 % R];
+        y[0] = C2{a.x + bb.x, a.y + bb.y};
+        y[1 % R] = C2{a.x - bb.x, a.y - bb.y};
+      } else {
+        const C2 a0 = v[kb][0], a1 = v[kb][1 % R], a2 = v[kb][2 % R], a3 = v[kb][3 % R];
+        const C2 t0{a0.x + a2.x, a0.y + a2.y}, t1{a0.x - a2.x, a0.y - a2.y};
+        const C2 t2{a1.x + a3.x, a1.y + a3.y};
+        const C2 d{a1.x - a3.x, a1.y - a3.y};
+        // forward: t3 = -i d; inverse: t3 = +i d
+        const C2 t3 = INVERSE ? C2{-d.y, d.x} : C2{d.y, -d.x};
+        y[0] = C2{t0.x + t2.x, t0.y + t2.y};
+        y[1 % R] = C2{t1.x + t3.x, t1.y + t3.y};
+        y[2 % R] = C2{t0.x - t2.x, t0.y - t2.y};
+        y[3 % R] = C2{t1.x - t3.x, t1.y - t3.y};
+      }
+      const int out = q + s * R * p;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        C2 val = y[r];
+        if (r > 0) {
+          const C2 w = tw[p * r * s];
+          val = INVERSE ? cmulc(val, w) : cmul(val, w);
+        }
+        buf[(out + s * r) * si + c * sc] = val;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// In-place Stockham FFT (radix 4, with one radix-2 pass first when log2 N is odd).
+template <typename T, bool INVERSE, bool COLS>
+__device__ void smem_fft(typename C2T<T>::type* buf, const typename C2T<T>::type* tw, int log2n,
+                         int log2c, int si, int sc) {
+  int log2s = 0;
+  int log2m = log2n;
+  if (log2n & 1) {
+    stockham_pass<T, INVERSE, COLS, 2>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 1));
+    log2s += 1;
+    log2m -= 1;
+  }
+  while (log2m > 0) {
+    stockham_pass<T, INVERSE, COLS, 4>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 2));
+    log2s += 2;
+    log2m -= 2;
+  }
+}
+
+// ------------------------------------------------------------------ row pass
+template <typename T>
+__global__ void __launch_bounds__(1024) row_pass_kernel(typename C2T<T>::type* __restrict__ data,
+                                                        const typename C2T<T>::type* __restrict__ tw,
+                                                        const typename C2T<T>::type* __restrict__ px,
+                                                        const typename C2T<T>::type* __restrict__ py,
+                                                        const RowPassArgs a) {
+  using C2 = typename C2T<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* tws = reinterpret_cast<C2*>(smem_raw);
+  C2* buf = tws + a.nx;
+  const int member = blockIdx.z;
+  const int row0 = blockIdx.x * a.rows;
+  const int rows = a.rows;
+  const long long plane = static_cast<long long>(a.nx) * a.ny;
+  C2* d = data + member * plane + static_cast<long long>(row0) * a.nx;
+  for (int k = threadIdx.x; k < a.nx; k += blockDim.x) tws[k] = tw[k];
+  const int count = rows * a.nx;
+  for (int e = threadIdx.x; e < count; e += blockDim.x) buf[e] = d[e];
+  __syncthreads();
+  if (a.forward) smem_fft<T, false, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
+  if (a.multiply) {
+    const C2* pxm = px + static_cast<long long>(member) * a.table_stride;
+    const C2* pym = py + static_cast<long long>(member) * a.table_stride;
+    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+      const int r = e >> a.log2nx;
+      const int j = e & (a.nx - 1);
+      buf[e] = cmul(buf[e], cmul(pxm[j], pym[row0 + r]));
+    }
+    __syncthreads();
+  }
+  if (a.inverse) smem_fft<T, true, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
+  for (int e = threadIdx.x; e < count; e += blockDim.x) d[e] = buf[e];
+}
+
+// ------------------------------------------------------------------ local operations
+template <typename T>
+__device__ __forceinline__ T expm1_t(T x);
+template <>
+__device__ __forceinline__ float expm1_t<float>(float x) { return expm1f(x); }
+template <>
+__device__ __forceinline__ double expm1_t<double>(double x) { return expm1(x); }
+template <typename T>
+__device__ __forceinline__ T exp_t(T x);
+template <>
+__device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
+template <>
+__device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
+__device__ __forceinline__ void sincos_t(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_t(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ float mul_rn_t(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn_t(double a, double b) { return __dmul_rn(a, b); }
+
+// Midpoint RK2 reservoir half step at frozen |psi|^2 with the final clamp
+// (polarism/reservoir/single_reservoir.py:100-111).
+template <typename T>
+__device__ __forceinline__ T reservoir_half(T n, T rho, T pump, T h, const SplitConst<T>& k) {
+  const T loss = k.gamma_R + k.R * rho;
+  const T k1 = pump - loss * n;
+  const T mid = n + T(0.5) * h * k1;
+  const T k2 = pump - loss * mid;
+  const T out = n + h * k2;
+  return out > T(0) ? out : T(0);
+}
+
+// Exact local step psi * exp(g dt - i phi) (split_step_fft_solver.py:121-139).
+template <typename T>
+__device__ __forceinline__ void nonlinear(T& re, T& im, T n, T vre, T vim, T dt,
+                                          const SplitConst<T>& k) {
+  const T rho = re * re + im * im;
+  const T gain = (k.R * n - k.gamma_C) * T(0.5) + vim * k.inv_hbar;
+  const T x = T(2) * gain * dt;
+  const T phase_time =
+      fabs(x) < T(1e-6) ? dt * (T(1) + x * T(0.5) + x * x / T(6)) : dt * expm1_t(x) / x;
+  const T phase = ((vre + k.g_R * n) * dt + k.g_C * rho * phase_time) * k.inv_hbar;
+  const T amp = exp_t(gain * dt);
+  T s, c;
+  sincos_t(phase, &s, &c);
+  const T r = re, i = im;
+  re = amp * (r * c + i * s);
+  im = amp * (i * c - r * s);
+}
+
+// ------------------------------------------------------------------ column pass
+template <typename T>
+__global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* __restrict__ data,
+                                                        T* __restrict__ res,
+                                                        const T* __restrict__ pump,
+                                                        const T* __restrict__ potential,
+                                                        const typename C2T<T>::type* __restrict__ tw,
+                                                        const SplitConst<T>* __restrict__ consts,
+                                                        const T* __restrict__ scales,
+                                                        const unsigned long long* __restrict__ step_base,
+                                                        const ColPassArgs a) {
+  using C2 = typename C2T<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2* tws = reinterpret_cast<C2*>(smem_raw);
+  C2* buf = tws + a.ny;
+  const int member = blockIdx.z;
+  const int x0 = blockIdx.x * a.cols;
+  const int C = a.cols;
+  const long long plane = static_cast<long long>(a.nx) * a.ny;
+  C2* d = data + member * plane;
+  for (int k = threadIdx.x; k < a.ny; k += blockDim.x) tws[k] = tw[k];
+  const int count = C * a.ny;
+  for (int e = threadIdx.x; e < count; e += blockDim.x) {
+    const int c = e & (C - 1), i = e >> a.log2cols;
+    buf[i * C + c] = d[static_cast<long long>(i) * a.nx + x0 + c];
+  }
+  __syncthreads();
+  if (a.inverse) smem_fft<T, true, true>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
+  if (a.op != SPLIT_OP_NONE) {
+    const SplitConst<T> k = consts[member];
+    const int m_count = a.members;
+    const T s0 = scales[(a.scale_offset + 0) * m_count + member];
+    const T s1 = scales[(a.scale_offset + 1) * m_count + member];
+    const T* pm = pump + member * a.pump_stride;
+    const T* vm = potential ? potential + member * a.pot_stride * (a.potential == 2 ? 2 : 1) : nullptr;
+    T* rm = res + member * plane;
+    const T dt = a.template dt_of<T>();
+    const T h = dt * T(0.5);
+    const unsigned long long step = a.noise ? step_base[0] + a.step_offset : 0ull;
+    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+      const int c = e & (C - 1), i = e >> a.log2cols;
+      const long long o = static_cast<long long>(i) * a.nx + x0 + c;
+      C2 v = buf[i * C + c];
+      T n = a.reservoir ? rm[o] : T(0);
+      const T P = pm[o];
+      T vre = T(0), vim = T(0);
+      if (vm) {
+        vre = a.potential == 2 ? vm[2 * o] : vm[o];
+        vim = a.potential == 2 ? vm[2 * o + 1] : T(0);
+      }
+      bool add_noise = false;
+      switch (a.op) {
+        case SPLIT_OP_KOUTER:
+          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
+          nonlinear(v.x, v.y, n, vre, vim, dt, k);
+          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s1, P), h, k);
+          add_noise = a.noise != 0;
+          break;
+        case SPLIT_OP_RES_START:
+          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
+          break;
+        case SPLIT_OP_RES_END_START:
+          if (a.reservoir) {
+            const T rho = v.x * v.x + v.y * v.y;
+            n = reservoir_half(n, rho, mul_rn_t(s0, P), h, k);
+            n = reservoir_half(n, rho, mul_rn_t(s1, P), h, k);
+          }
+          break;
+        case SPLIT_OP_NONLINEAR:
+          nonlinear(v.x, v.y, n, vre, vim, dt, k);
+          add_noise = a.noise != 0;
+          break;
+        case SPLIT_OP_RES_END:
+          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
+          break;
+        default:
+          break;
+      }
+      if (add_noise) {
+        const Words4 w = wigner_words(static_cast<uint32_t>(o), step, 1u, k.seed);
+        WignerDraw<T>::apply(w, k.noise_a + k.noise_b * n, v.x, v.y);
+      }
+      buf[i * C + c] = v;
+      if (a.reservoir) rm[o] = n;
+    }
+    __syncthreads();
+  }
+  if (a.forward) smem_fft<T, false, true>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
+  for (int e = threadIdx.x; e < count; e += blockDim.x) {
+    const int c = e & (C - 1), i = e >> a.log2cols;
+    d[static_cast<long long>(i) * a.nx + x0 + c] = buf[i * C + c];
+  }
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_row_pass(T* data, const T* tw, const T* px, const T* py, const RowPassArgs& a,
+                            int members, cudaStream_t stream) {
+  using C2 = typename C2T<T>::type;
+  const int blocks = (a.ny + a.rows - 1) / a.rows;
+  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.nx) + static_cast<size_t>(a.rows) * a.nx);
+  row_pass_kernel<T><<<dim3(blocks, 1, members), a.threads, smem, stream>>>(
+      reinterpret_cast<C2*>(data), reinterpret_cast<const C2*>(tw), reinterpret_cast<const C2*>(px),
+      reinterpret_cast<const C2*>(py), a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_col_pass(T* data, T* res, const T* pump, const T* potential, const T* tw,
+                            const SplitConst<T>* consts, const T* scales,
+                            const unsigned long long* step_base, const ColPassArgs& a,
+                            cudaStream_t stream) {
+  using C2 = typename C2T<T>::type;
+  const int blocks = (a.nx + a.cols - 1) / a.cols;
+  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.ny) + static_cast<size_t>(a.cols) * a.ny);
+  col_pass_kernel<T><<<dim3(blocks, 1, a.members), a.threads, smem, stream>>>(
+      reinterpret_cast<C2*>(data), res, pump, potential, reinterpret_cast<const C2*>(tw), consts,
+      scales, step_base, a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t configure_split_kernels(size_t max_smem) {
+  cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(max_smem));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(col_pass_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(max_smem));
+}
+
+template cudaError_t launch_row_pass<float>(float*, const float*, const float*, const float*,
+                                            const RowPassArgs&, int, cudaStream_t);
+template cudaError_t launch_row_pass<double>(double*, const double*, const double*, const double*,
+                                             const RowPassArgs&, int, cudaStream_t);
+template cudaError_t launch_col_pass<float>(float*, float*, const float*, const float*, const float*,
+                                            const SplitConst<float>*, const float*,
+                                            const unsigned long long*, const ColPassArgs&,
+                                            cudaStream_t);
+template cudaError_t launch_col_pass<double>(double*, double*, const double*, const double*,
+                                             const double*, const SplitConst<double>*, const double*,
+                                             const unsigned long long*, const ColPassArgs&,
+                                             cudaStream_t);
+int split_max_vals(bool is_double) { return is_double ? MaxVals<double>::value : MaxVals<float>::value; }
+
+template cudaError_t configure_split_kernels<float>(size_t);
+template cudaError_t configure_split_kernels<double>(size_t);
+
+}  // namespace pg

@@ -1,0 +1,73 @@
+// Internal declarations of the split-step (Stockham FFT) passes.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace pg {
+
+enum SplitOp {
+  SPLIT_OP_NONE = 0,
+  SPLIT_OP_KOUTER = 1,         // R(dt/2) at P(t+dt/4), N(dt), R(dt/2) at P(t+3dt/4), Wigner
+  SPLIT_OP_RES_START = 2,      // R(dt/2) at P(t+dt/4)
+  SPLIT_OP_RES_END_START = 3,  // R(dt/2) at P(t-dt/4) of the previous step, then at P(t+dt/4)
+  SPLIT_OP_NONLINEAR = 4,      // N(dt), then Wigner with the current n_R
+  SPLIT_OP_RES_END = 5,        // R(dt/2) at P(t+3dt/4)
+};
+
+// Per-member constants of the local split-step operations.
+template <typename T>
+struct SplitConst {
+  T inv_hbar, g_C, g_R, R, gamma_C, gamma_R;
+  T noise_a, noise_b;
+  unsigned long long seed;
+};
+
+struct RowPassArgs {
+  int nx, ny, log2nx;
+  int rows, log2rows;   // rows per block (power of two)
+  int threads;
+  int forward, inverse, multiply;
+  int table_stride;     // complex values between consecutive members' propagator factors
+};
+
+struct ColPassArgs {
+  int nx, ny, log2ny;
+  int cols, log2cols;   // columns per block (power of two)
+  int threads;
+  int members;
+  int forward, inverse;
+  int op;               // SplitOp
+  int reservoir;        // single reservoir present
+  int potential;        // 0 none, 1 real, 2 complex
+  int noise;
+  long long pump_stride, pot_stride;
+  int scale_offset;     // index into scales ([k][member]) of the first coefficient
+  int step_offset;      // noise step = step_base[0] + step_offset
+  double dt_d;
+  float dt_f;
+  // dt in the working precision is read through dt_of<T>().
+  template <typename T>
+  __host__ __device__ T dt_of() const;
+};
+
+template <>
+inline __host__ __device__ float ColPassArgs::dt_of<float>() const { return dt_f; }
+template <>
+inline __host__ __device__ double ColPassArgs::dt_of<double>() const { return dt_d; }
+
+template <typename T>
+cudaError_t launch_row_pass(T* data, const T* tw, const T* px, const T* py, const RowPassArgs& a,
+                            int members, cudaStream_t stream);
+
+template <typename T>
+cudaError_t launch_col_pass(T* data, T* res, const T* pump, const T* potential, const T* tw,
+                            const SplitConst<T>* consts, const T* scales,
+                            const unsigned long long* step_base, const ColPassArgs& a,
+                            cudaStream_t stream);
+
+template <typename T>
+cudaError_t configure_split_kernels(size_t max_smem);
+
+// Complex values one thread stages per FFT pass: blocks need N * C <= this * threads.
+int split_max_vals(bool is_double);
+
+}  // namespace pg

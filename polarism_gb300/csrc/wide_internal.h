@@ -1,0 +1,25 @@
+// Internal declarations of the full-width FP32 RK4 kernel.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pg_internal.h"
+
+namespace pg {
+
+struct WideGeom {
+  int nx, ny, members;
+  int blocks;              // persistent grid size
+  long long pump_stride;   // 0: shared envelope; nx*ny: one per member
+};
+
+bool wide_rk4_supported(int nx, int ny);
+size_t wide_rk4_smem(int nx);
+cudaError_t configure_wide_rk4();
+int wide_rk4_blocks_per_sm(int nx, bool noise);
+cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float* pump,
+                            float* psi_out, float* n_out, const RhsConst<float>* consts,
+                            const float* scales, const unsigned long long* step_base,
+                            int step_offset, float dt, bool noise, const WideGeom& g,
+                            int* err_flag, cudaStream_t stream);
+
+}  // namespace pg

@@ -71,7 +71,8 @@ class MemberPhysics:
 
 
 class RK4Engine:
-    """Fused RK4 stepping of ``members`` same-shape fields on the GPU."""
+    """One device solver handle: ``members`` same-shape fields stepped on the GPU by the
+    fused RK4 kernels or the split-step Fourier passes."""
 
     def __init__(self, nx, ny, members, dx, dy, dt, physics, precision="single", reservoir=True,
                  potential=_lib.PG_POT_NONE, pump_per_member=False, potential_per_member=False):
@@ -178,6 +179,15 @@ class RK4Engine:
         _lib.check(self.lib.pg_rk4_set_geometry(self.handle, int(tile_w), int(strip_h)),
                    "pg_rk4_set_geometry")
 
+    def set_kernel(self, kind):
+        """0 automatic, 1 tiled streaming kernel, 2 full-width FP32 kernel."""
+        _lib.check(self.lib.pg_rk4_set_kernel(self.handle, int(kind)), "pg_rk4_set_kernel")
+
+    def kernel(self) -> int:
+        k = C.c_int32()
+        _lib.check(self.lib.pg_rk4_get_kernel(self.handle, C.byref(k)), "pg_rk4_get_kernel")
+        return k.value
+
     def geometry(self):
         t, h = C.c_int32(), C.c_int32()
         _lib.check(self.lib.pg_rk4_get_geometry(self.handle, C.byref(t), C.byref(h)),
@@ -192,6 +202,24 @@ class RK4Engine:
         _lib.check(self.lib.pg_rk4_advance(self.handle, int(start_step), int(n_steps),
                                            scales.ctypes.data, int(bool(use_graphs))),
                    "pg_rk4_advance")
+
+    def split_advance(self, ordering, start_step, n_steps, half_scales, use_graphs=True):
+        """Split-step Fourier steps; ``half_scales`` is (n_steps, 2, members): the pump
+        coefficients at t + dt/4 and t + 3 dt/4.  ordering 0 = R/2 K/2 N K/2 R/2 (real-space
+        state), 1 = K/2 [R/2 N R/2] K/2 (leaves the unnormalised spectrum)."""
+        scales = np.ascontiguousarray(np.broadcast_to(
+            np.asarray(half_scales, dtype=np.float64), (int(n_steps), 2, self.members)))
+        _lib.check(self.lib.pg_split_advance(self.handle, int(ordering), int(start_step),
+                                             int(n_steps), scales.ctypes.data,
+                                             int(bool(use_graphs))), "pg_split_advance")
+
+    def set_state_kind(self, spectral: bool):
+        _lib.check(self.lib.pg_set_state_kind(self.handle, int(bool(spectral))), "pg_set_state_kind")
+
+    def state_kind(self) -> bool:
+        k = C.c_int32()
+        _lib.check(self.lib.pg_get_state_kind(self.handle, C.byref(k)), "pg_get_state_kind")
+        return bool(k.value)
 
     @property
     def last_launch_count(self) -> int:
@@ -209,3 +237,20 @@ def philox_words(counters, key: int) -> np.ndarray:
     _lib.check(lib.pg_philox_words(ctr.ctypes.data, C.c_uint64(int(key)), out.ctypes.data, n),
                "pg_philox_words")
     return out
+
+
+
+def wigner_normals(counters, key: int, precision: str = "single") -> np.ndarray:
+    """The device Box-Muller normals (2, ...) drawn from each counter's Philox words."""
+    lib = _lib.load()
+    ctr = np.ascontiguousarray(np.asarray(counters, dtype=np.uint32))
+    n = ctr.size // 4
+    dtype = np.float32 if precision == "single" else np.float64
+    out = np.empty((n, 2), dtype=dtype)
+    _lib.check(lib.pg_wigner_normals(ctr.ctypes.data, C.c_uint64(int(key)),
+                                     _lib.PG_SINGLE if precision == "single" else _lib.PG_DOUBLE,
+                                     out.ctypes.data, n), "pg_wigner_normals")
+    return out.T.reshape(2, *ctr.shape[:-1])
+
+
+Engine = RK4Engine

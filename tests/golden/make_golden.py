@@ -303,6 +303,8 @@ def main(root):
     trajectory_case(HERE, "split_cpu", "split-step-fft", 20, **common)
     trajectory_case(HERE, "rk4_fdm_quiet", "rk4-fdm", 20,
                     **dict(common, wigner=False, seed=0, p0=0.02, sigma=12.0))
+    trajectory_case(HERE, "split_cpu_p2", "split-step-fft", 12,
+                    **dict(common, nx=32, ny=16, lx=40.0, ly=20.0))
     kouter_case(HERE)
     ifrk4_cases(HERE, root)
     dp5_case(HERE)

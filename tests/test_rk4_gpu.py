@@ -223,3 +223,73 @@ def test_launch_count_and_error_status(cuda_lib):
     assert eng.last_launch_count == 70
     with pytest.raises(RuntimeError, match="strip height"):
         eng.set_geometry(8, 6)
+
+
+@pytest.mark.parametrize("nx,ny,members", [(64, 48, 3), (128, 20, 2), (1024, 8, 1)])
+def test_full_width_kernel_matches_oracle_and_tiled(cuda_lib, nx, ny, members):
+    """The TMA full-width FP32 kernel against the oracle (1e-4) and the tiled kernel (1e-5)."""
+    from polarism_gb300.engine import MemberPhysics, RK4Engine
+
+    rng = np.random.default_rng(nx + ny)
+    p = dict(hbar=0.6582119514, m_eff=0.284, g_C=0.001, g_R=0.002, g_I=0.0, R=0.02,
+             gamma_C=0.083, gamma_R=0.005)
+    dx, dy, dt = 0.5, 0.6, 1e-3
+    psi0 = 0.05 * (rng.standard_normal((members, 1, ny, nx))
+                   + 1j * rng.standard_normal((members, 1, ny, nx)))
+    res0 = np.abs(rng.standard_normal((members, 1, ny, nx))) * 0.02
+    env = np.abs(rng.standard_normal((members, 1, ny, nx)))
+    seeds = [5 + m for m in range(members)]
+    steps = 7
+    outs = {}
+    for kernel in (2, 1):
+        eng = RK4Engine(nx, ny, members, dx, dy, dt, MemberPhysics(**p), "single",
+                        pump_per_member=True)
+        eng.set_kernel(kernel)
+        assert eng.kernel() == kernel
+        eng.set_pump(env.astype(np.float32))
+        eng.set_noise(seeds, p["gamma_C"], p["R"], 1.0, dt / (4 * dx * dy))
+        eng.set_state(psi0.astype(np.complex64), res0.astype(np.float32))
+        eng.advance(0, steps, np.full((steps, 3, members), 0.04))
+        outs[kernel] = eng.get_state()
+    noise = gpe.Noise(seeds, [p["gamma_C"]] * members, [p["R"]] * members, [1.0] * members, dt,
+                      dx * dy, "double", normals_precision="single")
+    psi_o, f_o = gpe.rk4_advance(psi0.copy(), (res0.copy(),), lambda t: env * 0.04, 0.0, p, dx,
+                                 dy, dt, 0, steps, noise=noise)
+    psi_w, res_w = outs[2]
+    psi_t, res_t = outs[1]
+    assert rel_l2(psi_w, psi_o) < 1e-4 and rel_l2(res_w, f_o[0]) < 1e-4
+    assert rel_l2(psi_w, psi_t) < 1e-5 and rel_l2(res_w, res_t) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_device_normals_within_error_bound(cuda_lib, precision):
+    """Device Box-Muller normals against the reference's normal_pair on the same words.
+
+    FP64 uses correctly rounded library functions (2e-14, the reference's own bound).  FP32
+    uses SFU approximations: |error| <= 4e-6 (1 + r) plus 3e-7 / r for the radius term."""
+    from oracle.philox import normal_pair
+    from polarism_gb300.engine import wigner_normals
+
+    counters = counter_words(np.arange(1 << 18), 987654321)
+    key = 0xDEADBEEF12345
+    got = wigner_normals(counters, key, precision)
+    words = philox4x32(counters, key)
+    if precision == "double":
+        re, im = normal_pair(words, "double")
+    else:
+        # The single-precision uniforms of normal_pair, transformed exactly (in FP64).
+        u1 = ((words[..., 0] >> 8).astype(np.float64) + 1.0) * 2.0 ** -24
+        u2 = ((words[..., 1] >> 8).astype(np.float64) + 1.0) * 2.0 ** -24
+        rr = np.sqrt(-2.0 * np.log(u1))
+        re, im = rr * np.cos(2 * np.pi * u2), rr * np.sin(2 * np.pi * u2)
+        ref32 = normal_pair(words, "single")
+        assert rel_l2(ref32[0], re) < 1e-6  # the reference's own FP32 path, same realisation
+    r = np.hypot(re, im)
+    if precision == "double":
+        np.testing.assert_allclose(got[0], re, rtol=2e-14, atol=2e-14)
+        np.testing.assert_allclose(got[1], im, rtol=2e-14, atol=2e-14)
+        return
+    bound = 4e-6 * (1 + r) + 3e-7 / np.maximum(r, 1e-30)
+    assert np.all(np.abs(got[0] - re) <= bound)
+    assert np.all(np.abs(got[1] - im) <= bound)
+    assert rel_l2(got[0], re) < 1e-6 and rel_l2(got[1], im) < 1e-6
