@@ -126,8 +126,8 @@ int pg_set_state_kind(pg_solver* s, int32_t spectral);
 int pg_get_state_kind(pg_solver* s, int32_t* spectral);
 
 /* Choose the RK4 kernel: 0 automatic, 1 the tiled streaming kernel (any size, FP32/FP64,
- * potential and relaxation terms), 2 the full-width FP32 kernel (nx a multiple of 64 up to
- * 1024, single reservoir, no potential).  pg_rk4_get_kernel reports the one in use (1 or 2). */
+ * potential and relaxation terms), 2 the full-width FP32 kernel (nx in {128, 256, 512, 1024},
+ * single reservoir, no potential).  pg_rk4_get_kernel reports the one in use (1 or 2). */
 int pg_rk4_set_kernel(pg_solver* s, int32_t kind);
 int pg_rk4_get_kernel(pg_solver* s, int32_t* kind);
 

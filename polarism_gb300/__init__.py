@@ -11,7 +11,11 @@ from __future__ import annotations
 
 __version__ = "0.1.0"
 
-SOLVER_NAMES = {"rk4-cuda": "RK4CudaSolver"}
+SOLVER_NAMES = {
+    "rk4-cuda": "RK4CudaSolver",
+    "split-step-fft": "SplitStepFFTSolver",
+    "split-step-fft-cuda": "SplitStepFFTCudaSolver",
+}
 
 
 def register(names=None):

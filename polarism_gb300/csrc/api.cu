@@ -428,7 +428,7 @@ int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
                  f.reservoir == 1 && pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny),
              PG_ERR_UNSUPPORTED,
              "pg_rk4_set_kernel: the full-width kernel needs FP32, a single reservoir, no "
-             "potential or relaxation term, and nx a multiple of 64 up to 1024");
+             "potential or relaxation term, and nx in {128, 256, 512, 1024}");
   }
   s->rk4_kernel = kind;
   free_graphs(s);

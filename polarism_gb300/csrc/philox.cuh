@@ -30,6 +30,98 @@ __host__ __device__ __forceinline__ Words4 philox4x32_10(Words4 x, uint32_t k0, 
   return x;
 }
 
+// Two counters under one key: the key schedule is shared between the two streams.
+__host__ __device__ __forceinline__ void philox4x32_10_pair(Words4& x, Words4& y, uint32_t k0,
+                                                           uint32_t k1) {
+#pragma unroll
+  for (int round = 0; round < 10; ++round) {
+    const uint64_t px0 = static_cast<uint64_t>(x.a) * 0xD2511F53ull;
+    const uint64_t px1 = static_cast<uint64_t>(x.c) * 0xCD9E8D57ull;
+    const uint64_t py0 = static_cast<uint64_t>(y.a) * 0xD2511F53ull;
+    const uint64_t py1 = static_cast<uint64_t>(y.c) * 0xCD9E8D57ull;
+    x = Words4{static_cast<uint32_t>(px1 >> 32) ^ x.b ^ k0, static_cast<uint32_t>(px1),
+               static_cast<uint32_t>(px0 >> 32) ^ x.d ^ k1, static_cast<uint32_t>(px0)};
+    y = Words4{static_cast<uint32_t>(py1 >> 32) ^ y.b ^ k0, static_cast<uint32_t>(py1),
+               static_cast<uint32_t>(py0 >> 32) ^ y.d ^ k1, static_cast<uint32_t>(py0)};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// Eight counters under one key (independent streams for instruction-level parallelism).
+__device__ __forceinline__ void philox4x32_10_octet(Words4 (&x)[8], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int round = 0; round < 10; ++round) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint64_t p0 = static_cast<uint64_t>(x[q].a) * 0xD2511F53ull;
+      const uint64_t p1 = static_cast<uint64_t>(x[q].c) * 0xCD9E8D57ull;
+      x[q] = Words4{static_cast<uint32_t>(p1 >> 32) ^ x[q].b ^ k0, static_cast<uint32_t>(p1),
+                    static_cast<uint32_t>(p0 >> 32) ^ x[q].d ^ k1, static_cast<uint32_t>(p0)};
+    }
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// Philox of the Wigner counters (cell, step_lo, step_hi, stream) for eight cells.  In
+// the first two rounds one of the two products depends only on (step, stream, key), so
+// it is formed once per call instead of once per cell (the words are identical to
+// philox4x32_10).
+struct PhiloxCellPrefix {
+  uint32_t a1, b1;     // words a, b after round 1 (cell independent)
+  uint32_t hi0, lo0;   // product a1 * M0 of round 2 (cell independent)
+  uint32_t stream_k1;  // stream ^ k1 (round 1)
+  uint32_t k0r2, k1r2; // round-2 keys
+  uint32_t k0, k1;     // round-3 keys
+};
+
+__device__ __forceinline__ PhiloxCellPrefix philox_cell_prefix(uint32_t step_lo, uint32_t step_hi,
+                                                               uint32_t stream, uint32_t k0,
+                                                               uint32_t k1) {
+  PhiloxCellPrefix p;
+  const uint64_t q1 = static_cast<uint64_t>(step_hi) * 0xCD9E8D57ull;
+  p.a1 = static_cast<uint32_t>(q1 >> 32) ^ step_lo ^ k0;
+  p.b1 = static_cast<uint32_t>(q1);
+  p.stream_k1 = stream ^ k1;
+  p.k0r2 = k0 + 0x9E3779B9u;
+  p.k1r2 = k1 + 0xBB67AE85u;
+  const uint64_t q0 = static_cast<uint64_t>(p.a1) * 0xD2511F53ull;
+  p.hi0 = static_cast<uint32_t>(q0 >> 32);
+  p.lo0 = static_cast<uint32_t>(q0);
+  p.k0 = p.k0r2 + 0x9E3779B9u;
+  p.k1 = p.k1r2 + 0xBB67AE85u;
+  return p;
+}
+
+__device__ __forceinline__ void philox_cells_octet(const uint32_t (&cell)[8], const PhiloxCellPrefix& p,
+                                                   Words4 (&x)[8]) {
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    // Round 1: a' = hi(c M1) ^ b ^ k0 and b' = lo(c M1) are cell independent.
+    const uint64_t r0 = static_cast<uint64_t>(cell[q]) * 0xD2511F53ull;
+    const uint32_t c1 = static_cast<uint32_t>(r0 >> 32) ^ p.stream_k1;
+    const uint32_t d1 = static_cast<uint32_t>(r0);
+    // Round 2: the product of a' is cell independent.
+    const uint64_t r1 = static_cast<uint64_t>(c1) * 0xCD9E8D57ull;
+    x[q] = Words4{static_cast<uint32_t>(r1 >> 32) ^ p.b1 ^ p.k0r2, static_cast<uint32_t>(r1),
+                  p.hi0 ^ d1 ^ p.k1r2, p.lo0};
+  }
+  uint32_t k0 = p.k0, k1 = p.k1;
+#pragma unroll
+  for (int round = 2; round < 10; ++round) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint64_t p0 = static_cast<uint64_t>(x[q].a) * 0xD2511F53ull;
+      const uint64_t p1 = static_cast<uint64_t>(x[q].c) * 0xCD9E8D57ull;
+      x[q] = Words4{static_cast<uint32_t>(p1 >> 32) ^ x[q].b ^ k0, static_cast<uint32_t>(p1),
+                    static_cast<uint32_t>(p0 >> 32) ^ x[q].d ^ k1, static_cast<uint32_t>(p0)};
+    }
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
 __device__ __forceinline__ Words4 wigner_words(uint32_t cell, uint64_t step, uint32_t stream,
                                                uint64_t seed) {
   return philox4x32_10(Words4{cell, static_cast<uint32_t>(step),
@@ -57,6 +149,14 @@ struct WignerDraw<float> {
     float u2 = static_cast<float>((b >> 8) + 1u) * 5.9604644775390625e-08f;
     u2 = u2 > 0.5f ? u2 - 1.0f : u2;
     __sincosf(6.283185307179586f * u2, s, c);
+  }
+  // Unit-variance normals (r cos theta, r sin theta) of one word quadruple.
+  static __device__ __forceinline__ float2 unit(const Words4& w) {
+    const float r2 = radius2(w.a);
+    const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+    float s, c;
+    angle(w.b, &s, &c);
+    return make_float2(r * c, r * s);
   }
   static __device__ __forceinline__ void apply(const Words4& w, float variance, float& re,
                                                float& im) {

@@ -56,35 +56,35 @@ __device__ __forceinline__ float2 axpy2(float h, float2 d, float2 y) {
   return __ffma2_rn(make_float2(h, h), d, y);
 }
 
-template <bool NOISE>
-__global__ void __launch_bounds__(512, 1)
+// At least 512 resident threads per SM for every row width (128 registers a thread).
+template <int NX, bool NOISE>
+__global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
     rk4_wide_kernel(const float2* __restrict__ psi_in, const float* __restrict__ n_in,
                     const float* __restrict__ pump, float2* __restrict__ psi_out,
                     float* __restrict__ n_out, const RhsConst<float>* __restrict__ consts,
                     const float* __restrict__ scales,
                     const unsigned long long* __restrict__ step_base, const int step_offset,
                     const float dt, const WideGeom g, int* __restrict__ err_flag) {
+  constexpr int HALF = NX / 2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  const int nx = g.nx, ny = g.ny;
-  float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][nx]
-  float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * nx); // [kRing][nx]
-  float* ring_p = ring_n + kRing * nx;                             // [kRing][nx]
-  float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * nx);   // [2][3][nx/2]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * (nx / 2));
+  float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][NX]
+  float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * NX); // [kRing][NX]
+  float* ring_p = ring_n + kRing * NX;                             // [kRing][NX]
+  float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * NX);   // [2][3][HALF]
+  float4* nbuf = xbuf + 6 * HALF;                                  // [4][HALF] unit normals
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(nbuf + (NOISE ? 4 * HALF : 0));
 
-  const int tid = threadIdx.x;
-  const int half = nx >> 1;
-  const bool active = tid < half;
-  const int t = active ? tid : half - 1;
+  const int ny = g.ny;
+  const int t = threadIdx.x;
   const int col0 = 2 * t;
-  const int lcol = col0 == 0 ? nx - 1 : col0 - 1;   // left neighbour of column 2t
-  const int rcol = col0 + 2 == nx ? 0 : col0 + 2;   // right neighbour of column 2t+1
-  const int lthr = t == 0 ? half - 1 : t - 1;       // thread owning lcol
-  const int rthr = t + 1 == half ? 0 : t + 1;       // thread owning rcol
-  const long long plane = static_cast<long long>(nx) * ny;
-  const uint32_t row_bytes = static_cast<uint32_t>(nx) * 16u;
+  const int lcol = col0 == 0 ? NX - 1 : col0 - 1;   // left neighbour of column 2t
+  const int rcol = col0 + 2 == NX ? 0 : col0 + 2;   // right neighbour of column 2t+1
+  const int lthr = t == 0 ? HALF - 1 : t - 1;       // thread owning lcol
+  const int rthr = t + 1 == HALF ? 0 : t + 1;       // thread owning rcol
+  const long long plane = static_cast<long long>(NX) * ny;
+  constexpr uint32_t kRowBytes = NX * 16u;
 
-  if (tid == 0) {
+  if (t == 0) {
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
     fence_mbar_init();
   }
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(512, 1)
   const long long r_begin = total_rows * blockIdx.x / gridDim.x;
   const long long r_end = total_rows * (blockIdx.x + 1) / gridDim.x;
   const float hh = 0.5f * dt, h6 = dt / 6.0f, h3 = dt / 3.0f;
-  unsigned it = 0;  // ring use counter, continues across segments (mbarrier phases)
+  unsigned it = 0;  // ring uses so far; always a multiple of kRing at a segment start
   bool timed_out = false;
 
   long long gr = r_begin;
@@ -103,7 +103,8 @@ __global__ void __launch_bounds__(512, 1)
     const int ya = static_cast<int>(gr - static_cast<long long>(member) * ny);
     const int yb = static_cast<int>(min(static_cast<long long>(ny), ya + (r_end - gr)));
     gr += yb - ya;
-    const int n_iter = ((yb - ya) + 8 + 3) & ~3;
+    const int h_rows = yb - ya;
+    const int n_iter = (h_rows + 8 + kRing - 1) & ~(kRing - 1);
 
     const RhsConst<float> kk = consts[member];
     WideConst k;
@@ -118,29 +119,34 @@ __global__ void __launch_bounds__(512, 1)
     k.gamma_R = kk.gamma_R;
     k.noise_a = kk.noise_a;
     k.noise_b = kk.noise_b;
-    k.seed = kk.seed;
+    const uint32_t key0 = static_cast<uint32_t>(kk.seed), key1 = static_cast<uint32_t>(kk.seed >> 32);
     const float s0 = scales[(step_offset * 3 + 0) * g.members + member];
     const float s1 = scales[(step_offset * 3 + 1) * g.members + member];
     const float s2 = scales[(step_offset * 3 + 2) * g.members + member];
     const unsigned long long noise_step = NOISE ? step_base[0] + step_offset : 0ull;
+    const PhiloxCellPrefix prefix =
+        philox_cell_prefix(static_cast<uint32_t>(noise_step), static_cast<uint32_t>(noise_step >> 32),
+                           1u, key0, key1);
     const float2* psi_m = psi_in + member * plane;
     const float* n_m = n_in + member * plane;
     const float* p_m = pump + member * g.pump_stride;
+    float2* out_psi_m = psi_out + member * plane + col0;
+    float* out_n_m = n_out + member * plane + col0;
     int row_first = (ya - 4) % ny;
     if (row_first < 0) row_first += ny;
 
-    // Issue the bulk copies of iteration `i` (row ya - 4 + i) into its ring slot.
+    // Issue the bulk copies of iteration `i` (row ya - 4 + i) into ring slot i % kRing.
     auto issue = [&](int i) {
-      const unsigned slot = (it + i) & (kRing - 1);
+      const int slot = i & (kRing - 1);
       int row = row_first + i;
       while (row >= ny) row -= ny;
       const uint32_t bar = smem_u32(&mbar[slot]);
-      mbar_arrive_expect_tx(bar, row_bytes);
-      bulk_g2s(smem_u32(ring_psi + slot * nx), psi_m + static_cast<long long>(row) * nx, nx * 8u, bar);
-      bulk_g2s(smem_u32(ring_n + slot * nx), n_m + static_cast<long long>(row) * nx, nx * 4u, bar);
-      bulk_g2s(smem_u32(ring_p + slot * nx), p_m + static_cast<long long>(row) * nx, nx * 4u, bar);
+      mbar_arrive_expect_tx(bar, kRowBytes);
+      bulk_g2s(smem_u32(ring_psi + slot * NX), psi_m + static_cast<long long>(row) * NX, NX * 8u, bar);
+      bulk_g2s(smem_u32(ring_n + slot * NX), n_m + static_cast<long long>(row) * NX, NX * 4u, bar);
+      bulk_g2s(smem_u32(ring_p + slot * NX), p_m + static_cast<long long>(row) * NX, NX * 4u, bar);
     };
-    if (tid == 0) {
+    if (t == 0) {
       for (int i = 0; i < 3 && i < n_iter; ++i) issue(i);
     }
 
@@ -154,32 +160,51 @@ __global__ void __launch_bounds__(512, 1)
     int row_out = (ya - 8) % ny;
     if (row_out < 0) row_out += ny;
 
-    for (int i0 = 0; i0 < n_iter; i0 += 4) {
+    for (int i0 = 0; i0 < n_iter; i0 += kRing) {
+      const uint32_t parity = ((it + i0) / kRing) & 1u;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < kRing; ++j) {
         const int i = i0 + j;
-        const int ja = (j + 3) & 3, jb = (j + 2) & 3, jc = (j + 1) & 3, jd = j;
-        const unsigned u_i = it + i;
-        const unsigned slot0 = u_i & (kRing - 1);          // row r
-        const unsigned slot1 = (u_i - 1) & (kRing - 1);    // row r-1
-        const unsigned slot2 = (u_i - 2) & (kRing - 1);    // row r-2
-        const unsigned slot3 = (u_i - 3) & (kRing - 1);    // row r-3
-        const unsigned slot4 = (u_i - 4) & (kRing - 1);    // row r-4
-        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), (u_i / kRing) & 1u, kWaitLimit))
-          timed_out = true;
-        const float4* xin = xbuf + ((j + 1) & 1) * 3 * half;
+        if (NOISE && (j & 3) == 0) {
+          // Unit normals for the output rows of iterations i..i+3: eight independent
+          // Philox streams (four rows, two columns) under one key schedule.
+          int row = row_out;
+          uint32_t cells[8];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            cells[2 * q] = static_cast<uint32_t>(row * NX + col0);
+            cells[2 * q + 1] = cells[2 * q] + 1u;
+            row = row + 1 == ny ? 0 : row + 1;
+          }
+          Words4 w[8];
+          philox_cells_octet(cells, prefix, w);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float2 za = WignerDraw<float>::unit(w[2 * q]);
+            const float2 zb = WignerDraw<float>::unit(w[2 * q + 1]);
+            nbuf[q * HALF + t] = make_float4(za.x, za.y, zb.x, zb.y);
+          }
+        }
+        const int ja = (j + 3) & 3, jb = (j + 2) & 3, jc = (j + 1) & 3, jd = j & 3;
+        const int slot0 = j;                        // row r
+        const int slot1 = (j + kRing - 1) % kRing;  // row r-1
+        const int slot2 = (j + kRing - 2) % kRing;  // row r-2
+        const int slot3 = (j + kRing - 3) % kRing;  // row r-3
+        const int slot4 = (j + kRing - 4) % kRing;  // row r-4
+        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitLimit)) timed_out = true;
+        const float4* xin = xbuf + ((j + 1) & 1) * 3 * HALF;
 
         // Stage 1 at row r-1 from the ring: k1 = f(psi0).
-        const float2* R1 = ring_psi + slot1 * nx;
+        const float2* R1 = ring_psi + slot1 * NX;
         const float4 c4 = *reinterpret_cast<const float4*>(R1 + col0);
-        const float4 u4 = *reinterpret_cast<const float4*>(ring_psi + slot2 * nx + col0);
-        const float4 d4 = *reinterpret_cast<const float4*>(ring_psi + slot0 * nx + col0);
+        const float4 u4 = *reinterpret_cast<const float4*>(ring_psi + slot2 * NX + col0);
+        const float4 d4 = *reinterpret_cast<const float4*>(ring_psi + slot0 * NX + col0);
         const float2 lt = R1[lcol], rt = R1[rcol];
         const float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
         const float2 up0 = make_float2(u4.x, u4.y), up1 = make_float2(u4.z, u4.w);
         const float2 dn0 = make_float2(d4.x, d4.y), dn1 = make_float2(d4.z, d4.w);
-        const float2 n1v = *reinterpret_cast<const float2*>(ring_n + slot1 * nx + col0);
-        const float2 P1 = *reinterpret_cast<const float2*>(ring_p + slot1 * nx + col0);
+        const float2 n1v = *reinterpret_cast<const float2*>(ring_n + slot1 * NX + col0);
+        const float2 P1 = *reinterpret_cast<const float2*>(ring_p + slot1 * NX + col0);
         {
           float2 da, db;
           const float dna = site_rhs(c0, lt, c1, up0, dn0, n1v.x, __fmul_rn(s0, P1.x), k, da);
@@ -193,8 +218,8 @@ __global__ void __launch_bounds__(512, 1)
         {
           const float4 L = xin[lthr], Rr = xin[rthr];
           const float2 lt2 = make_float2(L.z, L.w), rt2 = make_float2(Rr.x, Rr.y);
-          const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * nx + col0);
-          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * nx + col0);
+          const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * NX + col0);
+          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * NX + col0);
           const Pair c = q1[jb];
           float2 da, db;
           const float dna = site_rhs(c.a, lt2, c.b, q1[jc].a, q1[ja].a, m1[jb].x,
@@ -208,11 +233,11 @@ __global__ void __launch_bounds__(512, 1)
         }
         // Stage 3 at row r-3: k3 = f(psi2).
         {
-          const float4 L = xin[half + lthr], Rr = xin[half + rthr];
+          const float4 L = xin[HALF + lthr], Rr = xin[HALF + rthr];
           const float2 lt3 = make_float2(L.z, L.w), rt3 = make_float2(Rr.x, Rr.y);
-          const float2 P3 = *reinterpret_cast<const float2*>(ring_p + slot3 * nx + col0);
-          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * nx + col0);
-          const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * nx + col0);
+          const float2 P3 = *reinterpret_cast<const float2*>(ring_p + slot3 * NX + col0);
+          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * NX + col0);
+          const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * NX + col0);
           const Pair c = q2[jc];
           float2 da, db;
           const float dna = site_rhs(c.a, lt3, c.b, q2[jd].a, q2[jb].a, m2[jc].x,
@@ -226,9 +251,9 @@ __global__ void __launch_bounds__(512, 1)
         }
         // Stage 4 at row r-4: k4 = f(psi3), final combine, clamp, Wigner increment.
         {
-          const float4 L = xin[2 * half + lthr], Rr = xin[2 * half + rthr];
+          const float4 L = xin[2 * HALF + lthr], Rr = xin[2 * HALF + rthr];
           const float2 lt4 = make_float2(L.z, L.w), rt4 = make_float2(Rr.x, Rr.y);
-          const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * nx + col0);
+          const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * NX + col0);
           const Pair c = q3[jd];
           float2 da, db;
           const float dna = site_rhs(c.a, lt4, c.b, q3[ja].a, q3[jc].a, m3[jd].x,
@@ -241,31 +266,32 @@ __global__ void __launch_bounds__(512, 1)
           float nb = fmaf(h6, dnb, accn[jd].y);
           na = na < 0.f ? 0.f : na;
           nb = nb < 0.f ? 0.f : nb;
-          if (i >= 8 && i - 8 < yb - ya && active) {
-            const long long o = static_cast<long long>(row_out) * nx + col0;
+          if (i >= 8 && i - 8 < h_rows) {
+            const int o = row_out * NX;
             if (NOISE) {
-              const Words4 wa = wigner_words(static_cast<uint32_t>(o), noise_step, 1u, k.seed);
-              WignerDraw<float>::apply(wa, k.noise_a + k.noise_b * na, oa.x, oa.y);
-              const Words4 wb = wigner_words(static_cast<uint32_t>(o + 1), noise_step, 1u, k.seed);
-              WignerDraw<float>::apply(wb, k.noise_a + k.noise_b * nb, ob.x, ob.y);
+              const float4 z = nbuf[(j & 3) * HALF + t];
+              const float va = fmaf(k.noise_b, na, k.noise_a);
+              const float vb = fmaf(k.noise_b, nb, k.noise_a);
+              const float sa = va > 0.f ? va * rsqrtf(va) : 0.f;
+              const float sb = vb > 0.f ? vb * rsqrtf(vb) : 0.f;
+              oa = __ffma2_rn(make_float2(sa, sa), make_float2(z.x, z.y), oa);
+              ob = __ffma2_rn(make_float2(sb, sb), make_float2(z.z, z.w), ob);
             }
-            *reinterpret_cast<float4*>(psi_out + member * plane + o) = make_float4(oa.x, oa.y, ob.x, ob.y);
-            *reinterpret_cast<float2*>(n_out + member * plane + o) = make_float2(na, nb);
+            *reinterpret_cast<float4*>(out_psi_m + o) = make_float4(oa.x, oa.y, ob.x, ob.y);
+            *reinterpret_cast<float2*>(out_n_m + o) = make_float2(na, nb);
           }
         }
         // Publish stage inputs for the horizontal neighbours.
         {
-          float4* xo = xbuf + (j & 1) * 3 * half;
-          if (active) {
-            xo[t] = make_float4(q1[ja].a.x, q1[ja].a.y, q1[ja].b.x, q1[ja].b.y);
-            xo[half + t] = make_float4(q2[jb].a.x, q2[jb].a.y, q2[jb].b.x, q2[jb].b.y);
-            xo[2 * half + t] = make_float4(q3[jc].a.x, q3[jc].a.y, q3[jc].b.x, q3[jc].b.y);
-          }
+          float4* xo = xbuf + (j & 1) * 3 * HALF;
+          xo[t] = make_float4(q1[ja].a.x, q1[ja].a.y, q1[ja].b.x, q1[ja].b.y);
+          xo[HALF + t] = make_float4(q2[jb].a.x, q2[jb].a.y, q2[jb].b.x, q2[jb].b.y);
+          xo[2 * HALF + t] = make_float4(q3[jc].a.x, q3[jc].a.y, q3[jc].b.x, q3[jc].b.y);
         }
         row_out = row_out + 1 == ny ? 0 : row_out + 1;
         __syncthreads();
         // Slot of row r+3 held row r-5, last read by stage 4 of the previous iteration.
-        if (tid == 0 && i + 3 < n_iter) issue(i + 3);
+        if (t == 0 && i + 3 < n_iter) issue(i + 3);
       }
     }
     it += n_iter;
@@ -276,31 +302,34 @@ __global__ void __launch_bounds__(512, 1)
 }  // namespace
 
 bool wide_rk4_supported(int nx, int ny) {
-  return nx >= 64 && nx <= 1024 && (nx % 64) == 0 && ny >= 4;
+  return (nx == 128 || nx == 256 || nx == 512 || nx == 1024) && ny >= 4;
 }
 
 size_t wide_rk4_smem(int nx) {
-  return static_cast<size_t>(kRing) * nx * 16 + static_cast<size_t>(6) * (nx / 2) * 16 +
+  return static_cast<size_t>(kRing) * nx * 16 + static_cast<size_t>(10) * (nx / 2) * 16 +
          kRing * sizeof(uint64_t);
 }
 
-cudaError_t configure_wide_rk4() {
-  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<true>,
+namespace {
+
+template <int NX>
+cudaError_t configure_nx() {
+  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(wide_rk4_smem(1024)));
+                                       static_cast<int>(wide_rk4_smem(NX)));
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(rk4_wide_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(wide_rk4_smem(1024)));
+  return cudaFuncSetAttribute(rk4_wide_kernel<NX, false>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(wide_rk4_smem(NX)));
 }
 
-int wide_rk4_blocks_per_sm(int nx, bool noise) {
+template <int NX>
+int blocks_nx(bool noise) {
   int blocks = 0;
-  const int threads = nx / 2;
-  cudaError_t e =
-      noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, rk4_wide_kernel<true>, threads,
-                                                            wide_rk4_smem(nx))
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, rk4_wide_kernel<false>,
-                                                            threads, wide_rk4_smem(nx));
+  cudaError_t e = noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                              &blocks, rk4_wide_kernel<NX, true>, NX / 2, wide_rk4_smem(NX))
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                              &blocks, rk4_wide_kernel<NX, false>, NX / 2, wide_rk4_smem(NX));
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -308,23 +337,64 @@ int wide_rk4_blocks_per_sm(int nx, bool noise) {
   return blocks < 1 ? 1 : blocks;
 }
 
+template <int NX>
+cudaError_t launch_nx(const float* psi_in, const float* n_in, const float* pump, float* psi_out,
+                      float* n_out, const RhsConst<float>* consts, const float* scales,
+                      const unsigned long long* step_base, int step_offset, float dt, bool noise,
+                      const WideGeom& g, int* err_flag, cudaStream_t stream) {
+  const size_t smem = wide_rk4_smem(NX);
+  if (noise) {
+    rk4_wide_kernel<NX, true><<<g.blocks, NX / 2, smem, stream>>>(
+        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
+        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  } else {
+    rk4_wide_kernel<NX, false><<<g.blocks, NX / 2, smem, stream>>>(
+        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
+        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t configure_wide_rk4() {
+  cudaError_t e = configure_nx<128>();
+  if (e == cudaSuccess) e = configure_nx<256>();
+  if (e == cudaSuccess) e = configure_nx<512>();
+  if (e == cudaSuccess) e = configure_nx<1024>();
+  return e;
+}
+
+int wide_rk4_blocks_per_sm(int nx, bool noise) {
+  switch (nx) {
+    case 128: return blocks_nx<128>(noise);
+    case 256: return blocks_nx<256>(noise);
+    case 512: return blocks_nx<512>(noise);
+    default: return blocks_nx<1024>(noise);
+  }
+}
+
 cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float* pump,
                             float* psi_out, float* n_out, const RhsConst<float>* consts,
                             const float* scales, const unsigned long long* step_base,
                             int step_offset, float dt, bool noise, const WideGeom& g,
                             int* err_flag, cudaStream_t stream) {
-  const int threads = g.nx / 2;
-  const size_t smem = wide_rk4_smem(g.nx);
-  if (noise) {
-    rk4_wide_kernel<true><<<g.blocks, threads, smem, stream>>>(
-        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
-        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
-  } else {
-    rk4_wide_kernel<false><<<g.blocks, threads, smem, stream>>>(
-        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
-        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  switch (g.nx) {
+    case 128:
+      return launch_nx<128>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                            step_offset, dt, noise, g, err_flag, stream);
+    case 256:
+      return launch_nx<256>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                            step_offset, dt, noise, g, err_flag, stream);
+    case 512:
+      return launch_nx<512>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                            step_offset, dt, noise, g, err_flag, stream);
+    case 1024:
+      return launch_nx<1024>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                             step_offset, dt, noise, g, err_flag, stream);
+    default:
+      return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace pg

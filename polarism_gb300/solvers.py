@@ -41,30 +41,21 @@ def _host(array):
     return np.asarray(array)
 
 
-class RK4CudaSolver(AbstractSolver):
-    """Fused whole-step RK4 on GB300 with in-kernel Philox Wigner noise."""
+class _GB300Solver(AbstractSolver):
+    """Shared engine management of the GB300 drop-in solvers."""
 
-    capabilities = SolverCapabilities(
-        components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
-        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
-        potential=True, kinetic_relaxation=True, dispersion=frozenset({"parabolic"}),
-        terms=False, noise=frozenset({"none", "wigner"}), adaptive=False,
-        quantitative_reservoirs=frozenset({"single", "none"}),
-        description="GB300 fused RK4 (one sm_103a kernel per step, stage-coupled reservoir, "
-                    "Philox Wigner noise in registers).")
+    name = "gb300"
     injects_noise = True
 
     def __init__(self, config, grid, model):
         super().__init__(config, grid, model)
         if getattr(model, "components", 1) != 1:
-            raise ValueError("rk4-cuda (GB300) supports scalar fields only")
+            raise ValueError(f"{self.name} (GB300) supports scalar fields only")
         if getattr(grid, "ndim", 2) != 2 or getattr(grid, "boundary", "periodic") != "periodic":
-            raise ValueError("rk4-cuda (GB300) supports two-dimensional periodic grids")
+            raise ValueError(f"{self.name} (GB300) supports two-dimensional periodic grids")
         reservoir_type = getattr(getattr(config, "reservoir", None), "reservoir_type", "single")
         if reservoir_type not in ("single", "none"):
-            raise ValueError(f"rk4-cuda (GB300) does not support reservoir_type={reservoir_type!r}")
-        if getattr(config.solver, "laplacian", "five-point") != "five-point":
-            raise ValueError("rk4-cuda (GB300) implements the five-point Laplacian")
+            raise ValueError(f"{self.name} (GB300) does not support reservoir_type={reservoir_type!r}")
         self._reservoir_type = reservoir_type
         self._grid = grid
         self._precision = getattr(config.solver, "precision", "double")
@@ -155,50 +146,163 @@ class RK4CudaSolver(AbstractSolver):
         return (isinstance(array, np.ndarray) and array.dtype == dtype
                 and array.flags.c_contiguous and array.flags.writeable)
 
+    def half_scales(self, coefficient, t0, start_step, n_steps, members):
+        """Pump coefficients at t + dt/4 and t + 3 dt/4 of each step (shape (n, 2, B))."""
+        dt = self._dt
+        out = np.empty((n_steps, 2, members), dtype=np.float64)
+        for k in range(n_steps):
+            t = t0 + (start_step + k) * dt
+            for s, time in enumerate((t + 0.25 * dt, t + 0.75 * dt)):
+                value = np.asarray(coefficient(time), dtype=np.float64).reshape(-1)
+                out[k, s] = value if value.size == members else value[0]
+        return out
+
     # ------------------------------------------------------------------ contract
     def step(self, model, state, dt):
         self.advance(model, state, 1)
         return ACCEPTED
 
-    def advance(self, model, state, n_steps: int) -> None:
-        if n_steps <= 0:
-            return
-        field = state.field
-        self.batch_physics.check(field, 1)
+    def _prepare(self, model, state):
+        """Create/refresh the device handle and upload pump, potential and noise."""
+        field = state.field if state.field_k is None or getattr(state, "_field", None) is not None \
+            else state.field_k
         members = int(field.shape[0])
         envelope, coefficient = self._pump_term(model.pump)
         potential = getattr(model, "potential", None)
         engine = self._ensure_engine(model, members, np.asarray(_host(envelope)),
                                      None if potential is None else _host(potential))
         self._upload_inputs(engine, model, envelope, potential)
-        reservoir = model.reservoir
-        res_state = reservoir.get_state()
-        device = _is_device(field)
-        if self._reservoir_type == "single":
-            res0 = res_state[0]
-            engine.set_state(field if device else np.ascontiguousarray(field, dtype=engine.complex),
+        return engine, members, coefficient
+
+    def _upload_state(self, engine, model, array):
+        res_state = model.reservoir.get_state()
+        device = _is_device(array)
+        res0 = res_state[0] if self._reservoir_type == "single" else None
+        if res0 is not None:
+            engine.set_state(array if device else np.ascontiguousarray(array, dtype=engine.complex),
                              res0 if device else np.ascontiguousarray(res0, dtype=engine.real))
         else:
-            engine.set_state(field if device else np.ascontiguousarray(field, dtype=engine.complex))
-        scales = self.stage_scales(coefficient, state.t0, state.step, n_steps, members)
-        engine.advance(state.step, n_steps, scales,
-                       use_graphs=bool(getattr(self.config.solver, "cuda_graphs", True)))
-        res_in = res_state[0] if self._reservoir_type == "single" else None
+            engine.set_state(array if device else np.ascontiguousarray(array, dtype=engine.complex))
+        return device, res0
+
+    def _download_state(self, engine, like, res_in, device):
         if device:
-            psi_out = field.new_empty(field.shape) if hasattr(field, "new_empty") else None
+            psi_out = like.new_empty(like.shape) if hasattr(like, "new_empty") else None
             res_out = res_in.new_empty(res_in.shape) if res_in is not None else None
-            psi, res = engine.get_state(psi_out, res_out)
-        elif self.inplace_host and self._writable(field, engine.complex) and (
+            return engine.get_state(psi_out, res_out)
+        if self.inplace_host and self._writable(like, engine.complex) and (
                 res_in is None or self._writable(res_in, engine.real)):
-            psi, res = engine.get_state(field, res_in)
-        else:
-            psi, res = engine.get_state()
-        state.field = psi
+            return engine.get_state(like, res_in)
+        return engine.get_state()
+
+    def _finish(self, model, state, res, n_steps):
         if self._reservoir_type == "single":
-            reservoir.set_state((res,))
+            model.reservoir.set_state((res,))
         state.step += n_steps
         state.t = state.t0 + state.step * self._dt
 
     @property
     def engine(self):
         return self._engine
+
+
+class RK4CudaSolver(_GB300Solver):
+    """Fused whole-step RK4 on GB300 with in-kernel Philox Wigner noise (``rk4-cuda``)."""
+
+    name = "rk4-cuda"
+    capabilities = SolverCapabilities(
+        components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
+        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
+        potential=True, kinetic_relaxation=True, dispersion=frozenset({"parabolic"}),
+        terms=False, noise=frozenset({"none", "wigner"}), adaptive=False,
+        quantitative_reservoirs=frozenset({"single", "none"}),
+        description="GB300 fused RK4 (one sm_103a kernel per step, stage-coupled reservoir, "
+                    "Philox Wigner noise in registers).")
+
+    def __init__(self, config, grid, model):
+        super().__init__(config, grid, model)
+        if getattr(config.solver, "laplacian", "five-point") != "five-point":
+            raise ValueError("rk4-cuda (GB300) implements the five-point Laplacian")
+
+    def advance(self, model, state, n_steps: int) -> None:
+        if n_steps <= 0:
+            return
+        field = state.field
+        self.batch_physics.check(field, 1)
+        engine, members, coefficient = self._prepare(model, state)
+        device, res_in = self._upload_state(engine, model, field)
+        scales = self.stage_scales(coefficient, state.t0, state.step, n_steps, members)
+        engine.advance(state.step, n_steps, scales,
+                       use_graphs=bool(getattr(self.config.solver, "cuda_graphs", True)))
+        psi, res = self._download_state(engine, field, res_in, device)
+        state.field = psi
+        self._finish(model, state, res, n_steps)
+
+
+class SplitStepFFTSolver(_GB300Solver):
+    """Strang splitting R/2 K/2 N K/2 R/2 on hand-written Stockham FFT passes
+    (``split-step-fft``; ``polarism/solver/split_step_fft_solver.py:24-159``).
+
+    The Wigner increment is drawn after the nonlinear step with the reservoir after the
+    first half step, as the reference does (``split_step_fft_solver.py:147-148``)."""
+
+    name = "split-step-fft"
+    ordering = 0
+    capabilities = SolverCapabilities(
+        components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
+        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
+        potential=True, kinetic_relaxation=False, dispersion=frozenset({"parabolic"}),
+        terms=False, noise=frozenset({"none", "wigner"}), adaptive=False,
+        quantitative_reservoirs=frozenset({"single", "none"}),
+        description="GB300 split-step Fourier (R/2 K/2 N K/2 R/2) with shared-memory Stockham "
+                    "FFT passes fused with the propagator and the local step; nx, ny powers "
+                    "of two.")
+
+    def __init__(self, config, grid, model):
+        super().__init__(config, grid, model)
+        for n in (grid.nx, grid.ny):
+            if n & (n - 1) or not 4 <= n <= 4096:
+                raise ValueError(f"{self.name} (GB300) needs power-of-two grid sizes in [4, 4096]")
+
+    def advance(self, model, state, n_steps: int) -> None:
+        if n_steps <= 0:
+            return
+        field = state.field  # materialises psi from a cached spectrum if needed
+        self.batch_physics.check(field, 1)
+        engine, members, coefficient = self._prepare(model, state)
+        device, res_in = self._upload_state(engine, model, field)
+        engine.set_state_kind(False)
+        scales = self.half_scales(coefficient, state.t0, state.step, n_steps, members)
+        engine.split_advance(self.ordering, state.step, n_steps, scales,
+                             use_graphs=bool(getattr(self.config.solver, "cuda_graphs", True)))
+        psi, res = self._download_state(engine, field, res_in, device)
+        state.field = psi
+        self._finish(model, state, res, n_steps)
+
+
+class SplitStepFFTCudaSolver(SplitStepFFTSolver):
+    """K(dt/2) [R(dt/2) N(dt) R(dt/2)] K(dt/2) keeping the spectrum between steps
+    (``split-step-fft-cuda``; ``polarism/solver/split_step_fft_cuda_solver.py:1144-1393``).
+
+    After ``advance`` the state holds ``field_k`` (the unnormalised 2-D spectrum) and no
+    real-space field, as the reference leaves it."""
+
+    name = "split-step-fft-cuda"
+    ordering = 1
+
+    def advance(self, model, state, n_steps: int) -> None:
+        if n_steps <= 0:
+            return
+        spectral = getattr(state, "_field", None) is None and state.field_k is not None
+        source = state.field_k if spectral else state.field
+        self.batch_physics.check(source, 1)
+        engine, members, coefficient = self._prepare(model, state)
+        device, res_in = self._upload_state(engine, model, source)
+        engine.set_state_kind(spectral)
+        scales = self.half_scales(coefficient, state.t0, state.step, n_steps, members)
+        engine.split_advance(self.ordering, state.step, n_steps, scales,
+                             use_graphs=bool(getattr(self.config.solver, "cuda_graphs", True)))
+        spec, res = self._download_state(engine, source, res_in, device)
+        state.field = None
+        state.field_k = spec
+        self._finish(model, state, res, n_steps)

@@ -225,7 +225,7 @@ def test_launch_count_and_error_status(cuda_lib):
         eng.set_geometry(8, 6)
 
 
-@pytest.mark.parametrize("nx,ny,members", [(64, 48, 3), (128, 20, 2), (1024, 8, 1)])
+@pytest.mark.parametrize("nx,ny,members", [(128, 48, 3), (256, 20, 2), (512, 12, 2), (1024, 8, 1)])
 def test_full_width_kernel_matches_oracle_and_tiled(cuda_lib, nx, ny, members):
     """The TMA full-width FP32 kernel against the oracle (1e-4) and the tiled kernel (1e-5)."""
     from polarism_gb300.engine import MemberPhysics, RK4Engine
