@@ -175,7 +175,7 @@ def _cpu_member_steps(args):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(sample_steps=8):
+def cpu_baseline(sample_steps=12):
     """Oracle port, one core, a bounded sample (sample_steps RK4 steps of one 1024^2 member)."""
     _cpu_member_steps((0, 1, "double"))  # warm-up
     elapsed = _cpu_member_steps((0, sample_steps, "double"))
@@ -354,12 +354,12 @@ def run_e2e(args, w, members, torch):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--members", type=int, default=32)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-calls", type=int, default=8)
-    ap.add_argument("--cpu-sample-steps", type=int, default=6)
+    ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
