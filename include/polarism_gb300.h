@@ -15,6 +15,8 @@
  *   pg_rk4_advance     <- polarism/solver/rk4_cuda_solver.py:3451-3642 (RK4CudaSolver.advance)
  *                         and _step_gpu :3251-3350 (tiled whole-step kernel :1296-1479)
  *   pg_philox_words    <- polarism/noise/philox.py:59-109 (philox_words kernel, test hook)
+ *   pg_ifrk_advance    <- polarism/solver/ifrk_fft_cuda_solver.py:148-241, ifrk_cuda_fused.py:851-1141
+ *   pg_ifrk_trial      <- polarism/solver/ifrk_fft_cuda_solver.py:243-311 (adaptive DP5 trial)
  *   pg_set_noise       <- polarism/noise/stochastic.py:15-37 (NoiseApplier member arrays)
  *   pg_split_advance   <- polarism/solver/split_step_fft_solver.py:97-159 (ordering 0) and
  *                         polarism/solver/split_step_fft_cuda_solver.py:1144-1325 (ordering 1)
@@ -124,6 +126,21 @@ int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t
 /* Whether the state buffer holds psi(x, y) (0) or its unnormalised spectrum (1). */
 int pg_set_state_kind(pg_solver* s, int32_t spectral);
 int pg_get_state_kind(pg_solver* s, int32_t* spectral);
+
+/* Lawson integrating-factor RK steps (nx, ny powers of two up to 4096; psi in real space
+ * before and after).  tableau 0 = classic RK4, 1 = Dormand-Prince 5(4).  Replaces the fixed-step
+ * path of polarism/solver/ifrk_fft_cuda_solver.py:148-241 and polarism/solver/ifrk_cuda_fused.py:
+ * 851-1141.  stage_scales holds stages * members pump coefficients per step,
+ * [step][stage (t + c_i dt)][member]; the Wigner increment follows each step (counter step =
+ * start_step + k, post-step clamped n_R). */
+int pg_ifrk_advance(pg_solver* s, int32_t tableau, int64_t start_step, int32_t n_steps,
+                    const double* stage_scales);
+/* One adaptive Dormand-Prince trial of size h (tableau must be 1): computes the embedded error
+ * norm of polarism/solver/ifrk_fft_cuda_solver.py:243-293 (accumulated in FP64) into err_out
+ * and commits the step when err <= 1 (accepted = 1); otherwise the state is unchanged.
+ * stage_scales holds 7 * members coefficients [stage (t + c_i h)][member]. */
+int pg_ifrk_trial(pg_solver* s, int32_t tableau, double h, const double* stage_scales, double rtol,
+                  double atol, double* err_out, int32_t* accepted);
 
 /* Choose the RK4 kernel: 0 automatic, 1 the tiled streaming kernel (any size, FP32/FP64,
  * potential and relaxation terms), 2 the full-width FP32 kernel (nx in {128, 256, 512, 1024},

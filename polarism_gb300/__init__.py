@@ -15,6 +15,8 @@ SOLVER_NAMES = {
     "rk4-cuda": "RK4CudaSolver",
     "split-step-fft": "SplitStepFFTSolver",
     "split-step-fft-cuda": "SplitStepFFTCudaSolver",
+    "ifrk-fft-cuda": "IFRKFFTCudaSolver",
+    "ifrk4-fft-cuda": "IFRK4FFTCudaSolver",
 }
 
 

@@ -61,6 +61,8 @@ SIGNATURES = {
     "pg_split_advance": (C.c_int, [_vp, _i32, _i64, _i32, _vp, C.c_int]),
     "pg_set_state_kind": (C.c_int, [_vp, _i32]),
     "pg_get_state_kind": (C.c_int, [_vp, C.POINTER(_i32)]),
+    "pg_ifrk_advance": (C.c_int, [_vp, _i32, _i64, _i32, _vp]),
+    "pg_ifrk_trial": (C.c_int, [_vp, _i32, _f64, _vp, _f64, _f64, C.POINTER(_f64), C.POINTER(_i32)]),
     "pg_rk4_set_kernel": (C.c_int, [_vp, _i32]),
     "pg_rk4_get_kernel": (C.c_int, [_vp, C.POINTER(_i32)]),
     "pg_last_launch_count": (_i64, [_vp]),

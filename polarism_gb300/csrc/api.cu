@@ -244,6 +244,7 @@ void release(pg_solver* s) {
   if (!s) return;
   free_graphs(s);
   pg::split_release(s);
+  pg::ifrk_release(s);
   for (auto& slot : s->staging) {
     if (slot.host) cudaFreeHost(slot.host);
     if (slot.done) cudaEventDestroy(slot.done);
@@ -398,6 +399,7 @@ int pg_set_state(pg_solver* s, const void* psi, const void* res, int on_device) 
   PG_CHECK(s->cfg.reservoir == PG_RES_NONE || res, PG_ERR_INVALID,
            "pg_set_state: reservoir array required");
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  pg::ifrk_invalidate(s);
   PG_CUDA(cudaMemcpyAsync(s->psi[s->cur], psi, static_cast<size_t>(s->sites) * 2 * s->real_size,
                           kind, s->stream));
   if (s->cfg.reservoir != PG_RES_NONE)
@@ -527,6 +529,7 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
   PG_CHECK(!s->spectral, PG_ERR_INVALID,
            "pg_rk4_advance: the state holds a spectrum; set real-space psi first");
   s->last_launches = 0;
+  pg::ifrk_invalidate(s);
   const int m = s->cfg.members;
   int done = 0;
   while (done < n_steps) {

@@ -314,6 +314,8 @@ int split_advance_t(pg_solver* s, int ordering, int64_t start_step, int n_steps,
 
 }  // namespace
 
+int split_ensure(pg_solver* s) { return ensure_split(s); }
+
 int split_release(pg_solver* s) {
   for (auto& kv : s->split_graphs) cudaGraphExecDestroy(kv.second);
   s->split_graphs.clear();
@@ -344,6 +346,7 @@ int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t
            "pg_split_advance: ordering must be 0 (R/2 K/2 N K/2 R/2) or 1 (K/2 [R/2 N R/2] K/2)");
   PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_split_advance: negative step count");
   if (n_steps == 0) return PG_OK;
+  pg::ifrk_invalidate(s);
   int rc = pg::ensure_split(s);
   if (rc != PG_OK) return rc;
   return s->cfg.precision == PG_DOUBLE

@@ -1,0 +1,58 @@
+// Internal declarations of the Lawson IFRK passes.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "split_internal.h"
+
+namespace pg {
+
+constexpr int kIfrkMaxTerms = 8;   // psi0_hat plus up to 7 stage spectra
+constexpr int kIfrkMaxStages = 7;  // dp5
+
+// Row pass: [F_x of `in` (+ store to `save`)] -> out_hat = sum_t coef_t E_t src_t ->
+// [F_x^-1] -> out.  A source pointer equal to nullptr selects the freshly transformed row.
+struct IfrkRowArgs {
+  int nx, ny, log2nx, rows, log2rows, threads, members;
+  int forward;                 // transform `in` along x first
+  int inverse;                 // F_x^-1 before writing `out`
+  int terms;
+  const void* src[kIfrkMaxTerms];   // full spectra (member-major), or nullptr = this row
+  double coef[kIfrkMaxTerms];       // h a_ij (1 for psi0_hat)
+  int table[kIfrkMaxTerms];         // index of the separable factor table (nx + ny complex)
+  long long member_stride;          // complex values per member of a spectrum
+};
+
+// Column pass of one stage: F_y^-1 -> psi_i; n_i = n0 + sum coef_j dn_j; rhs_i; dn_i -> F_y.
+struct IfrkColArgs {
+  int nx, ny, log2ny, cols, log2cols, threads, members;
+  int mode;                    // 0 stage RHS, 1 step end, 2 error norm, 3 forward only
+  int inverse, forward;
+  int reservoir;               // single reservoir present
+  int potential;               // 0 none, 1 real, 2 complex
+  int noise;                   // Wigner increment at the step end (mode 1)
+  int terms;
+  const void* dn[kIfrkMaxStages];   // stage reservoir derivatives
+  double coef[kIfrkMaxStages];      // h a_ij (stage) or h b_j (step end) or h (b_j - bhat_j)
+  long long pump_stride, pot_stride;
+  int scale_index;             // pump coefficient index into `scales` ([k][member])
+  int step_offset;
+  double rtol, atol;
+};
+
+template <typename T>
+cudaError_t launch_ifrk_row(const T* in, T* save, T* out, const T* tables, const IfrkRowArgs& a,
+                            const T* twiddle, cudaStream_t stream);
+
+// Column pass.  psi: in/out panel array; n0/n_out/dn_out: reservoir arrays; start/extra:
+// mode-dependent (step start psi for the error norm; new psi output of the step end).
+template <typename T>
+cudaError_t launch_ifrk_col(T* psi, const T* n0, T* dn_out, T* n_out, const T* psi_start,
+                            const T* psi_new, const T* pump, const T* potential, const T* twiddle,
+                            const SplitConst<T>* consts, const T* scales,
+                            const unsigned long long* step_base, double* partials,
+                            const IfrkColArgs& a, cudaStream_t stream);
+
+template <typename T>
+cudaError_t configure_ifrk_kernels(size_t max_smem);
+
+}  // namespace pg

@@ -21,130 +21,10 @@
 #include "philox.cuh"
 #include "pg_internal.h"
 #include "split_internal.h"
+#include "fft.cuh"
 
 namespace pg {
 namespace {
-
-template <typename T>
-struct C2T;
-template <>
-struct C2T<float> {
-  using type = float2;
-};
-template <>
-struct C2T<double> {
-  using type = double2;
-};
-
-template <typename C2>
-__device__ __forceinline__ C2 cmul(C2 a, C2 b) {
-  return C2{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
-}
-template <typename C2>
-__device__ __forceinline__ C2 cmulc(C2 a, C2 b) {  // a * conj(b)
-  return C2{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
-}
-
-// Complex values a thread stages per pass (keeps the 1024-thread blocks within 64 registers).
-template <typename T>
-struct MaxVals {
-  static constexpr int value = sizeof(T) == 4 ? 16 : 8;
-};
-
-// One in-place radix-R Stockham pass over C sequences of length N (all powers of two).
-// Element (i, c) of the shared buffer sits at buf[i * si + c * sc].  COLS selects which
-// index varies fastest across threads (c for column panels, i within a row) so shared
-// memory accesses stay contiguous.  s = stride (product of the radices already done),
-// m = N / (R s).  Requires N * C <= MaxVals<T>::value * blockDim.x.
-template <typename T, bool INVERSE, bool COLS, int R>
-__device__ __forceinline__ void stockham_pass(typename C2T<T>::type* buf,
-                                              const typename C2T<T>::type* tw, int log2n,
-                                              int log2c, int si, int sc, int log2s, int m) {
-  using C2 = typename C2T<T>::type;
-  constexpr int MAXB = MaxVals<T>::value / R;
-  constexpr int LOG2R = R == 4 ? 2 : 1;
-  const int log2per = log2n - LOG2R;  // butterflies per sequence = N / R
-  const int nb = 1 << (log2per + log2c);
-  const int s = 1 << log2s;
-  C2 v[MAXB][R];
-  int base_in[MAXB], cidx[MAXB];
-#pragma unroll
-  for (int kb = 0; kb < MAXB; ++kb) {
-    const int b = threadIdx.x + kb * blockDim.x;
-    if (b < nb) {
-      int c, rest;
-      if (COLS) {
-        c = b & ((1 << log2c) - 1);
-        rest = b >> log2c;
-      } else {
-        c = b >> log2per;
-        rest = b & ((1 << log2per) - 1);
-      }
-      const int q = rest & (s - 1);
-      const int p = rest >> log2s;
-      base_in[kb] = q + s * p;
-      cidx[kb] = c;
-#pragma unroll
-      for (int t = 0; t < R; ++t) v[kb][t] = buf[(base_in[kb] + s * m * t) * si + c * sc];
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int kb = 0; kb < MAXB; ++kb) {
-    const int b = threadIdx.x + kb * blockDim.x;
-    if (b < nb) {
-      const int c = cidx[kb];
-      const int q = base_in[kb] & (s - 1);
-      const int p = base_in[kb] >> log2s;
-      C2 y[R];
-      if (R == 2) {
-        const C2 a = v[kb][0], bb = v[kb][1 % R];
-        y[0] = C2{a.x + bb.x, a.y + bb.y};
-        y[1 % R] = C2{a.x - bb.x, a.y - bb.y};
-      } else {
-        const C2 a0 = v[kb][0], a1 = v[kb][1 % R], a2 = v[kb][2 % R], a3 = v[kb][3 % R];
-        const C2 t0{a0.x + a2.x, a0.y + a2.y}, t1{a0.x - a2.x, a0.y - a2.y};
-        const C2 t2{a1.x + a3.x, a1.y + a3.y};
-        const C2 d{a1.x - a3.x, a1.y - a3.y};
-        // forward: t3 = -i d; inverse: t3 = +i d
-        const C2 t3 = INVERSE ? C2{-d.y, d.x} : C2{d.y, -d.x};
-        y[0] = C2{t0.x + t2.x, t0.y + t2.y};
-        y[1 % R] = C2{t1.x + t3.x, t1.y + t3.y};
-        y[2 % R] = C2{t0.x - t2.x, t0.y - t2.y};
-        y[3 % R] = C2{t1.x - t3.x, t1.y - t3.y};
-      }
-      const int out = q + s * R * p;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        C2 val = y[r];
-        if (r > 0) {
-          const C2 w = tw[p * r * s];
-          val = INVERSE ? cmulc(val, w) : cmul(val, w);
-        }
-        buf[(out + s * r) * si + c * sc] = val;
-      }
-    }
-  }
-  __syncthreads();
-}
-
-// In-place Stockham FFT (radix 4, with one radix-2 pass first when log2 N is odd).
-template <typename T, bool INVERSE, bool COLS>
-__device__ void smem_fft(typename C2T<T>::type* buf, const typename C2T<T>::type* tw, int log2n,
-                         int log2c, int si, int sc) {
-  int log2s = 0;
-  int log2m = log2n;
-  if (log2n & 1) {
-    stockham_pass<T, INVERSE, COLS, 2>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 1));
-    log2s += 1;
-    log2m -= 1;
-  }
-  while (log2m > 0) {
-    stockham_pass<T, INVERSE, COLS, 4>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 2));
-    log2s += 2;
-    log2m -= 2;
-  }
-}
 
 // ------------------------------------------------------------------ row pass
 template <typename T>

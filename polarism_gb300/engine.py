@@ -70,6 +70,15 @@ class MemberPhysics:
         return _lib.PgPhysics(**self.__dict__)
 
 
+_TABLEAUS = {"rk4": (0, 4), "dp5": (1, 7)}
+
+# Stage nodes c_i of the tableaus (for the pump coefficients at t + c_i h).
+TABLEAU_NODES = {
+    "rk4": (0.0, 0.5, 0.5, 1.0),
+    "dp5": (0.0, 1 / 5, 3 / 10, 4 / 5, 8 / 9, 1.0, 1.0),
+}
+
+
 class RK4Engine:
     """One device solver handle: ``members`` same-shape fields stepped on the GPU by the
     fused RK4 kernels or the split-step Fourier passes."""
@@ -212,6 +221,26 @@ class RK4Engine:
         _lib.check(self.lib.pg_split_advance(self.handle, int(ordering), int(start_step),
                                              int(n_steps), scales.ctypes.data,
                                              int(bool(use_graphs))), "pg_split_advance")
+
+    def ifrk_advance(self, tableau, start_step, n_steps, stage_scales):
+        """Fixed-step Lawson IFRK steps; tableau "rk4" or "dp5"; ``stage_scales`` is
+        (n_steps, stages, members): pump coefficients at t + c_i dt."""
+        tab, stages = _TABLEAUS[tableau]
+        scales = np.ascontiguousarray(np.broadcast_to(
+            np.asarray(stage_scales, dtype=np.float64), (int(n_steps), stages, self.members)))
+        _lib.check(self.lib.pg_ifrk_advance(self.handle, tab, int(start_step), int(n_steps),
+                                            scales.ctypes.data), "pg_ifrk_advance")
+
+    def ifrk_trial(self, h, stage_scales, rtol, atol):
+        """One adaptive Dormand-Prince trial; returns (error, accepted).  Accepted trials
+        become the state."""
+        scales = np.ascontiguousarray(np.broadcast_to(
+            np.asarray(stage_scales, dtype=np.float64), (7, self.members)))
+        err = C.c_double()
+        acc = C.c_int32()
+        _lib.check(self.lib.pg_ifrk_trial(self.handle, 1, float(h), scales.ctypes.data, float(rtol),
+                                          float(atol), C.byref(err), C.byref(acc)), "pg_ifrk_trial")
+        return err.value, bool(acc.value)
 
     def set_state_kind(self, spectral: bool):
         _lib.check(self.lib.pg_set_state_kind(self.handle, int(bool(spectral))), "pg_set_state_kind")

@@ -306,3 +306,118 @@ class SplitStepFFTCudaSolver(SplitStepFFTSolver):
         state.field = None
         state.field_k = spec
         self._finish(model, state, res, n_steps)
+
+
+class IFRKFFTCudaSolver(_GB300Solver):
+    """Lawson interaction-picture RK on the Stockham FFT passes (``ifrk-fft-cuda``;
+    ``polarism/solver/ifrk_fft_cuda_solver.py:23-329``), tableaus ``rk4`` and ``dp5``.
+
+    Fixed steps run the fused stage passes with the Wigner increment after each step.
+    With ``solver.adaptive`` the Dormand-Prince trials run on the device (FP64 error
+    norm) and the PI controller of ``polarism/solver/step_controller.py`` runs on the host
+    while the state stays in device memory for the whole ``advance`` call."""
+
+    name = "ifrk-fft-cuda"
+    tableau_name = None
+    capabilities = SolverCapabilities(
+        components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
+        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
+        potential=True, kinetic_relaxation=False, dispersion=frozenset({"parabolic"}),
+        terms=False, noise=frozenset({"none", "wigner"}), adaptive=True,
+        quantitative_reservoirs=frozenset({"single", "none"}),
+        description="GB300 Lawson IFRK (rk4, dp5) with fused Stockham stage passes, FP64 "
+                    "embedded error norm; nx, ny powers of two.")
+
+    def __init__(self, config, grid, model):
+        super().__init__(config, grid, model)
+        self.tableau = self.tableau_name or getattr(config.solver, "tableau", "rk4")
+        if self.tableau not in ("rk4", "dp5"):
+            raise ValueError(f"{self.name} (GB300) implements the rk4 and dp5 tableaus")
+        for n in (grid.nx, grid.ny):
+            if n & (n - 1) or not 4 <= n <= 4096:
+                raise ValueError(f"{self.name} (GB300) needs power-of-two grid sizes in [4, 4096]")
+        if MemberPhysics.from_object(self.batch_physics, 0).kinetic_relaxation_eta != 0.0:
+            raise ValueError(f"{self.name} (GB300) does not evaluate kinetic_relaxation_eta")
+        self.adaptive = bool(getattr(config.solver, "adaptive", False))
+        if self.adaptive and self.tableau != "dp5":
+            raise ValueError("solver.adaptive requires the embedded dp5 tableau")
+        if self.adaptive and getattr(model, "noise", None) is not None and \
+                getattr(model.noise, "active", True):
+            raise ValueError("solver.adaptive requires stochastic noise off")
+
+    def _stage_scales(self, coefficient, times, members):
+        out = np.empty((len(times), members), dtype=np.float64)
+        for i, time in enumerate(times):
+            value = np.asarray(coefficient(time), dtype=np.float64).reshape(-1)
+            out[i] = value if value.size == members else value[0]
+        return out
+
+    def advance(self, model, state, n_steps: int) -> None:
+        from polarism_gb300.engine import TABLEAU_NODES
+
+        if n_steps <= 0:
+            return
+        field = state.field
+        self.batch_physics.check(field, 1)
+        engine, members, coefficient = self._prepare(model, state)
+        device, res_in = self._upload_state(engine, model, field)
+        engine.set_state_kind(False)
+        nodes = TABLEAU_NODES[self.tableau]
+        if not self.adaptive:
+            dt = self._dt
+            scales = np.stack([
+                self._stage_scales(coefficient,
+                                   [state.t0 + (state.step + k) * dt + c * dt for c in nodes], members)
+                for k in range(n_steps)])
+            engine.ifrk_advance(self.tableau, state.step, n_steps, scales)
+        else:
+            controller = getattr(self, "step_controller", None)
+            if controller is None:
+                from polarism_gb300.step_control import StepController
+
+                controller = StepController(self._dt, getattr(self.config.solver, "dt_max", None))
+                self.step_controller = controller
+            rtol = float(self.config.solver.rtol)
+            atol = float(self.config.solver.atol)
+            target = state.t0 + (state.step + n_steps) * self._dt
+            t = state.t
+            while t < target:
+                h, clamped, proposal = controller.propose(t, target)
+                scales = self._stage_scales(coefficient, [t + c * h for c in nodes], members)
+                err, accepted = engine.ifrk_trial(h, scales, rtol, atol)
+                if accepted:
+                    t = target if clamped else t + h
+                controller.update(h, clamped, proposal, accepted, err)
+        psi, res = self._download_state(engine, field, res_in, device)
+        state.field = psi
+        self._finish(model, state, res, n_steps)
+
+    def step(self, model, state, dt):
+        if not self.adaptive:
+            self.advance(model, state, 1)
+            return ACCEPTED
+        from polarism_gb300.engine import TABLEAU_NODES
+
+        field = state.field
+        engine, members, coefficient = self._prepare(model, state)
+        device, res_in = self._upload_state(engine, model, field)
+        engine.set_state_kind(False)
+        scales = self._stage_scales(coefficient, [state.t + c * dt for c in TABLEAU_NODES["dp5"]],
+                                    members)
+        err, accepted = engine.ifrk_trial(dt, scales, float(self.config.solver.rtol),
+                                          float(self.config.solver.atol))
+        if accepted:
+            psi, res = self._download_state(engine, field, res_in, device)
+            state.field = psi
+            if self._reservoir_type == "single":
+                model.reservoir.set_state((res,))
+            state.t += dt
+        return StepReport(accepted, err, None)
+
+
+class IFRK4FFTCudaSolver(IFRKFFTCudaSolver):
+    """``ifrk4-fft-cuda``: the RK4 tableau whatever ``solver.tableau`` says."""
+
+    name = "ifrk4-fft-cuda"
+    tableau_name = "rk4"
+    capabilities = SolverCapabilities(**{**IFRKFFTCudaSolver.capabilities.__dict__, "adaptive": False})

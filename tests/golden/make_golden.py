@@ -262,14 +262,14 @@ def ifrk4_cases(out, root):
     np.savez_compressed(out / "ifrk4.npz", **result)
 
 
-def dp5_case(out):
+def dp5_case(out, name="dp5", nx=12, ny=8):
     """A nonuniform adaptive DP5 run of the reference's generic Lawson path."""
     from polarism.config.simulation_parameters import ComputeEngineParameters
     from polarism.simulation_controller import SimulationController
     from tests.unit.conftest import small_config
 
     cfg = small_config(
-        grid__nx=12, grid__ny=8, grid__lx=12.0, grid__ly=8.0,
+        grid__nx=nx, grid__ny=ny, grid__lx=float(nx), grid__ly=float(ny),
         solver__method="ifrk-fft-cuda", solver__tableau="dp5", solver__adaptive=True,
         solver__dt=0.05, solver__total_time=0.4, solver__rtol=1e-6, solver__atol=1e-8,
         reservoir__reservoir_type="single", noise__enabled=True, laser__P0=0.3,
@@ -283,7 +283,7 @@ def dp5_case(out):
     ctl.solver.advance(ctl.model, ctl.state, 8)
     stats = ctl.solver.step_controller.statistics
     np.savez_compressed(
-        out / "dp5.npz", psi0=psi0, res0=res0, envelope=np.asarray(ctl.lasers[0]._spatial_envelope),
+        out / f"{name}.npz", psi0=psi0, res0=res0, envelope=np.asarray(ctl.lasers[0]._spatial_envelope),
         p0=np.float64(cfg.laser.P0), dt=np.float64(cfg.solver.dt), ticks=np.int64(8),
         rtol=np.float64(cfg.solver.rtol), atol=np.float64(cfg.solver.atol),
         dx=np.float64(ctl.grid.dx), dy=np.float64(ctl.grid.dy),
@@ -308,6 +308,7 @@ def main(root):
     kouter_case(HERE)
     ifrk4_cases(HERE, root)
     dp5_case(HERE)
+    dp5_case(HERE, "dp5_p2", nx=16, ny=8)
     print("golden fixtures written to", HERE)
 
 
