@@ -142,6 +142,28 @@ int pg_ifrk_advance(pg_solver* s, int32_t tableau, int64_t start_step, int32_t n
 int pg_ifrk_trial(pg_solver* s, int32_t tableau, double h, const double* stage_scales, double rtol,
                   double atol, double* err_out, int32_t* accepted);
 
+/* FP64 observables of the current (real-space) state.
+ * pg_accumulate adds one sample: kinds bit 1 = per-site sum |psi|^2 and sum |psi|^4
+ * (polarism/results/accumulators.py:134-172, G2Accumulator), bit 2 = per-mode sum |FFT2 psi|^2
+ * (accumulators.py:95-131, MomentumDistribution; nx, ny powers of two).
+ * pg_accumulator_sums copies B*nx*ny sums of kind 0 (rho), 1 (rho^2) or 2 (|psi_k|^2) to the host
+ * with their sample count; pg_accumulator_reset clears them. */
+int pg_accumulate(pg_solver* s, int32_t kinds);
+int pg_accumulator_sums(pg_solver* s, int32_t kind, double* out, int64_t* samples);
+int pg_accumulator_reset(pg_solver* s);
+/* Per-member norm sum |psi|^2 dx dy in FP64 (polarism/simulation_controller.py:92-103). */
+int pg_norms(pg_solver* s, double* out);
+/* Steady-state comparison against the previous call (polarism/simulation_controller.py:710-734):
+ * per member ||rho - rho_prev|| / ||rho_prev||, |N - N_prev| / N_prev (infinite on the first call)
+ * and the norms N; the current density becomes the reference for the next call. */
+int pg_steady_check(pg_solver* s, double* rel_density, double* rel_norm, double* norms);
+/* FP64 norms (sum |psi|^2 * cell per member) of caller-owned device fields psi
+ * (members * sites_per_member complex values of the given precision) into the device array
+ * norms_out, on `stream` (a cudaStream_t, NULL for the default stream); per-block partial sums
+ * live in scratch memory allocated for the call. */
+int pg_field_norms(const void* psi, int32_t precision, int32_t members, int64_t sites_per_member,
+                   double cell, double* norms_out, void* stream);
+
 /* Choose the RK4 kernel: 0 automatic, 1 the tiled streaming kernel (any size, FP32/FP64,
  * potential and relaxation terms), 2 the full-width FP32 kernel (nx in {128, 256, 512, 1024},
  * single reservoir, no potential).  pg_rk4_get_kernel reports the one in use (1 or 2). */

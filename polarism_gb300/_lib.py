@@ -63,6 +63,12 @@ SIGNATURES = {
     "pg_get_state_kind": (C.c_int, [_vp, C.POINTER(_i32)]),
     "pg_ifrk_advance": (C.c_int, [_vp, _i32, _i64, _i32, _vp]),
     "pg_ifrk_trial": (C.c_int, [_vp, _i32, _f64, _vp, _f64, _f64, C.POINTER(_f64), C.POINTER(_i32)]),
+    "pg_accumulate": (C.c_int, [_vp, _i32]),
+    "pg_accumulator_sums": (C.c_int, [_vp, _i32, _vp, C.POINTER(_i64)]),
+    "pg_accumulator_reset": (C.c_int, [_vp]),
+    "pg_norms": (C.c_int, [_vp, _vp]),
+    "pg_steady_check": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pg_field_norms": (C.c_int, [_vp, _i32, _i32, _i64, _f64, _vp, _vp]),
     "pg_rk4_set_kernel": (C.c_int, [_vp, _i32]),
     "pg_rk4_get_kernel": (C.c_int, [_vp, C.POINTER(_i32)]),
     "pg_last_launch_count": (_i64, [_vp]),

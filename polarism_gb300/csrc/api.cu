@@ -245,6 +245,7 @@ void release(pg_solver* s) {
   free_graphs(s);
   pg::split_release(s);
   pg::ifrk_release(s);
+  pg::accum_release(s);
   for (auto& slot : s->staging) {
     if (slot.host) cudaFreeHost(slot.host);
     if (slot.done) cudaEventDestroy(slot.done);

@@ -53,6 +53,7 @@ struct pg_solver {
   void* split_consts = nullptr;
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> split_graphs;  // (ordering, len, parity)
   void* ifrk = nullptr;       // IFRK stage buffers (created on first use)
+  void* accum = nullptr;      // FP64 observable sums (created on first use)
   long long last_launches = 0;
 };
 
@@ -62,6 +63,7 @@ int split_release(pg_solver* s);
 int split_ensure(pg_solver* s);
 void ifrk_release(pg_solver* s);
 void ifrk_invalidate(pg_solver* s);
+void accum_release(pg_solver* s);
 int split_refresh_consts(pg_solver* s);
 // Stage a chunk's per-step coefficients (per_step * members doubles per step) and the step base.
 int stage_coefficients(pg_solver* s, const double* coeffs, int len, int per_step, int64_t step);

@@ -242,6 +242,37 @@ class RK4Engine:
                                           float(atol), C.byref(err), C.byref(acc)), "pg_ifrk_trial")
         return err.value, bool(acc.value)
 
+    # -- FP64 observables ----------------------------------------------------------
+    def accumulate(self, density=True, momentum=False):
+        kinds = (1 if density else 0) | (2 if momentum else 0)
+        _lib.check(self.lib.pg_accumulate(self.handle, kinds), "pg_accumulate")
+
+    def accumulator_sums(self, kind):
+        """(sums, samples) for kind "rho", "rho2" or "k" (shape (B, 1, ny, nx), FP64)."""
+        index = {"rho": 0, "rho2": 1, "k": 2}[kind]
+        out = np.empty(self.shape, dtype=np.float64)
+        samples = C.c_int64()
+        _lib.check(self.lib.pg_accumulator_sums(self.handle, index, out.ctypes.data, C.byref(samples)),
+                   "pg_accumulator_sums")
+        return out, samples.value
+
+    def accumulator_reset(self):
+        _lib.check(self.lib.pg_accumulator_reset(self.handle), "pg_accumulator_reset")
+
+    def norms(self):
+        out = np.empty(self.members, dtype=np.float64)
+        _lib.check(self.lib.pg_norms(self.handle, out.ctypes.data), "pg_norms")
+        return out
+
+    def steady_check(self):
+        """(relative density change, relative norm change, norms) per member."""
+        rd = np.empty(self.members)
+        rn = np.empty(self.members)
+        nm = np.empty(self.members)
+        _lib.check(self.lib.pg_steady_check(self.handle, rd.ctypes.data, rn.ctypes.data,
+                                            nm.ctypes.data), "pg_steady_check")
+        return rd, rn, nm
+
     def set_state_kind(self, spectral: bool):
         _lib.check(self.lib.pg_set_state_kind(self.handle, int(bool(spectral))), "pg_set_state_kind")
 
