@@ -164,6 +164,18 @@ int pg_steady_check(pg_solver* s, double* rel_density, double* rel_norm, double*
 int pg_field_norms(const void* psi, int32_t precision, int32_t members, int64_t sites_per_member,
                    double cell, double* norms_out, void* stream);
 
+/* Allocation-free variant of pg_field_norms (no counterpart in the reference).  For callers
+ * that must not allocate device memory -- an application whose device memory is owned by another
+ * framework's pooling allocator, or a stepping loop that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree.  The per-block partial sums use a fixed 64 KiB device
+ * array (8192 doubles) that every GPU loading the library holds until the process exits; at most
+ * 8192 members per call (PG_ERR_INVALID beyond).  All calls share the array: calls whose kernels
+ * overlap on the GPU race and must be serialised by the caller.  The call is asynchronous on
+ * `stream`; the first call on each device looks up the array's address and should come before
+ * any stream capture. */
+int pg_field_norms_noalloc(const void* psi, int32_t precision, int32_t members,
+                           int64_t sites_per_member, double cell, double* norms_out, void* stream);
+
 /* Choose the RK4 kernel: 0 automatic, 1 the tiled streaming kernel (any size, FP32/FP64,
  * potential and relaxation terms), 2 the full-width FP32 kernel (nx in {128, 256, 512, 1024},
  * single reservoir, no potential).  pg_rk4_get_kernel reports the one in use (1 or 2). */

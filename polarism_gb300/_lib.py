@@ -69,6 +69,7 @@ SIGNATURES = {
     "pg_norms": (C.c_int, [_vp, _vp]),
     "pg_steady_check": (C.c_int, [_vp, _vp, _vp, _vp]),
     "pg_field_norms": (C.c_int, [_vp, _i32, _i32, _i64, _f64, _vp, _vp]),
+    "pg_field_norms_noalloc": (C.c_int, [_vp, _i32, _i32, _i64, _f64, _vp, _vp]),
     "pg_rk4_set_kernel": (C.c_int, [_vp, _i32]),
     "pg_rk4_get_kernel": (C.c_int, [_vp, C.POINTER(_i32)]),
     "pg_last_launch_count": (_i64, [_vp]),

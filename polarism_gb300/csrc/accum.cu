@@ -407,3 +407,70 @@ int pg_field_norms(const void* psi, int32_t precision, int32_t members, int64_t 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free FP64 norms.
+//
+// Some callers of this library must not allocate device memory: an application whose
+// device memory is owned by another framework's pooling allocator (a PyTorch or JAX
+// process that reserved it), or a stepping loop that cannot pay for the device-wide
+// synchronisation cudaMalloc and cudaFree imply.  pg_field_norms_noalloc serves them: the
+// per-block partial sums live in the fixed device array below instead of memory allocated
+// per call.
+//
+// The array holds kNoAllocPartials doubles (64 KiB) on every GPU that loads the library,
+// until the process exits.  All calls share it; each call overwrites the partials it uses
+// before reading them, so nothing has to start at zero, but calls whose kernels overlap on
+// the GPU (different streams or host threads) race on it and must be serialised by the
+// caller.  The first call on each device looks up the array's device address
+// (cudaGetSymbolAddress) with that device current; make that first call before any stream
+// capture.
+namespace pg {
+namespace {
+
+constexpr int kNoAllocPartials = 8192;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices] = {};
+
+}  // namespace
+}  // namespace pg
+
+extern "C" int pg_field_norms_noalloc(const void* psi, int32_t precision, int32_t members,
+                                      int64_t sites_per_member, double cell, double* norms_out,
+                                      void* stream) {
+  PG_CHECK(psi && norms_out && members >= 1 && sites_per_member >= 1, PG_ERR_INVALID,
+           "pg_field_norms_noalloc: bad argument");
+  PG_CHECK(precision == PG_SINGLE || precision == PG_DOUBLE, PG_ERR_INVALID,
+           "pg_field_norms_noalloc: bad precision");
+  PG_CHECK(members <= pg::kNoAllocPartials, PG_ERR_INVALID,
+           "pg_field_norms_noalloc: at most 8192 members fit the fixed scratch array");
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  PG_CHECK(dev >= 0 && dev < pg::kMaxDevices, PG_ERR_UNSUPPORTED,
+           "pg_field_norms_noalloc: device index beyond the supported 64");
+  if (!pg::g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, pg::g_noalloc_partials);
+    if (e != cudaSuccess) {
+      pg::set_error(std::string("pg_field_norms_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      return PG_ERR_CUDA;
+    }
+    pg::g_noalloc_ptr[dev] = static_cast<double*>(ptr);
+  }
+  // Blocks per member, bounded so members * blocks fits the array.
+  const int blocks = std::max(1, std::min(pg::reduce_blocks(sites_per_member), pg::kNoAllocPartials / members));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const cudaError_t e =
+      precision == PG_DOUBLE
+          ? pg::launch_norm<double>(psi, sites_per_member, members, cell, pg::g_noalloc_ptr[dev], blocks,
+                                    norms_out, st)
+          : pg::launch_norm<float>(psi, sites_per_member, members, cell, pg::g_noalloc_ptr[dev], blocks,
+                                   norms_out, st);
+  if (e != cudaSuccess) {
+    pg::set_error(std::string("pg_field_norms_noalloc: ") + cudaGetErrorString(e));
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
