@@ -351,6 +351,119 @@ def run_e2e(args, w, members, torch):
             "calls": calls}
 
 
+# ----------------------------------------------------------------------------- sweep leg
+SWEEP_SIZES = (128, 256, 512)
+SWEEP_DX = 100.0 / 128  # lx scaled with nx so every member has the same cell
+
+
+def sweep_members(members):
+    """Uneven-size sweep workload: sizes cycle 128^2 / 256^2 / 512^2 (a third each, the same
+    dx), P0 uniform in [0.5, 3] x threshold, sigma uniform in [8, 20] um, seeds 0..members-1
+    (parameters drawn from numpy default_rng(1234)); single reservoir, no Wigner noise (the
+    steady-state criterion needs a deterministic run)."""
+    from polarism_gb300 import host
+
+    rng = np.random.default_rng(1234)
+    p_th = PHYSICS["gamma_R"] * PHYSICS["gamma_C"] / PHYSICS["R"]
+    p0 = rng.uniform(0.5, 3.0, size=members) * p_th
+    sigma = rng.uniform(8.0, 20.0, size=members)
+    cfgs = []
+    for m in range(members):
+        c = host.Config()
+        n = SWEEP_SIZES[m % 3]
+        c.grid.nx = c.grid.ny = n
+        c.grid.lx = c.grid.ly = n * SWEEP_DX
+        c.solver.dt, c.solver.precision, c.solver.total_time = 1e-3, "single", 1000.0
+        c.noise.seed, c.noise.stochastic = m, "none"
+        c.laser.P0, c.laser.sigma_space = float(p0[m]), float(sigma[m])
+        c.stop.steady_state, c.stop.rtol, c.stop.check_every = True, 1e-6, 10.0
+        cfgs.append(c)
+    return cfgs
+
+
+def run_sweep_bench(args):
+    """Device throughput of the one-launch uneven sweep (site-updates/s over all members)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from polarism_gb300 import build as _build
+
+    _build.build()
+    from polarism_gb300.engine import MemberPhysics
+    from polarism_gb300.sweep import SweepEngine, _member_inputs, autotune_tiling, run_sweep
+
+    cfgs = sweep_members(args.members)
+    inputs = [_member_inputs(c) for c in cfgs]
+    grids = [(g.nx, g.ny, g.dx, g.dy) for g, *_ in inputs]
+    eng = SweepEngine(grids, [MemberPhysics(**PHYSICS)] * len(cfgs), 1e-3)
+    eng.set_pump([laser._spatial_envelope for _, laser, *_ in inputs])
+    psi0 = [p for _, _, p, _, _ in inputs]
+    n0 = [np.zeros((g.ny, g.nx), np.float32) for g, *_ in inputs]
+    eng.set_state(psi0, n0)
+    tune = autotune_tiling(eng, noise=False, use_cache=False, steps=32)
+    p0 = np.asarray([c.laser.P0 for c in cfgs])
+    total = args.warmup + args.steps
+    scales = np.broadcast_to(p0, (total, 3, len(cfgs))).copy()
+    eng.advance(0, args.warmup, scales[:args.warmup])
+    eng.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    eng.advance(args.warmup, args.steps, scales[args.warmup:])
+    elapsed_ms = eng.last_time_ms()
+    clocks = sampler.stop()
+    launches = eng.last_launch_count
+    sites = eng.sites
+    value = sites * args.steps / (elapsed_ms / 1e3)
+    achieved = BYTES_PER_SITE * sites / (elapsed_ms / 1e3 / args.steps) / 1e9
+    peak, peak_kind = measured_peak()
+
+    # End to end through SweepEngine with host arrays: upload, 64 steps, download.
+    chunk = 64
+    psi_h, n_h = eng.get_packed_state()
+    t0 = time.perf_counter()
+    calls = 4
+    for c in range(calls):
+        eng.set_state([eng.unpack(psi_h, m) for m in range(eng.members)],
+                      [eng.unpack(n_h, m) for m in range(eng.members)])
+        eng.advance(total + c * chunk, chunk, scales[:chunk])
+        psi_h, n_h = eng.get_packed_state()
+    e2e_s = time.perf_counter() - t0
+    line = {
+        "metric": "sweep RK4 site-updates/s (uneven sizes, one persistent launch per step)",
+        "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"uneven sweep: {len(cfgs)} members, 128^2/256^2/512^2 a third each, "
+                               "dx fixed, P0 in [0.5,3] x threshold, sigma in [8,20] um, seeds "
+                               "0..N-1, single reservoir, dt=1e-3, complex64",
+                   "members": len(cfgs), "sites": sites, "tiling": eng.tiling,
+                   "autotune_ms_per_step": tune["timings"],
+                   "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_site": BYTES_PER_SITE},
+        "e2e": {"value": sites * chunk * calls / e2e_s, "unit": "site-updates/s",
+                "h2d_bytes_per_step": sites * 12, "d2h_bytes_per_step": sites * 12,
+                "step": f"SweepEngine set_state + {chunk} steps + get_state from host arrays"},
+        "clocks": clocks,
+    }
+    eng.close()
+    if args.steady_time > 0:
+        for c in cfgs:
+            c.solver.total_time = args.steady_time
+        res = run_sweep(cfgs, autotune=True, freeze_stopped=args.freeze_stopped)
+        line["steady_state"] = {
+            "wall_s": res.wall_time, "t_end_ps": res.t, "steps": res.steps,
+            "stopped": int(np.isfinite(res.stop_times).sum()), "members": len(cfgs),
+            "stop_time_ps_median": float(np.nanmedian(res.stop_times)) if np.isfinite(res.stop_times).any() else None,
+            "freeze_stopped": bool(args.freeze_stopped), "rtol": 1e-6, "check_every_ps": 10.0}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,9 +474,19 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=8)
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["rk4", "sweep"], default="rk4",
+                    help="rk4: the 1024^2 fused-step benchmark; sweep: the uneven-size sweep")
+    ap.add_argument("--steady-time", type=float, default=0.0,
+                    help="sweep workload: also run to steady state (up to this many ps)")
+    ap.add_argument("--freeze-stopped", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.workload == "sweep":
+        if args.members == 32 and "--members" not in sys.argv:
+            args.members = 256
+        run_sweep_bench(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

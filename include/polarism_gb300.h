@@ -22,6 +22,8 @@
  *                         polarism/solver/split_step_fft_cuda_solver.py:1144-1325 (ordering 1)
  *   pg_set_pump        <- polarism/laser/pump_field.py:71-79 (separable envelope) and
  *                         rk4_cuda_solver.py:3564-3578 (per-stage pump scales)
+ *   pg_sweep_*         <- polarism/sweep.py:98-324 (Sweep.run over groups of grid sizes) with
+ *                         rk4_cuda_solver.py:1482-1536 (batched per-member constants)
  */
 #ifndef POLARISM_GB300_H
 #define POLARISM_GB300_H
@@ -194,6 +196,54 @@ int pg_philox_words(const uint32_t* counters, uint64_t key, uint32_t* out, int64
  * polarism/noise/philox.py:41-56 (normal_pair). */
 int pg_wigner_normals(const uint32_t* counters, uint64_t key, int32_t precision, void* out,
                       int64_t n);
+
+/* Uneven-size sweep.  Polarism runs each grid size of a sweep as its own batch
+ * (polarism/sweep.py:98-324: grid.* overrides are non-batchable, so members are grouped and each
+ * group runs through its own SimulationController and rk4-cuda launches, rk4_cuda_solver.py:
+ * 1482-1536 for the per-member constants).  A pg_sweep steps members of different power-of-two
+ * grids (nx in [64, 1024]) with one persistent kernel launch per RK4 step: FP32 (complex64),
+ * single reservoir, no potential, a pump envelope per member.  Member m's sites occupy
+ * [offset_m, offset_m + nx_m * ny_m) of the packed arrays (pg_sweep_offsets, members + 1
+ * entries); psi (interleaved complex64), n_R and the envelopes all use that packing. */
+typedef struct pg_sweep pg_sweep;
+typedef struct pg_sweep_grid {
+  int32_t nx, ny;
+  double dx, dy;
+} pg_sweep_grid;
+
+int pg_sweep_create(int32_t members, const pg_sweep_grid* grids, const pg_physics* physics,
+                    double dt, pg_sweep** out);
+void pg_sweep_destroy(pg_sweep* w);
+void* pg_sweep_stream(pg_sweep* w);
+int64_t pg_sweep_total_sites(pg_sweep* w);
+int pg_sweep_offsets(pg_sweep* w, int64_t* offsets);
+int pg_sweep_set_state(pg_sweep* w, const void* psi, const void* res, int on_device);
+int pg_sweep_get_state(pg_sweep* w, void* psi, void* res, int on_device);
+int pg_sweep_state_pointers(pg_sweep* w, void** psi, void** res);
+int pg_sweep_set_pump(pg_sweep* w, const void* envelope, int on_device);
+/* Wigner noise per member (NoiseApplier arrays, polarism/noise/stochastic.py:15-37) with each
+ * member's own cell volume dx*dy; seeds == NULL turns the noise off. */
+int pg_sweep_set_noise(pg_sweep* w, const uint64_t* seeds, const double* gamma,
+                       const double* scattering, const double* strength);
+/* Tile shape of the persistent launch: `lanes` columns per block (512 or 1024; a block stacks
+ * lanes / nx strips of equally wide members side by side, so every member needs
+ * lanes / 8 <= nx <= lanes) and `strip_rows` rows per work item (>= 8).  The choice changes
+ * speed only, never results.  pg_sweep_get_tiling also reports the work items and the grid. */
+int pg_sweep_set_tiling(pg_sweep* w, int32_t lanes, int32_t strip_rows);
+int pg_sweep_get_tiling(pg_sweep* w, int32_t* lanes, int32_t* strip_rows, int32_t* items,
+                        int32_t* blocks);
+/* Leave members whose entry is 0 out of the launch (their state is kept); NULL = all active. */
+int pg_sweep_set_active(pg_sweep* w, const uint8_t* active);
+/* n_steps RK4 steps (rk4_cuda_solver.py:3451-3642 semantics per member); stage_scales holds
+ * [n_steps][3][members] pump coefficients at t, t + dt/2, t + dt. */
+int pg_sweep_advance(pg_sweep* w, int64_t start_step, int32_t n_steps, const double* stage_scales,
+                     int use_graphs);
+/* Device time of the last pg_sweep_advance (CUDA events on the sweep's stream), in ms. */
+int pg_sweep_last_time_ms(pg_sweep* w, float* ms);
+int64_t pg_sweep_last_launch_count(pg_sweep* w);
+int pg_sweep_synchronize(pg_sweep* w);
+/* Per-member steady-state comparison with the previous call, as pg_steady_check. */
+int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, double* norms);
 
 #ifdef __cplusplus
 }

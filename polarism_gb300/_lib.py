@@ -37,6 +37,12 @@ class PgConfig(C.Structure):
                 ("dx", C.c_double), ("dy", C.c_double), ("dt", C.c_double)]
 
 
+class PgSweepGrid(C.Structure):
+    """Mirror of pg_sweep_grid (one sweep member's periodic grid)."""
+
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("dx", C.c_double), ("dy", C.c_double)]
+
+
 _vp = C.c_void_p
 _i32, _i64, _u64, _f64 = C.c_int32, C.c_int64, C.c_uint64, C.c_double
 
@@ -75,6 +81,26 @@ SIGNATURES = {
     "pg_last_launch_count": (_i64, [_vp]),
     "pg_philox_words": (C.c_int, [_vp, _u64, _vp, _i64]),
     "pg_wigner_normals": (C.c_int, [_vp, _u64, _i32, _vp, _i64]),
+    "pg_sweep_create": (C.c_int, [_i32, C.POINTER(PgSweepGrid), C.POINTER(PgPhysics), _f64,
+                                  C.POINTER(_vp)]),
+    "pg_sweep_destroy": (None, [_vp]),
+    "pg_sweep_stream": (_vp, [_vp]),
+    "pg_sweep_total_sites": (_i64, [_vp]),
+    "pg_sweep_offsets": (C.c_int, [_vp, _vp]),
+    "pg_sweep_set_state": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "pg_sweep_get_state": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "pg_sweep_state_pointers": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
+    "pg_sweep_set_pump": (C.c_int, [_vp, _vp, C.c_int]),
+    "pg_sweep_set_noise": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "pg_sweep_set_tiling": (C.c_int, [_vp, _i32, _i32]),
+    "pg_sweep_get_tiling": (C.c_int, [_vp, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32),
+                                      C.POINTER(_i32)]),
+    "pg_sweep_set_active": (C.c_int, [_vp, _vp]),
+    "pg_sweep_advance": (C.c_int, [_vp, _i64, _i32, _vp, C.c_int]),
+    "pg_sweep_last_time_ms": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "pg_sweep_last_launch_count": (_i64, [_vp]),
+    "pg_sweep_synchronize": (C.c_int, [_vp]),
+    "pg_sweep_steady_check": (C.c_int, [_vp, _vp, _vp, _vp]),
 }
 
 _lock = threading.Lock()

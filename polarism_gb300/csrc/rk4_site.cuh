@@ -1,0 +1,60 @@
+// FP32 site arithmetic shared by the full-width RK4 kernel and the uneven-size sweep
+// kernel: the right-hand side of polarism/model.py:89-127 with the single reservoir of
+// polarism/reservoir/single_reservoir.py:81-98 at one site, on packed FP32x2 values.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pg_internal.h"
+
+namespace pg {
+
+struct Pair {
+  float2 a, b;  // complex values of the thread's two columns
+};
+
+struct WideConst {
+  float2 nax, nay;      // (-ax, -ax), (-ay, -ay)
+  float w0, gc, gr, half_R, half_gC, R, gamma_R, noise_a, noise_b;
+  uint64_t seed;
+};
+
+__device__ __forceinline__ WideConst wide_const(const RhsConst<float>& kk) {
+  WideConst k;
+  k.nax = make_float2(-kk.ax, -kk.ax);
+  k.nay = make_float2(-kk.ay, -kk.ay);
+  k.w0 = kk.w0;
+  k.gc = kk.gc;
+  k.gr = kk.gr;
+  k.half_R = kk.half_R;
+  k.half_gC = kk.half_gC;
+  k.R = kk.R;
+  k.gamma_R = kk.gamma_R;
+  k.noise_a = kk.noise_a;
+  k.noise_b = kk.noise_b;
+  k.seed = kk.seed;
+  return k;
+}
+
+// Right-hand side at one site: c centre, (lt, rt, up, dn) neighbours.  Writes
+// d = dpsi/dt and returns dn/dt.
+__device__ __forceinline__ float site_rhs(float2 c, float2 lt, float2 rt, float2 up, float2 dn,
+                                          float n, float sP, const WideConst& k, float2& d) {
+  const float2 sx = __fadd2_rn(lt, rt);
+  const float2 sy = __fadd2_rn(up, dn);
+  const float2 nl = __ffma2_rn(k.nay, sy, __fmul2_rn(k.nax, sx));  // -a (lap without centre)
+  const float rho = fmaf(c.x, c.x, c.y * c.y);
+  const float w = fmaf(k.gr, n, fmaf(k.gc, rho, k.w0));
+  const float gl = fmaf(k.half_R, n, -k.half_gC);
+  const float2 u = __ffma2_rn(make_float2(w, w), c, nl);  // w c - a lap_neighbours
+  d.x = fmaf(gl, c.x, u.y);
+  d.y = fmaf(gl, c.y, -u.x);
+  return fmaf(-fmaf(k.R, rho, k.gamma_R), n, sP);
+}
+
+__device__ __forceinline__ float2 axpy2(float h, float2 d, float2 y) {
+  return __ffma2_rn(make_float2(h, h), d, y);
+}
+
+}  // namespace pg

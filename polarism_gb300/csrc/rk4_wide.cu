@@ -17,6 +17,7 @@
 //   fill whenever it crosses into the next member.
 #include "philox.cuh"
 #include "pg_internal.h"
+#include "rk4_site.cuh"
 #include "tma.cuh"
 #include "wide_internal.h"
 
@@ -25,36 +26,6 @@ namespace {
 
 constexpr int kRing = 8;          // rows resident: r-4..r plus three in flight
 constexpr int kWaitLimit = 100000;
-
-struct Pair {
-  float2 a, b;  // complex values of the thread's two columns
-};
-
-struct WideConst {
-  float2 nax, nay;      // (-ax, -ax), (-ay, -ay)
-  float w0, gc, gr, half_R, half_gC, R, gamma_R, noise_a, noise_b;
-  uint64_t seed;
-};
-
-// Right-hand side at one site: c centre, (lt, rt, up, dn) neighbours.  Writes
-// d = dpsi/dt and returns dn/dt.
-__device__ __forceinline__ float site_rhs(float2 c, float2 lt, float2 rt, float2 up, float2 dn,
-                                          float n, float sP, const WideConst& k, float2& d) {
-  const float2 sx = __fadd2_rn(lt, rt);
-  const float2 sy = __fadd2_rn(up, dn);
-  const float2 nl = __ffma2_rn(k.nay, sy, __fmul2_rn(k.nax, sx));  // -a (lap without centre)
-  const float rho = fmaf(c.x, c.x, c.y * c.y);
-  const float w = fmaf(k.gr, n, fmaf(k.gc, rho, k.w0));
-  const float gl = fmaf(k.half_R, n, -k.half_gC);
-  const float2 u = __ffma2_rn(make_float2(w, w), c, nl);  // w c - a lap_neighbours
-  d.x = fmaf(gl, c.x, u.y);
-  d.y = fmaf(gl, c.y, -u.x);
-  return fmaf(-fmaf(k.R, rho, k.gamma_R), n, sP);
-}
-
-__device__ __forceinline__ float2 axpy2(float h, float2 d, float2 y) {
-  return __ffma2_rn(make_float2(h, h), d, y);
-}
 
 // At least 512 resident threads per SM for every row width (128 registers a thread).
 template <int NX, bool NOISE>
@@ -107,18 +78,7 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
     const int n_iter = (h_rows + 8 + kRing - 1) & ~(kRing - 1);
 
     const RhsConst<float> kk = consts[member];
-    WideConst k;
-    k.nax = make_float2(-kk.ax, -kk.ax);
-    k.nay = make_float2(-kk.ay, -kk.ay);
-    k.w0 = kk.w0;
-    k.gc = kk.gc;
-    k.gr = kk.gr;
-    k.half_R = kk.half_R;
-    k.half_gC = kk.half_gC;
-    k.R = kk.R;
-    k.gamma_R = kk.gamma_R;
-    k.noise_a = kk.noise_a;
-    k.noise_b = kk.noise_b;
+    const WideConst k = wide_const(kk);
     const uint32_t key0 = static_cast<uint32_t>(kk.seed), key1 = static_cast<uint32_t>(kk.seed >> 32);
     const float s0 = scales[(step_offset * 3 + 0) * g.members + member];
     const float s1 = scales[(step_offset * 3 + 1) * g.members + member];
