@@ -281,19 +281,69 @@ def _ifft(x):
     return np.fft.ifft2(x, axes=(-2, -1))
 
 
+def spinor_exponential(kx, ky, p, tau):
+    """exp(-i H tau / hbar) of the circular-basis spinor Hamiltonian on the FFT grid,
+    H = [[E + Z/2, beta (kx - i ky)^2], [beta (kx + i ky)^2, E - Z/2]], E = hbar^2 k^2 / 2m
+    (``polarism/dispersion.py:34-63``), from the identity
+    exp(-i t (e I + B)) = exp(-i e t) (cos(w t) I - i sin(w t) / w B) for traceless B with
+    B^2 = w^2 I (``polarism/dispersion.py:66-83``).  Returns the (2, 2, ny, nx) matrix."""
+    hbar, m = _get(p, "hbar"), _get(p, "m_eff")
+    energy = hbar ** 2 * (kx * kx + ky * ky) / (2.0 * m)
+    z = _get(p, "zeeman") / 2.0
+    upper = _get(p, "te_tm") * (kx - 1j * ky) ** 2
+    lower = np.conj(upper)
+    omega = np.sqrt(z * z + (upper * lower).real)
+    t = tau / hbar
+    phase = np.exp(-1j * energy * t)
+    cos = np.cos(omega * t)
+    sin_over = t * np.sinc(omega * t / np.pi)
+    return np.stack((np.stack((phase * (cos - 1j * sin_over * z), -1j * phase * sin_over * upper)),
+                     np.stack((-1j * phase * sin_over * lower, phase * (cos + 1j * sin_over * z)))))
+
+
+def _apply2(matrix, field):
+    return np.stack((matrix[0, 0] * field[:, 0] + matrix[0, 1] * field[:, 1],
+                     matrix[1, 0] * field[:, 0] + matrix[1, 1] * field[:, 1]), axis=1)
+
+
 def ifrk_step(state: IFRKState, h, tableau, pump_at, potential, p, k_squared, dx, dy,
-              kind="single", adaptive=False, rtol=1e-6, atol=1e-8):
+              kind="single", adaptive=False, rtol=1e-6, atol=1e-8, spinor=None):
     """One Lawson step of size ``h``.
 
     Returns the embedded error for adaptive steps (and accepts the step only if
     it is <= 1), otherwise ``None``.
+
+    ``spinor`` (a dict with ``kx``, ``ky`` -- the FFT wavenumber grids -- and ``weights``,
+    the per-member pump weights ``(B, 2)`` used when the reservoir has one field per
+    component) switches to the two-component field of ``ifrk_fft_cuda_solver.py:96-142``:
+    the matrix Lawson factor, the cross-spin term alpha_2 |psi_-+|^2 and per-component
+    (or shared, summed-density) reservoirs (``ifrk_fft_cuda_solver.py:118-126``).
     """
     A, b, c = tableau["A"], tableau["b"], tableau["c"]
     hbar, m = _get(p, "hbar"), _get(p, "m_eff")
     rate = -hbar / (2.0 * m)
+    spin_cache = {}
 
     def phase(fraction):
+        if spinor is not None:
+            key = float(fraction)
+            if key not in spin_cache:
+                spin_cache[key] = spinor_exponential(spinor["kx"], spinor["ky"], p, h * key)
+            return spin_cache[key]
         return np.exp(1j * rate * (h * float(fraction)) * k_squared)
+
+    def lin(fraction, field):
+        return _apply2(phase(fraction), field) if spinor is not None else phase(fraction) * field
+
+    def res_derivs(res_i, rho, pump):
+        if spinor is None:
+            return reservoir_derivatives(kind, res_i, rho, pump, p, dx, dy)
+        if kind == "none":
+            return ()
+        if res_i[0].shape[1] == 2:
+            weights = np.asarray(spinor["weights"], dtype=np.float64).reshape(-1, 2, 1, 1)
+            return reservoir_derivatives(kind, res_i, rho, pump * weights, p, dx, dy)
+        return reservoir_derivatives(kind, res_i, rho.sum(axis=1, keepdims=True), pump, p, dx, dy)
 
     psi0 = state.psi
     psi0_k = state.psi_k if state.psi_k is not None else _fft(psi0)
@@ -306,16 +356,18 @@ def ifrk_step(state: IFRKState, h, tableau, pump_at, potential, p, k_squared, dx
         if i == 0 and psi0 is not None:
             psi_i, psi_i_k = psi0, psi0_k
         else:
-            psi_i_k = phase(ci) * psi0_k
+            psi_i_k = lin(ci, psi0_k)
             for j in range(i):
                 if A[i][j]:
-                    psi_i_k = psi_i_k + (h * float(A[i][j])) * phase(ci - c[j]) * f[j]
+                    psi_i_k = psi_i_k + (h * float(A[i][j])) * lin(ci - c[j], f[j])
             psi_i = _ifft(psi_i_k)
         res_i = tuple(r0 + sum((h * float(A[i][j])) * derivs[j][q] for j in range(i) if A[i][j])
                       for q, r0 in enumerate(res0))
         rho = psi_i.real * psi_i.real + psi_i.imag * psi_i.imag
         n_a, n_i = _active(kind, res_i), _inactive(kind, res_i)
         eff = potential + _get(p, "g_C") * rho + _get(p, "g_R") * n_a + _get(p, "g_I") * n_i
+        if spinor is not None:
+            eff = eff + _get(p, "alpha_2") * rho[:, ::-1]
         gain = 0.5 * (_get(p, "R") * n_a - _get(p, "gamma_C"))
         rhs = (-1j / hbar) * eff * psi_i + gain * psi_i
         eta = _get(p, "kinetic_relaxation_eta")
@@ -323,11 +375,11 @@ def ifrk_step(state: IFRKState, h, tableau, pump_at, potential, p, k_squared, dx
             lap = _ifft(-k_squared * psi_i_k)
             rhs = rhs + eta * n_a * (hbar / (2.0 * m)) * lap
         f.append(_fft(rhs))
-        derivs.append(reservoir_derivatives(kind, res_i, rho, pump_at(stage_time), p, dx, dy))
-    psi_new_k = phase(1) * psi0_k
+        derivs.append(res_derivs(res_i, rho, pump_at(stage_time)))
+    psi_new_k = lin(1, psi0_k)
     for j, bj in enumerate(b):
         if bj:
-            psi_new_k = psi_new_k + (h * float(bj)) * phase(1 - c[j]) * f[j]
+            psi_new_k = psi_new_k + (h * float(bj)) * lin(1 - c[j], f[j])
     res_new = tuple(np.maximum(r0 + sum((h * float(bj)) * derivs[j][q]
                                         for j, bj in enumerate(b) if bj), 0)
                     for q, r0 in enumerate(res0))
@@ -339,20 +391,21 @@ def ifrk_step(state: IFRKState, h, tableau, pump_at, potential, p, k_squared, dx
     psi_new = _ifft(psi_new_k)
     weights = [float(bj - bh) for bj, bh in zip(b, tableau["b_hat"])]
     err = ifrk_error(h, psi_start, psi_new, psi0_k, f, res0, res_new, derivs, weights, c,
-                     phase, rtol, atol)
+                     lin, rtol, atol)
     if err <= 1:
         state.psi, state.psi_k, state.fields = psi_new, psi_new_k, res_new
         state.t = state.t + h
     return err
 
 
-def ifrk_error(h, psi_start, psi_new, psi0_k, f, res0, res_new, derivs, weights, c, phase,
+def ifrk_error(h, psi_start, psi_new, psi0_k, f, res0, res_new, derivs, weights, c, lin,
                rtol, atol):
-    """Embedded RMS error, scaled by atol + rtol max(|y0|, |y1|), max over members."""
+    """Embedded RMS error, scaled by atol + rtol max(|y0|, |y1|), max over members.
+    ``lin(fraction, field)`` applies the Lawson factor of ``(1 - c_j) h``."""
     e_k = np.zeros_like(psi0_k)
     for j, w in enumerate(weights):
         if w:
-            e_k = e_k + (h * w) * phase(1 - c[j]) * f[j]
+            e_k = e_k + (h * w) * lin(1 - c[j], f[j])
     e = _ifft(e_k)
     axes = tuple(range(1, psi_new.ndim))
 

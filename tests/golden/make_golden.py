@@ -293,6 +293,61 @@ def dp5_case(out, name="dp5", nx=12, ny=8):
         t=np.float64(ctl.state.t))
 
 
+def spinor_case(out, name, tableau="dp5", adaptive=True, reservoir="double", res_components=2,
+                wigner=False, ticks=6, nx=16, ny=16, polarization=0.0):
+    """Two-component (circular basis) field with TE-TM, Zeeman and cross-spin terms through the
+    reference's generic Lawson path: ring pump, double (or single) reservoir per component or
+    shared, adaptive DP5 or fixed-step RK4 with the Wigner hook."""
+    from polarism.config.simulation_parameters import ComputeEngineParameters
+    from polarism.simulation_controller import SimulationController
+    from tests.unit.conftest import small_config
+
+    cfg = small_config(
+        grid__nx=nx, grid__ny=ny, grid__lx=2.0 * nx, grid__ly=2.0 * ny,
+        solver__method="ifrk-fft-cuda", solver__tableau=tableau, solver__adaptive=adaptive,
+        solver__dt=0.0625, solver__total_time=2.0, solver__rtol=1e-6, solver__atol=1e-8,
+        reservoir__reservoir_type=reservoir, noise__enabled=True,
+        compute_engine=ComputeEngineParameters(use_gpu=False))
+    cfg.reservoir.components = res_components
+    cfg.physics.spin = "spinor"
+    cfg.physics.zeeman = 0.05
+    cfg.physics.te_tm = 0.02
+    cfg.physics.alpha_2 = -0.1 * cfg.physics.g_C
+    cfg.physics.g_I = 0.0005
+    cfg.laser.laser_type = "profile"
+    cfg.laser.profile = {"type": "ring", "radius": 0.35 * nx, "width": 2.0}
+    cfg.laser.P0 = 0.4
+    cfg.laser.circular_polarization = polarization
+    if wigner:
+        cfg.noise.stochastic = "wigner"
+        cfg.noise.seed = 7
+    ctl = SimulationController(cfg)
+    x, y = ctl.grid.X, ctl.grid.Y
+    blob = np.exp(-0.5 * (x ** 2 + y ** 2) / (0.2 * nx) ** 2)
+    field = np.stack((0.6 * blob * np.exp(1j * 0.5 * x), 0.4 * blob * np.exp(-1j * 0.3 * y)))
+    ctl.state.psi = np.asarray(field, dtype=np.complex128)
+    fields = ctl.reservoir.get_state()
+    seeded = tuple(np.asarray(0.2 * (q + 1) * np.broadcast_to(blob, f.shape), dtype=f.dtype)
+                   for q, f in enumerate(fields))
+    ctl.reservoir.set_state(seeded)
+    psi0 = np.array(ctl.state.field, copy=True)
+    res0 = np.stack([np.array(f, copy=True) for f in ctl.reservoir.get_state()])
+    ctl.solver.advance(ctl.model, ctl.state, ticks)
+    stats = getattr(getattr(ctl.solver, "step_controller", None), "statistics", {"accepted": ticks, "rejected": 0})
+    np.savez_compressed(
+        out / f"{name}.npz", psi0=psi0, res0=res0, envelope=np.asarray(ctl.lasers[0]._spatial_envelope),
+        p0=np.float64(cfg.laser.P0), dt=np.float64(cfg.solver.dt), ticks=np.int64(ticks),
+        rtol=np.float64(cfg.solver.rtol), atol=np.float64(cfg.solver.atol),
+        dx=np.float64(ctl.grid.dx), dy=np.float64(ctl.grid.dy), kx=np.asarray(ctl.grid.KX),
+        ky=np.asarray(ctl.grid.KY), k_squared=np.asarray(ctl.grid.k_squared),
+        weights=np.asarray(ctl.model.pump_weights).reshape(-1, 2), physics=_physics_json(cfg),
+        reservoir=reservoir, tableau=tableau, adaptive=np.bool_(adaptive), wigner=np.bool_(wigner),
+        seed=np.uint64(cfg.noise.seed or 0), psi=np.asarray(ctl.state.field),
+        res=np.stack([np.asarray(f) for f in ctl.reservoir.get_state()]),
+        accepted=np.int64(stats["accepted"]), rejected=np.int64(stats["rejected"]),
+        t=np.float64(ctl.state.t))
+
+
 def main(root):
     _import_reference(root)
     HERE.mkdir(exist_ok=True)
@@ -309,6 +364,10 @@ def main(root):
     ifrk4_cases(HERE, root)
     dp5_case(HERE)
     dp5_case(HERE, "dp5_p2", nx=16, ny=8)
+    spinor_case(HERE, "spinor_dp5", ticks=16)
+    spinor_case(HERE, "spinor_dp5_shared", reservoir="single", res_components=1, nx=16, ny=8, ticks=16,
+                polarization=0.3)
+    spinor_case(HERE, "spinor_rk4_wigner", tableau="rk4", adaptive=False, wigner=True, ticks=4)
     print("golden fixtures written to", HERE)
 
 

@@ -142,6 +142,41 @@ def test_dp5_adaptive_matches_reference(golden):
     assert rel_l2(state.fields[0], g["res"][0]) < 1e-12
 
 
+@pytest.mark.parametrize("case", ["spinor_dp5", "spinor_dp5_shared", "spinor_rk4_wigner"])
+def test_spinor_ifrk_matches_reference(golden, case):
+    """Two-component Lawson steps (matrix exponential, TE-TM, Zeeman, cross-spin term, double or
+    shared reservoir, ring pump, pump weights) against the reference's generic path."""
+    g = golden(case)
+    p = g["physics"]
+    pump = g["envelope"] * g["p0"]
+    dx, dy, dt = float(g["dx"]), float(g["dy"]), float(g["dt"])
+    kind = str(g["reservoir"])
+    spin = {"kx": g["kx"], "ky": g["ky"], "weights": g["weights"]}
+    state = gpe.IFRKState(psi=g["psi0"].copy(), fields=tuple(g["res0"]))
+    if bool(g["adaptive"]):
+        control = gpe.StepControl(dt, None, 5, 4)
+
+        def trial(st, h):
+            return gpe.ifrk_step(st, h, gpe.DP5_TABLEAU, lambda t: pump, 0.0, p, g["k_squared"], dx,
+                                 dy, kind=kind, adaptive=True, rtol=float(g["rtol"]),
+                                 atol=float(g["atol"]), spinor=spin)
+
+        gpe.ifrk_adaptive_advance(state, control, trial, int(g["ticks"]) * dt)
+        assert control.accepted == int(g["accepted"])
+        assert control.rejected == int(g["rejected"])
+    else:
+        noise = gpe.Noise([int(g["seed"])], [p["gamma_C"]], [p["R"]], [1.0], dt, dx * dy, "double")
+        for step in range(int(g["ticks"])):
+            gpe.ifrk_step(state, dt, gpe.TABLEAUS[str(g["tableau"])], lambda t: pump, 0.0, p,
+                          g["k_squared"], dx, dy, kind=kind, spinor=spin)
+            state.psi, state.psi_k = state.real_space(), None
+            if bool(g["wigner"]):
+                noise.apply(state.psi, state.fields[0], step)
+    assert rel_l2(state.real_space(), g["psi"]) < 1e-12
+    for q in range(len(g["res"])):
+        assert rel_l2(state.fields[q], g["res"][q]) < 1e-12
+
+
 def test_dp5_uniform_decay_known_answer():
     """Uniform nonlinear decay psi(t) = exp(-gamma t/2 + i phi(t)) (analytic)."""
     p = dict(hbar=0.6582119514, m_eff=0.284, g_C=2.0, gamma_C=0.7)
