@@ -46,6 +46,7 @@ extern "C" {
 
 #define PG_RES_NONE 0
 #define PG_RES_SINGLE 1
+#define PG_RES_DOUBLE 2      /* active + inactive reservoirs (IFRK only) */
 
 #define PG_POT_NONE 0
 #define PG_POT_REAL 1
@@ -56,6 +57,13 @@ extern "C" {
 typedef struct pg_physics {
   double hbar, m_eff, g_C, g_R, g_I, R, gamma_C, gamma_R;
   double kinetic_relaxation_eta;
+  /* Double reservoir (polarism/reservoir/double_reservoir.py:106-130). */
+  double gamma_I, gamma_A, R_IA, R_AI;
+  /* Two-component fields: cross-spin interaction, Zeeman splitting and TE-TM coefficient
+   * (polarism/model.py:129-173, polarism/dispersion.py:34-63), and the pump share of each
+   * component, (1 +- circular_polarization) / 2 (polarism/simulation_controller.py:974-979). */
+  double alpha_2, zeeman, te_tm;
+  double pump_weight_plus, pump_weight_minus;
 } pg_physics;
 
 typedef struct pg_config {
@@ -67,6 +75,9 @@ typedef struct pg_config {
   int32_t pump_per_member; /* 0: one envelope shared by all members; 1: one per member */
   int32_t potential_per_member;
   double dx, dy, dt;
+  int32_t components;           /* 1 scalar field, 2 circular-basis spinor (0 means 1) */
+  int32_t reservoir_components; /* reservoir fields per component set: 1 shared or = components
+                                   (0 means = components) */
 } pg_config;
 
 typedef struct pg_solver pg_solver;

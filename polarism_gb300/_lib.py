@@ -16,7 +16,7 @@ LIBRARY_PATH = _PKG / "_build" / "libpolarism_gb300.so"
 
 PG_OK, PG_ERR_INVALID, PG_ERR_CUDA, PG_ERR_UNSUPPORTED, PG_ERR_TIMEOUT = 0, 1, 2, 3, 4
 PG_SINGLE, PG_DOUBLE = 0, 1
-PG_RES_NONE, PG_RES_SINGLE = 0, 1
+PG_RES_NONE, PG_RES_SINGLE, PG_RES_DOUBLE = 0, 1, 2
 PG_POT_NONE, PG_POT_REAL, PG_POT_COMPLEX = 0, 1, 2
 
 
@@ -25,7 +25,8 @@ class PgPhysics(C.Structure):
 
     _fields_ = [(name, C.c_double) for name in (
         "hbar", "m_eff", "g_C", "g_R", "g_I", "R", "gamma_C", "gamma_R",
-        "kinetic_relaxation_eta")]
+        "kinetic_relaxation_eta", "gamma_I", "gamma_A", "R_IA", "R_AI", "alpha_2", "zeeman",
+        "te_tm", "pump_weight_plus", "pump_weight_minus")]
 
 
 class PgConfig(C.Structure):
@@ -34,7 +35,8 @@ class PgConfig(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("members", C.c_int32),
                 ("precision", C.c_int32), ("reservoir", C.c_int32), ("potential", C.c_int32),
                 ("pump_per_member", C.c_int32), ("potential_per_member", C.c_int32),
-                ("dx", C.c_double), ("dy", C.c_double), ("dt", C.c_double)]
+                ("dx", C.c_double), ("dy", C.c_double), ("dt", C.c_double),
+                ("components", C.c_int32), ("reservoir_components", C.c_int32)]
 
 
 class PgSweepGrid(C.Structure):

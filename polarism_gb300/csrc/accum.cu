@@ -93,18 +93,23 @@ __global__ void finalize_partials_kernel(const double* __restrict__ partials, in
 }
 
 // Steady-state partials: sum (rho - rho_old)^2, sum rho_old^2, sum rho; rho_old <- rho.
+// With two components the density is summed over them (simulation_controller.py:714-716).
 template <typename T>
 __global__ void steady_partials_kernel(const typename C2T<T>::type* __restrict__ psi,
-                                       T* __restrict__ rho_old, long long sites, int have_old,
-                                       double* __restrict__ partials) {
+                                       T* __restrict__ rho_old, long long sites, int comps,
+                                       int have_old, double* __restrict__ partials) {
   __shared__ double red[3][32];
   const int member = blockIdx.y;
   const long long base = static_cast<long long>(member) * sites;
   double d2 = 0.0, o2 = 0.0, n = 0.0;
   for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < sites;
        e += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const auto v = psi[base + e];
-    const T rho = v.x * v.x + v.y * v.y;
+    const auto v = psi[base * comps + e];
+    T rho = v.x * v.x + v.y * v.y;
+    if (comps == 2) {
+      const auto w = psi[base * comps + sites + e];
+      rho += w.x * w.x + w.y * w.y;
+    }
     if (have_old) {
       const double old = static_cast<double>(rho_old[base + e]);
       const double diff = static_cast<double>(rho) - old;
@@ -202,7 +207,10 @@ int pg_accumulate(pg_solver* s, int32_t kinds) {
   if (rc != PG_OK) return rc;
   pg::AccumBuffers& a = pg::acc(s);
   const bool dbl = s->cfg.precision == PG_DOUBLE;
-  const size_t dbytes = static_cast<size_t>(s->sites) * sizeof(double);
+  // Two-component fields accumulate per component (accumulators.py:103-113, 142-148).
+  const long long values = s->field_values;
+  const int planes = s->cfg.members * s->comps;
+  const size_t dbytes = static_cast<size_t>(values) * sizeof(double);
   if (kinds & 1) {
     if (!a.sum_rho) {
       PG_CUDA(cudaMalloc(&a.sum_rho, dbytes));
@@ -210,20 +218,20 @@ int pg_accumulate(pg_solver* s, int32_t kinds) {
       PG_CUDA(cudaMemsetAsync(a.sum_rho, 0, dbytes, s->stream));
       PG_CUDA(cudaMemsetAsync(a.sum_rho2, 0, dbytes, s->stream));
     }
-    const int blocks = static_cast<int>(std::min<long long>(4096, (s->sites + 255) / 256));
+    const int blocks = static_cast<int>(std::min<long long>(4096, (values + 255) / 256));
     if (dbl)
       pg::density_moments_kernel<double><<<blocks, 256, 0, s->stream>>>(
-          static_cast<const double2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, s->sites);
+          static_cast<const double2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, values);
     else
       pg::density_moments_kernel<float><<<blocks, 256, 0, s->stream>>>(
-          static_cast<const float2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, s->sites);
+          static_cast<const float2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, values);
     PG_CUDA(cudaGetLastError());
     a.samples_rho += 1;
   }
   if (kinds & 2) {
     rc = pg::split_ensure(s);
     if (rc != PG_OK) return rc;
-    const size_t cbytes = static_cast<size_t>(s->sites) * 2 * s->real_size;
+    const size_t cbytes = static_cast<size_t>(values) * 2 * s->real_size;
     if (!a.sum_k) {
       PG_CUDA(cudaMalloc(&a.sum_k, dbytes));
       PG_CUDA(cudaMemsetAsync(a.sum_k, 0, dbytes, s->stream));
@@ -249,7 +257,8 @@ int pg_accumulate(pg_solver* s, int32_t kinds) {
     c.cols = cols;
     c.log2cols = ilog2(cols);
     c.threads = std::max(32, (((cols * ny + mv - 1) / mv + 31) / 32) * 32);
-    c.members = s->cfg.members;
+    c.members = planes;
+    c.comps = 1;
     c.mode = 3;
     c.forward = 1;
     if (dbl) {
@@ -272,13 +281,13 @@ int pg_accumulate(pg_solver* s, int32_t kinds) {
     if (dbl) {
       cudaFuncSetAttribute(pg::spectrum_power_row_kernel<double>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      pg::spectrum_power_row_kernel<double><<<dim3(ny / rows, 1, s->cfg.members), threads, smem, s->stream>>>(
+      pg::spectrum_power_row_kernel<double><<<dim3(ny / rows, 1, planes), threads, smem, s->stream>>>(
           static_cast<const double2*>(a.half), static_cast<const double2*>(s->tw_x), a.sum_k, nx, ny,
           ilog2(nx), rows, ilog2(rows));
     } else {
       cudaFuncSetAttribute(pg::spectrum_power_row_kernel<float>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      pg::spectrum_power_row_kernel<float><<<dim3(ny / rows, 1, s->cfg.members), threads, smem, s->stream>>>(
+      pg::spectrum_power_row_kernel<float><<<dim3(ny / rows, 1, planes), threads, smem, s->stream>>>(
           static_cast<const float2*>(a.half), static_cast<const float2*>(s->tw_x), a.sum_k, nx, ny,
           ilog2(nx), rows, ilog2(rows));
     }
@@ -292,7 +301,7 @@ int pg_accumulator_sums(pg_solver* s, int32_t kind, double* out, int64_t* sample
   PG_CHECK(s && out && samples, PG_ERR_INVALID, "pg_accumulator_sums: null argument");
   PG_CHECK(s->accum, PG_ERR_INVALID, "pg_accumulator_sums: nothing accumulated");
   pg::AccumBuffers& a = pg::acc(s);
-  const size_t bytes = static_cast<size_t>(s->sites) * sizeof(double);
+  const size_t bytes = static_cast<size_t>(s->field_values) * sizeof(double);
   double* src = kind == 0 ? a.sum_rho : kind == 1 ? a.sum_rho2 : kind == 2 ? a.sum_k : nullptr;
   PG_CHECK(src, PG_ERR_INVALID, "pg_accumulator_sums: kind 0 sum rho, 1 sum rho^2, 2 sum |psi_k|^2");
   PG_CUDA(cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, s->stream));
@@ -305,7 +314,7 @@ int pg_accumulator_reset(pg_solver* s) {
   PG_CHECK(s, PG_ERR_INVALID, "pg_accumulator_reset: null solver");
   if (!s->accum) return PG_OK;
   pg::AccumBuffers& a = pg::acc(s);
-  const size_t bytes = static_cast<size_t>(s->sites) * sizeof(double);
+  const size_t bytes = static_cast<size_t>(s->field_values) * sizeof(double);
   if (a.sum_rho) PG_CUDA(cudaMemsetAsync(a.sum_rho, 0, bytes, s->stream));
   if (a.sum_rho2) PG_CUDA(cudaMemsetAsync(a.sum_rho2, 0, bytes, s->stream));
   if (a.sum_k) PG_CUDA(cudaMemsetAsync(a.sum_k, 0, bytes, s->stream));
@@ -324,10 +333,10 @@ int pg_norms(pg_solver* s, double* out) {
   const double cell = s->cfg.dx * s->cfg.dy;
   const cudaError_t e =
       s->cfg.precision == PG_DOUBLE
-          ? pg::launch_norm<double>(s->psi[s->cur], s->plane, s->cfg.members, cell, a.partials,
-                                    a.partial_blocks, a.out, s->stream)
-          : pg::launch_norm<float>(s->psi[s->cur], s->plane, s->cfg.members, cell, a.partials,
-                                   a.partial_blocks, a.out, s->stream);
+          ? pg::launch_norm<double>(s->psi[s->cur], s->plane * s->comps, s->cfg.members, cell,
+                                    a.partials, a.partial_blocks, a.out, s->stream)
+          : pg::launch_norm<float>(s->psi[s->cur], s->plane * s->comps, s->cfg.members, cell,
+                                   a.partials, a.partial_blocks, a.out, s->stream);
   PG_CUDA(e);
   PG_CUDA(cudaMemcpyAsync(out, a.out, sizeof(double) * s->cfg.members, cudaMemcpyDeviceToHost, s->stream));
   PG_CUDA(cudaStreamSynchronize(s->stream));
@@ -346,11 +355,11 @@ int pg_steady_check(pg_solver* s, double* rel_density, double* rel_norm, double*
   if (s->cfg.precision == PG_DOUBLE)
     pg::steady_partials_kernel<double><<<dim3(blocks, m), 256, 0, s->stream>>>(
         static_cast<const double2*>(s->psi[s->cur]), static_cast<double*>(a.rho_old), s->plane,
-        a.have_old ? 1 : 0, a.partials);
+        s->comps, a.have_old ? 1 : 0, a.partials);
   else
     pg::steady_partials_kernel<float><<<dim3(blocks, m), 256, 0, s->stream>>>(
         static_cast<const float2*>(s->psi[s->cur]), static_cast<float*>(a.rho_old), s->plane,
-        a.have_old ? 1 : 0, a.partials);
+        s->comps, a.have_old ? 1 : 0, a.partials);
   PG_CUDA(cudaGetLastError());
   std::vector<double> host(static_cast<size_t>(3) * blocks * m);
   PG_CUDA(cudaMemcpyAsync(host.data(), a.partials, host.size() * sizeof(double), cudaMemcpyDeviceToHost,

@@ -287,8 +287,15 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   PG_CHECK(cfg->members >= 1, PG_ERR_INVALID, "pg_create: members must be >= 1");
   PG_CHECK(cfg->precision == PG_SINGLE || cfg->precision == PG_DOUBLE, PG_ERR_INVALID,
            "pg_create: precision must be PG_SINGLE or PG_DOUBLE");
-  PG_CHECK(cfg->reservoir == PG_RES_NONE || cfg->reservoir == PG_RES_SINGLE, PG_ERR_UNSUPPORTED,
-           "pg_create: reservoir must be PG_RES_NONE or PG_RES_SINGLE");
+  PG_CHECK(cfg->reservoir == PG_RES_NONE || cfg->reservoir == PG_RES_SINGLE ||
+               cfg->reservoir == PG_RES_DOUBLE,
+           PG_ERR_UNSUPPORTED, "pg_create: reservoir must be PG_RES_NONE, PG_RES_SINGLE or PG_RES_DOUBLE");
+  PG_CHECK(cfg->components >= 0 && cfg->components <= 2, PG_ERR_INVALID,
+           "pg_create: components must be 1 or 2");
+  const int comps = cfg->components == 0 ? 1 : cfg->components;
+  const int res_comps = cfg->reservoir_components == 0 ? comps : cfg->reservoir_components;
+  PG_CHECK(res_comps == 1 || res_comps == comps, PG_ERR_INVALID,
+           "pg_create: reservoir_components must be 1 or equal to components");
   PG_CHECK(cfg->potential >= PG_POT_NONE && cfg->potential <= PG_POT_COMPLEX, PG_ERR_INVALID,
            "pg_create: bad potential kind");
   PG_CHECK(cfg->dx > 0 && cfg->dy > 0 && cfg->dt > 0, PG_ERR_INVALID,
@@ -302,6 +309,11 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   s->real_size = cfg->precision == PG_DOUBLE ? 8 : 4;
   s->plane = static_cast<long long>(cfg->nx) * cfg->ny;
   s->sites = s->plane * cfg->members;
+  s->comps = comps;
+  s->res_fields = cfg->reservoir;
+  s->res_comps = res_comps;
+  s->field_values = s->sites * comps;
+  s->res_values = s->sites * s->res_fields * res_comps;
   int dev = 0;
   auto fail = [&](cudaError_t e, const char* what) {
     pg::set_error(std::string("pg_create: ") + what + ": " + cudaGetErrorString(e));
@@ -314,8 +326,8 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   if (e != cudaSuccess) return fail(e, "device attribute");
   e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail(e, "stream");
-  const size_t field_bytes = static_cast<size_t>(s->sites) * 2 * s->real_size;
-  const size_t res_bytes = static_cast<size_t>(s->sites) * s->real_size;
+  const size_t field_bytes = static_cast<size_t>(s->field_values) * 2 * s->real_size;
+  const size_t res_bytes = static_cast<size_t>(std::max<long long>(1, s->res_values)) * s->real_size;
   for (int i = 0; i < 2; ++i) {
     if ((e = cudaMalloc(&s->psi[i], field_bytes)) != cudaSuccess) return fail(e, "psi buffers");
     if ((e = cudaMalloc(&s->res[i], res_bytes)) != cudaSuccess) return fail(e, "reservoir buffers");
@@ -401,11 +413,11 @@ int pg_set_state(pg_solver* s, const void* psi, const void* res, int on_device) 
            "pg_set_state: reservoir array required");
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   pg::ifrk_invalidate(s);
-  PG_CUDA(cudaMemcpyAsync(s->psi[s->cur], psi, static_cast<size_t>(s->sites) * 2 * s->real_size,
+  PG_CUDA(cudaMemcpyAsync(s->psi[s->cur], psi, static_cast<size_t>(s->field_values) * 2 * s->real_size,
                           kind, s->stream));
   if (s->cfg.reservoir != PG_RES_NONE)
-    PG_CUDA(cudaMemcpyAsync(s->res[s->cur], res, static_cast<size_t>(s->sites) * s->real_size, kind,
-                            s->stream));
+    PG_CUDA(cudaMemcpyAsync(s->res[s->cur], res, static_cast<size_t>(s->res_values) * s->real_size,
+                            kind, s->stream));
   PG_CUDA(cudaStreamSynchronize(s->stream));
   return PG_OK;
 }
@@ -413,11 +425,11 @@ int pg_set_state(pg_solver* s, const void* psi, const void* res, int on_device) 
 int pg_get_state(pg_solver* s, void* psi, void* res, int on_device) {
   PG_CHECK(s && psi, PG_ERR_INVALID, "pg_get_state: null argument");
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  PG_CUDA(cudaMemcpyAsync(psi, s->psi[s->cur], static_cast<size_t>(s->sites) * 2 * s->real_size,
+  PG_CUDA(cudaMemcpyAsync(psi, s->psi[s->cur], static_cast<size_t>(s->field_values) * 2 * s->real_size,
                           kind, s->stream));
   if (res && s->cfg.reservoir != PG_RES_NONE)
-    PG_CUDA(cudaMemcpyAsync(res, s->res[s->cur], static_cast<size_t>(s->sites) * s->real_size, kind,
-                            s->stream));
+    PG_CUDA(cudaMemcpyAsync(res, s->res[s->cur], static_cast<size_t>(s->res_values) * s->real_size,
+                            kind, s->stream));
   PG_CUDA(cudaStreamSynchronize(s->stream));
   return check_device_flag(s);
 }
@@ -529,6 +541,8 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
   PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_rk4_advance: negative step count");
   PG_CHECK(!s->spectral, PG_ERR_INVALID,
            "pg_rk4_advance: the state holds a spectrum; set real-space psi first");
+  PG_CHECK(s->comps == 1 && s->res_fields <= 1, PG_ERR_UNSUPPORTED,
+           "pg_rk4_advance: two-component fields and the double reservoir run on the IFRK path");
   s->last_launches = 0;
   pg::ifrk_invalidate(s);
   const int m = s->cfg.members;

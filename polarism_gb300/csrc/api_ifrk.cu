@@ -86,6 +86,7 @@ struct IfrkBuffers {
   int partial_blocks = 0;
   std::vector<double> host_partials;
   bool w_valid = false;  // W holds F_y of the current state
+  SpinorConst* spin = nullptr;  // two-component Lawson constants per member
 };
 
 IfrkBuffers& bufs(pg_solver* s) { return *static_cast<IfrkBuffers*>(s->ifrk); }
@@ -103,8 +104,8 @@ int ensure_ifrk(pg_solver* s) {
   if (rc != PG_OK) return rc;
   IfrkBuffers* b = new IfrkBuffers();
   s->ifrk = b;
-  const size_t cbytes = static_cast<size_t>(s->sites) * 2 * s->real_size;
-  const size_t rbytes = static_cast<size_t>(s->sites) * s->real_size;
+  const size_t cbytes = static_cast<size_t>(s->field_values) * 2 * s->real_size;
+  const size_t rbytes = static_cast<size_t>(std::max<long long>(1, s->res_values)) * s->real_size;
   b->csize = cbytes;
   PG_CUDA(cudaMalloc(&b->W, cbytes));
   PG_CUDA(cudaMalloc(&b->psi0_hat, cbytes));
@@ -120,6 +121,15 @@ int ensure_ifrk(pg_solver* s) {
   b->partial_blocks = cols_blocks;
   PG_CUDA(cudaMalloc(&b->partials, sizeof(double) * static_cast<size_t>(cols_blocks) * c.members));
   b->host_partials.resize(static_cast<size_t>(cols_blocks) * c.members);
+  if (s->comps == 2) {
+    std::vector<SpinorConst> host(c.members);
+    for (int m = 0; m < c.members; ++m) {
+      const pg_physics& p = s->physics[m];
+      host[m] = SpinorConst{p.hbar / (2.0 * p.m_eff), 0.5 * p.zeeman, p.te_tm, 1.0 / p.hbar};
+    }
+    PG_CUDA(cudaMalloc(&b->spin, host.size() * sizeof(SpinorConst)));
+    PG_CUDA(cudaMemcpy(b->spin, host.data(), host.size() * sizeof(SpinorConst), cudaMemcpyHostToDevice));
+  }
   const size_t esize = s->real_size;
   if (c.precision == PG_DOUBLE)
     PG_CUDA(configure_ifrk_kernels<double>(200 * 1024));
@@ -184,28 +194,39 @@ Plan make_plan(const pg_solver* s) {
   r.nx = c.nx;
   r.ny = c.ny;
   r.log2nx = ilog2i(c.nx);
+  const int comps = s->comps;
   int rows = 1;
-  while (rows * 2 <= c.ny && rows * 2 * c.nx <= 4096) rows *= 2;
+  while (rows * 2 <= c.ny && rows * 2 * c.nx * comps <= 4096) rows *= 2;
   r.rows = rows;
   r.log2rows = ilog2i(rows);
-  int threads = (rows * c.nx + mv - 1) / mv;
+  int threads = (rows * c.nx * comps + mv - 1) / mv;
   r.threads = std::max(32, ((threads + 31) / 32) * 32);
   r.members = c.members;
-  r.member_stride = s->plane;
+  r.comps = comps;
+  r.member_stride = s->plane * comps;
+  r.spinor = comps == 2 ? 1 : 0;
+  r.kx_unit = 2.0 * kPi2 / (static_cast<double>(c.nx) * c.dx);
+  r.ky_unit = 2.0 * kPi2 / (static_cast<double>(c.ny) * c.dy);
+  r.inv_n = 1.0 / (static_cast<double>(c.nx) * c.ny);
+  r.spin = s->ifrk ? static_cast<const void*>(static_cast<IfrkBuffers*>(s->ifrk)->spin) : nullptr;
   IfrkColArgs& k = p.col;
   k.nx = c.nx;
   k.ny = c.ny;
   k.log2ny = ilog2i(c.ny);
   int cols = 1;
-  while (cols * 2 <= c.nx && cols * 2 <= 16 && cols * 2 * c.ny * csize <= 160 * 1024 &&
-         cols * 2 * c.ny <= mv * 1024)
+  while (cols * 2 <= c.nx && cols * 2 <= 16 && cols * 2 * comps * c.ny * csize <= 160 * 1024 &&
+         cols * 2 * comps * c.ny <= mv * 1024)
     cols *= 2;
   k.cols = cols;
   k.log2cols = ilog2i(cols);
-  threads = (cols * c.ny + mv - 1) / mv;
+  threads = (cols * comps * c.ny + mv - 1) / mv;
   k.threads = std::max(32, ((threads + 31) / 32) * 32);
   k.members = c.members;
-  k.reservoir = c.reservoir == PG_RES_SINGLE;
+  k.comps = comps;
+  k.log2comps = comps == 2 ? 1 : 0;
+  k.res_fields = s->res_fields;
+  k.res_comps = s->res_comps;
+  k.reservoir = s->res_fields > 0;
   k.potential = c.potential;
   k.pump_stride = c.pump_per_member ? s->plane : 0;
   k.pot_stride = c.potential_per_member ? s->plane : 0;
@@ -240,6 +261,11 @@ StepTables build_tables(const Tableau& tb, double h) {
     st.err_tab[j] = st.final_tab[1 + j];
   }
   return st;
+}
+
+// The spinor row pass evaluates its Lawson factors from tau instead of the tables.
+void set_taus(IfrkRowArgs& r, const StepTables& st) {
+  for (int t = 0; t < r.terms; ++t) r.tau[t] = st.taus[r.table[t]];
 }
 
 template <typename T>
@@ -285,6 +311,7 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
       ++r.terms;
     }
     T* save = static_cast<T*>(i == 0 ? b.psi0_hat : b.fhat[i - 1]);
+    set_taus(r, st);
     PG_CUDA(launch_ifrk_row<T>(W, save, W, tables, r, tw_x, s->stream));
     IfrkColArgs a = p.col;
     a.mode = 0;
@@ -321,6 +348,7 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
       r.table[r.terms] = st.final_tab[1 + j];
       ++r.terms;
     }
+    set_taus(r, st);
     PG_CUDA(launch_ifrk_row<T>(W, static_cast<T*>(b.fhat[tb.stages - 1]), W, tables, r, tw_x,
                                s->stream));
     IfrkColArgs a = p.col;
@@ -355,6 +383,7 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
       r.table[r.terms] = st.err_tab[j];
       ++r.terms;
     }
+    set_taus(r, st);
     PG_CUDA(launch_ifrk_row<T>(nullptr, nullptr, static_cast<T*>(b.ehat), tables, r, tw_x, s->stream));
     IfrkColArgs a = p.col;
     a.mode = 2;
@@ -380,7 +409,8 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
     PG_CUDA(cudaMemcpyAsync(b.host_partials.data(), b.partials, count * sizeof(double),
                             cudaMemcpyDeviceToHost, s->stream));
     PG_CUDA(cudaStreamSynchronize(s->stream));
-    const double sites = static_cast<double>(s->plane) * (s->cfg.reservoir == PG_RES_SINGLE ? 2 : 1);
+    // Values per member entering the RMS: every field component and reservoir plane.
+    const double sites = static_cast<double>(s->plane) * (s->comps + s->res_fields * s->res_comps);
     double err = 0.0;
     for (int m = 0; m < s->cfg.members; ++m) {
       double sum = 0.0;
@@ -406,7 +436,7 @@ int ifrk_advance_t(pg_solver* s, int tab, int64_t start_step, int n_steps, const
   const Plan p = make_plan(s);
   const double h = s->cfg.dt;
   StepTables st = build_tables(tb, h);
-  int rc = upload_tables<T>(s, st.taus);
+  int rc = s->comps == 1 ? upload_tables<T>(s, st.taus) : PG_OK;
   if (rc != PG_OK) return rc;
   IfrkBuffers& b = bufs(s);
   b.w_valid = false;
@@ -436,7 +466,7 @@ int ifrk_trial_t(pg_solver* s, int tab, double h, const double* scales, double r
   PG_CHECK(tb.embedded, PG_ERR_INVALID, "pg_ifrk_trial: the tableau has no embedded pair");
   const Plan p = make_plan(s);
   StepTables st = build_tables(tb, h);
-  int rc = upload_tables<T>(s, st.taus);
+  int rc = s->comps == 1 ? upload_tables<T>(s, st.taus) : PG_OK;
   if (rc != PG_OK) return rc;
   rc = stage_coefficients(s, scales, 1, tb.stages, 0);
   if (rc != PG_OK) return rc;
@@ -471,6 +501,7 @@ void ifrk_release(pg_solver* s) {
   cudaFree(b->n_new);
   cudaFree(b->tables);
   cudaFree(b->partials);
+  cudaFree(b->spin);
   delete b;
   s->ifrk = nullptr;
 }

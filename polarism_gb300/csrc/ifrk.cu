@@ -16,6 +16,16 @@
 namespace pg {
 namespace {
 
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+// sin and cos of an FP64 phase angle in the working precision: FP32 takes the angle reduced
+// to [-pi, pi] in FP64 first, so the only FP32 error is that of the reduced angle.
+__device__ __forceinline__ void sincos_angle(double a, float* s, float* c) {
+  const double n = rint(a * (1.0 / kTwoPi));
+  sincosf(static_cast<float>(fma(-n, kTwoPi, a)), s, c);
+}
+__device__ __forceinline__ void sincos_angle(double a, double* s, double* c) { sincos(a, s, c); }
+
 template <typename T>
 __global__ void __launch_bounds__(1024) ifrk_row_kernel(const typename C2T<T>::type* __restrict__ in,
                                                         typename C2T<T>::type* __restrict__ save,
@@ -26,42 +36,109 @@ __global__ void __launch_bounds__(1024) ifrk_row_kernel(const typename C2T<T>::t
   using C2 = typename C2T<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C2* tws = reinterpret_cast<C2*>(smem_raw);
-  C2* buf = tws + a.nx;
+  C2* buf = tws + a.nx;  // [component][row][x]
   const int member = blockIdx.z;
   const int row0 = blockIdx.x * a.rows;
-  const int count = a.rows * a.nx;
+  const int count = a.rows * a.nx;  // values per component
+  const int comps = a.comps;
+  const long long plane = static_cast<long long>(a.nx) * a.ny;
   const long long moff = member * a.member_stride + static_cast<long long>(row0) * a.nx;
+  const int all = count * comps;
   for (int k = threadIdx.x; k < a.nx; k += blockDim.x) tws[k] = tw[k];
   if (in) {
-    for (int e = threadIdx.x; e < count; e += blockDim.x) buf[e] = in[moff + e];
-  }
-  __syncthreads();
-  if (a.forward) smem_fft<T, false, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
-  if (save) {
-    for (int e = threadIdx.x; e < count; e += blockDim.x) save[moff + e] = buf[e];
-  }
-  const long long table_stride = static_cast<long long>(a.members) * (a.nx + a.ny);
-  for (int e = threadIdx.x; e < count; e += blockDim.x) {
-    const int r = e >> a.log2nx;
-    const int j = e & (a.nx - 1);
-    const int i = row0 + r;
-    C2 acc{T(0), T(0)};
-#pragma unroll
-    for (int t = 0; t < kIfrkMaxTerms; ++t) {
-      if (t >= a.terms) break;
-      const C2* tab = tables + a.table[t] * table_stride + static_cast<long long>(member) * (a.nx + a.ny);
-      const C2 E = cmul(tab[j], tab[a.nx + i]);
-      const C2 v = a.src[t] ? static_cast<const C2*>(a.src[t])[moff + e] : buf[e];
-      const C2 ev = cmul(E, v);
-      const T c = static_cast<T>(a.coef[t]);
-      acc.x += c * ev.x;
-      acc.y += c * ev.y;
+    for (int e = threadIdx.x; e < all; e += blockDim.x) {
+      const int c = e >= count ? 1 : 0;
+      buf[e] = in[moff + c * plane + (e - c * count)];
     }
-    buf[e] = acc;
   }
   __syncthreads();
-  if (a.inverse) smem_fft<T, true, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
-  for (int e = threadIdx.x; e < count; e += blockDim.x) out[moff + e] = buf[e];
+  const int log2batch = a.log2rows + (comps == 2 ? 1 : 0);
+  if (a.forward) smem_fft<T, false, false>(buf, tws, a.log2nx, log2batch, 1, a.nx);
+  if (save) {
+    for (int e = threadIdx.x; e < all; e += blockDim.x) {
+      const int c = e >= count ? 1 : 0;
+      save[moff + c * plane + (e - c * count)] = buf[e];
+    }
+  }
+  if (!a.spinor) {
+    const long long table_stride = static_cast<long long>(a.members) * (a.nx + a.ny);
+    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+      const int r = e >> a.log2nx;
+      const int j = e & (a.nx - 1);
+      const int i = row0 + r;
+      C2 acc{T(0), T(0)};
+#pragma unroll
+      for (int t = 0; t < kIfrkMaxTerms; ++t) {
+        if (t >= a.terms) break;
+        const C2* tab = tables + a.table[t] * table_stride + static_cast<long long>(member) * (a.nx + a.ny);
+        const C2 E = cmul(tab[j], tab[a.nx + i]);
+        const C2 v = a.src[t] ? static_cast<const C2*>(a.src[t])[moff + e] : buf[e];
+        const C2 ev = cmul(E, v);
+        const T c = static_cast<T>(a.coef[t]);
+        acc.x += c * ev.x;
+        acc.y += c * ev.y;
+      }
+      buf[e] = acc;
+    }
+  } else {
+    // Two components: out = sum_t coef_t / N exp(-i H(k) tau_t / hbar) src_t with
+    // exp(-i H t) = exp(-i E t) [[cos - i s z, -i s u], [-i s u*, cos + i s z]],
+    // s = sin(w t) / w, w = sqrt(z^2 + |u|^2), u = beta (kx - i ky)^2 (dispersion.py:66-83).
+    const SpinorConst sc = static_cast<const SpinorConst*>(a.spin)[member];
+    const T zf = static_cast<T>(sc.half_z);
+    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+      const int j = e & (a.nx - 1);
+      const int i = row0 + (e >> a.log2nx);
+      const double kx = a.kx_unit * static_cast<double>(j < (a.nx >> 1) ? j : j - a.nx);
+      const double ky = a.ky_unit * static_cast<double>(i < (a.ny >> 1) ? i : i - a.ny);
+      const double k2 = kx * kx + ky * ky;
+      const double rate_e = sc.rate * k2;                 // E(k) / hbar
+      const double bk2 = sc.beta * k2;
+      const double omega = sqrt(sc.half_z * sc.half_z + bk2 * bk2);
+      const double rate_w = omega * sc.inv_hbar;
+      const T ure = static_cast<T>(sc.beta * (kx * kx - ky * ky));
+      const T uim = static_cast<T>(-2.0 * sc.beta * kx * ky);
+      const T om = static_cast<T>(omega);
+      C2 acc0{T(0), T(0)}, acc1{T(0), T(0)};
+#pragma unroll 1
+      for (int t = 0; t < a.terms; ++t) {
+        const double tau = a.tau[t];
+        T se, ce, sw, cw;
+        sincos_angle(rate_e * tau, &se, &ce);
+        sincos_angle(rate_w * tau, &sw, &cw);
+        const T so = omega > 0.0 ? sw / om : static_cast<T>(tau * sc.inv_hbar);
+        C2 s0, s1;
+        if (a.src[t]) {
+          const C2* src = static_cast<const C2*>(a.src[t]) + moff;
+          s0 = src[e];
+          s1 = src[plane + e];
+        } else {
+          s0 = buf[e];
+          s1 = buf[count + e];
+        }
+        const T sz = so * zf;
+        // (cos - i s z) s0 + (-i s u) s1  and  (-i s u*) s0 + (cos + i s z) s1
+        const C2 a0{cw * s0.x + sz * s0.y + so * (uim * s1.x + ure * s1.y),
+                    cw * s0.y - sz * s0.x + so * (uim * s1.y - ure * s1.x)};
+        const C2 a1{cw * s1.x - sz * s1.y + so * (ure * s0.y - uim * s0.x),
+                    cw * s1.y + sz * s1.x - so * (ure * s0.x + uim * s0.y)};
+        const T w = static_cast<T>(a.coef[t] * a.inv_n);
+        // phase exp(-i E t) = (ce, -se)
+        acc0.x += w * (ce * a0.x + se * a0.y);
+        acc0.y += w * (ce * a0.y - se * a0.x);
+        acc1.x += w * (ce * a1.x + se * a1.y);
+        acc1.y += w * (ce * a1.y - se * a1.x);
+      }
+      buf[e] = acc0;
+      buf[count + e] = acc1;
+    }
+  }
+  __syncthreads();
+  if (a.inverse) smem_fft<T, true, false>(buf, tws, a.log2nx, log2batch, 1, a.nx);
+  for (int e = threadIdx.x; e < all; e += blockDim.x) {
+    const int c = e >= count ? 1 : 0;
+    out[moff + c * plane + (e - c * count)] = buf[e];
+  }
 }
 
 template <typename T>
@@ -77,6 +154,11 @@ __device__ __forceinline__ T scaled_square(T mag, T scale) {
 __device__ __forceinline__ float mul_rn_i(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn_i(double a, double b) { return __dmul_rn(a, b); }
 
+// Column pass over a panel of `cols` columns of every component of one member.  Reservoir
+// planes are laid out [field][member][reservoir component][y][x]; with one reservoir
+// component per field component each component feeds its own reservoirs with its own
+// density and pump share, otherwise one shared set sees the summed density
+// (ifrk_fft_cuda_solver.py:118-126; single_reservoir.py:81-98; double_reservoir.py:106-130).
 template <typename T>
 __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* __restrict__ psi,
                                                         const T* __restrict__ n0,
@@ -95,21 +177,27 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
   using C2 = typename C2T<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C2* tws = reinterpret_cast<C2*>(smem_raw);
-  C2* buf = tws + a.ny;
+  C2* buf = tws + a.ny;  // [y][component][column]
   __shared__ double red[32];
   const int member = blockIdx.z;
   const int x0 = blockIdx.x * a.cols;
   const int C = a.cols;
+  const int comps = a.comps;
+  const int lcc = a.log2cols + a.log2comps;
+  const int CC = 1 << lcc;  // panel columns over all components
   const long long plane = static_cast<long long>(a.nx) * a.ny;
-  C2* d = psi + member * plane;
+  const long long fbase = static_cast<long long>(member) * comps * plane;
+  C2* d = psi + fbase;
   for (int k = threadIdx.x; k < a.ny; k += blockDim.x) tws[k] = tw[k];
-  const int count = C * a.ny;
-  for (int e = threadIdx.x; e < count; e += blockDim.x) {
-    const int c = e & (C - 1), i = e >> a.log2cols;
-    buf[i * C + c] = d[static_cast<long long>(i) * a.nx + x0 + c];
+  const int count = C * a.ny;  // sites of the panel
+  const int all = count * comps;
+  for (int e = threadIdx.x; e < all; e += blockDim.x) {
+    const int c2 = e & (CC - 1), i = e >> lcc;
+    const int comp = c2 >> a.log2cols, c = c2 & (C - 1);
+    buf[i * CC + c2] = d[comp * plane + static_cast<long long>(i) * a.nx + x0 + c];
   }
   __syncthreads();
-  if (a.inverse) smem_fft<T, true, true>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
+  if (a.inverse) smem_fft<T, true, true>(buf, tws, a.log2ny, lcc, CC, 1);
   double local = 0.0;
   if (a.mode != 3) {
     const SplitConst<T> k = consts[member];
@@ -117,54 +205,112 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
     const T* pm = pump + member * a.pump_stride;
     const T* vm = potential ? potential + member * a.pot_stride * (a.potential == 2 ? 2 : 1) : nullptr;
     const unsigned long long step = a.noise ? step_base[0] + a.step_offset : 0ull;
+    const int F = a.res_fields, Cr = a.res_comps;
+    const int NQ = F * Cr;
+    const long long qstride = static_cast<long long>(Cr) * plane;      // reservoir member stride
+    const long long fstride = static_cast<long long>(a.members) * qstride;  // field stride
     for (int e = threadIdx.x; e < count; e += blockDim.x) {
       const int c = e & (C - 1), i = e >> a.log2cols;
       const long long o = static_cast<long long>(i) * a.nx + x0 + c;
-      const long long mo = member * plane + o;
-      C2 v = buf[i * C + c];
-      // Stage (or final) reservoir: n0 + sum coef_j dn_j (the sum alone is the error term).
-      T n = T(0), dsum = T(0);
-      if (a.reservoir) {
+      C2 v[2];
+      v[0] = buf[i * CC + c];
+      v[1] = comps == 2 ? buf[i * CC + C + c] : C2{T(0), T(0)};
+      // Stage (or final) reservoir values n0 + sum coef_j dn_j; the sum alone is the error term.
+      T nval[4] = {T(0), T(0), T(0), T(0)}, dsum[4] = {T(0), T(0), T(0), T(0)};
+      long long ridx[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (q >= NQ) break;
+        const int f = Cr == 2 ? (q >> 1) : q, cr = Cr == 2 ? (q & 1) : 0;
+        ridx[q] = f * fstride + member * qstride + cr * plane + o;
+        T acc = T(0);
 #pragma unroll
         for (int j = 0; j < kIfrkMaxStages; ++j) {
           if (j >= a.terms) break;
-          dsum += static_cast<T>(a.coef[j]) * static_cast<const T*>(a.dn[j])[mo];
+          acc += static_cast<T>(a.coef[j]) * static_cast<const T*>(a.dn[j])[ridx[q]];
         }
-        n = n0[mo] + dsum;
+        dsum[q] = acc;
+        nval[q] = n0[ridx[q]] + acc;
       }
       if (a.mode == 0) {
-        if (psi_start) psi_start[mo] = v;
-        const T rho = v.x * v.x + v.y * v.y;
+        T rho[2];
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          rho[comp] = v[comp].x * v[comp].x + v[comp].y * v[comp].y;
+          if (comp < comps && psi_start) psi_start[fbase + comp * plane + o] = v[comp];
+        }
         T vre = T(0), vim = T(0);
         if (vm) {
           vre = a.potential == 2 ? vm[2 * o] : vm[o];
           vim = a.potential == 2 ? vm[2 * o + 1] : T(0);
         }
-        // rhs = (-i/hbar) (V_re + g_C rho + g_R n) psi + (R n - gamma_C)/2 psi + (V_im/hbar) psi
-        const T e_over = (vre + k.g_C * rho + k.g_R * n) * k.inv_hbar;
-        const T g = T(0.5) * (k.R * n - k.gamma_C) + vim * k.inv_hbar;
-        buf[i * C + c] = C2{g * v.x + e_over * v.y, g * v.y - e_over * v.x};
-        if (a.reservoir) dn_out[mo] = mul_rn_i(s0, pm[o]) - (k.gamma_R + k.R * rho) * n;
-      } else if (a.mode == 1) {
-        n = n > T(0) ? n : T(0);
-        if (a.reservoir) n_out[mo] = n;
-        if (a.noise) {
-          const Words4 w = wigner_words(static_cast<uint32_t>(o), step, 1u, k.seed);
-          WignerDraw<T>::apply(w, k.noise_a + k.noise_b * n, v.x, v.y);
-          buf[i * C + c] = v;
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          if (comp >= comps) break;
+          const int ra = Cr == comps ? comp : 0;
+          const T nA = F >= 1 ? nval[ra] : T(0);
+          const T nI = F == 2 ? nval[Cr + ra] : T(0);
+          // rhs = (-i/hbar) (V_re + g_C rho + alpha_2 rho_other + g_R n_A + g_I n_I) psi
+          //       + (R n_A - gamma_C)/2 psi + (V_im / hbar) psi
+          T eff = vre + k.g_C * rho[comp] + k.g_R * nA;
+          if (comps == 2) eff += k.alpha_2 * rho[1 - comp];
+          if (F == 2) eff += k.g_I * nI;
+          const T e_over = eff * k.inv_hbar;
+          const T g = T(0.5) * (k.R * nA - k.gamma_C) + vim * k.inv_hbar;
+          buf[i * CC + comp * C + c] = C2{g * v[comp].x + e_over * v[comp].y, g * v[comp].y - e_over * v[comp].x};
         }
-        psi_new[mo] = v;
-      } else {  // mode 2: error norm, v = condensate error, n = reservoir error
-        const C2 y0 = psi_start[mo];
-        const C2 y1 = psi_new[mo];
-        const T a0 = sqrt(y0.x * y0.x + y0.y * y0.y), a1 = sqrt(y1.x * y1.x + y1.y * y1.y);
-        const T scale = static_cast<T>(a.atol) + static_cast<T>(a.rtol) * (a0 > a1 ? a0 : a1);
-        local += static_cast<double>(scaled_square(sqrt(v.x * v.x + v.y * v.y), scale));
-        if (a.reservoir) {
-          const T en = dsum;  // h sum_j (b_j - bhat_j) dn_j
-          const T r0 = fabs(n0[mo]), r1 = fabs(n_out[mo]);
+        if (F >= 1) {
+          const T p_site = mul_rn_i(s0, pm[o]);
+#pragma unroll
+          for (int cr = 0; cr < 2; ++cr) {
+            if (cr >= Cr) break;
+            const T rr = Cr == comps ? rho[cr] : (comps == 2 ? rho[0] + rho[1] : rho[0]);
+            const T P = Cr == 2 ? mul_rn_i(p_site, k.weight[cr]) : p_site;
+            if (F == 1) {
+              dn_out[ridx[cr]] = P - (k.gamma_R + k.R * rr) * nval[cr];
+            } else {
+              const T nA = nval[cr], nI = nval[Cr + cr];
+              dn_out[ridx[Cr + cr]] = P - (k.gamma_I + k.R_IA) * nI + k.R_AI * nA;
+              dn_out[ridx[cr]] = k.R_IA * nI - (k.gamma_A + k.R_AI + k.R * rr) * nA;
+            }
+          }
+        }
+      } else if (a.mode == 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (q >= NQ) break;
+          nval[q] = nval[q] > T(0) ? nval[q] : T(0);
+          n_out[ridx[q]] = nval[q];
+        }
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          if (comp >= comps) break;
+          C2 w = v[comp];
+          if (a.noise) {
+            const T nA = F >= 1 ? nval[Cr == comps ? comp : 0] : T(0);
+            const Words4 words = wigner_words(static_cast<uint32_t>(o), step, 1u + comp, k.seed);
+            WignerDraw<T>::apply(words, k.noise_a + k.noise_b * nA, w.x, w.y);
+            buf[i * CC + comp * C + c] = w;
+          }
+          psi_new[fbase + comp * plane + o] = w;
+        }
+      } else {  // mode 2: error norm, v = condensate error, dsum = reservoir error
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          if (comp >= comps) break;
+          const C2 y0 = psi_start[fbase + comp * plane + o];
+          const C2 y1 = psi_new[fbase + comp * plane + o];
+          const T a0 = sqrt(y0.x * y0.x + y0.y * y0.y), a1 = sqrt(y1.x * y1.x + y1.y * y1.y);
+          const T scale = static_cast<T>(a.atol) + static_cast<T>(a.rtol) * (a0 > a1 ? a0 : a1);
+          local += static_cast<double>(
+              scaled_square(sqrt(v[comp].x * v[comp].x + v[comp].y * v[comp].y), scale));
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (q >= NQ) break;
+          const T r0 = fabs(n0[ridx[q]]), r1 = fabs(n_out[ridx[q]]);
           const T rs = static_cast<T>(a.atol) + static_cast<T>(a.rtol) * (r0 > r1 ? r0 : r1);
-          local += static_cast<double>(scaled_square(fabs(en), rs));
+          local += static_cast<double>(scaled_square(fabs(dsum[q]), rs));
         }
       }
     }
@@ -184,11 +330,12 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
     }
     return;
   }
-  if (a.forward) smem_fft<T, false, true>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
+  if (a.forward) smem_fft<T, false, true>(buf, tws, a.log2ny, lcc, CC, 1);
   if (a.mode == 1 && !a.forward) return;
-  for (int e = threadIdx.x; e < count; e += blockDim.x) {
-    const int c = e & (C - 1), i = e >> a.log2cols;
-    d[static_cast<long long>(i) * a.nx + x0 + c] = buf[i * C + c];
+  for (int e = threadIdx.x; e < all; e += blockDim.x) {
+    const int c2 = e & (CC - 1), i = e >> lcc;
+    const int comp = c2 >> a.log2cols, c = c2 & (C - 1);
+    d[comp * plane + static_cast<long long>(i) * a.nx + x0 + c] = buf[i * CC + c2];
   }
 }
 
@@ -199,7 +346,7 @@ cudaError_t launch_ifrk_row(const T* in, T* save, T* out, const T* tables, const
                             const T* twiddle, cudaStream_t stream) {
   using C2 = typename C2T<T>::type;
   const int blocks = a.ny / a.rows;
-  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.nx) + static_cast<size_t>(a.rows) * a.nx);
+  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.nx) + static_cast<size_t>(a.rows) * a.nx * a.comps);
   ifrk_row_kernel<T><<<dim3(blocks, 1, a.members), a.threads, smem, stream>>>(
       reinterpret_cast<const C2*>(in), reinterpret_cast<C2*>(save), reinterpret_cast<C2*>(out),
       reinterpret_cast<const C2*>(tables), reinterpret_cast<const C2*>(twiddle), a);
@@ -214,7 +361,7 @@ cudaError_t launch_ifrk_col(T* psi, const T* n0, T* dn_out, T* n_out, const T* p
                             const IfrkColArgs& a, cudaStream_t stream) {
   using C2 = typename C2T<T>::type;
   const int blocks = a.nx / a.cols;
-  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.ny) + static_cast<size_t>(a.cols) * a.ny);
+  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.ny) + static_cast<size_t>(a.cols) * a.ny * a.comps);
   ifrk_col_kernel<T><<<dim3(blocks, 1, a.members), a.threads, smem, stream>>>(
       reinterpret_cast<C2*>(psi), n0, dn_out, n_out,
       reinterpret_cast<C2*>(const_cast<T*>(psi_start)), reinterpret_cast<C2*>(const_cast<T*>(psi_new)),

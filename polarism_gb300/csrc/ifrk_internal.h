@@ -13,6 +13,7 @@ constexpr int kIfrkMaxStages = 7;  // dp5
 // [F_x^-1] -> out.  A source pointer equal to nullptr selects the freshly transformed row.
 struct IfrkRowArgs {
   int nx, ny, log2nx, rows, log2rows, threads, members;
+  int comps;                   // field components (1, or 2 for the spinor)
   int forward;                 // transform `in` along x first
   int inverse;                 // F_x^-1 before writing `out`
   int terms;
@@ -20,14 +21,32 @@ struct IfrkRowArgs {
   double coef[kIfrkMaxTerms];       // h a_ij (1 for psi0_hat)
   int table[kIfrkMaxTerms];         // index of the separable factor table (nx + ny complex)
   long long member_stride;          // complex values per member of a spectrum
+  // Spinor: the 2x2 Lawson factor exp(-i H(k) tau / hbar) is evaluated per mode from the
+  // per-member constants (FP64 phase angles) instead of separable tables.
+  int spinor;
+  double tau[kIfrkMaxTerms];        // tau of each term
+  double kx_unit, ky_unit;          // 2 pi / (n d) along x and y
+  double inv_n;                     // 1 / (nx ny): normalisation of the inverse transforms
+  const void* spin;                 // SpinorConst per member
+};
+
+// Per-member constants of the two-component Lawson factor (polarism/dispersion.py:34-83).
+struct SpinorConst {
+  double rate;      // hbar / 2m: E(k) / hbar = rate k^2
+  double half_z;    // Zeeman splitting / 2 (meV)
+  double beta;      // TE-TM coefficient
+  double inv_hbar;
 };
 
 // Column pass of one stage: F_y^-1 -> psi_i; n_i = n0 + sum coef_j dn_j; rhs_i; dn_i -> F_y.
 struct IfrkColArgs {
   int nx, ny, log2ny, cols, log2cols, threads, members;
+  int comps, log2comps;        // field components
+  int res_fields;              // 0 none, 1 single, 2 active + inactive
+  int res_comps;               // reservoir planes per field (1 shared or comps)
   int mode;                    // 0 stage RHS, 1 step end, 2 error norm, 3 forward only
   int inverse, forward;
-  int reservoir;               // single reservoir present
+  int reservoir;               // any reservoir present
   int potential;               // 0 none, 1 real, 2 complex
   int noise;                   // Wigner increment at the step end (mode 1)
   int terms;

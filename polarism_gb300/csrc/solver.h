@@ -21,6 +21,11 @@ struct pg_solver {
   size_t real_size = 4;
   long long plane = 0;     // nx * ny
   long long sites = 0;     // members * plane
+  int comps = 1;           // field components (2: circular-basis spinor)
+  int res_fields = 1;      // 0 none, 1 single reservoir, 2 active + inactive
+  int res_comps = 1;       // reservoir planes per field: 1 shared or = comps
+  long long field_values = 0;  // complex values of the state: members * comps * plane
+  long long res_values = 0;    // reals of the reservoir: res_fields * members * res_comps * plane
   void* psi[2] = {nullptr, nullptr};
   void* res[2] = {nullptr, nullptr};
   void* pump = nullptr;

@@ -19,6 +19,10 @@ struct SplitConst {
   T inv_hbar, g_C, g_R, R, gamma_C, gamma_R;
   T noise_a, noise_b;
   unsigned long long seed;
+  // Inactive-reservoir coupling, cross-spin term, double-reservoir rates and the pump share
+  // of each component (used by the IFRK passes).
+  T g_I, alpha_2, gamma_I, gamma_A, R_IA, R_AI;
+  T weight[2];
 };
 
 struct RowPassArgs {

@@ -50,6 +50,15 @@ class MemberPhysics:
     gamma_C: float = 0.083
     gamma_R: float = 0.005
     kinetic_relaxation_eta: float = 0.0
+    gamma_I: float = 0.001
+    gamma_A: float = 0.005
+    R_IA: float = 5e-2
+    R_AI: float = 2.5e-3
+    alpha_2: float = 0.0
+    zeeman: float = 0.0
+    te_tm: float = 0.0
+    pump_weight_plus: float = 0.5
+    pump_weight_minus: float = 0.5
 
     @classmethod
     def from_object(cls, physics, index=None):
@@ -84,20 +93,32 @@ class RK4Engine:
     fused RK4 kernels or the split-step Fourier passes."""
 
     def __init__(self, nx, ny, members, dx, dy, dt, physics, precision="single", reservoir=True,
-                 potential=_lib.PG_POT_NONE, pump_per_member=False, potential_per_member=False):
+                 potential=_lib.PG_POT_NONE, pump_per_member=False, potential_per_member=False,
+                 components=1, reservoir_components=None):
+        """``reservoir``: True/"single", False/"none" or "double" (active + inactive, IFRK only);
+        ``components``: 1, or 2 for a circular-basis spinor (IFRK only);
+        ``reservoir_components``: reservoir planes per field, 1 (shared) or ``components``."""
         self.lib = _lib.load()
         self.nx, self.ny, self.members = int(nx), int(ny), int(members)
         self.precision = precision
         self.real = np.float32 if precision == "single" else np.float64
         self.complex = np.complex64 if precision == "single" else np.complex128
-        self.reservoir = bool(reservoir)
+        kind = {True: "single", False: "none"}.get(reservoir, reservoir)
+        if kind not in ("none", "single", "double"):
+            raise ValueError(f"unknown reservoir {reservoir!r}")
+        self.res_fields = {"none": 0, "single": 1, "double": 2}[kind]
+        self.reservoir = self.res_fields > 0
+        self.components = int(components)
+        self.res_components = int(reservoir_components or self.components)
         self.potential_kind = int(potential)
         cfg = _lib.PgConfig(nx=self.nx, ny=self.ny, members=self.members,
                             precision=_lib.PG_SINGLE if precision == "single" else _lib.PG_DOUBLE,
-                            reservoir=_lib.PG_RES_SINGLE if reservoir else _lib.PG_RES_NONE,
+                            reservoir=self.res_fields,
                             potential=self.potential_kind, pump_per_member=int(pump_per_member),
                             potential_per_member=int(potential_per_member),
-                            dx=float(dx), dy=float(dy), dt=float(dt))
+                            dx=float(dx), dy=float(dy), dt=float(dt),
+                            components=self.components,
+                            reservoir_components=self.res_components)
         if isinstance(physics, (list, tuple)):
             plist = list(physics)
         else:
@@ -132,7 +153,14 @@ class RK4Engine:
 
     @property
     def shape(self):
-        return (self.members, 1, self.ny, self.nx)
+        return (self.members, self.components, self.ny, self.nx)
+
+    @property
+    def res_shape(self):
+        """Reservoir layout: (B, Cr, ny, nx) for one field, (2, B, Cr, ny, nx) for the
+        active and inactive fields of the double reservoir."""
+        plane = (self.members, self.res_components, self.ny, self.nx)
+        return plane if self.res_fields <= 1 else (self.res_fields,) + plane
 
     # -- data --------------------------------------------------------------------
     def set_state(self, psi, res=None):
@@ -150,7 +178,7 @@ class RK4Engine:
 
     def get_state(self, psi_out=None, res_out=None):
         psi = np.empty(self.shape, dtype=self.complex) if psi_out is None else psi_out
-        res = (np.empty(self.shape, dtype=self.real) if res_out is None else res_out) if self.reservoir else None
+        res = (np.empty(self.res_shape, dtype=self.real) if res_out is None else res_out) if self.reservoir else None
         p, dev, _ = _pointer(psi, self.complex, writable=True)
         r = _pointer(res, self.real, writable=True)[0] if res is not None else None
         _lib.check(self.lib.pg_get_state(self.handle, p, r, dev), "pg_get_state")

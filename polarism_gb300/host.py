@@ -84,6 +84,8 @@ class LaserParameters:
     y0: float = 0.0
     sigma_space: float = 15.0
     delay: float = 0.0
+    circular_polarization: float = 0.0
+    profile: dict = field(default_factory=dict)
 
 
 @dataclass
@@ -187,6 +189,40 @@ class ContinuousGaussian:
         return 0.0 if t < self.delay else self.P0
 
 
+class ProfileLaser:
+    """P(r, t) = P0 profile(r) for t >= delay with the ``gaussian`` and ``ring`` profiles
+    (``polarism/laser/profile_laser.py:26-52``, ``polarism/profiles/builtin_profiles.py:34-73``:
+    ring = exp(-((r - radius) / width)^2 / 2))."""
+
+    time_independent = True
+
+    def __init__(self, cfg: LaserParameters, X, Y, precision="double"):
+        spec = dict(cfg.profile)
+        kind = spec.get("type")
+        x0, y0 = float(spec.get("x0", cfg.x0)), float(spec.get("y0", cfg.y0))
+        r2 = (X - x0) ** 2 + (Y - y0) ** 2
+        if kind == "ring":
+            shape = np.exp(-0.5 * ((np.sqrt(r2) - float(spec["radius"])) / float(spec["width"])) ** 2)
+        elif kind == "gaussian":
+            shape = np.exp(-0.5 * r2 / float(spec["sigma"]) ** 2)
+        else:
+            raise ValueError(f"unsupported profile {kind!r}")
+        self.P0 = float(cfg.P0)
+        self.delay = float(cfg.delay)
+        self._spatial_envelope = shape.astype(real_dtype(precision), copy=False)
+
+    def power_coefficient(self, t: float) -> float:
+        return 0.0 if t < self.delay else self.P0
+
+
+def make_laser(cfg: LaserParameters, X, Y, precision="double"):
+    if cfg.laser_type == "profile":
+        return ProfileLaser(cfg, X, Y, precision)
+    if cfg.laser_type == "continuous-gaussian":
+        return ContinuousGaussian(cfg, X, Y, precision)
+    raise ValueError(f"unsupported laser_type {cfg.laser_type!r}")
+
+
 class PumpField:
     """Total pump with one cached separable (envelope, coefficient) term."""
 
@@ -247,10 +283,11 @@ class SingleReservoir:
 
     state_names = ("nR",)
 
-    def __init__(self, physics: PhysicsConstants, grid, precision="double", batch_size=None):
-        self.components = 1
+    def __init__(self, physics: PhysicsConstants, grid, precision="double", batch_size=None,
+                 components=1):
+        self.components = components
         self._dtype = real_dtype(precision)
-        self.nR = np.zeros((batch_size or 1, 1, *grid.shape), dtype=self._dtype)
+        self.nR = np.zeros((batch_size or 1, components, *grid.shape), dtype=self._dtype)
         self._batched = batch_size is not None
 
     def get_state(self):
@@ -270,6 +307,38 @@ class SingleReservoir:
 
     def get_inactive_density(self, state):
         return state[0] * 0.0
+
+
+class DoubleReservoir:
+    """Active and inactive reservoirs (``polarism/reservoir/double_reservoir.py:22-130``):
+    dn_I = P - (gamma_I + R_IA) n_I + R_AI n_A, dn_A = R_IA n_I - (gamma_A + R_AI + R |psi|^2) n_A;
+    both clamped at zero on set_state; one pair per field component or one shared pair."""
+
+    state_names = ("nA", "nI")
+
+    def __init__(self, physics: PhysicsConstants, grid, precision="double", batch_size=None,
+                 components=1):
+        self.components = components
+        self._dtype = real_dtype(precision)
+        shape = (batch_size or 1, components, *grid.shape)
+        self.nA = np.zeros(shape, dtype=self._dtype)
+        self.nI = np.zeros(shape, dtype=self._dtype)
+
+    def get_state(self):
+        return (self.nA, self.nI)
+
+    def set_state(self, state):
+        n_a, n_i = state
+        if n_a.shape != self.nA.shape or n_i.shape != self.nI.shape:
+            raise ValueError(f"reservoir state shapes must be {self.nA.shape}")
+        self.nA = np.maximum(n_a, 0).astype(self._dtype, copy=False)
+        self.nI = np.maximum(n_i, 0).astype(self._dtype, copy=False)
+
+    def get_active_density(self, state):
+        return state[0]
+
+    def get_inactive_density(self, state):
+        return state[1]
 
 
 class NoReservoir:
@@ -422,6 +491,7 @@ class Model:
     time_dependent_potential: bool = False
     reservoir_components: int = 1
     member_configs: list | None = None
+    pump_weights: Any = None
 
 
 def build_simulation(cfg: Config, members: list[Config] | None = None):
@@ -435,21 +505,35 @@ def build_simulation(cfg: Config, members: list[Config] | None = None):
     for m in member_cfgs:
         if m.noise.seed is None:
             m.noise.seed = cfg.noise.seed if cfg.noise.seed is not None else 0
-    lasers = [[ContinuousGaussian(m.laser, grid.X, grid.Y, precision)] for m in member_cfgs]
+    components = 2 if cfg.physics.spin == "spinor" else 1
+    res_components = cfg.reservoir.components or components
+    lasers = [[make_laser(m.laser, grid.X, grid.Y, precision)] for m in member_cfgs]
     pump = BatchedPumpField(lasers, grid, precision) if batched else PumpField(lasers[0], grid, precision)
-    res_cls = {"single": SingleReservoir, "none": NoReservoir}[cfg.reservoir.reservoir_type]
-    reservoir = res_cls(cfg.physics, grid, precision, batch_size=len(member_cfgs) if batched else None)
-    fields_ = [make_initial_psi(grid.shape, m.noise.initial_amplitude if m.noise.enabled else 0.0,
-                                m.noise.seed, complex_dtype(precision), real_dtype(precision),
+    res_cls = {"single": SingleReservoir, "double": DoubleReservoir,
+               "none": NoReservoir}[cfg.reservoir.reservoir_type]
+    reservoir = res_cls(cfg.physics, grid, precision, batch_size=len(member_cfgs) if batched else None,
+                        components=res_components)
+
+    def initial(m, seed):
+        return make_initial_psi(grid.shape, m.noise.initial_amplitude if m.noise.enabled else 0.0,
+                                seed, complex_dtype(precision), real_dtype(precision),
                                 m.noise.initial if m.noise.enabled else "none")
-               for m in member_cfgs]
-    field_ = np.stack(fields_)[:, None]
+
+    # The second component draws with seed + 1 (polarism/simulation_state.py:59-73).
+    field_ = np.stack([np.stack([initial(m, m.noise.seed + c) for c in range(components)])
+                       for m in member_cfgs])
     state = SimulationState(np.ascontiguousarray(field_), batched=batched)
     noise = NoiseParametersArrays(cfg, grid, member_cfgs)
+    weights = None
+    if components == 2:
+        weights = np.asarray([[(1 + m.laser.circular_polarization) / 2,
+                               (1 - m.laser.circular_polarization) / 2] for m in member_cfgs],
+                             dtype=real_dtype(precision)).reshape(len(member_cfgs), 2, 1, 1)
     model = Model(grid=grid, physics=BatchPhysicsLite(cfg.physics, member_cfgs), precision=precision,
                   potential=np.zeros((), dtype=real_dtype(precision)), pump=pump,
                   reservoir=reservoir, noise=noise if noise.active else None,
-                  member_configs=member_cfgs)
+                  member_configs=member_cfgs, components=components,
+                  reservoir_components=res_components, pump_weights=weights)
     return grid, model, state
 
 

@@ -46,17 +46,23 @@ class _GB300Solver(AbstractSolver):
 
     name = "gb300"
     injects_noise = True
+    #: Two-component fields and the double reservoir run on the IFRK passes only.
+    spinor_and_double = False
 
     def __init__(self, config, grid, model):
         super().__init__(config, grid, model)
-        if getattr(model, "components", 1) != 1:
+        self._components = int(getattr(model, "components", 1))
+        if self._components not in ((1, 2) if self.spinor_and_double else (1,)):
             raise ValueError(f"{self.name} (GB300) supports scalar fields only")
         if getattr(grid, "ndim", 2) != 2 or getattr(grid, "boundary", "periodic") != "periodic":
             raise ValueError(f"{self.name} (GB300) supports two-dimensional periodic grids")
         reservoir_type = getattr(getattr(config, "reservoir", None), "reservoir_type", "single")
-        if reservoir_type not in ("single", "none"):
+        allowed = ("single", "none", "double") if self.spinor_and_double else ("single", "none")
+        if reservoir_type not in allowed:
             raise ValueError(f"{self.name} (GB300) does not support reservoir_type={reservoir_type!r}")
         self._reservoir_type = reservoir_type
+        self._res_components = int(getattr(model, "reservoir_components", None)
+                                   or getattr(model.reservoir, "components", None) or 1)
         self._grid = grid
         self._precision = getattr(config.solver, "precision", "double")
         self._dt = float(config.solver.dt)
@@ -68,9 +74,15 @@ class _GB300Solver(AbstractSolver):
         _lib.load()
 
     # ------------------------------------------------------------------ helpers
-    def _physics_list(self, members):
+    def _physics_list(self, members, model=None):
         bp = self.batch_physics
-        return [MemberPhysics.from_object(bp, m) for m in range(members)]
+        out = [MemberPhysics.from_object(bp, m) for m in range(members)]
+        weights = getattr(model, "pump_weights", None) if model is not None else None
+        if weights is not None:
+            w = np.asarray(_host(weights), dtype=np.float64).reshape(-1, 2)
+            for m, phys in enumerate(out):
+                phys.pump_weight_plus, phys.pump_weight_minus = (float(v) for v in w[m if len(w) > 1 else 0])
+        return out
 
     def _ensure_engine(self, model, members, pump_env, potential):
         pump_per_member = np.ndim(pump_env) == 4 and pump_env.shape[0] > 1
@@ -85,10 +97,12 @@ class _GB300Solver(AbstractSolver):
                 self._engine.close()
             g = self._grid
             self._engine = RK4Engine(g.nx, g.ny, members, g.dx, g.dy, self._dt,
-                                     self._physics_list(members), self._precision,
-                                     reservoir=self._reservoir_type == "single", potential=pot_kind,
+                                     self._physics_list(members, model), self._precision,
+                                     reservoir=self._reservoir_type, potential=pot_kind,
                                      pump_per_member=pump_per_member,
-                                     potential_per_member=pot_per_member)
+                                     potential_per_member=pot_per_member,
+                                     components=self._components,
+                                     reservoir_components=self._res_components)
             self._engine_key = key
             self._pump_key = self._noise_key = self._potential_key = None
         return self._engine
@@ -177,7 +191,17 @@ class _GB300Solver(AbstractSolver):
     def _upload_state(self, engine, model, array):
         res_state = model.reservoir.get_state()
         device = _is_device(array)
-        res0 = res_state[0] if self._reservoir_type == "single" else None
+        if self._reservoir_type == "single":
+            res0 = res_state[0]
+        elif self._reservoir_type == "double":  # active then inactive, (2, B, Cr, ny, nx)
+            if device:
+                import torch
+
+                res0 = torch.stack(list(res_state))
+            else:
+                res0 = np.stack([np.asarray(f, dtype=engine.real) for f in res_state])
+        else:
+            res0 = None
         if res0 is not None:
             engine.set_state(array if device else np.ascontiguousarray(array, dtype=engine.complex),
                              res0 if device else np.ascontiguousarray(res0, dtype=engine.real))
@@ -198,6 +222,8 @@ class _GB300Solver(AbstractSolver):
     def _finish(self, model, state, res, n_steps):
         if self._reservoir_type == "single":
             model.reservoir.set_state((res,))
+        elif self._reservoir_type == "double":
+            model.reservoir.set_state((res[0], res[1]))
         state.step += n_steps
         state.t = state.t0 + state.step * self._dt
 
@@ -319,14 +345,16 @@ class IFRKFFTCudaSolver(_GB300Solver):
 
     name = "ifrk-fft-cuda"
     tableau_name = None
+    spinor_and_double = True
     capabilities = SolverCapabilities(
-        components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
-        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
+        components=frozenset({1, 2}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
+        reservoirs=frozenset({"single", "double", "none"}), custom_reservoirs="unsupported",
         potential=True, kinetic_relaxation=False, dispersion=frozenset({"parabolic"}),
         terms=False, noise=frozenset({"none", "wigner"}), adaptive=True,
-        quantitative_reservoirs=frozenset({"single", "none"}),
+        quantitative_reservoirs=frozenset({"single", "double", "none"}),
         description="GB300 Lawson IFRK (rk4, dp5) with fused Stockham stage passes, FP64 "
-                    "embedded error norm; nx, ny powers of two.")
+                    "embedded error norm, spinor (TE-TM, Zeeman, cross-spin) and double "
+                    "reservoirs; nx, ny powers of two.")
 
     def __init__(self, config, grid, model):
         super().__init__(config, grid, model)
@@ -358,7 +386,7 @@ class IFRKFFTCudaSolver(_GB300Solver):
         if n_steps <= 0:
             return
         field = state.field
-        self.batch_physics.check(field, 1)
+        self.batch_physics.check(field, self._components)
         engine, members, coefficient = self._prepare(model, state)
         device, res_in = self._upload_state(engine, model, field)
         engine.set_state_kind(False)
@@ -411,6 +439,8 @@ class IFRKFFTCudaSolver(_GB300Solver):
             state.field = psi
             if self._reservoir_type == "single":
                 model.reservoir.set_state((res,))
+            elif self._reservoir_type == "double":
+                model.reservoir.set_state((res[0], res[1]))
             state.t += dt
         return StepReport(accepted, err, None)
 
