@@ -464,6 +464,130 @@ def run_sweep_bench(args):
         print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- spinor leg
+SPINOR_N = 512
+SPINOR_L = 128.0          # um: dx = 0.25 um, the ring (r = 30, w = 4) well inside the box
+SPINOR_TE_TM = 0.05       # meV um^2 (the config leaves beta open; this value is ours)
+
+
+def spinor_setup(precision="single"):
+    """Config 3: circular-basis spinor with TE-TM (beta = 0.05 meV um^2), Zeeman 0.05 meV,
+    alpha_2 = -0.1 g_C, double reservoir per component, ring pump (r = 30 um, w = 4 um),
+    linear polarisation, P0 = 1.5 x threshold (the double-reservoir threshold with n_A = gamma_C/R
+    at psi = 0 and half the pump per component), 512^2 periodic, lx = ly = 128 um."""
+    from polarism_gb300 import host
+
+    cfg = host.Config()
+    cfg.grid.nx = cfg.grid.ny = SPINOR_N
+    cfg.grid.lx = cfg.grid.ly = SPINOR_L
+    cfg.solver.precision, cfg.solver.dt, cfg.solver.tableau = precision, 0.1, "dp5"
+    cfg.solver.adaptive, cfg.solver.rtol, cfg.solver.atol = True, 1e-6, 1e-8
+    cfg.reservoir.reservoir_type = "double"
+    ph = cfg.physics
+    ph.spin, ph.zeeman, ph.te_tm, ph.alpha_2 = "spinor", 0.05, SPINOR_TE_TM, -0.1 * ph.g_C
+    n_a = ph.gamma_C / ph.R
+    per_component = ((ph.gamma_I + ph.R_IA) * (ph.gamma_A + ph.R_AI) / ph.R_IA - ph.R_AI) * n_a
+    p_th = 2.0 * per_component
+    cfg.laser.laser_type, cfg.laser.P0 = "profile", 1.5 * p_th
+    cfg.laser.profile = {"type": "ring", "radius": 30.0, "width": 4.0}
+    cfg.laser.circular_polarization = 0.0
+    cfg.noise.seed = 0
+    return cfg, p_th
+
+
+def run_spinor_bench(args):
+    """Adaptive DP5 spinor run to --spinor-time ps with FP64 observable accumulation every ps
+    after the first fifth of the run; device-resident (engine API)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from polarism_gb300 import build as _build
+
+    _build.build()
+    from polarism_gb300 import host
+    from polarism_gb300.engine import TABLEAU_NODES, Engine, MemberPhysics
+    from polarism_gb300.step_control import StepController
+
+    cfg, p_th = spinor_setup()
+    grid, model, state = host.build_simulation(cfg)
+    phys = MemberPhysics.from_object(cfg.physics)
+    phys.pump_weight_plus = phys.pump_weight_minus = 0.5
+    eng = Engine(grid.nx, grid.ny, 1, grid.dx, grid.dy, cfg.solver.dt, phys, "single",
+                 reservoir="double", components=2, reservoir_components=2)
+    eng.set_pump(model.pump.lasers[0]._spatial_envelope.astype(np.float32))
+    eng.set_state(state.field.astype(np.complex64),
+                  np.stack([f.astype(np.float32) for f in model.reservoir.get_state()]))
+    ctl = StepController(cfg.solver.dt)
+    nodes = TABLEAU_NODES["dp5"]
+    scales = np.full((len(nodes), 1), cfg.laser.P0)
+    total = float(args.spinor_time)
+    sample_from = 0.2 * total
+    sites = 2 * grid.nx * grid.ny
+    t, next_sample, samples = 0.0, sample_from, 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sampler = ClockSampler(local)
+    sampler.start()
+    while t < total - 1e-12:
+        target = min(total, math.floor(t + 1.0 + 1e-9))
+        while t < target - 1e-12:
+            h, clamped, proposal = ctl.propose(t, target)
+            err, acc = eng.ifrk_trial(h, scales, cfg.solver.rtol, cfg.solver.atol)
+            if acc:
+                t = target if clamped else t + h
+            ctl.update(h, clamped, proposal, acc, err)
+        if t >= next_sample - 1e-9:
+            eng.accumulate(density=True, momentum=True)
+            samples += 1
+            next_sample += 1.0
+    eng.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    norms = eng.norms()
+    line = {
+        "metric": "spinor DP5 accepted site-updates/s (config 3)",
+        "value": ctl.accepted * sites / wall, "unit": "site-updates/s", "n_gpus": world,
+        "higher_is_better": True, "dtype": "f32 state, f64 error norm and observables",
+        "data": "synthetic",
+        "config": {"workload": "spinor 512^2, lx=ly=128 um, TE-TM beta=0.05 meV um^2, Zeeman 0.05 meV, "
+                               "alpha_2=-0.1 g_C, double reservoir per component, ring r=30 w=4, "
+                               "linear polarisation, P0=1.5 P_th, IFRK dp5 rtol 1e-6",
+                   "p_th": p_th, "P0": cfg.laser.P0, "t_end_ps": t},
+        "wall_s": wall, "ps_per_s": t / wall, "trials_accepted": ctl.accepted,
+        "trials_rejected": ctl.rejected, "observable_samples": samples,
+        "final_norm": float(norms[0]), "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = spinor_cpu_baseline(cfg, grid, model, state)
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def spinor_cpu_baseline(cfg, grid, model, state, trials=2):
+    """FP64 NumPy oracle (the reference's generic Lawson path restated) on one core: a bounded
+    sample of adaptive DP5 trials of the same 512^2 spinor."""
+    from oracle import gpe
+
+    p = {k: getattr(cfg.physics, k) for k in ("hbar", "m_eff", "g_C", "g_R", "g_I", "R", "gamma_C",
+                                              "gamma_R", "gamma_I", "gamma_A", "R_IA", "R_AI",
+                                              "alpha_2", "zeeman", "te_tm")}
+    spin = {"kx": grid.KX, "ky": grid.KY, "weights": model.pump_weights.reshape(-1, 2)}
+    pump = model.pump.lasers[0]._spatial_envelope * cfg.laser.P0
+    st = gpe.IFRKState(psi=state.field.astype(np.complex128),
+                       fields=tuple(f.astype(np.float64) for f in model.reservoir.get_state()))
+    t0 = time.perf_counter()
+    for _ in range(trials):
+        gpe.ifrk_step(st, cfg.solver.dt, gpe.DP5_TABLEAU, lambda t: pump, 0.0, p, grid.k_squared,
+                      grid.dx, grid.dy, kind="double", adaptive=True, rtol=1e-6, atol=1e-8,
+                      spinor=spin)
+    elapsed = time.perf_counter() - t0
+    sites = 2 * grid.nx * grid.ny
+    return {"value": trials * sites / elapsed, "unit": "site-updates/s", "cores": 1, "kind": "port",
+            "sample": f"{trials} DP5 trials of the 512^2 spinor, FP64 NumPy oracle, 1 thread"}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -474,14 +598,19 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=8)
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["rk4", "sweep"], default="rk4",
-                    help="rk4: the 1024^2 fused-step benchmark; sweep: the uneven-size sweep")
+    ap.add_argument("--workload", choices=["rk4", "sweep", "spinor"], default="rk4",
+                    help="rk4: the 1024^2 fused-step benchmark; sweep: the uneven-size sweep; "
+                         "spinor: the adaptive two-component IFRK run")
+    ap.add_argument("--spinor-time", type=float, default=500.0)
     ap.add_argument("--steady-time", type=float, default=0.0,
                     help="sweep workload: also run to steady state (up to this many ps)")
     ap.add_argument("--freeze-stopped", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.workload == "spinor":
+        run_spinor_bench(args)
+        return
     if args.workload == "sweep":
         if args.members == 32 and "--members" not in sys.argv:
             args.members = 256

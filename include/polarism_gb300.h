@@ -256,6 +256,46 @@ int pg_sweep_synchronize(pg_sweep* w);
 /* Per-member steady-state comparison with the previous call, as pg_steady_check. */
 int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, double* norms);
 
+/* Learned warm start (no counterpart in the reference: Polarism has no learned component).
+ * Kernels of a Fourier neural operator trained on solver-made steady states.  All run
+ * asynchronously on `stream` (a cudaStream_t) on caller-owned device arrays.
+ *
+ * pg_gemm_bf16: C = alpha op(A) op(B) + beta C for `batch` matrices (element strides
+ * strideA/B/C), A, B row-major BF16 (op = transpose when transA/transB: A stored K x M, B stored
+ * N x K), C row-major FP32, FP32 accumulation on the tensor cores. */
+int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
+                 int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
+                 int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, void* stream);
+/* y = bf16(x) (round to nearest even). */
+int pg_fno_to_bf16(const float* x, void* y, int64_t n, void* stream);
+/* u[b, c, :] += bias[c] (bias may be NULL); act = GELU(u) (tanh form) if gelu else u, written to
+ * act (FP32) and/or act_bf16 when not NULL.  C channels of `plane` values. */
+int pg_fno_bias_act(float* u, const float* bias, float* act, void* act_bf16, int32_t C, int64_t plane,
+                    int64_t n, int32_t gelu, void* stream);
+/* grad_pre = grad_act * GELU'(pre) (FP32 and/or BF16 outputs). */
+int pg_fno_gelu_backward(const float* pre, const float* grad_act, float* grad_pre, void* grad_bf16,
+                         int64_t n, void* stream);
+/* out[c] (+)= sum over b and the plane of x[b, c, :]. */
+int pg_fno_channel_sum(const float* x, float* out, int32_t B, int32_t C, int64_t plane, int32_t accumulate,
+                       void* stream);
+/* Per-mode complex mixing of the kept spectrum: out[b, o, k] = sum_i y[b, i, k] w[k, i, o].
+ * Spectra are [b][channel][ky (2 modes)][kx re (modes) | kx im (modes)]; BF16 weights
+ * [ky][kx][in][out] as separate real and imaginary arrays. */
+int pg_fno_mode_mix(const float* y, const void* wre, const void* wim, float* out, int32_t B, int32_t cin,
+                    int32_t cout, int32_t modes, void* stream);
+/* Adjoints: dy = dout conj(w) (if dy != NULL), dw = conj(y) dout summed over b (if dwre/dwim). */
+int pg_fno_mode_mix_backward(const float* y, const float* dout, const void* wre, const void* wim, float* dy,
+                             float* dwre, float* dwim, int32_t B, int32_t cin, int32_t cout, int32_t modes,
+                             void* stream);
+/* Adam on FP32 weights (bias-corrected, optional L2 decay), refreshing the BF16 copy. */
+int pg_fno_adam(float* w, const float* g, float* m1, float* m2, void* w_bf16, int64_t n, float lr,
+                float beta1, float beta2, float eps, int64_t step, float decay, void* stream);
+/* Weighted squared error over C channels of `plane` values: grad = 2 w_c (pred - target) scale;
+ * per-block FP64 partial sums of w_c (pred - target)^2 in partials (blocks_used entries). */
+int pg_fno_mse(const float* pred, const float* target, const float* weight, int32_t C, int64_t plane,
+               float* grad, void* grad_bf16, double* partials, int32_t max_partials, int64_t n, float scale,
+               int32_t* blocks_used, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,19 @@ SIGNATURES = {
     "pg_sweep_last_launch_count": (_i64, [_vp]),
     "pg_sweep_synchronize": (C.c_int, [_vp]),
     "pg_sweep_steady_check": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pg_gemm_bf16": (C.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _i32,
+                               C.c_float, C.c_float, _i32, _i64, _i64, _i64, _vp]),
+    "pg_fno_to_bf16": (C.c_int, [_vp, _vp, _i64, _vp]),
+    "pg_fno_bias_act": (C.c_int, [_vp, _vp, _vp, _vp, _i32, _i64, _i64, _i32, _vp]),
+    "pg_fno_gelu_backward": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _vp]),
+    "pg_fno_channel_sum": (C.c_int, [_vp, _vp, _i32, _i32, _i64, _i32, _vp]),
+    "pg_fno_mode_mix": (C.c_int, [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "pg_fno_mode_mix_backward": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32,
+                                           _i32, _vp]),
+    "pg_fno_adam": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, C.c_float, C.c_float, C.c_float,
+                              C.c_float, _i64, C.c_float, _vp]),
+    "pg_fno_mse": (C.c_int, [_vp, _vp, _vp, _i32, _i64, _vp, _vp, _vp, _i32, _i64, C.c_float,
+                             C.POINTER(_i32), _vp]),
 }
 
 _lock = threading.Lock()

@@ -1,0 +1,451 @@
+// Kernels of the learned warm start: a BF16 tensor-core GEMM with FP32 accumulation and the
+// elementwise, mode-mixing and optimiser kernels of a Fourier neural operator.
+//
+// Every linear map of the network -- the pointwise channel mixes, the truncated DFTs along x
+// and y that replace the FFTs of the spectral convolution, and their adjoints in the backward
+// pass -- is a (batched, strided, optionally transposed) GEMM C = alpha op(A) op(B) + beta C
+// with BF16 operands and FP32 accumulators.  The per-mode complex mixing of the spectral
+// layer is a small batched contraction done in FP32 on the CUDA cores.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "pg_internal.h"
+
+namespace pg {
+namespace {
+
+constexpr int kBM = 64, kBN = 64, kBK = 32, kPad = 8;
+
+struct GemmArgs {
+  const __nv_bfloat16* A;
+  const __nv_bfloat16* B;
+  float* C;
+  int M, N, K, lda, ldb, ldc, transA, transB;
+  float alpha, beta;
+  long long sA, sB, sC;
+};
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// 64x64 output tile per block of 4 warps (2x2, 32x32 each); K staged 32 at a time through
+// shared memory as [row][k] for A and [col][k] for B (k contiguous), the operand orders of
+// the m16n8k16 fragments.  Out-of-range elements are staged as zero.
+__global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
+  __shared__ __align__(16) __nv_bfloat16 As[kBM][kBK + kPad];
+  __shared__ __align__(16) __nv_bfloat16 Bs[kBN][kBK + kPad];
+  const long long bz = blockIdx.z;
+  const __nv_bfloat16* A = g.A + bz * g.sA;
+  const __nv_bfloat16* B = g.B + bz * g.sB;
+  float* C = g.C + bz * g.sC;
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int gq = lane >> 2, tq = lane & 3;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+  for (int k0 = 0; k0 < g.K; k0 += kBK) {
+    for (int e = tid; e < kBM * kBK; e += 128) {
+      int m, k;
+      if (!g.transA) {
+        m = e / kBK;
+        k = e % kBK;
+      } else {
+        k = e / kBM;
+        m = e % kBM;
+      }
+      const int gm = m0 + m, gk = k0 + k;
+      __nv_bfloat16 v = zero;
+      if (gm < g.M && gk < g.K)
+        v = g.transA ? A[static_cast<long long>(gk) * g.lda + gm] : A[static_cast<long long>(gm) * g.lda + gk];
+      As[m][k] = v;
+    }
+    for (int e = tid; e < kBN * kBK; e += 128) {
+      int n, k;
+      if (g.transB) {
+        n = e / kBK;
+        k = e % kBK;
+      } else {
+        k = e / kBN;
+        n = e % kBN;
+      }
+      const int gn = n0 + n, gk = k0 + k;
+      __nv_bfloat16 v = zero;
+      if (gn < g.N && gk < g.K)
+        v = g.transB ? B[static_cast<long long>(gn) * g.ldb + gk] : B[static_cast<long long>(gk) * g.ldb + gn];
+      Bs[n][k] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kBK; kk += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r = wm + i * 16 + gq;
+        af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * tq]);
+        af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * tq]);
+        af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * tq + 8]);
+        af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * tq + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = wn + j * 8 + gq;
+        bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * tq]);
+        bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * tq + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = m0 + wm + i * 16 + gq + 8 * h;
+        if (r >= g.M) continue;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int c = n0 + wn + j * 8 + 2 * tq + q;
+          if (c >= g.N) continue;
+          float* dst = C + static_cast<long long>(r) * g.ldc + c;
+          const float v = g.alpha * acc[i][j][2 * h + q];
+          *dst = g.beta == 0.f ? v : v + g.beta * *dst;
+        }
+      }
+    }
+  }
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ x, __nv_bfloat16* __restrict__ y, long long n) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    y[i] = __float2bfloat16_rn(x[i]);
+}
+
+constexpr float kGeluC = 0.7978845608028654f;  // sqrt(2 / pi)
+
+__device__ __forceinline__ float gelu_f(float x) {
+  return 0.5f * x * (1.f + tanhf(kGeluC * (x + 0.044715f * x * x * x)));
+}
+
+__device__ __forceinline__ float gelu_grad_f(float x) {
+  const float t = tanhf(kGeluC * (x + 0.044715f * x * x * x));
+  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * kGeluC * (1.f + 3.f * 0.044715f * x * x);
+}
+
+// u[b, c, p] += bias[c]; act = gelu(u) (or u) in FP32 and, optionally, in BF16.
+__global__ void bias_act_kernel(float* __restrict__ u, const float* __restrict__ bias,
+                                float* __restrict__ act, __nv_bfloat16* __restrict__ act_bf,
+                                int C, long long plane, long long n, int gelu) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>((i / plane) % C);
+    const float v = u[i] + (bias ? bias[c] : 0.f);
+    u[i] = v;
+    const float a = gelu ? gelu_f(v) : v;
+    if (act) act[i] = a;
+    if (act_bf) act_bf[i] = __float2bfloat16_rn(a);
+  }
+}
+
+// g_pre = g_act * gelu'(pre), also in BF16.
+__global__ void gelu_back_kernel(const float* __restrict__ pre, const float* __restrict__ g_act,
+                                 float* __restrict__ g_pre, __nv_bfloat16* __restrict__ g_bf, long long n) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float v = g_act[i] * gelu_grad_f(pre[i]);
+    if (g_pre) g_pre[i] = v;
+    if (g_bf) g_bf[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// out[c] = (accumulate ? out[c] : 0) + sum over b, p of x[b, c, p]; one block per channel.
+__global__ void channel_sum_kernel(const float* __restrict__ x, float* __restrict__ out, int B, int C,
+                                   long long plane, int accumulate) {
+  __shared__ float red[32];
+  const int c = blockIdx.x;
+  float s = 0.f;
+  for (int b = 0; b < B; ++b) {
+    const float* p = x + (static_cast<long long>(b) * C + c) * plane;
+    for (long long i = threadIdx.x; i < plane; i += blockDim.x) s += p[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) out[c] = (accumulate ? out[c] : 0.f) + v;
+  }
+}
+
+// Spectra are stored [b][channel][ky (2m)][kx re (m) | kx im (m)]; weights [ky][kx][in][out].
+__global__ void mode_mix_kernel(const float* __restrict__ y, const __nv_bfloat16* __restrict__ wre,
+                                const __nv_bfloat16* __restrict__ wim, float* __restrict__ out,
+                                int B, int cin, int cout, int m) {
+  const long long total = static_cast<long long>(B) * cout * 2 * m * m;
+  const int mm = 2 * m * m;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int mode = static_cast<int>(t % mm);
+    const int o = static_cast<int>((t / mm) % cout);
+    const int b = static_cast<int>(t / (static_cast<long long>(mm) * cout));
+    const int ky = mode / m, kx = mode % m;
+    float re = 0.f, im = 0.f;
+    const float* yb = y + static_cast<long long>(b) * cin * 4 * m * m + ky * 2 * m;
+    const long long wbase = (static_cast<long long>(ky) * m + kx) * cin * cout + o;
+    for (int i = 0; i < cin; ++i) {
+      const float a = yb[static_cast<long long>(i) * 4 * m * m + kx];
+      const float c = yb[static_cast<long long>(i) * 4 * m * m + m + kx];
+      const float r = __bfloat162float(wre[wbase + static_cast<long long>(i) * cout]);
+      const float s = __bfloat162float(wim[wbase + static_cast<long long>(i) * cout]);
+      re += a * r - c * s;
+      im += a * s + c * r;
+    }
+    float* ob = out + (static_cast<long long>(b) * cout + o) * 4 * m * m + ky * 2 * m;
+    ob[kx] = re;
+    ob[m + kx] = im;
+  }
+}
+
+// dY[b, i] = sum_o dO[b, o] conj(W[i, o]) per mode.
+__global__ void mode_mix_back_input_kernel(const float* __restrict__ dout, const __nv_bfloat16* __restrict__ wre,
+                                           const __nv_bfloat16* __restrict__ wim, float* __restrict__ dy,
+                                           int B, int cin, int cout, int m) {
+  const long long total = static_cast<long long>(B) * cin * 2 * m * m;
+  const int mm = 2 * m * m;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int mode = static_cast<int>(t % mm);
+    const int i = static_cast<int>((t / mm) % cin);
+    const int b = static_cast<int>(t / (static_cast<long long>(mm) * cin));
+    const int ky = mode / m, kx = mode % m;
+    float re = 0.f, im = 0.f;
+    const float* gb = dout + static_cast<long long>(b) * cout * 4 * m * m + ky * 2 * m;
+    const long long wbase = ((static_cast<long long>(ky) * m + kx) * cin + i) * cout;
+    for (int o = 0; o < cout; ++o) {
+      const float gr = gb[static_cast<long long>(o) * 4 * m * m + kx];
+      const float gi = gb[static_cast<long long>(o) * 4 * m * m + m + kx];
+      const float r = __bfloat162float(wre[wbase + o]);
+      const float s = __bfloat162float(wim[wbase + o]);
+      re += gr * r + gi * s;
+      im += gi * r - gr * s;
+    }
+    float* db = dy + (static_cast<long long>(b) * cin + i) * 4 * m * m + ky * 2 * m;
+    db[kx] = re;
+    db[m + kx] = im;
+  }
+}
+
+// dW[i, o] = sum_b conj(Y[b, i]) dO[b, o] per mode (overwrites).
+__global__ void mode_mix_back_weight_kernel(const float* __restrict__ y, const float* __restrict__ dout,
+                                            float* __restrict__ dwre, float* __restrict__ dwim,
+                                            int B, int cin, int cout, int m) {
+  const long long total = static_cast<long long>(2 * m) * m * cin * cout;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int o = static_cast<int>(t % cout);
+    const int i = static_cast<int>((t / cout) % cin);
+    const int mode = static_cast<int>(t / (static_cast<long long>(cout) * cin));
+    const int ky = mode / m, kx = mode % m;
+    float re = 0.f, im = 0.f;
+    for (int b = 0; b < B; ++b) {
+      const float* yb = y + (static_cast<long long>(b) * cin + i) * 4 * m * m + ky * 2 * m;
+      const float* gb = dout + (static_cast<long long>(b) * cout + o) * 4 * m * m + ky * 2 * m;
+      const float a = yb[kx], c = yb[m + kx];
+      const float gr = gb[kx], gi = gb[m + kx];
+      re += a * gr + c * gi;
+      im += a * gi - c * gr;
+    }
+    dwre[t] = re;
+    dwim[t] = im;
+  }
+}
+
+// Adam on FP32 master weights; the BF16 copy the GEMMs read is refreshed in the same pass.
+__global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m1,
+                            float* __restrict__ m2, __nv_bfloat16* __restrict__ w_bf, long long n,
+                            float lr, float b1, float b2, float eps, float c1, float c2, float decay) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float gi = g[i] + decay * w[i];
+    const float a = b1 * m1[i] + (1.f - b1) * gi;
+    const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+    m1[i] = a;
+    m2[i] = b;
+    const float v = w[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+    w[i] = v;
+    if (w_bf) w_bf[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// Weighted squared error: grad = 2 w (pred - target) / count, per-block FP64 partial sums.
+__global__ void mse_kernel(const float* __restrict__ pred, const float* __restrict__ target,
+                           const float* __restrict__ weight, int C, long long plane,
+                           float* __restrict__ grad, __nv_bfloat16* __restrict__ grad_bf,
+                           double* __restrict__ partial, long long n, float scale) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float wc = weight ? weight[(i / plane) % C] : 1.f;
+    const float d = pred[i] - target[i];
+    s += static_cast<double>(wc) * d * d;
+    const float gv = 2.f * wc * d * scale;
+    if (grad) grad[i] = gv;
+    if (grad_bf) grad_bf[i] = __float2bfloat16_rn(gv);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
+  }
+}
+
+int grid_for(long long n) {
+  const long long b = (n + 255) / 256;
+  return static_cast<int>(b < 1 ? 1 : (b > 4096 ? 4096 : b));
+}
+
+}  // namespace
+}  // namespace pg
+
+extern "C" {
+
+int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
+                 int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
+                 int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, void* stream) {
+  PG_CHECK(A && B && C, PG_ERR_INVALID, "pg_gemm_bf16: null operand");
+  PG_CHECK(M >= 0 && N >= 0 && K >= 0 && batch >= 1, PG_ERR_INVALID, "pg_gemm_bf16: bad sizes");
+  PG_CHECK(lda >= (transA ? M : K) && ldb >= (transB ? K : N) && ldc >= N, PG_ERR_INVALID,
+           "pg_gemm_bf16: leading dimension smaller than the row");
+  PG_CHECK(batch <= 65535 && (M + pg::kBM - 1) / pg::kBM <= 65535, PG_ERR_INVALID,
+           "pg_gemm_bf16: grid too large");
+  if (M == 0 || N == 0) return PG_OK;
+  pg::GemmArgs g{static_cast<const __nv_bfloat16*>(A), static_cast<const __nv_bfloat16*>(B), C, M, N, K,
+                 lda, ldb, ldc, transA ? 1 : 0, transB ? 1 : 0, alpha, beta, strideA, strideB, strideC};
+  dim3 grid((N + pg::kBN - 1) / pg::kBN, (M + pg::kBM - 1) / pg::kBM, batch);
+  pg::gemm_bf16_kernel<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(g);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_to_bf16(const float* x, void* y, int64_t n, void* stream) {
+  PG_CHECK(x && y && n >= 0, PG_ERR_INVALID, "pg_fno_to_bf16: bad argument");
+  if (n == 0) return PG_OK;
+  pg::to_bf16_kernel<<<pg::grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      x, static_cast<__nv_bfloat16*>(y), n);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_bias_act(float* u, const float* bias, float* act, void* act_bf16, int32_t C, int64_t plane,
+                    int64_t n, int32_t gelu, void* stream) {
+  PG_CHECK(u && C > 0 && plane > 0 && n >= 0, PG_ERR_INVALID, "pg_fno_bias_act: bad argument");
+  if (n == 0) return PG_OK;
+  pg::bias_act_kernel<<<pg::grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      u, bias, act, static_cast<__nv_bfloat16*>(act_bf16), C, plane, n, gelu);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_gelu_backward(const float* pre, const float* grad_act, float* grad_pre, void* grad_bf16,
+                         int64_t n, void* stream) {
+  PG_CHECK(pre && grad_act && n >= 0, PG_ERR_INVALID, "pg_fno_gelu_backward: bad argument");
+  if (n == 0) return PG_OK;
+  pg::gelu_back_kernel<<<pg::grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      pre, grad_act, grad_pre, static_cast<__nv_bfloat16*>(grad_bf16), n);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_channel_sum(const float* x, float* out, int32_t B, int32_t C, int64_t plane, int32_t accumulate,
+                       void* stream) {
+  PG_CHECK(x && out && B > 0 && C > 0 && plane > 0, PG_ERR_INVALID, "pg_fno_channel_sum: bad argument");
+  pg::channel_sum_kernel<<<C, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, out, B, C, plane, accumulate);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_mode_mix(const float* y, const void* wre, const void* wim, float* out, int32_t B, int32_t cin,
+                    int32_t cout, int32_t modes, void* stream) {
+  PG_CHECK(y && wre && wim && out && B > 0 && cin > 0 && cout > 0 && modes > 0, PG_ERR_INVALID,
+           "pg_fno_mode_mix: bad argument");
+  const long long total = static_cast<long long>(B) * cout * 2 * modes * modes;
+  pg::mode_mix_kernel<<<pg::grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      y, static_cast<const __nv_bfloat16*>(wre), static_cast<const __nv_bfloat16*>(wim), out, B, cin, cout, modes);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_mode_mix_backward(const float* y, const float* dout, const void* wre, const void* wim, float* dy,
+                             float* dwre, float* dwim, int32_t B, int32_t cin, int32_t cout, int32_t modes,
+                             void* stream) {
+  PG_CHECK(y && dout && wre && wim && B > 0 && cin > 0 && cout > 0 && modes > 0, PG_ERR_INVALID,
+           "pg_fno_mode_mix_backward: bad argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (dy) {
+    const long long total = static_cast<long long>(B) * cin * 2 * modes * modes;
+    pg::mode_mix_back_input_kernel<<<pg::grid_for(total), 256, 0, st>>>(
+        dout, static_cast<const __nv_bfloat16*>(wre), static_cast<const __nv_bfloat16*>(wim), dy, B, cin, cout,
+        modes);
+  }
+  if (dwre && dwim) {
+    const long long total = static_cast<long long>(2 * modes) * modes * cin * cout;
+    pg::mode_mix_back_weight_kernel<<<pg::grid_for(total), 256, 0, st>>>(y, dout, dwre, dwim, B, cin, cout,
+                                                                         modes);
+  }
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_adam(float* w, const float* g, float* m1, float* m2, void* w_bf16, int64_t n, float lr,
+                float beta1, float beta2, float eps, int64_t step, float decay, void* stream) {
+  PG_CHECK(w && g && m1 && m2 && n >= 0 && step >= 1, PG_ERR_INVALID, "pg_fno_adam: bad argument");
+  if (n == 0) return PG_OK;
+  const float c1 = 1.f - std::pow(beta1, static_cast<float>(step));
+  const float c2 = 1.f - std::pow(beta2, static_cast<float>(step));
+  pg::adam_kernel<<<pg::grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      w, g, m1, m2, static_cast<__nv_bfloat16*>(w_bf16), n, lr, beta1, beta2, eps, c1, c2, decay);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_fno_mse(const float* pred, const float* target, const float* weight, int32_t C, int64_t plane,
+               float* grad, void* grad_bf16, double* partials, int32_t max_partials, int64_t n, float scale,
+               int32_t* blocks_used, void* stream) {
+  PG_CHECK(pred && target && partials && blocks_used && n > 0 && C > 0 && plane > 0, PG_ERR_INVALID,
+           "pg_fno_mse: bad argument");
+  int blocks = pg::grid_for(n);
+  if (blocks > max_partials) blocks = max_partials;
+  PG_CHECK(blocks >= 1, PG_ERR_INVALID, "pg_fno_mse: no partial slots");
+  pg::mse_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      pred, target, weight, C, plane, grad, static_cast<__nv_bfloat16*>(grad_bf16), partials, n, scale);
+  PG_CUDA(cudaGetLastError());
+  *blocks_used = blocks;
+  return PG_OK;
+}
+
+}  // extern "C"
