@@ -588,6 +588,62 @@ def spinor_cpu_baseline(cfg, grid, model, state, trials=2):
             "sample": f"{trials} DP5 trials of the 512^2 spinor, FP64 NumPy oracle, 1 thread"}
 
 
+# ----------------------------------------------------------------------------- warm-start leg
+def run_fno_bench(args):
+    """Config 5: solver-made steady states of random pumps at --fno-n^2, FNO training with the
+    BF16 tensor-core kernels, then held-out members started plain and warm (time to the
+    steady-state criterion, steady density within 1e-3)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from polarism_gb300 import build as _build
+
+    _build.build()
+    from polarism_gb300 import warmstart as ws
+
+    n = args.fno_n
+    train_cfgs = ws.pump_members(args.fno_train, seed=11, n=n, total_time=args.fno_time, dt=args.fno_dt)
+    test_cfgs = ws.pump_members(args.fno_test, seed=12, n=n, total_time=args.fno_time, dt=args.fno_dt)
+    t0 = time.perf_counter()
+    data = ws.run_uniform(train_cfgs)
+    gen_s = time.perf_counter() - t0
+    # Lasing members that became stationary (decayed members have nothing to learn).
+    keep = np.isfinite(data.stop_times) & (data.final_norms > 1e-6)
+    a = ws.features([c for c, k in zip(train_cfgs, keep) if k])
+    y = ws.targets([p for p, k in zip(data.psi, keep) if k], [r for r, k in zip(data.reservoir, keep) if k])
+    model = ws.WarmStart(n, width=args.fno_width, modes=args.fno_modes)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    losses = model.fit(a, y, epochs=args.fno_epochs, batch=args.fno_batch, lr=args.fno_lr)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    plain = ws.run_uniform(test_cfgs)
+    ev = ws.evaluate(model, test_cfgs, plain)
+    valid = np.isfinite(ev.plain_time) & (plain.final_norms > 1e-6)
+    line = {
+        "metric": "sweep time-to-steady-state, plain start / warm start (config 5)",
+        "value": ev.speedup_time, "unit": "x (simulated time)", "n_gpus": world,
+        "higher_is_better": True, "dtype": "f32 solver, bf16 network with f32 accumulate",
+        "data": "synthetic (solver-generated steady states)",
+        "config": {"workload": f"{n}^2, lx=ly=128 um, dt={args.fno_dt} ps, pumps gaussian/ring/square lattice, "
+                               "P0 in [1,3] P_th, rtol 1e-6 per 10 ps, FNO width "
+                               f"{args.fno_width} modes {args.fno_modes} 4 layers",
+                   "train_members": len(train_cfgs), "train_steady": int(keep.sum()),
+                   "test_members": len(test_cfgs), "test_plain_steady": int(valid.sum()),
+                   "epochs": args.fno_epochs, "batch": args.fno_batch},
+        "speedup_wall": ev.speedup_wall, "plain_wall_s": ev.plain_wall, "warm_wall_s": ev.warm_wall,
+        "accepted": int(ev.accepted[valid].sum()),
+        "plain_time_ps_mean": float(np.mean(ev.plain_time[valid])) if valid.any() else None,
+        "warm_cost_ps_mean": float(np.mean(ev.cost_time[valid])) if valid.any() else None,
+        "density_error_median": float(np.median(ev.density_error[valid])) if valid.any() else None,
+        "train_loss_first_last": [losses[0], float(np.mean(losses[-10:]))],
+        "data_generation_s": gen_s, "training_s": train_s,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -598,10 +654,20 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=8)
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["rk4", "sweep", "spinor"], default="rk4",
+    ap.add_argument("--workload", choices=["rk4", "sweep", "spinor", "fno"], default="rk4",
                     help="rk4: the 1024^2 fused-step benchmark; sweep: the uneven-size sweep; "
                          "spinor: the adaptive two-component IFRK run")
     ap.add_argument("--spinor-time", type=float, default=500.0)
+    ap.add_argument("--fno-n", type=int, default=256)
+    ap.add_argument("--fno-train", type=int, default=2000)
+    ap.add_argument("--fno-test", type=int, default=200)
+    ap.add_argument("--fno-time", type=float, default=4000.0)
+    ap.add_argument("--fno-dt", type=float, default=0.01)
+    ap.add_argument("--fno-epochs", type=int, default=20)
+    ap.add_argument("--fno-batch", type=int, default=16)
+    ap.add_argument("--fno-lr", type=float, default=1e-3)
+    ap.add_argument("--fno-width", type=int, default=32)
+    ap.add_argument("--fno-modes", type=int, default=16)
     ap.add_argument("--steady-time", type=float, default=0.0,
                     help="sweep workload: also run to steady state (up to this many ps)")
     ap.add_argument("--freeze-stopped", action="store_true")
@@ -610,6 +676,9 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     if args.workload == "spinor":
         run_spinor_bench(args)
+        return
+    if args.workload == "fno":
+        run_fno_bench(args)
         return
     if args.workload == "sweep":
         if args.members == 32 and "--members" not in sys.argv:

@@ -205,6 +205,8 @@ class ProfileLaser:
             shape = np.exp(-0.5 * ((np.sqrt(r2) - float(spec["radius"])) / float(spec["width"])) ** 2)
         elif kind == "gaussian":
             shape = np.exp(-0.5 * r2 / float(spec["sigma"]) ** 2)
+        elif kind == "lattice":
+            shape = square_lattice(X, Y, float(spec["constant"]), float(spec["width"]), x0, y0)
         else:
             raise ValueError(f"unsupported profile {kind!r}")
         self.P0 = float(cfg.P0)
@@ -213,6 +215,24 @@ class ProfileLaser:
 
     def power_coefficient(self, t: float) -> float:
         return 0.0 if t < self.delay else self.P0
+
+
+def square_lattice(X, Y, constant, width, x0=0.0, y0=0.0):
+    """Unit-depth Gaussian wells of ``width`` on a square lattice of pitch ``constant`` with a
+    site at (x0, y0), covering the box plus one cell (the square case of the ``lattice``
+    profile, ``polarism/profiles/builtin_profiles.py:180-237``, without disorder)."""
+    dx = float(X[0, 1] - X[0, 0]) if X.shape[1] > 1 else 1.0
+    dy = float(Y[1, 0] - Y[0, 0]) if Y.shape[0] > 1 else 1.0
+    half_x = 0.5 * (X.max() - X.min() + dx) + constant
+    half_y = 0.5 * (Y.max() - Y.min() + dy) + constant
+    out = np.zeros(X.shape)
+    for i in range(-int(half_x // constant) - 1, int(half_x // constant) + 2):
+        for j in range(-int(half_y // constant) - 1, int(half_y // constant) + 2):
+            sx, sy = x0 + i * constant, y0 + j * constant
+            if abs(sx) > half_x or abs(sy) > half_y:
+                continue
+            out += np.exp(-0.5 * ((X - sx) ** 2 + (Y - sy) ** 2) / width ** 2)
+    return out
 
 
 def make_laser(cfg: LaserParameters, X, Y, precision="double"):

@@ -305,7 +305,7 @@ def _member_inputs(cfg):
     from polarism_gb300 import host
 
     grid = host.PeriodicGrid(cfg.grid)
-    laser = host.ContinuousGaussian(cfg.laser, grid.X, grid.Y, "single")
+    laser = host.make_laser(cfg.laser, grid.X, grid.Y, "single")
     seed = cfg.noise.seed if cfg.noise.seed is not None else 0
     psi0 = host.make_initial_psi(grid.shape, cfg.noise.initial_amplitude if cfg.noise.enabled else 0.0,
                                  seed, np.complex64, np.float32,
