@@ -266,6 +266,12 @@ int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, do
 int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
                  int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
                  int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, void* stream);
+/* GEMM engine: 0 = tcgen05.mma with FP32 accumulators in tensor memory (default), 1 = mma.sync
+ * (the pre-Blackwell tensor-core path, kept as the cross-check).  pg_gemm_timeouts reports
+ * (and optionally clears) whether a tcgen05 GEMM's bounded completion wait gave up; its
+ * results are then invalid. */
+int pg_gemm_set_engine(int32_t engine);
+int pg_gemm_timeouts(int32_t* count, int32_t clear);
 /* y = bf16(x) (round to nearest even). */
 int pg_fno_to_bf16(const float* x, void* y, int64_t n, void* stream);
 /* u[b, c, :] += bias[c] (bias may be NULL); act = GELU(u) (tanh form) if gelu else u, written to

@@ -13,6 +13,7 @@
 #include <cstdint>
 
 #include "pg_internal.h"
+#include "tma.cuh"
 
 namespace pg {
 namespace {
@@ -132,6 +133,165 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
         }
       }
     }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// The same GEMM on the 5th-generation tensor cores: tcgen05.mma (kind::f16, BF16 operands,
+// FP32 accumulators in tensor memory), issued by one thread per CTA.
+//
+// A CTA computes a 128 x 64 tile of C.  Per 64-wide K slab the 128 threads stage A (128 x 64)
+// and B (64 x 64, as N x K) into shared memory in the canonical K-major layout without
+// swizzle: 8-row x 16-byte core matrices, core matrix (row group g, k group j) at byte
+// offset g * 1024 + j * 128 (so the K-direction stride between core matrices -- the leading
+// byte offset -- is 128 and the 8-row-group stride -- the stride byte offset -- is 1024).
+// After a proxy fence and a barrier, thread 0 issues four M128 N64 K16 MMAs (the descriptor
+// start address advances 256 bytes per K16 step) and commits them to an mbarrier every thread
+// waits on (bounded) before the slab is overwritten.  The accumulators (128 lanes x 64
+// columns) are read back with tcgen05.ld (warp w owns lanes 32w..32w+31) for the epilogue.
+// ---------------------------------------------------------------------------------------
+constexpr int kTcM = 128, kTcN = 64, kTcK = 64;
+constexpr uint32_t kTcCols = 64;                         // TMEM columns (power of two >= 32)
+constexpr int kTcSmemA = kTcM * kTcK * 2;                // 16 KB
+constexpr int kTcSmemB = kTcN * kTcK * 2;                // 8 KB
+// 28 KB per CTA keeps at most 8 CTAs (8 x 64 TMEM columns = 512) on an SM.
+constexpr int kTcSmem = 28 * 1024;
+constexpr int kTcWaitLimit = 200000;
+
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr & 0x3FFFF) >> 4);            // start address
+  d |= static_cast<uint64_t>(128 >> 4) << 16;                    // leading byte offset (K)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;                   // stride byte offset (8 rows)
+  d |= static_cast<uint64_t>(1) << 46;                           // descriptor version
+  return d;                                                      // base offset 0, no swizzle
+}
+
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N = 64, M = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(kTcN >> 3) << 17) |
+                              (static_cast<uint32_t>(kTcM >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(128, 1) gemm_bf16_tc05_kernel(const GemmArgs g, int* err_flag) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(tc_smem);
+  __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(tc_smem + kTcSmemA);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(tc_smem + kTcSmemA + kTcSmemB);
+  uint32_t* taddr_slot = reinterpret_cast<uint32_t*>(tc_smem + kTcSmemA + kTcSmemB + 16);
+  const long long bz = blockIdx.z;
+  const __nv_bfloat16* A = g.A + bz * g.sA;
+  const __nv_bfloat16* B = g.B + bz * g.sB;
+  float* C = g.C + bz * g.sC;
+  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(taddr_slot)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(smem_u32(mbar), 1);
+    fence_mbar_init();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *taddr_slot;
+  const uint32_t a_base = smem_u32(As), b_base = smem_u32(Bs);
+  bool ok = true;
+  uint32_t phase = 0;
+  int slab = 0;
+  for (int k0 = 0; k0 < g.K; k0 += kTcK, ++slab) {
+    // Stage the slabs in the canonical layout: element (r, k) of a [rows][64] slab lives at
+    // ((r / 8) * 8 + k / 8) * 64 + (r % 8) * 8 + k % 8 (elements).
+    for (int e = tid; e < kTcM * kTcK; e += 128) {
+      int r, k;
+      if (!g.transA) { r = e / kTcK; k = e % kTcK; } else { k = e / kTcM; r = e % kTcM; }
+      const int gm = m0 + r, gk = k0 + k;
+      __nv_bfloat16 v = zero;
+      if (gm < g.M && gk < g.K)
+        v = g.transA ? A[static_cast<long long>(gk) * g.lda + gm] : A[static_cast<long long>(gm) * g.lda + gk];
+      As[((r >> 3) * 8 + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
+    }
+    for (int e = tid; e < kTcN * kTcK; e += 128) {
+      int n, k;
+      if (g.transB) { n = e / kTcK; k = e % kTcK; } else { k = e / kTcN; n = e % kTcN; }
+      const int gn = n0 + n, gk = k0 + k;
+      __nv_bfloat16 v = zero;
+      if (gn < g.N && gk < g.K)
+        v = g.transB ? B[static_cast<long long>(gn) * g.ldb + gk] : B[static_cast<long long>(gk) * g.ldb + gn];
+      Bs[((n >> 3) * 8 + (k >> 3)) * 64 + (n & 7) * 8 + (k & 7)] = v;
+    }
+    // Make the generic-proxy stores visible to the tensor core's async proxy.
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int s = 0; s < kTcK / 16; ++s)
+        tc_mma(tmem, tc_smem_desc(a_base + 256 * s), tc_smem_desc(b_base + 256 * s), kTcIdesc,
+               (slab > 0 || s > 0) ? 1 : 0);
+      tc_commit(smem_u32(mbar));
+    }
+    // Every thread waits for the MMAs before the slab is restaged (or the result is read).
+    if (!mbar_wait_bounded(smem_u32(mbar), phase, kTcWaitLimit)) ok = false;
+    phase ^= 1u;
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // Epilogue: thread t of warp w holds row 32 w + lane of the tile, 64 FP32 columns.
+  uint32_t v[64];
+  const uint32_t lane_addr = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+      "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+      "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]),
+        "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]), "=r"(v[38]), "=r"(v[39]),
+        "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]), "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]),
+        "=r"(v[48]), "=r"(v[49]), "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
+        "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
+      : "r"(lane_addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  const int row = m0 + tid;
+  if (ok && row < g.M && g.K > 0) {
+    float* dst = C + static_cast<long long>(row) * g.ldc;
+#pragma unroll
+    for (int j = 0; j < 64; ++j) {
+      const int c = n0 + j;
+      if (c < g.N) {
+        const float x = g.alpha * __uint_as_float(v[j]);
+        dst[c] = g.beta == 0.f ? x : x + g.beta * dst[c];
+      }
+    }
+  }
+  if (!ok && tid == 0) atomicOr(err_flag, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
   }
 }
 
@@ -324,6 +484,9 @@ __global__ void mse_kernel(const float* __restrict__ pred, const float* __restri
   }
 }
 
+__device__ int g_gemm_timeouts = 0;  // set when a tcgen05 GEMM's bounded wait gave up
+int g_gemm_engine = 0;                // 0: tcgen05 (default), 1: mma.sync
+
 int grid_for(long long n) {
   const long long b = (n + 255) / 256;
   return static_cast<int>(b < 1 ? 1 : (b > 4096 ? 4096 : b));
@@ -346,9 +509,36 @@ int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, i
   if (M == 0 || N == 0) return PG_OK;
   pg::GemmArgs g{static_cast<const __nv_bfloat16*>(A), static_cast<const __nv_bfloat16*>(B), C, M, N, K,
                  lda, ldb, ldc, transA ? 1 : 0, transB ? 1 : 0, alpha, beta, strideA, strideB, strideC};
-  dim3 grid((N + pg::kBN - 1) / pg::kBN, (M + pg::kBM - 1) / pg::kBM, batch);
-  pg::gemm_bf16_kernel<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(g);
+  if (pg::g_gemm_engine == 0 && K > 0) {
+    PG_CHECK((M + pg::kTcM - 1) / pg::kTcM <= 65535, PG_ERR_INVALID, "pg_gemm_bf16: grid too large");
+    int* flag = nullptr;
+    PG_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&flag), pg::g_gemm_timeouts));
+    dim3 grid((N + pg::kTcN - 1) / pg::kTcN, (M + pg::kTcM - 1) / pg::kTcM, batch);
+    pg::gemm_bf16_tc05_kernel<<<grid, 128, pg::kTcSmem, static_cast<cudaStream_t>(stream)>>>(g, flag);
+  } else {
+    dim3 grid((N + pg::kBN - 1) / pg::kBN, (M + pg::kBM - 1) / pg::kBM, batch);
+    pg::gemm_bf16_kernel<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(g);
+  }
   PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_gemm_set_engine(int32_t engine) {
+  PG_CHECK(engine == 0 || engine == 1, PG_ERR_INVALID,
+           "pg_gemm_set_engine: 0 (tcgen05 tensor cores) or 1 (mma.sync)");
+  pg::g_gemm_engine = engine;
+  return PG_OK;
+}
+
+int pg_gemm_timeouts(int32_t* count, int32_t clear) {
+  PG_CHECK(count, PG_ERR_INVALID, "pg_gemm_timeouts: null argument");
+  int v = 0;
+  PG_CUDA(cudaMemcpyFromSymbol(&v, pg::g_gemm_timeouts, sizeof(int)));
+  if (clear) {
+    const int zero = 0;
+    PG_CUDA(cudaMemcpyToSymbol(pg::g_gemm_timeouts, &zero, sizeof(int)));
+  }
+  *count = v;
   return PG_OK;
 }
 

@@ -25,15 +25,20 @@ def _bf16_round(a):
     return u.astype(np.uint32).view(np.float32)
 
 
+@pytest.mark.parametrize("engine", [0, 1])
 @pytest.mark.parametrize("ta,tb", [(0, 0), (0, 1), (1, 0), (1, 1)])
-def test_gemm_bf16_matches_numpy(cuda_lib, ta, tb):
+def test_gemm_bf16_matches_numpy(cuda_lib, ta, tb, engine):
+    """Both engines: 0 = tcgen05 (accumulators in tensor memory), 1 = mma.sync."""
+    import ctypes
+
     import torch
 
     from polarism_gb300 import _lib
 
     lib = _lib.load()
+    _lib.check(lib.pg_gemm_set_engine(engine), "pg_gemm_set_engine")
     rng = np.random.default_rng(ta * 2 + tb)
-    for M, N, K, batch in [(70, 45, 33, 3), (128, 64, 256, 1), (5, 130, 7, 2)]:
+    for M, N, K, batch in [(70, 45, 33, 3), (128, 64, 256, 1), (5, 130, 7, 2), (300, 200, 96, 1)]:
         a_shape = (batch, K, M) if ta else (batch, M, K)
         b_shape = (batch, N, K) if tb else (batch, K, N)
         a = _bf16_round(rng.standard_normal(a_shape))
@@ -49,7 +54,11 @@ def test_gemm_bf16_matches_numpy(cuda_lib, ta, tb):
         am = np.swapaxes(a, 1, 2) if ta else a
         bm = np.swapaxes(b, 1, 2) if tb else b
         expect = 0.75 * np.einsum("bmk,bkn->bmn", am.astype(np.float64), bm.astype(np.float64)) - 0.5 * c0
-        assert rel_l2(Cm.cpu().numpy(), expect) < 1e-5, (M, N, K, batch)
+        assert rel_l2(Cm.cpu().numpy(), expect) < 1e-5, (M, N, K, batch, engine)
+    count = ctypes.c_int32()
+    _lib.check(lib.pg_gemm_timeouts(ctypes.byref(count), 1), "pg_gemm_timeouts")
+    assert count.value == 0
+    _lib.check(lib.pg_gemm_set_engine(0), "pg_gemm_set_engine")
 
 
 def _small():
