@@ -55,22 +55,54 @@ def dist_info():
     return rank, world, local
 
 
-def workload(members, precision="single"):
-    """Host arrays of the benchmark workload: psi0, n0, per-member envelopes, physics."""
+def rank_members(rank, world, members):
+    """Weak scaling: every rank steps its own `members` replicas, global indices
+    rank * members .. rank * members + members - 1 (no data-path exchange between ranks)."""
+    if not 0 <= rank < world:
+        raise ValueError("rank out of range")
+    return list(range(rank * members, (rank + 1) * members))
+
+
+def max_over_ranks(value, world, device="cpu"):
+    """The slowest rank's time (MAX all-reduce); the value itself for one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def partition_by_sites(sites, world):
+    """Split uneven members over ranks, largest first onto the least-loaded rank."""
+    loads = [0] * world
+    parts = [[] for _ in range(world)]
+    for m in sorted(range(len(sites)), key=lambda i: -sites[i]):
+        r = min(range(world), key=lambda i: loads[i])
+        parts[r].append(m)
+        loads[r] += sites[m]
+    return [sorted(p) for p in parts]
+
+
+def workload(members, precision="single", first=0):
+    """Host arrays of the benchmark workload (members first .. first + members - 1):
+    psi0, n0, per-member envelopes and seeds."""
     from polarism_gb300.host import make_initial_psi
 
     dx, dy = LX / NX, LY / NY
     x = (np.arange(NX) - (NX - 1) * 0.5) * dx
     y = (np.arange(NY) - (NY - 1) * 0.5) * dy
     rng = np.random.default_rng(1234)
-    sigmas = rng.uniform(8.0, 20.0, size=members)
+    sigmas = rng.uniform(8.0, 20.0, size=first + members)[first:]
     cdt = np.complex64 if precision == "single" else np.complex128
     rdt = np.float32 if precision == "single" else np.float64
     env = np.stack([np.exp(-0.5 * (x[None, :] ** 2 + y[:, None] ** 2) / s ** 2) for s in sigmas])
-    psi = np.stack([make_initial_psi((NY, NX), 1e-3, 42 + m, cdt, rdt) for m in range(members)])
+    seeds = [42 + first + m for m in range(members)]
+    psi = np.stack([make_initial_psi((NY, NX), 1e-3, sd, cdt, rdt) for sd in seeds])
     return dict(dx=dx, dy=dy, psi=psi[:, None], n=np.zeros((members, 1, NY, NX), rdt),
-                env=env[:, None].astype(rdt), seeds=[42 + m for m in range(members)],
-                sigmas=sigmas)
+                env=env[:, None].astype(rdt), seeds=seeds, sigmas=sigmas)
 
 
 PHYSICS = dict(hbar=0.6582119514, m_eff=0.284, g_C=0.001, g_R=0.002, g_I=0.0, R=0.02,
@@ -235,7 +267,7 @@ def run_ours(args):
     from polarism_gb300.engine import MemberPhysics, RK4Engine
 
     members = args.members
-    w = workload(members)
+    w = workload(members, first=rank_members(rank, world, members)[0])
     eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**PHYSICS), "single",
                     pump_per_member=True)
     eng.set_pump(w["env"])
@@ -266,13 +298,7 @@ def run_ours(args):
     barrier()
     clocks = sampler.stop()
     launches = eng.last_launch_count
-    elapsed_ms = start.elapsed_time(stop)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(start.elapsed_time(stop), world, "cuda")
     sites = members * NX * NY
     value = world * sites * args.steps / (elapsed_ms / 1e3)
     kernel_s = elapsed_ms / 1e3 / args.steps
@@ -322,7 +348,7 @@ def run_e2e(args, w, members, torch):
 
     for m in range(members):
         c = copy.deepcopy(cfg)
-        c.noise.seed = 42 + m
+        c.noise.seed = int(w["seeds"][m])
         c.laser.sigma_space = float(w["sigmas"][m])
         member_cfgs.append(c)
     grid, model, state = build_simulation(cfg, member_cfgs if members > 1 else None)
@@ -393,7 +419,15 @@ def run_sweep_bench(args):
     from polarism_gb300.engine import MemberPhysics
     from polarism_gb300.sweep import SweepEngine, _member_inputs, autotune_tiling, run_sweep
 
-    cfgs = sweep_members(args.members)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    cfgs_all = sweep_members(args.members)
+    sites_all = [c.grid.nx * c.grid.ny for c in cfgs_all]
+    # Several GPUs: members are independent, so each rank takes a site-balanced share.
+    mine = partition_by_sites(sites_all, world)[rank] if world > 1 else list(range(len(cfgs_all)))
+    cfgs = [cfgs_all[m] for m in mine]
     inputs = [_member_inputs(c) for c in cfgs]
     grids = [(g.nx, g.ny, g.dx, g.dy) for g, *_ in inputs]
     eng = SweepEngine(grids, [MemberPhysics(**PHYSICS)] * len(cfgs), 1e-3)
@@ -411,11 +445,11 @@ def run_sweep_bench(args):
     sampler.start()
     time.sleep(0.3)
     eng.advance(args.warmup, args.steps, scales[args.warmup:])
-    elapsed_ms = eng.last_time_ms()
+    elapsed_ms = max_over_ranks(eng.last_time_ms(), world, "cuda")
     clocks = sampler.stop()
     launches = eng.last_launch_count
     sites = eng.sites
-    value = sites * args.steps / (elapsed_ms / 1e3)
+    value = sum(sites_all) * args.steps / (elapsed_ms / 1e3)
     achieved = BYTES_PER_SITE * sites / (elapsed_ms / 1e3 / args.steps) / 1e9
     peak, peak_kind = measured_peak()
 
@@ -433,9 +467,11 @@ def run_sweep_bench(args):
     line = {
         "metric": "sweep RK4 site-updates/s (uneven sizes, one persistent launch per step)",
         "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": args.steps,
+        "scaling_note": "members split over ranks by sites (strong scaling of one sweep)" if world > 1 else None,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"uneven sweep: {len(cfgs)} members, 128^2/256^2/512^2 a third each, "
+        "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"uneven sweep: {len(cfgs_all)} members, 128^2/256^2/512^2 a third each, "
                                "dx fixed, P0 in [0.5,3] x threshold, sigma in [8,20] um, seeds "
                                "0..N-1, single reservoir, dt=1e-3, complex64",
                    "members": len(cfgs), "sites": sites, "tiling": eng.tiling,
