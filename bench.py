@@ -435,7 +435,11 @@ def run_sweep_bench(args):
     psi0 = [p for _, _, p, _, _ in inputs]
     n0 = [np.zeros((g.ny, g.nx), np.float32) for g, *_ in inputs]
     eng.set_state(psi0, n0)
-    tune = autotune_tiling(eng, noise=False, use_cache=False, steps=32)
+    if args.sweep_tiling:
+        eng.set_tiling(*args.sweep_tiling)
+        tune = {"timings": None}
+    else:
+        tune = autotune_tiling(eng, noise=False, use_cache=False, steps=32)
     p0 = np.asarray([c.laser.P0 for c in cfgs])
     total = args.warmup + args.steps
     scales = np.broadcast_to(p0, (total, 3, len(cfgs))).copy()
@@ -461,7 +465,7 @@ def run_sweep_bench(args):
     for c in range(calls):
         eng.set_state([eng.unpack(psi_h, m) for m in range(eng.members)],
                       [eng.unpack(n_h, m) for m in range(eng.members)])
-        eng.advance(total + c * chunk, chunk, scales[:chunk])
+        eng.advance(total + c * chunk, chunk, np.broadcast_to(p0, (chunk, 3, len(cfgs))).copy())
         psi_h, n_h = eng.get_packed_state()
     e2e_s = time.perf_counter() - t0
     line = {
@@ -707,6 +711,8 @@ def main():
     ap.add_argument("--steady-time", type=float, default=0.0,
                     help="sweep workload: also run to steady state (up to this many ps)")
     ap.add_argument("--freeze-stopped", action="store_true")
+    ap.add_argument("--sweep-tiling", type=int, nargs=2, metavar=("LANES", "ROWS"),
+                    help="sweep workload: use this tile shape instead of the autotuner's")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
