@@ -648,8 +648,12 @@ def run_fno_bench(args):
     t0 = time.perf_counter()
     data = ws.run_uniform(train_cfgs)
     gen_s = time.perf_counter() - t0
-    # Lasing members that became stationary (decayed members have nothing to learn).
-    keep = np.isfinite(data.stop_times) & (data.final_norms > 1e-6)
+    # Lasing members that became stationary (decayed members have nothing to learn); with
+    # --fno-targets final every lasing member's final state is a target (short profiling runs).
+    lasing = data.final_norms > 1e-6
+    keep = lasing if args.fno_targets == "final" else np.isfinite(data.stop_times) & lasing
+    if not keep.any():
+        raise SystemExit("no training targets: no member reached a lasing steady state")
     a = ws.features([c for c, k in zip(train_cfgs, keep) if k])
     y = ws.targets([p for p, k in zip(data.psi, keep) if k], [r for r, k in zip(data.reservoir, keep) if k])
     model = ws.WarmStart(n, width=args.fno_width, modes=args.fno_modes)
@@ -708,6 +712,7 @@ def main():
     ap.add_argument("--fno-lr", type=float, default=1e-3)
     ap.add_argument("--fno-width", type=int, default=32)
     ap.add_argument("--fno-modes", type=int, default=16)
+    ap.add_argument("--fno-targets", choices=["steady", "final"], default="steady")
     ap.add_argument("--steady-time", type=float, default=0.0,
                     help="sweep workload: also run to steady state (up to this many ps)")
     ap.add_argument("--freeze-stopped", action="store_true")
