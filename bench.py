@@ -649,9 +649,9 @@ def run_fno_bench(args):
     data = ws.run_uniform(train_cfgs)
     gen_s = time.perf_counter() - t0
     # Lasing members that became stationary (decayed members have nothing to learn); with
-    # --fno-targets final every lasing member's final state is a target (short profiling runs).
+    # --fno-targets final every member's final state is a target (short profiling runs).
     lasing = data.final_norms > 1e-6
-    keep = lasing if args.fno_targets == "final" else np.isfinite(data.stop_times) & lasing
+    keep = np.ones_like(lasing) if args.fno_targets == "final" else np.isfinite(data.stop_times) & lasing
     if not keep.any():
         raise SystemExit("no training targets: no member reached a lasing steady state")
     a = ws.features([c for c, k in zip(train_cfgs, keep) if k])
