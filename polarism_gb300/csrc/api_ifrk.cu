@@ -195,8 +195,14 @@ Plan make_plan(const pg_solver* s) {
   r.ny = c.ny;
   r.log2nx = ilog2i(c.nx);
   const int comps = s->comps;
+  // Fill the GPU first: stop growing the tiles once fewer than two blocks per SM would remain
+  // (a single 512^2 spinor otherwise runs on 32 column blocks); columns stay at least one
+  // 32-byte sector wide so the panel loads remain coalesced.
+  const long long want_blocks = 2LL * std::max(1, s->sm_count);
   int rows = 1;
-  while (rows * 2 <= c.ny && rows * 2 * c.nx * comps <= 4096) rows *= 2;
+  while (rows * 2 <= c.ny && rows * 2 * c.nx * comps <= 4096 &&
+         static_cast<long long>(c.ny / (rows * 2)) * c.members >= want_blocks)
+    rows *= 2;
   r.rows = rows;
   r.log2rows = ilog2i(rows);
   int threads = (rows * c.nx * comps + mv - 1) / mv;
@@ -213,9 +219,11 @@ Plan make_plan(const pg_solver* s) {
   k.nx = c.nx;
   k.ny = c.ny;
   k.log2ny = ilog2i(c.ny);
+  const int min_cols = static_cast<int>(std::min<size_t>(static_cast<size_t>(c.nx), 32 / csize));
   int cols = 1;
   while (cols * 2 <= c.nx && cols * 2 <= 16 && cols * 2 * comps * c.ny * csize <= 160 * 1024 &&
-         cols * 2 * comps * c.ny <= mv * 1024)
+         cols * 2 * comps * c.ny <= mv * 1024 &&
+         (cols < min_cols || static_cast<long long>(c.nx / (cols * 2)) * c.members >= want_blocks))
     cols *= 2;
   k.cols = cols;
   k.log2cols = ilog2i(cols);
