@@ -266,6 +266,16 @@ int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, do
 int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
                  int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
                  int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, void* stream);
+/* Two-level batch: `batch` outer x `inner` inner matrices, operand offsets
+ * outer * stride + inner * stride2 (a split-K reduction writes its K slices through the inner
+ * level, then pg_fno_sum_slices adds them in a fixed order). */
+int pg_gemm_bf16_2d(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
+                    int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
+                    int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, int32_t inner,
+                    int64_t strideA2, int64_t strideB2, int64_t strideC2, void* stream);
+/* out (+)= sum of `count` consecutive slices of n floats. */
+int pg_fno_sum_slices(const float* parts, float* out, int64_t n, int32_t count, int32_t accumulate,
+                      void* stream);
 /* GEMM engine: 0 = tcgen05.mma with FP32 accumulators in tensor memory (default), 1 = mma.sync
  * (the pre-Blackwell tensor-core path, kept as the cross-check).  pg_gemm_timeouts reports
  * (and optionally clears) whether a tcgen05 GEMM's bounded completion wait gave up; its

@@ -105,6 +105,10 @@ SIGNATURES = {
     "pg_sweep_steady_check": (C.c_int, [_vp, _vp, _vp, _vp]),
     "pg_gemm_bf16": (C.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _i32,
                                C.c_float, C.c_float, _i32, _i64, _i64, _i64, _vp]),
+    "pg_gemm_bf16_2d": (C.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _i32,
+                                  C.c_float, C.c_float, _i32, _i64, _i64, _i64, _i32, _i64, _i64,
+                                  _i64, _vp]),
+    "pg_fno_sum_slices": (C.c_int, [_vp, _vp, _i64, _i32, _i32, _vp]),
     "pg_gemm_set_engine": (C.c_int, [_i32]),
     "pg_gemm_timeouts": (C.c_int, [C.POINTER(_i32), _i32]),
     "pg_fno_to_bf16": (C.c_int, [_vp, _vp, _i64, _vp]),

@@ -26,8 +26,18 @@ struct GemmArgs {
   float* C;
   int M, N, K, lda, ldb, ldc, transA, transB;
   float alpha, beta;
-  long long sA, sB, sC;
+  long long sA, sB, sC;       // outer batch strides
+  int inner;                  // inner batch count: blockIdx.z = outer * inner + inner index
+  long long sA2, sB2, sC2;    // inner batch strides
 };
+
+__device__ __forceinline__ void batch_offsets(const GemmArgs& g, long long& oa, long long& ob, long long& oc) {
+  const long long z = blockIdx.z;
+  const long long outer = z / g.inner, in = z % g.inner;
+  oa = outer * g.sA + in * g.sA2;
+  ob = outer * g.sB + in * g.sB2;
+  oc = outer * g.sC + in * g.sC2;
+}
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
   asm volatile(
@@ -43,10 +53,11 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
 __global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
   __shared__ __align__(16) __nv_bfloat16 As[kBM][kBK + kPad];
   __shared__ __align__(16) __nv_bfloat16 Bs[kBN][kBK + kPad];
-  const long long bz = blockIdx.z;
-  const __nv_bfloat16* A = g.A + bz * g.sA;
-  const __nv_bfloat16* B = g.B + bz * g.sB;
-  float* C = g.C + bz * g.sC;
+  long long oa, ob, oc;
+  batch_offsets(g, oa, ob, oc);
+  const __nv_bfloat16* A = g.A + oa;
+  const __nv_bfloat16* B = g.B + ob;
+  float* C = g.C + oc;
   const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
@@ -193,10 +204,11 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16_tc05_kernel(const GemmArgs g
   __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(tc_smem + kTcSmemA);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(tc_smem + kTcSmemA + kTcSmemB);
   uint32_t* taddr_slot = reinterpret_cast<uint32_t*>(tc_smem + kTcSmemA + kTcSmemB + 16);
-  const long long bz = blockIdx.z;
-  const __nv_bfloat16* A = g.A + bz * g.sA;
-  const __nv_bfloat16* B = g.B + bz * g.sB;
-  float* C = g.C + bz * g.sC;
+  long long oa, ob, oc;
+  batch_offsets(g, oa, ob, oc);
+  const __nv_bfloat16* A = g.A + oa;
+  const __nv_bfloat16* B = g.B + ob;
+  float* C = g.C + oc;
   const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
   const int tid = threadIdx.x, warp = tid >> 5;
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
@@ -292,6 +304,17 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16_tc05_kernel(const GemmArgs g
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+  }
+}
+
+// out (+)= sum of `count` consecutive slices of n floats (fixed order: deterministic).
+__global__ void sum_slices_kernel(const float* __restrict__ parts, float* __restrict__ out, long long n,
+                                  int count, int accumulate) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    float s = accumulate ? out[i] : 0.f;
+    for (int c = 0; c < count; ++c) s += parts[static_cast<long long>(c) * n + i];
+    out[i] = s;
   }
 }
 
@@ -497,18 +520,21 @@ int grid_for(long long n) {
 
 extern "C" {
 
-int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
-                 int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
-                 int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, void* stream) {
+int pg_gemm_bf16_2d(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
+                    int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
+                    int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, int32_t inner,
+                    int64_t strideA2, int64_t strideB2, int64_t strideC2, void* stream) {
   PG_CHECK(A && B && C, PG_ERR_INVALID, "pg_gemm_bf16: null operand");
-  PG_CHECK(M >= 0 && N >= 0 && K >= 0 && batch >= 1, PG_ERR_INVALID, "pg_gemm_bf16: bad sizes");
+  PG_CHECK(M >= 0 && N >= 0 && K >= 0 && batch >= 1 && inner >= 1, PG_ERR_INVALID, "pg_gemm_bf16: bad sizes");
   PG_CHECK(lda >= (transA ? M : K) && ldb >= (transB ? K : N) && ldc >= N, PG_ERR_INVALID,
            "pg_gemm_bf16: leading dimension smaller than the row");
-  PG_CHECK(batch <= 65535 && (M + pg::kBM - 1) / pg::kBM <= 65535, PG_ERR_INVALID,
-           "pg_gemm_bf16: grid too large");
+  PG_CHECK(static_cast<long long>(batch) * inner <= 65535 && (M + pg::kBM - 1) / pg::kBM <= 65535,
+           PG_ERR_INVALID, "pg_gemm_bf16: grid too large");
   if (M == 0 || N == 0) return PG_OK;
+  batch *= inner;
   pg::GemmArgs g{static_cast<const __nv_bfloat16*>(A), static_cast<const __nv_bfloat16*>(B), C, M, N, K,
-                 lda, ldb, ldc, transA ? 1 : 0, transB ? 1 : 0, alpha, beta, strideA, strideB, strideC};
+                 lda, ldb, ldc, transA ? 1 : 0, transB ? 1 : 0, alpha, beta, strideA, strideB, strideC,
+                 inner, strideA2, strideB2, strideC2};
   if (pg::g_gemm_engine == 0 && K > 0) {
     PG_CHECK((M + pg::kTcM - 1) / pg::kTcM <= 65535, PG_ERR_INVALID, "pg_gemm_bf16: grid too large");
     int* flag = nullptr;
@@ -519,6 +545,23 @@ int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, i
     dim3 grid((N + pg::kBN - 1) / pg::kBN, (M + pg::kBM - 1) / pg::kBM, batch);
     pg::gemm_bf16_kernel<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(g);
   }
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int pg_gemm_bf16(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, int32_t lda,
+                 int32_t ldb, int32_t ldc, int32_t transA, int32_t transB, float alpha, float beta,
+                 int32_t batch, int64_t strideA, int64_t strideB, int64_t strideC, void* stream) {
+  return pg_gemm_bf16_2d(A, B, C, M, N, K, lda, ldb, ldc, transA, transB, alpha, beta, batch, strideA,
+                         strideB, strideC, 1, 0, 0, 0, stream);
+}
+
+int pg_fno_sum_slices(const float* parts, float* out, int64_t n, int32_t count, int32_t accumulate,
+                      void* stream) {
+  PG_CHECK(parts && out && n >= 0 && count >= 1, PG_ERR_INVALID, "pg_fno_sum_slices: bad argument");
+  if (n == 0) return PG_OK;
+  pg::sum_slices_kernel<<<pg::grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(parts, out, n, count,
+                                                                                          accumulate);
   PG_CUDA(cudaGetLastError());
   return PG_OK;
 }

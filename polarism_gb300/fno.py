@@ -204,10 +204,18 @@ class FNO2d:
 
     def _pointwise_back(self, wname, x_bf, g_bf, g32, batch, cin, cout, grads, dx=None, dx_accumulate=False):
         P = self.n * self.n
+        # dW = sum over samples and sites of g x^T: a split-K GEMM (the samples and 4096-site
+        # slices of the plane each give one partial product), then a fixed-order sum.
+        chunk = 4096 if P % 4096 == 0 else P
+        slices = P // chunk
+        parts = self._empty(batch * slices, cout, cin)
+        self._check(self.lib.pg_gemm_bf16_2d(
+            _ptr(g_bf), _ptr(x_bf), _ptr(parts), cout, cin, chunk, P, P, cin, 0, 1, 1.0, 0.0,
+            batch, cout * P, cin * P, slices * cout * cin, slices, chunk, chunk, cout * cin,
+            self.stream), "pg_gemm_bf16_2d")
         dw = self._empty(cout, cin)
-        for b in range(batch):
-            self._gemm(g_bf, x_bf, dw, cout, cin, P, P, P, cin, ta=0, tb=1, beta=0.0 if b == 0 else 1.0,
-                       a_off=b * cout * P, b_off=b * cin * P)
+        self._check(self.lib.pg_fno_sum_slices(_ptr(parts), _ptr(dw), cout * cin, batch * slices, 0,
+                                               self.stream), "pg_fno_sum_slices")
         grads[wname] = dw
         db = self._empty(cout)
         self._check(self.lib.pg_fno_channel_sum(_ptr(g32), _ptr(db), batch, cout, P, 0, self.stream),

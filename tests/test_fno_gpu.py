@@ -115,3 +115,31 @@ def test_adam_steps_reduce_the_loss(cuda_lib):
         losses.append(loss)
         net.adam_step(net.backward(cache, grad), lr=3e-3)
     assert losses[-1] < 0.5 * losses[0] and losses[-1] < min(losses[:5]), losses[::8]
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+def test_split_k_two_level_batch_and_slice_sum(cuda_lib, engine):
+    """dW = sum_b G_b X_b^T with each sample's K split in slices through the inner batch level,
+    summed in a fixed order (the weight-gradient path of the network)."""
+    import torch
+
+    from polarism_gb300 import _lib
+
+    lib = _lib.load()
+    _lib.check(lib.pg_gemm_set_engine(engine), "pg_gemm_set_engine")
+    rng = np.random.default_rng(7)
+    B, M, N, P, chunk = 3, 32, 24, 4096 * 2, 4096
+    g = _bf16_round(rng.standard_normal((B, M, P)))
+    x = _bf16_round(rng.standard_normal((B, N, P)))
+    G = torch.tensor(g, device="cuda").to(torch.bfloat16)
+    X = torch.tensor(x, device="cuda").to(torch.bfloat16)
+    S = P // chunk
+    parts = torch.empty((B * S, M, N), device="cuda")
+    _lib.check(lib.pg_gemm_bf16_2d(G.data_ptr(), X.data_ptr(), parts.data_ptr(), M, N, chunk, P, P, N, 0, 1,
+                                   1.0, 0.0, B, M * P, N * P, S * M * N, S, chunk, chunk, M * N, None),
+               "pg_gemm_bf16_2d")
+    out = torch.full((M, N), 1.5, device="cuda")
+    _lib.check(lib.pg_fno_sum_slices(parts.data_ptr(), out.data_ptr(), M * N, B * S, 1, None), "sum")
+    expect = 1.5 + np.einsum("bmp,bnp->mn", g.astype(np.float64), x.astype(np.float64))
+    assert rel_l2(out.cpu().numpy(), expect) < 1e-5
+    _lib.check(lib.pg_gemm_set_engine(0), "pg_gemm_set_engine")
