@@ -46,7 +46,8 @@ extern "C" {
 
 #define PG_RES_NONE 0
 #define PG_RES_SINGLE 1
-#define PG_RES_DOUBLE 2      /* active + inactive reservoirs (IFRK only) */
+#define PG_RES_DOUBLE 2      /* active + inactive reservoirs (RK4 tiled kernel and IFRK) */
+#define PG_RES_QDOUBLE 3     /* quadratic-double: n_R fed by kappa n_I^2 (RK4 tiled kernel and IFRK) */
 
 #define PG_POT_NONE 0
 #define PG_POT_REAL 1
@@ -64,6 +65,8 @@ typedef struct pg_physics {
    * component, (1 +- circular_polarization) / 2 (polarism/simulation_controller.py:974-979). */
   double alpha_2, zeeman, te_tm;
   double pump_weight_plus, pump_weight_minus;
+  /* Quadratic inactive-to-active transfer rate (polarism/reservoir/quadratic_double_reservoir.py). */
+  double kappa;
 } pg_physics;
 
 typedef struct pg_config {

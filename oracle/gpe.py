@@ -66,6 +66,13 @@ def reservoir_derivatives(kind: str, fields, rho, pump, p, dx, dy):
         if np.any(_get(p, "reservoir_diffusion_A")):
             dn_a = dn_a + _get(p, "reservoir_diffusion_A") * laplacian(n_a, dx, dy)
         return (dn_a, dn_i)
+    if kind == "quadratic-double":
+        # polarism/reservoir/quadratic_double_reservoir.py:13-14,160-164: state (n_R, n_I).
+        n_r, n_i = fields
+        transfer = _get(p, "kappa") * n_i * n_i
+        dn_r = transfer - _get(p, "gamma_R") * n_r - _get(p, "R") * n_r * rho
+        dn_i = pump - transfer - _get(p, "gamma_I") * n_i
+        return (dn_r, dn_i)
     raise ValueError(f"unsupported reservoir {kind!r}")
 
 
@@ -74,7 +81,7 @@ def _active(kind, fields):
 
 
 def _inactive(kind, fields):
-    return fields[1] if kind == "double" else 0.0
+    return fields[1] if kind in ("double", "quadratic-double") else 0.0
 
 
 def gpe_rhs(psi, fields, pump, potential, p, dx, dy, kind="single"):

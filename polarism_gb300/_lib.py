@@ -16,7 +16,7 @@ LIBRARY_PATH = _PKG / "_build" / "libpolarism_gb300.so"
 
 PG_OK, PG_ERR_INVALID, PG_ERR_CUDA, PG_ERR_UNSUPPORTED, PG_ERR_TIMEOUT = 0, 1, 2, 3, 4
 PG_SINGLE, PG_DOUBLE = 0, 1
-PG_RES_NONE, PG_RES_SINGLE, PG_RES_DOUBLE = 0, 1, 2
+PG_RES_NONE, PG_RES_SINGLE, PG_RES_DOUBLE, PG_RES_QDOUBLE = 0, 1, 2, 3
 PG_POT_NONE, PG_POT_REAL, PG_POT_COMPLEX = 0, 1, 2
 
 
@@ -26,7 +26,7 @@ class PgPhysics(C.Structure):
     _fields_ = [(name, C.c_double) for name in (
         "hbar", "m_eff", "g_C", "g_R", "g_I", "R", "gamma_C", "gamma_R",
         "kinetic_relaxation_eta", "gamma_I", "gamma_A", "R_IA", "R_AI", "alpha_2", "zeeman",
-        "te_tm", "pump_weight_plus", "pump_weight_minus")]
+        "te_tm", "pump_weight_plus", "pump_weight_minus", "kappa")]
 
 
 class PgConfig(C.Structure):

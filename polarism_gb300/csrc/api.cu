@@ -121,6 +121,12 @@ void build_consts(const pg_solver* s, std::vector<pg::RhsConst<T>>& out) {
     k.gamma_R = static_cast<T>(p.gamma_R);
     k.eta_a = static_cast<T>(p.kinetic_relaxation_eta);
     k.pad_ = T(0);
+    k.gamma_I = static_cast<T>(p.gamma_I);
+    k.gamma_A = static_cast<T>(p.gamma_A);
+    k.R_IA = static_cast<T>(p.R_IA);
+    k.R_AI = static_cast<T>(p.R_AI);
+    k.kappa = static_cast<T>(p.kappa);
+    k.pad2_ = T(0);
     if (s->noise) {
       k.noise_a = static_cast<T>(s->noise_strength[m] * s->noise_gamma[m] * s->dt_over_4dv);
       k.noise_b = static_cast<T>(s->noise_strength[m] * s->noise_R[m] * s->dt_over_4dv);
@@ -287,9 +293,8 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   PG_CHECK(cfg->members >= 1, PG_ERR_INVALID, "pg_create: members must be >= 1");
   PG_CHECK(cfg->precision == PG_SINGLE || cfg->precision == PG_DOUBLE, PG_ERR_INVALID,
            "pg_create: precision must be PG_SINGLE or PG_DOUBLE");
-  PG_CHECK(cfg->reservoir == PG_RES_NONE || cfg->reservoir == PG_RES_SINGLE ||
-               cfg->reservoir == PG_RES_DOUBLE,
-           PG_ERR_UNSUPPORTED, "pg_create: reservoir must be PG_RES_NONE, PG_RES_SINGLE or PG_RES_DOUBLE");
+  PG_CHECK(cfg->reservoir >= PG_RES_NONE && cfg->reservoir <= PG_RES_QDOUBLE, PG_ERR_UNSUPPORTED,
+           "pg_create: reservoir must be PG_RES_NONE, PG_RES_SINGLE, PG_RES_DOUBLE or PG_RES_QDOUBLE");
   PG_CHECK(cfg->components >= 0 && cfg->components <= 2, PG_ERR_INVALID,
            "pg_create: components must be 1 or 2");
   const int comps = cfg->components == 0 ? 1 : cfg->components;
@@ -310,7 +315,7 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   s->plane = static_cast<long long>(cfg->nx) * cfg->ny;
   s->sites = s->plane * cfg->members;
   s->comps = comps;
-  s->res_fields = cfg->reservoir;
+  s->res_fields = cfg->reservoir >= PG_RES_DOUBLE ? 2 : cfg->reservoir;
   s->res_comps = res_comps;
   s->field_values = s->sites * comps;
   s->res_values = s->sites * s->res_fields * res_comps;
@@ -541,8 +546,10 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
   PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_rk4_advance: negative step count");
   PG_CHECK(!s->spectral, PG_ERR_INVALID,
            "pg_rk4_advance: the state holds a spectrum; set real-space psi first");
-  PG_CHECK(s->comps == 1 && s->res_fields <= 1, PG_ERR_UNSUPPORTED,
-           "pg_rk4_advance: two-component fields and the double reservoir run on the IFRK path");
+  PG_CHECK(s->comps == 1, PG_ERR_UNSUPPORTED,
+           "pg_rk4_advance: two-component fields run on the IFRK path");
+  PG_CHECK(s->res_comps == 1, PG_ERR_UNSUPPORTED,
+           "pg_rk4_advance: one reservoir plane per field");
   s->last_launches = 0;
   pg::ifrk_invalidate(s);
   const int m = s->cfg.members;

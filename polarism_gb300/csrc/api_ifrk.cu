@@ -233,6 +233,7 @@ Plan make_plan(const pg_solver* s) {
   k.comps = comps;
   k.log2comps = comps == 2 ? 1 : 0;
   k.res_fields = s->res_fields;
+  k.res_kind = s->cfg.reservoir;
   k.res_comps = s->res_comps;
   k.reservoir = s->res_fields > 0;
   k.potential = c.potential;

@@ -122,6 +122,7 @@ int upload_split_consts(pg_solver* s) {
     k.R_AI = static_cast<T>(p.R_AI);
     k.weight[0] = static_cast<T>(p.pump_weight_plus);
     k.weight[1] = static_cast<T>(p.pump_weight_minus);
+    k.kappa = static_cast<T>(p.kappa);
     if (s->noise) {
       k.noise_a = static_cast<T>(s->noise_strength[i] * s->noise_gamma[i] * s->dt_over_4dv);
       k.noise_b = static_cast<T>(s->noise_strength[i] * s->noise_R[i] * s->dt_over_4dv);
@@ -354,7 +355,8 @@ int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t
            "pg_split_advance: ordering must be 0 (R/2 K/2 N K/2 R/2) or 1 (K/2 [R/2 N R/2] K/2)");
   PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_split_advance: negative step count");
   PG_CHECK(s->comps == 1 && s->res_fields <= 1, PG_ERR_UNSUPPORTED,
-           "pg_split_advance: two-component fields and the double reservoir run on the IFRK path");
+           "pg_split_advance: two-component fields and two-field reservoirs run on the RK4 and IFRK "
+           "paths");
   if (n_steps == 0) return PG_OK;
   pg::ifrk_invalidate(s);
   int rc = pg::ensure_split(s);

@@ -268,6 +268,12 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
             const T P = Cr == 2 ? mul_rn_i(p_site, k.weight[cr]) : p_site;
             if (F == 1) {
               dn_out[ridx[cr]] = P - (k.gamma_R + k.R * rr) * nval[cr];
+            } else if (a.res_kind == PG_RES_QDOUBLE) {
+              // quadratic_double_reservoir.py:13-14: n_R fed by kappa n_I^2.
+              const T nR = nval[cr], nI = nval[Cr + cr];
+              const T transfer = k.kappa * nI * nI;
+              dn_out[ridx[cr]] = transfer - k.gamma_R * nR - k.R * nR * rr;
+              dn_out[ridx[Cr + cr]] = P - transfer - k.gamma_I * nI;
             } else {
               const T nA = nval[cr], nI = nval[Cr + cr];
               dn_out[ridx[Cr + cr]] = P - (k.gamma_I + k.R_IA) * nI + k.R_AI * nA;

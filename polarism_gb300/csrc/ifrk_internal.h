@@ -44,6 +44,7 @@ struct IfrkColArgs {
   int comps, log2comps;        // field components
   int res_fields;              // 0 none, 1 single, 2 active + inactive
   int res_comps;               // reservoir planes per field (1 shared or comps)
+  int res_kind;                // PG_RES_*: two fields are double (2) or quadratic-double (3)
   int mode;                    // 0 stage RHS, 1 step end, 2 error norm, 3 forward only
   int inverse, forward;
   int reservoir;               // any reservoir present

@@ -45,6 +45,8 @@ struct RhsConst {
   T noise_a, noise_b;// sigma^2 = noise_a + noise_b * n_A  (strength (gamma_C + R n) dt / (4 dV))
   T pad_;
   unsigned long long seed;
+  // Two-field reservoirs: double (active n_A, inactive n_I) and quadratic-double (n_R, n_I).
+  T gamma_I, gamma_A, R_IA, R_AI, kappa, pad2_;
 };
 
 // Geometry of one RK4 launch (one time step over every member).
@@ -60,11 +62,13 @@ struct RK4Geom {
 struct RK4Features {
   int potential;     // 0 none, 1 real, 2 complex
   int relax;         // kinetic relaxation term on
-  int reservoir;     // 0 none, 1 single
+  int reservoir;     // PG_RES_*: 0 none, 1 single, 2 double, 3 quadratic-double
 };
 
 // Launch one fused whole-step RK4 update; scales points at [3][members] pump
 // coefficients (device memory) and step_base at the global step counter (device).
+// With a two-field reservoir n_in/n_out hold the active field of every member followed by
+// the inactive field of every member.
 template <typename T>
 cudaError_t launch_rk4_step(const T* psi_in, const T* n_in, const T* pump, const T* potential,
                             T* psi_out, T* n_out, const RhsConst<T>* consts,

@@ -50,14 +50,18 @@ struct MaxThreads<double> {
 
 // One right-hand-side evaluation at a site.  c is the centre, (lt, rt, up, dn) the
 // four neighbours, n the active reservoir density, sP the scaled pump.
-template <typename T, bool GENERAL>
+// n2 is the inactive reservoir of the two-field reservoirs (double: n_I feeding n_A,
+// polarism/reservoir/double_reservoir.py:106-130; quadratic-double: n_I feeding n_R through
+// kappa n_I^2, quadratic_double_reservoir.py:13-14); dn2 its derivative.
+template <typename T, bool GENERAL, bool TWO>
 __device__ __forceinline__ void site_rhs(const typename Cplx<T>::type c,
                                          const typename Cplx<T>::type lt,
                                          const typename Cplx<T>::type rt,
                                          const typename Cplx<T>::type up,
                                          const typename Cplx<T>::type dn, const T n, const T sP,
                                          const RhsConst<T>& k, const T vre, const T vim,
-                                         const RK4Features& f, T& dre, T& dim, T& dnr) {
+                                         const RK4Features& f, T& dre, T& dim, T& dnr,
+                                         const T n2, T& dn2) {
   const T rho = c.x * c.x + c.y * c.y;
   const T lre = k.ax * (lt.x + rt.x) + k.ay * (up.x + dn.x);
   const T lim = k.ax * (lt.y + rt.y) + k.ay * (up.y + dn.y);
@@ -66,6 +70,7 @@ __device__ __forceinline__ void site_rhs(const typename Cplx<T>::type c,
   if (GENERAL) {
     w += vre * k.inv_hbar;
     gl += vim * k.inv_hbar;
+    if (TWO) w += k.gi * n2;
   }
   dre = gl * c.x + w * c.y - lim;
   dim = gl * c.y - w * c.x + lre;
@@ -75,10 +80,22 @@ __device__ __forceinline__ void site_rhs(const typename Cplx<T>::type c,
     dim += en * (lim - k.w0 * c.y);
   }
   dnr = sP - (k.gamma_R + k.R * rho) * n;
-  if (GENERAL && f.reservoir == 0) dnr = T(0);
+  dn2 = T(0);
+  if (GENERAL) {
+    if (f.reservoir == 0) {
+      dnr = T(0);
+    } else if (TWO && f.reservoir == 2) {
+      dn2 = sP - (k.gamma_I + k.R_IA) * n2 + k.R_AI * n;
+      dnr = k.R_IA * n2 - (k.gamma_A + k.R_AI + k.R * rho) * n;
+    } else if (TWO && f.reservoir == 3) {
+      const T transfer = k.kappa * n2 * n2;
+      dnr = transfer - k.gamma_R * n - k.R * n * rho;
+      dn2 = sP - transfer - k.gamma_I * n2;
+    }
+  }
 }
 
-template <typename T, bool NOISE, bool GENERAL>
+template <typename T, bool NOISE, bool GENERAL, bool TWO>
 __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
     rk4_stream_kernel(const typename Cplx<T>::type* __restrict__ psi_in,
                       const T* __restrict__ n_in, const T* __restrict__ pump,
@@ -124,6 +141,9 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
 
   const C2* psi_m = psi_in + member * plane;
   const T* n_m = n_in + member * plane;
+  constexpr bool two = GENERAL && TWO;  // a second (inactive) reservoir field
+  const long long field2 = static_cast<long long>(g.members) * plane;  // offset of the inactive field
+  const T* n2_m = n_m + field2;
   const T* pump_m = pump + member * g.pump_stride;
   const T* pot_m = potential ? potential + member * g.pot_stride * (f.potential == 2 ? 2 : 1) : nullptr;
 
@@ -134,10 +154,12 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
   // Ring registers indexed by row & 3.
   C2 p0[4], q1[4], q2[4], q3[4], acc[4];
   T n0[4], m1[4], m2[4], m3[4], accn[4], P[4];
+  T u0[4], v1[4], v2[4], v3[4], accu[4];  // the inactive field's ring (two-field reservoirs)
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
     p0[s] = q1[s] = q2[s] = q3[s] = acc[s] = C2{T(0), T(0)};
     n0[s] = m1[s] = m2[s] = m3[s] = accn[s] = P[s] = T(0);
+    u0[s] = v1[s] = v2[s] = v3[s] = accu[s] = T(0);
   }
   for (int s = tid; s < 8 * nthreads; s += nthreads) xbuf[s] = C2{T(0), T(0)};
 
@@ -149,7 +171,7 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
 
   // Prefetch distance of two rows.
   C2 pf_psi[2];
-  T pf_n[2], pf_p[2];
+  T pf_n[2], pf_p[2], pf_u[2];
   {
     int rl = row_load, rp = row_pump;
 #pragma unroll
@@ -157,6 +179,7 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
       const long long o = static_cast<long long>(rl) * nx + gx;
       pf_psi[d] = psi_m[o];
       pf_n[d] = f.reservoir ? n_m[o] : T(0);
+      pf_u[d] = two ? n2_m[o] : T(0);
       pf_p[d] = pump_m[static_cast<long long>(rp) * nx + gx];
       rl = rl + 1 == ny ? 0 : rl + 1;
       rp = rp + 1 == ny ? 0 : rp + 1;
@@ -181,11 +204,13 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
       // Receive row r (psi0, n0) and pump row r-1; refill the prefetch slot.
       p0[j] = pf_psi[j & 1];
       n0[j] = pf_n[j & 1];
+      u0[j] = pf_u[j & 1];
       P[sa] = pf_p[j & 1];
       {
         const long long o = static_cast<long long>(row_pf) * nx + gx;
         pf_psi[j & 1] = psi_m[o];
         pf_n[j & 1] = f.reservoir ? n_m[o] : T(0);
+        pf_u[j & 1] = two ? n2_m[o] : T(0);
         pf_p[j & 1] = pump_m[static_cast<long long>(row_pf_pump) * nx + gx];
         row_pf = row_pf + 1 == ny ? 0 : row_pf + 1;
         row_pf_pump = row_pf_pump + 1 == ny ? 0 : row_pf_pump + 1;
@@ -201,13 +226,17 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
           vre = f.potential == 2 ? pot_m[2 * o] : pot_m[o];
           vim = f.potential == 2 ? pot_m[2 * o + 1] : T(0);
         }
-        T dre, dim, dnr;
-        site_rhs<T, GENERAL>(p0[sa], xin[lt_i], xin[rt_i], p0[sb], p0[j], n0[sa],
-                             mul_rn(s0, P[sa]), k, vre, vim, f, dre, dim, dnr);
+        T dre, dim, dnr, du;
+        site_rhs<T, GENERAL, TWO>(p0[sa], xin[lt_i], xin[rt_i], p0[sb], p0[j], n0[sa],
+                             mul_rn(s0, P[sa]), k, vre, vim, f, dre, dim, dnr, u0[sa], du);
         q1[sa] = C2{p0[sa].x + hh * dre, p0[sa].y + hh * dim};
         m1[sa] = n0[sa] + hh * dnr;
         acc[sa] = C2{p0[sa].x + h6 * dre, p0[sa].y + h6 * dim};
         accn[sa] = n0[sa] + h6 * dnr;
+        if (two) {
+          v1[sa] = u0[sa] + hh * du;
+          accu[sa] = u0[sa] + h6 * du;
+        }
       }
       // Stage 2 at row r-2: k2 = f(psi1).
       {
@@ -218,14 +247,18 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
           vre = f.potential == 2 ? pot_m[2 * o] : pot_m[o];
           vim = f.potential == 2 ? pot_m[2 * o + 1] : T(0);
         }
-        T dre, dim, dnr;
+        T dre, dim, dnr, du;
         const C2* xr = xin + nthreads;
-        site_rhs<T, GENERAL>(q1[sb], xr[lt_i], xr[rt_i], q1[sc], q1[sa], m1[sb],
-                             mul_rn(s1, P[sb]), k, vre, vim, f, dre, dim, dnr);
+        site_rhs<T, GENERAL, TWO>(q1[sb], xr[lt_i], xr[rt_i], q1[sc], q1[sa], m1[sb],
+                             mul_rn(s1, P[sb]), k, vre, vim, f, dre, dim, dnr, v1[sb], du);
         q2[sb] = C2{p0[sb].x + hh * dre, p0[sb].y + hh * dim};
         m2[sb] = n0[sb] + hh * dnr;
         acc[sb] = C2{acc[sb].x + h3 * dre, acc[sb].y + h3 * dim};
         accn[sb] = accn[sb] + h3 * dnr;
+        if (two) {
+          v2[sb] = u0[sb] + hh * du;
+          accu[sb] = accu[sb] + h3 * du;
+        }
       }
       // Stage 3 at row r-3: k3 = f(psi2).
       {
@@ -236,14 +269,18 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
           vre = f.potential == 2 ? pot_m[2 * o] : pot_m[o];
           vim = f.potential == 2 ? pot_m[2 * o + 1] : T(0);
         }
-        T dre, dim, dnr;
+        T dre, dim, dnr, du;
         const C2* xr = xin + 2 * nthreads;
-        site_rhs<T, GENERAL>(q2[sc], xr[lt_i], xr[rt_i], q2[sd], q2[sb], m2[sc],
-                             mul_rn(s1, P[sc]), k, vre, vim, f, dre, dim, dnr);
+        site_rhs<T, GENERAL, TWO>(q2[sc], xr[lt_i], xr[rt_i], q2[sd], q2[sb], m2[sc],
+                             mul_rn(s1, P[sc]), k, vre, vim, f, dre, dim, dnr, v2[sc], du);
         q3[sc] = C2{p0[sc].x + dt * dre, p0[sc].y + dt * dim};
         m3[sc] = n0[sc] + dt * dnr;
         acc[sc] = C2{acc[sc].x + h3 * dre, acc[sc].y + h3 * dim};
         accn[sc] = accn[sc] + h3 * dnr;
+        if (two) {
+          v3[sc] = u0[sc] + dt * du;
+          accu[sc] = accu[sc] + h3 * du;
+        }
       }
       // Stage 4 at row r-4: k4 = f(psi3), final combine, clamp, Wigner increment.
       {
@@ -252,14 +289,16 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
           vre = f.potential == 2 ? pot_m[2 * o] : pot_m[o];
           vim = f.potential == 2 ? pot_m[2 * o + 1] : T(0);
         }
-        T dre, dim, dnr;
+        T dre, dim, dnr, du;
         const C2* xr = xin + 3 * nthreads;
-        site_rhs<T, GENERAL>(q3[sd], xr[lt_i], xr[rt_i], q3[sa], q3[sc], m3[sd],
-                             mul_rn(s2, P[sd]), k, vre, vim, f, dre, dim, dnr);
+        site_rhs<T, GENERAL, TWO>(q3[sd], xr[lt_i], xr[rt_i], q3[sa], q3[sc], m3[sd],
+                             mul_rn(s2, P[sd]), k, vre, vim, f, dre, dim, dnr, v3[sd], du);
         T ore = acc[sd].x + h6 * dre;
         T oim = acc[sd].y + h6 * dim;
         T on = accn[sd] + h6 * dnr;
         on = on < T(0) ? T(0) : on;
+        T ou = two ? accu[sd] + h6 * du : T(0);
+        ou = ou < T(0) ? T(0) : ou;
         if (i >= 8 && i - 8 < h_eff && col_writes) {
           const long long o = static_cast<long long>(row_out) * nx + gx;
           if (NOISE) {
@@ -268,6 +307,7 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
           }
           psi_out[member * plane + o] = C2{ore, oim};
           if (!GENERAL || f.reservoir) n_out[member * plane + o] = on;
+          if (two) n_out[field2 + member * plane + o] = ou;
         }
       }
       // Publish this iteration's stage inputs for the horizontal neighbours.
@@ -285,7 +325,7 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
   }
 }
 
-template <typename T, bool NOISE, bool GENERAL>
+template <typename T, bool NOISE, bool GENERAL, bool TWO>
 cudaError_t launch_variant(const T* psi_in, const T* n_in, const T* pump, const T* potential,
                            T* psi_out, T* n_out, const RhsConst<T>* consts, const T* scales,
                            const unsigned long long* step_base, int step_offset, T dt,
@@ -296,7 +336,7 @@ cudaError_t launch_variant(const T* psi_in, const T* n_in, const T* pump, const 
   const int ntx = g.wrap ? 1 : (g.nx + g.tile_w - 1) / g.tile_w;
   const int nstrips = (g.ny + g.strip_h - 1) / g.strip_h;
   const size_t smem = sizeof(C2) * 8 * static_cast<size_t>(threads);
-  auto kern = rk4_stream_kernel<T, NOISE, GENERAL>;
+  auto kern = rk4_stream_kernel<T, NOISE, GENERAL, TWO>;
   kern<<<dim3(ntx, nstrips, g.members), threads, smem, stream>>>(
       reinterpret_cast<const C2*>(psi_in), n_in, pump, potential, reinterpret_cast<C2*>(psi_out),
       n_out, consts, scales, step_base, step_offset, dt, g, f);
@@ -311,20 +351,17 @@ cudaError_t launch_rk4_step(const T* psi_in, const T* n_in, const T* pump, const
                             const unsigned long long* step_base, int step_offset, T dt, bool noise,
                             const RK4Geom& g, const RK4Features& f, cudaStream_t stream) {
   const bool general = f.potential != 0 || f.relax != 0 || f.reservoir != 1;
+  const bool two = f.reservoir >= 2;
+#define PG_RK4_VARIANT(N, G, W)                                                                  \
+  launch_variant<T, N, G, W>(psi_in, n_in, pump, potential, psi_out, n_out, consts, scales,     \
+                             step_base, step_offset, dt, g, f, stream)
   if (noise) {
-    return general ? launch_variant<T, true, true>(psi_in, n_in, pump, potential, psi_out, n_out,
-                                                   consts, scales, step_base, step_offset, dt, g,
-                                                   f, stream)
-                   : launch_variant<T, true, false>(psi_in, n_in, pump, potential, psi_out, n_out,
-                                                    consts, scales, step_base, step_offset, dt, g,
-                                                    f, stream);
+    if (two) return PG_RK4_VARIANT(true, true, true);
+    return general ? PG_RK4_VARIANT(true, true, false) : PG_RK4_VARIANT(true, false, false);
   }
-  return general ? launch_variant<T, false, true>(psi_in, n_in, pump, potential, psi_out, n_out,
-                                                  consts, scales, step_base, step_offset, dt, g, f,
-                                                  stream)
-                 : launch_variant<T, false, false>(psi_in, n_in, pump, potential, psi_out, n_out,
-                                                   consts, scales, step_base, step_offset, dt, g,
-                                                   f, stream);
+  if (two) return PG_RK4_VARIANT(false, true, true);
+  return general ? PG_RK4_VARIANT(false, true, false) : PG_RK4_VARIANT(false, false, false);
+#undef PG_RK4_VARIANT
 }
 
 template cudaError_t launch_rk4_step<float>(const float*, const float*, const float*, const float*,

@@ -23,6 +23,7 @@ struct SplitConst {
   // of each component (used by the IFRK passes).
   T g_I, alpha_2, gamma_I, gamma_A, R_IA, R_AI;
   T weight[2];
+  T kappa;
 };
 
 struct RowPassArgs {

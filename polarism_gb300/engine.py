@@ -59,6 +59,7 @@ class MemberPhysics:
     te_tm: float = 0.0
     pump_weight_plus: float = 0.5
     pump_weight_minus: float = 0.5
+    kappa: float = 0.05
 
     @classmethod
     def from_object(cls, physics, index=None):
@@ -104,16 +105,17 @@ class RK4Engine:
         self.real = np.float32 if precision == "single" else np.float64
         self.complex = np.complex64 if precision == "single" else np.complex128
         kind = {True: "single", False: "none"}.get(reservoir, reservoir)
-        if kind not in ("none", "single", "double"):
+        if kind not in ("none", "single", "double", "quadratic-double"):
             raise ValueError(f"unknown reservoir {reservoir!r}")
-        self.res_fields = {"none": 0, "single": 1, "double": 2}[kind]
+        self.reservoir_kind = kind
+        self.res_fields = {"none": 0, "single": 1, "double": 2, "quadratic-double": 2}[kind]
         self.reservoir = self.res_fields > 0
         self.components = int(components)
         self.res_components = int(reservoir_components or self.components)
         self.potential_kind = int(potential)
         cfg = _lib.PgConfig(nx=self.nx, ny=self.ny, members=self.members,
                             precision=_lib.PG_SINGLE if precision == "single" else _lib.PG_DOUBLE,
-                            reservoir=self.res_fields,
+                            reservoir={"none": 0, "single": 1, "double": 2, "quadratic-double": 3}[kind],
                             potential=self.potential_kind, pump_per_member=int(pump_per_member),
                             potential_per_member=int(potential_per_member),
                             dx=float(dx), dy=float(dy), dt=float(dt),

@@ -361,6 +361,13 @@ class DoubleReservoir:
         return state[1]
 
 
+class QuadraticDoubleReservoir(DoubleReservoir):
+    """n_R fed by kappa n_I^2 from the inactive reservoir
+    (``polarism/reservoir/quadratic_double_reservoir.py:13-14``); state (n_R, n_I)."""
+
+    state_names = ("nR", "nI")
+
+
 class NoReservoir:
     state_names = ()
 
@@ -530,6 +537,7 @@ def build_simulation(cfg: Config, members: list[Config] | None = None):
     lasers = [[make_laser(m.laser, grid.X, grid.Y, precision)] for m in member_cfgs]
     pump = BatchedPumpField(lasers, grid, precision) if batched else PumpField(lasers[0], grid, precision)
     res_cls = {"single": SingleReservoir, "double": DoubleReservoir,
+               "quadratic-double": QuadraticDoubleReservoir,
                "none": NoReservoir}[cfg.reservoir.reservoir_type]
     reservoir = res_cls(cfg.physics, grid, precision, batch_size=len(member_cfgs) if batched else None,
                         components=res_components)

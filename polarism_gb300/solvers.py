@@ -46,8 +46,10 @@ class _GB300Solver(AbstractSolver):
 
     name = "gb300"
     injects_noise = True
-    #: Two-component fields and the double reservoir run on the IFRK passes only.
+    #: Two-component fields run on the IFRK passes only.
     spinor_and_double = False
+    #: Reservoir types the class steps.
+    reservoir_types = ("single", "none")
 
     def __init__(self, config, grid, model):
         super().__init__(config, grid, model)
@@ -57,8 +59,7 @@ class _GB300Solver(AbstractSolver):
         if getattr(grid, "ndim", 2) != 2 or getattr(grid, "boundary", "periodic") != "periodic":
             raise ValueError(f"{self.name} (GB300) supports two-dimensional periodic grids")
         reservoir_type = getattr(getattr(config, "reservoir", None), "reservoir_type", "single")
-        allowed = ("single", "none", "double") if self.spinor_and_double else ("single", "none")
-        if reservoir_type not in allowed:
+        if reservoir_type not in self.reservoir_types:
             raise ValueError(f"{self.name} (GB300) does not support reservoir_type={reservoir_type!r}")
         self._reservoir_type = reservoir_type
         self._res_components = int(getattr(model, "reservoir_components", None)
@@ -193,7 +194,7 @@ class _GB300Solver(AbstractSolver):
         device = _is_device(array)
         if self._reservoir_type == "single":
             res0 = res_state[0]
-        elif self._reservoir_type == "double":  # active then inactive, (2, B, Cr, ny, nx)
+        elif self._reservoir_type in ("double", "quadratic-double"):  # (2, B, Cr, ny, nx)
             if device:
                 import torch
 
@@ -222,7 +223,7 @@ class _GB300Solver(AbstractSolver):
     def _finish(self, model, state, res, n_steps):
         if self._reservoir_type == "single":
             model.reservoir.set_state((res,))
-        elif self._reservoir_type == "double":
+        elif self._reservoir_type in ("double", "quadratic-double"):
             model.reservoir.set_state((res[0], res[1]))
         state.step += n_steps
         state.t = state.t0 + state.step * self._dt
@@ -236,12 +237,14 @@ class RK4CudaSolver(_GB300Solver):
     """Fused whole-step RK4 on GB300 with in-kernel Philox Wigner noise (``rk4-cuda``)."""
 
     name = "rk4-cuda"
+    reservoir_types = ("single", "none", "double", "quadratic-double")
     capabilities = SolverCapabilities(
         components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
-        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
+        reservoirs=frozenset({"single", "double", "quadratic-double", "none"}),
+        custom_reservoirs="unsupported",
         potential=True, kinetic_relaxation=True, dispersion=frozenset({"parabolic"}),
         terms=False, noise=frozenset({"none", "wigner"}), adaptive=False,
-        quantitative_reservoirs=frozenset({"single", "none"}),
+        quantitative_reservoirs=frozenset({"single", "double", "quadratic-double", "none"}),
         description="GB300 fused RK4 (one sm_103a kernel per step, stage-coupled reservoir, "
                     "Philox Wigner noise in registers).")
 
@@ -346,12 +349,14 @@ class IFRKFFTCudaSolver(_GB300Solver):
     name = "ifrk-fft-cuda"
     tableau_name = None
     spinor_and_double = True
+    reservoir_types = ("single", "none", "double", "quadratic-double")
     capabilities = SolverCapabilities(
         components=frozenset({1, 2}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
-        reservoirs=frozenset({"single", "double", "none"}), custom_reservoirs="unsupported",
+        reservoirs=frozenset({"single", "double", "quadratic-double", "none"}),
+        custom_reservoirs="unsupported",
         potential=True, kinetic_relaxation=False, dispersion=frozenset({"parabolic"}),
         terms=False, noise=frozenset({"none", "wigner"}), adaptive=True,
-        quantitative_reservoirs=frozenset({"single", "double", "none"}),
+        quantitative_reservoirs=frozenset({"single", "double", "quadratic-double", "none"}),
         description="GB300 Lawson IFRK (rk4, dp5) with fused Stockham stage passes, FP64 "
                     "embedded error norm, spinor (TE-TM, Zeeman, cross-spin) and double "
                     "reservoirs; nx, ny powers of two.")
@@ -439,7 +444,7 @@ class IFRKFFTCudaSolver(_GB300Solver):
             state.field = psi
             if self._reservoir_type == "single":
                 model.reservoir.set_state((res,))
-            elif self._reservoir_type == "double":
+            elif self._reservoir_type in ("double", "quadratic-double"):
                 model.reservoir.set_state((res[0], res[1]))
             state.t += dt
         return StepReport(accepted, err, None)

@@ -157,6 +157,12 @@ def _controller(method, nx, ny, lx, ly, dt, p0, sigma, seed, wigner, precision="
 
 def trajectory_case(out, name, method, steps, **kw):
     ctl = _controller(method, **kw)
+    if ctl.reservoir.get_state() and len(ctl.reservoir.get_state()) == 2:
+        # Start the two-field reservoirs away from zero so both fields take part.
+        g = ctl.grid
+        blob = np.exp(-0.5 * (g.X ** 2 + g.Y ** 2) / 8.0 ** 2)
+        ctl.reservoir.set_state(tuple(np.asarray((0.5 + 0.5 * q) * np.broadcast_to(blob, f.shape), dtype=f.dtype)
+                                      for q, f in enumerate(ctl.reservoir.get_state())))
     grid = ctl.grid
     psi0 = np.array(ctl.state.field, copy=True)
     res0 = tuple(np.array(f, copy=True) for f in ctl.reservoir.get_state())
@@ -169,6 +175,7 @@ def trajectory_case(out, name, method, steps, **kw):
         out / f"{name}.npz", psi0=psi0, res0=np.stack(res0), envelope=env,
         p0=np.float64(kw["p0"]), dt=np.float64(kw["dt"]), dx=np.float64(grid.dx),
         dy=np.float64(grid.dy), k_squared=np.asarray(grid.k_squared), steps=np.int64(steps),
+        reservoir=kw.get("reservoir", "single"),
         seed=np.uint64(kw["seed"]), wigner=np.bool_(kw["wigner"]),
         physics=_physics_json(ctl.cfg), psi=np.asarray(ctl.state.field),
         res=np.stack([np.asarray(f) for f in ctl.reservoir.get_state()]),
@@ -360,6 +367,9 @@ def main(root):
                     **dict(common, wigner=False, seed=0, p0=0.02, sigma=12.0))
     trajectory_case(HERE, "split_cpu_p2", "split-step-fft", 12,
                     **dict(common, nx=32, ny=16, lx=40.0, ly=20.0))
+    for res in ("double", "quadratic-double"):
+        trajectory_case(HERE, "rk4_fdm_" + res.replace("-", "_"), "rk4-fdm", 20,
+                        **dict(common, reservoir=res, p0=0.3))
     kouter_case(HERE)
     ifrk4_cases(HERE, root)
     dp5_case(HERE)

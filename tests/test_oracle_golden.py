@@ -65,8 +65,9 @@ def _trajectory(g, method, normals=None):
     psi, fields = g["psi0"].copy(), tuple(g["res0"])
     norms = []
     if method == "rk4":
+        kind = {1: "single", 2: str(g["reservoir"]) if "reservoir" in g else "double"}[len(fields)]
         psi, fields = gpe.rk4_advance(psi, fields, lambda t: pump, 0.0, p, dx, dy, dt, 0,
-                                      int(g["steps"]), noise=noise, norm_trace=norms)
+                                      int(g["steps"]), noise=noise, norm_trace=norms, kind=kind)
     else:
         psi, fields = gpe.split_advance("cpu", psi, fields, lambda t: pump, 0.0, p, g["k_squared"],
                                         dx, dy, dt, 0, int(g["steps"]), noise=noise,
@@ -75,12 +76,14 @@ def _trajectory(g, method, normals=None):
 
 
 @pytest.mark.parametrize("case,method", [("rk4_fdm", "rk4"), ("rk4_fdm_quiet", "rk4"),
-                                         ("split_cpu", "split")])
+                                         ("split_cpu", "split"), ("rk4_fdm_double", "rk4"),
+                                         ("rk4_fdm_quadratic_double", "rk4")])
 def test_fp64_trajectories_match_reference(golden, case, method):
     g = golden(case)
     psi, fields, norms = _trajectory(g, method)
     assert rel_l2(psi, g["psi"]) < 1e-12
-    assert rel_l2(fields[0], g["res"][0]) < 1e-12
+    for q in range(len(fields)):
+        assert rel_l2(fields[q], g["res"][q]) < 1e-12, q
     assert rel_l2(norms, g["norms"]) < 1e-12
 
 
