@@ -188,6 +188,7 @@ PassPlan plan(const pg_solver* s) {
   k.threads = threads < 32 ? 32 : threads;
   k.members = c.members;
   k.reservoir = c.reservoir == PG_RES_SINGLE;
+  k.res_kind = c.reservoir;
   k.potential = c.potential;
   k.noise = s->noise ? 1 : 0;
   k.pump_stride = c.pump_per_member ? s->plane : 0;
@@ -354,9 +355,8 @@ int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t
   PG_CHECK(ordering == 0 || ordering == 1, PG_ERR_INVALID,
            "pg_split_advance: ordering must be 0 (R/2 K/2 N K/2 R/2) or 1 (K/2 [R/2 N R/2] K/2)");
   PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_split_advance: negative step count");
-  PG_CHECK(s->comps == 1 && s->res_fields <= 1, PG_ERR_UNSUPPORTED,
-           "pg_split_advance: two-component fields and two-field reservoirs run on the RK4 and IFRK "
-           "paths");
+  PG_CHECK(s->comps == 1 && s->res_comps == 1, PG_ERR_UNSUPPORTED,
+           "pg_split_advance: two-component fields run on the IFRK path");
   if (n_steps == 0) return PG_OK;
   pg::ifrk_invalidate(s);
   int rc = pg::ensure_split(s);

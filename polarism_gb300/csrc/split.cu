@@ -91,16 +91,48 @@ __device__ __forceinline__ T reservoir_half(T n, T rho, T pump, T h, const Split
   return out > T(0) ? out : T(0);
 }
 
-// Exact local step psi * exp(g dt - i phi) (split_step_fft_solver.py:121-139).
+// Right-hand sides of the two-field reservoirs, state (active, inactive): the double
+// reservoir (polarism/reservoir/double_reservoir.py:106-130) and the quadratic-double one,
+// fed by kappa n_I^2 (polarism/reservoir/quadratic_double_reservoir.py:13-14).
 template <typename T>
-__device__ __forceinline__ void nonlinear(T& re, T& im, T n, T vre, T vim, T dt,
+__device__ __forceinline__ void two_field_rhs(T a, T b, T rho, T pump, bool quadratic,
+                                              const SplitConst<T>& k, T& da, T& db) {
+  if (quadratic) {
+    const T transfer = k.kappa * b * b;
+    da = transfer - k.gamma_R * a - k.R * a * rho;
+    db = pump - transfer - k.gamma_I * b;
+  } else {
+    da = k.R_IA * b - (k.gamma_A + k.R_AI + k.R * rho) * a;
+    db = pump - (k.gamma_I + k.R_IA) * b + k.R_AI * a;
+  }
+}
+
+// The same midpoint half step for both fields of a two-field reservoir, each clamped at 0.
+template <typename T>
+__device__ __forceinline__ void reservoir_half2(T& a, T& b, T rho, T pump, T h, bool quadratic,
+                                                const SplitConst<T>& k) {
+  T da, db;
+  two_field_rhs(a, b, rho, pump, quadratic, k, da, db);
+  T da2, db2;
+  two_field_rhs(a + T(0.5) * h * da, b + T(0.5) * h * db, rho, pump, quadratic, k, da2, db2);
+  const T na = a + h * da2, nb = b + h * db2;
+  a = na > T(0) ? na : T(0);
+  b = nb > T(0) ? nb : T(0);
+}
+
+// Exact local step psi * exp(g dt - i phi) (split_step_fft_solver.py:121-139); n2 is the
+// inactive reservoir (0 without one), which enters the phase through g_I.
+template <typename T>
+__device__ __forceinline__ void nonlinear(T& re, T& im, T n, T n2, bool two, T vre, T vim, T dt,
                                           const SplitConst<T>& k) {
   const T rho = re * re + im * im;
   const T gain = (k.R * n - k.gamma_C) * T(0.5) + vim * k.inv_hbar;
   const T x = T(2) * gain * dt;
   const T phase_time =
       fabs(x) < T(1e-6) ? dt * (T(1) + x * T(0.5) + x * x / T(6)) : dt * expm1_t(x) / x;
-  const T phase = ((vre + k.g_R * n) * dt + k.g_C * rho * phase_time) * k.inv_hbar;
+  T pot = vre + k.g_R * n;
+  if (two) pot += k.g_I * n2;
+  const T phase = (pot * dt + k.g_C * rho * phase_time) * k.inv_hbar;
   const T amp = exp_t(gain * dt);
   T s, c;
   sincos_t(phase, &s, &c);
@@ -145,14 +177,27 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
     const T* pm = pump + member * a.pump_stride;
     const T* vm = potential ? potential + member * a.pot_stride * (a.potential == 2 ? 2 : 1) : nullptr;
     T* rm = res + member * plane;
+    // Second reservoir field (inactive) one field after the first: [field][member][y][x].
+    const bool two = a.res_kind >= 2;
+    const bool quadratic = a.res_kind == 3;
+    T* rm2 = two ? rm + static_cast<long long>(a.members) * plane : nullptr;
     const T dt = a.template dt_of<T>();
     const T h = dt * T(0.5);
     const unsigned long long step = a.noise ? step_base[0] + a.step_offset : 0ull;
+    // One reservoir half step at the given pump coefficient on the chosen model.
+    auto res_half = [&](T& n, T& n2, T rho, T pump_value) {
+      if (two) {
+        reservoir_half2(n, n2, rho, pump_value, h, quadratic, k);
+      } else if (a.reservoir) {
+        n = reservoir_half(n, rho, pump_value, h, k);
+      }
+    };
     for (int e = threadIdx.x; e < count; e += blockDim.x) {
       const int c = e & (C - 1), i = e >> a.log2cols;
       const long long o = static_cast<long long>(i) * a.nx + x0 + c;
       C2 v = buf[i * C + c];
-      T n = a.reservoir ? rm[o] : T(0);
+      T n = (a.reservoir || two) ? rm[o] : T(0);
+      T n2 = two ? rm2[o] : T(0);
       const T P = pm[o];
       T vre = T(0), vim = T(0);
       if (vm) {
@@ -162,27 +207,26 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
       bool add_noise = false;
       switch (a.op) {
         case SPLIT_OP_KOUTER:
-          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
-          nonlinear(v.x, v.y, n, vre, vim, dt, k);
-          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s1, P), h, k);
+          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s0, P));
+          nonlinear(v.x, v.y, n, n2, two, vre, vim, dt, k);
+          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s1, P));
           add_noise = a.noise != 0;
           break;
         case SPLIT_OP_RES_START:
-          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
+          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s0, P));
           break;
-        case SPLIT_OP_RES_END_START:
-          if (a.reservoir) {
-            const T rho = v.x * v.x + v.y * v.y;
-            n = reservoir_half(n, rho, mul_rn_t(s0, P), h, k);
-            n = reservoir_half(n, rho, mul_rn_t(s1, P), h, k);
-          }
+        case SPLIT_OP_RES_END_START: {
+          const T rho = v.x * v.x + v.y * v.y;
+          res_half(n, n2, rho, mul_rn_t(s0, P));
+          res_half(n, n2, rho, mul_rn_t(s1, P));
           break;
+        }
         case SPLIT_OP_NONLINEAR:
-          nonlinear(v.x, v.y, n, vre, vim, dt, k);
+          nonlinear(v.x, v.y, n, n2, two, vre, vim, dt, k);
           add_noise = a.noise != 0;
           break;
         case SPLIT_OP_RES_END:
-          if (a.reservoir) n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
+          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s0, P));
           break;
         default:
           break;
@@ -192,7 +236,8 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
         WignerDraw<T>::apply(w, k.noise_a + k.noise_b * n, v.x, v.y);
       }
       buf[i * C + c] = v;
-      if (a.reservoir) rm[o] = n;
+      if (a.reservoir || two) rm[o] = n;
+      if (two) rm2[o] = n2;
     }
     __syncthreads();
   }

@@ -19,8 +19,9 @@ struct SplitConst {
   T inv_hbar, g_C, g_R, R, gamma_C, gamma_R;
   T noise_a, noise_b;
   unsigned long long seed;
-  // Inactive-reservoir coupling, cross-spin term, double-reservoir rates and the pump share
-  // of each component (used by the IFRK passes).
+  // Inactive-reservoir coupling, cross-spin term, two-field reservoir rates and the pump
+  // share of each component (the cross-spin term and the shares are read by the IFRK
+  // passes only).
   T g_I, alpha_2, gamma_I, gamma_A, R_IA, R_AI;
   T weight[2];
   T kappa;
@@ -42,6 +43,7 @@ struct ColPassArgs {
   int forward, inverse;
   int op;               // SplitOp
   int reservoir;        // single reservoir present
+  int res_kind;         // PG_RES_*: 2 double, 3 quadratic-double use the second field
   int potential;        // 0 none, 1 real, 2 complex
   int noise;
   long long pump_stride, pot_stride;

@@ -277,12 +277,14 @@ class SplitStepFFTSolver(_GB300Solver):
 
     name = "split-step-fft"
     ordering = 0
+    reservoir_types = ("single", "none", "double", "quadratic-double")
     capabilities = SolverCapabilities(
         components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
-        reservoirs=frozenset({"single", "none"}), custom_reservoirs="unsupported",
+        reservoirs=frozenset({"single", "double", "quadratic-double", "none"}),
+        custom_reservoirs="unsupported",
         potential=True, kinetic_relaxation=False, dispersion=frozenset({"parabolic"}),
         terms=False, noise=frozenset({"none", "wigner"}), adaptive=False,
-        quantitative_reservoirs=frozenset({"single", "none"}),
+        quantitative_reservoirs=frozenset({"single", "double", "quadratic-double", "none"}),
         description="GB300 split-step Fourier (R/2 K/2 N K/2 R/2) with shared-memory Stockham "
                     "FFT passes fused with the propagator and the local step; nx, ny powers "
                     "of two.")

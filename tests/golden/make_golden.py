@@ -370,6 +370,8 @@ def main(root):
     for res in ("double", "quadratic-double"):
         trajectory_case(HERE, "rk4_fdm_" + res.replace("-", "_"), "rk4-fdm", 20,
                         **dict(common, reservoir=res, p0=0.3))
+        trajectory_case(HERE, "split_cpu_p2_" + res.replace("-", "_"), "split-step-fft", 12,
+                        **dict(common, nx=32, ny=16, lx=40.0, ly=20.0, reservoir=res, p0=0.3))
     kouter_case(HERE)
     ifrk4_cases(HERE, root)
     dp5_case(HERE)

@@ -64,20 +64,22 @@ def _trajectory(g, method, normals=None):
                           "double", normals)
     psi, fields = g["psi0"].copy(), tuple(g["res0"])
     norms = []
+    kind = str(g["reservoir"])
     if method == "rk4":
-        kind = {1: "single", 2: str(g["reservoir"]) if "reservoir" in g else "double"}[len(fields)]
         psi, fields = gpe.rk4_advance(psi, fields, lambda t: pump, 0.0, p, dx, dy, dt, 0,
                                       int(g["steps"]), noise=noise, norm_trace=norms, kind=kind)
     else:
         psi, fields = gpe.split_advance("cpu", psi, fields, lambda t: pump, 0.0, p, g["k_squared"],
                                         dx, dy, dt, 0, int(g["steps"]), noise=noise,
-                                        norm_trace=norms)
+                                        norm_trace=norms, kind=kind)
     return psi, fields, np.asarray(norms).ravel()
 
 
 @pytest.mark.parametrize("case,method", [("rk4_fdm", "rk4"), ("rk4_fdm_quiet", "rk4"),
                                          ("split_cpu", "split"), ("rk4_fdm_double", "rk4"),
-                                         ("rk4_fdm_quadratic_double", "rk4")])
+                                         ("rk4_fdm_quadratic_double", "rk4"),
+                                         ("split_cpu_p2_double", "split"),
+                                         ("split_cpu_p2_quadratic_double", "split")])
 def test_fp64_trajectories_match_reference(golden, case, method):
     g = golden(case)
     psi, fields, norms = _trajectory(g, method)
