@@ -94,10 +94,11 @@ __device__ __forceinline__ PhiloxCellPrefix philox_cell_prefix(uint32_t step_lo,
   return p;
 }
 
-__device__ __forceinline__ void philox_cells_octet(const uint32_t (&cell)[8], const PhiloxCellPrefix& p,
-                                                   Words4 (&x)[8]) {
+template <int N>
+__device__ __forceinline__ void philox_cells(const uint32_t (&cell)[N], const PhiloxCellPrefix& p,
+                                             Words4 (&x)[N]) {
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
+  for (int q = 0; q < N; ++q) {
     // Round 1: a' = hi(c M1) ^ b ^ k0 and b' = lo(c M1) are cell independent.
     const uint64_t r0 = static_cast<uint64_t>(cell[q]) * 0xD2511F53ull;
     const uint32_t c1 = static_cast<uint32_t>(r0 >> 32) ^ p.stream_k1;
@@ -111,7 +112,7 @@ __device__ __forceinline__ void philox_cells_octet(const uint32_t (&cell)[8], co
 #pragma unroll
   for (int round = 2; round < 10; ++round) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < N; ++q) {
       const uint64_t p0 = static_cast<uint64_t>(x[q].a) * 0xD2511F53ull;
       const uint64_t p1 = static_cast<uint64_t>(x[q].c) * 0xCD9E8D57ull;
       x[q] = Words4{static_cast<uint32_t>(p1 >> 32) ^ x[q].b ^ k0, static_cast<uint32_t>(p1),
@@ -158,14 +159,24 @@ struct WignerDraw<float> {
     angle(w.b, &s, &c);
     return make_float2(r * c, r * s);
   }
-  static __device__ __forceinline__ void apply(const Words4& w, float variance, float& re,
-                                               float& im) {
-    const float x = variance * radius2(w.a);
-    const float amp = x > 0.0f ? x * rsqrtf(x) : 0.0f;
-    float s, c;
+  // The part of the draw that does not depend on the variance: -2 ln u1 and the angle.
+  static __device__ __forceinline__ void prepare(const Words4& w, float& r2, float& s, float& c) {
+    r2 = radius2(w.a);
     angle(w.b, &s, &c);
+  }
+  // Adds sqrt(variance * r2) (cos, sin) to (re, im).
+  static __device__ __forceinline__ void add(float variance, float r2, float s, float c, float& re,
+                                             float& im) {
+    const float x = variance * r2;
+    const float amp = x > 0.0f ? x * rsqrtf(x) : 0.0f;
     re = fmaf(amp, c, re);
     im = fmaf(amp, s, im);
+  }
+  static __device__ __forceinline__ void apply(const Words4& w, float variance, float& re,
+                                               float& im) {
+    float r2, s, c;
+    prepare(w, r2, s, c);
+    add(variance, r2, s, c, re, im);
   }
 };
 

@@ -69,18 +69,23 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
                      const unsigned long long* __restrict__ step_base, const int step_offset,
                      const float dt, int* __restrict__ err_flag) {
   constexpr int HALF = LANES / 2;
+  // One block per SM (1024 lanes): a split arrive/wait barrier lets its warps drift apart
+  // by up to a row, which measured faster; with two blocks per SM the blocks already
+  // interleave and a block-wide barrier is cheaper.
+  constexpr bool kSplit = LANES >= 1024;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float2* ring_psi = reinterpret_cast<float2*>(smem_raw);             // [kRing][LANES]
   float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * LANES); // [kRing][LANES]
   float* ring_p = ring_n + kRing * LANES;                             // [kRing][LANES]
   float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * LANES);   // [2][3][HALF]
-  float4* nbuf = xbuf + 6 * HALF;                                     // [4][HALF]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(nbuf + (NOISE ? 4 * HALF : 0));
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kRing] + exchange barrier
+  const uint32_t xbar = smem_u32(&mbar[kRing]);
 
   const int t = threadIdx.x;
   const int col0 = 2 * t;  // ring column of the thread's first site
   if (t == 0) {
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
+    if (kSplit) mbar_init(xbar, LANES / 2);
     fence_mbar_init();
   }
   __syncthreads();
@@ -144,7 +149,7 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
       bulk_g2s(smem_u32(ring_p + slot * LANES + base), p_m + src, W * 4u, bar);
     };
     if (t == 0) {
-      for (int i = 0; i < 3 && i < n_iter; ++i) arm(i);
+      for (int i = 0; i < (kSplit ? 4 : 3) && i < n_iter; ++i) arm(i);
     }
     __syncthreads();
     if (lt == 0) {
@@ -166,24 +171,6 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
 #pragma unroll
       for (int j = 0; j < kRing; ++j) {
         const int i = i0 + j;
-        if (NOISE && (j & 3) == 0) {
-          int row = row_out;
-          uint32_t cells[8];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            cells[2 * q] = static_cast<uint32_t>((row << wl2) + lc);
-            cells[2 * q + 1] = cells[2 * q] + 1u;
-            row = row + 1 == ny ? 0 : row + 1;
-          }
-          Words4 w[8];
-          philox_cells_octet(cells, prefix, w);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float2 za = WignerDraw<float>::unit(w[2 * q]);
-            const float2 zb = WignerDraw<float>::unit(w[2 * q + 1]);
-            nbuf[q * HALF + t] = make_float4(za.x, za.y, zb.x, zb.y);
-          }
-        }
         const int ja = (j + 3) & 3, jb = (j + 2) & 3, jc = (j + 1) & 3, jd = j & 3;
         const int slot0 = j;
         const int slot1 = (j + kRing - 1) % kRing;
@@ -191,6 +178,18 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
         const int slot3 = (j + kRing - 3) % kRing;
         const int slot4 = (j + kRing - 4) % kRing;
         if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitLimit)) timed_out = true;
+        // Philox words and the variance-free part of the Box-Muller draw for this
+        // iteration's output row, in the same straight-line code as the four stages so
+        // that the integer and SFU work fills the stencil's issue gaps.
+        float r2a = 0.f, sna = 0.f, csa = 0.f, r2b = 0.f, snb = 0.f, csb = 0.f;
+        if (NOISE) {
+          const uint32_t cell = static_cast<uint32_t>((row_out << wl2) + lc);
+          const uint32_t cells[2] = {cell, cell + 1u};
+          Words4 w[2];
+          philox_cells(cells, prefix, w);
+          WignerDraw<float>::prepare(w[0], r2a, sna, csa);
+          WignerDraw<float>::prepare(w[1], r2b, snb, csb);
+        }
         const float4* xin = xbuf + ((j + 1) & 1) * 3 * HALF;
 
         // Stage 1 at row r-1 from the ring.
@@ -212,6 +211,15 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
           acc[ja] = Pair{axpy2(h6, da, c0), axpy2(h6, db, c1)};
           m1[ja] = make_float2(fmaf(hh, dna, n1v.x), fmaf(hh, dnb, n1v.y));
           accn[ja] = make_float2(fmaf(h6, dna, n1v.x), fmaf(h6, dnb, n1v.y));
+        }
+        if (kSplit) {
+          // Split barrier: wait until every thread has arrived at the end of iteration
+          // i-1 (published its stage values, finished reading the exchange buffer written
+          // below and the ring slot of row r-5 that the copy of row r+3 reuses).  Thread 0
+          // armed that slot's barrier before arriving, so the copies follow the arming.
+          const unsigned g = it + i;
+          if (g > 0 && !mbar_wait_bounded(xbar, (g - 1) & 1u, kWaitLimit)) timed_out = true;
+          if (lt == 0 && i + 3 < n_iter) issue(i + 3);
         }
         // Stage 2 at row r-2.
         {
@@ -268,13 +276,8 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
           if (writer && i >= 8 && i - 8 < h_rows) {
             const long long o = static_cast<long long>(row_out) << wl2;
             if (NOISE) {
-              const float4 z = nbuf[(j & 3) * HALF + t];
-              const float va = fmaf(k.noise_b, na, k.noise_a);
-              const float vb = fmaf(k.noise_b, nb, k.noise_a);
-              const float sa = va > 0.f ? va * rsqrtf(va) : 0.f;
-              const float sb = vb > 0.f ? vb * rsqrtf(vb) : 0.f;
-              oa = __ffma2_rn(make_float2(sa, sa), make_float2(z.x, z.y), oa);
-              ob = __ffma2_rn(make_float2(sb, sb), make_float2(z.z, z.w), ob);
+              WignerDraw<float>::add(fmaf(k.noise_b, na, k.noise_a), r2a, sna, csa, oa.x, oa.y);
+              WignerDraw<float>::add(fmaf(k.noise_b, nb, k.noise_a), r2b, snb, csb, ob.x, ob.y);
             }
             *reinterpret_cast<float4*>(out_psi_m + o) = make_float4(oa.x, oa.y, ob.x, ob.y);
             *reinterpret_cast<float2*>(out_n_m + o) = make_float2(na, nb);
@@ -287,10 +290,18 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
           xo[2 * HALF + t] = make_float4(q3[jc].a.x, q3[jc].a.y, q3[jc].b.x, q3[jc].b.y);
         }
         row_out = row_out + 1 == ny ? 0 : row_out + 1;
-        // The slot of row r+3 held row r-5, last read by stage 4 of the previous iteration.
-        if (t == 0 && i + 3 < n_iter) arm(i + 3);
-        __syncthreads();
-        if (lt == 0 && i + 3 < n_iter) issue(i + 3);
+        if (kSplit) {
+          // Arm the slot the next iteration's copies fill (its last phase, row r-4, has
+          // completed), then arrive on the exchange barrier.
+          if (t == 0 && i + 4 < n_iter) arm(i + 4);
+          mbar_arrive(xbar);
+        } else {
+          // The slot of row r+3 held row r-5, last read by stage 4 of the previous
+          // iteration.
+          if (t == 0 && i + 3 < n_iter) arm(i + 3);
+          __syncthreads();
+          if (lt == 0 && i + 3 < n_iter) issue(i + 3);
+        }
       }
     }
     it += n_iter;
@@ -299,8 +310,8 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
 }
 
 size_t sweep_smem(int lanes) {
-  return static_cast<size_t>(kRing) * lanes * 16 + static_cast<size_t>(10) * (lanes / 2) * 16 +
-         kRing * sizeof(uint64_t);
+  return static_cast<size_t>(kRing) * lanes * 16 + static_cast<size_t>(6) * (lanes / 2) * 16 +
+         (kRing + 1) * sizeof(uint64_t);
 }
 
 template <int LANES>

@@ -10,7 +10,9 @@
 //   through 1-D bulk copies (TMA) that complete on per-slot mbarriers, three rows
 //   ahead of use.  Stage 1 reads its whole stencil straight from the ring; stages 2-4
 //   get vertical neighbours from per-thread register rings and horizontal ones from
-//   one double-buffered shared exchange per row.
+//   one double-buffered shared exchange per row, ordered (for 1024-site rows) by a
+//   split arrive/wait mbarrier rather than a block-wide barrier, so warps drift apart
+//   by up to a row.
 // * Complex arithmetic uses packed FP32x2 instructions (__ffma2_rn and friends).
 // * Blocks are persistent: block c advances rows [c R / G, (c+1) R / G) of the
 //   member-major row space (R = members * ny rows), restarting the 4-row pipeline
@@ -37,13 +39,17 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
                     const unsigned long long* __restrict__ step_base, const int step_offset,
                     const float dt, const WideGeom g, int* __restrict__ err_flag) {
   constexpr int HALF = NX / 2;
+  // One block per SM (1024-site rows): a split arrive/wait barrier lets its warps drift
+  // apart by up to a row, which measured faster; with several blocks per SM the blocks
+  // already interleave and a block-wide barrier is cheaper.
+  constexpr bool kSplit = NX >= 1024;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][NX]
   float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * NX); // [kRing][NX]
   float* ring_p = ring_n + kRing * NX;                             // [kRing][NX]
   float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * NX);   // [2][3][HALF]
-  float4* nbuf = xbuf + 6 * HALF;                                  // [4][HALF] unit normals
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(nbuf + (NOISE ? 4 * HALF : 0));
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kRing] + exchange barrier
+  const uint32_t xbar = smem_u32(&mbar[kRing]);
 
   const int ny = g.ny;
   const int t = threadIdx.x;
@@ -57,6 +63,7 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
 
   if (t == 0) {
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
+    if (kSplit) mbar_init(xbar, HALF);
     fence_mbar_init();
   }
   __syncthreads();
@@ -125,26 +132,6 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
 #pragma unroll
       for (int j = 0; j < kRing; ++j) {
         const int i = i0 + j;
-        if (NOISE && (j & 3) == 0) {
-          // Unit normals for the output rows of iterations i..i+3: eight independent
-          // Philox streams (four rows, two columns) under one key schedule.
-          int row = row_out;
-          uint32_t cells[8];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            cells[2 * q] = static_cast<uint32_t>(row * NX + col0);
-            cells[2 * q + 1] = cells[2 * q] + 1u;
-            row = row + 1 == ny ? 0 : row + 1;
-          }
-          Words4 w[8];
-          philox_cells_octet(cells, prefix, w);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float2 za = WignerDraw<float>::unit(w[2 * q]);
-            const float2 zb = WignerDraw<float>::unit(w[2 * q + 1]);
-            nbuf[q * HALF + t] = make_float4(za.x, za.y, zb.x, zb.y);
-          }
-        }
         const int ja = (j + 3) & 3, jb = (j + 2) & 3, jc = (j + 1) & 3, jd = j & 3;
         const int slot0 = j;                        // row r
         const int slot1 = (j + kRing - 1) % kRing;  // row r-1
@@ -152,6 +139,18 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
         const int slot3 = (j + kRing - 3) % kRing;  // row r-3
         const int slot4 = (j + kRing - 4) % kRing;  // row r-4
         if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitLimit)) timed_out = true;
+        // Philox words and the variance-free part of the Box-Muller draw for this
+        // iteration's output row, in the same straight-line code as the four stages so
+        // that the integer and SFU work fills the stencil's issue gaps.
+        float r2a = 0.f, sna = 0.f, csa = 0.f, r2b = 0.f, snb = 0.f, csb = 0.f;
+        if (NOISE) {
+          const uint32_t cell = static_cast<uint32_t>(row_out * NX + col0);
+          const uint32_t cells[2] = {cell, cell + 1u};
+          Words4 w[2];
+          philox_cells(cells, prefix, w);
+          WignerDraw<float>::prepare(w[0], r2a, sna, csa);
+          WignerDraw<float>::prepare(w[1], r2b, snb, csb);
+        }
         const float4* xin = xbuf + ((j + 1) & 1) * 3 * HALF;
 
         // Stage 1 at row r-1 from the ring: k1 = f(psi0).
@@ -173,6 +172,16 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
           acc[ja] = Pair{axpy2(h6, da, c0), axpy2(h6, db, c1)};
           m1[ja] = make_float2(fmaf(hh, dna, n1v.x), fmaf(hh, dnb, n1v.y));
           accn[ja] = make_float2(fmaf(h6, dna, n1v.x), fmaf(h6, dnb, n1v.y));
+        }
+        if (kSplit) {
+          // Split barrier: wait until every thread has arrived at the end of iteration
+          // i-1, i.e. published its stage values there and finished every read of
+          // iteration i-1 (the exchange buffer written below and the ring slot of row
+          // r-5, which the copy of row r+3 reuses).  The wait sits after stage 1 so that
+          // the draw and stage 1 overlap with the slower warps of the previous row.
+          const unsigned g = it + i;
+          if (g > 0 && !mbar_wait_bounded(xbar, (g - 1) & 1u, kWaitLimit)) timed_out = true;
+          if (t == 0 && i + 3 < n_iter) issue(i + 3);
         }
         // Stage 2 at row r-2: k2 = f(psi1).
         {
@@ -229,13 +238,8 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
           if (i >= 8 && i - 8 < h_rows) {
             const int o = row_out * NX;
             if (NOISE) {
-              const float4 z = nbuf[(j & 3) * HALF + t];
-              const float va = fmaf(k.noise_b, na, k.noise_a);
-              const float vb = fmaf(k.noise_b, nb, k.noise_a);
-              const float sa = va > 0.f ? va * rsqrtf(va) : 0.f;
-              const float sb = vb > 0.f ? vb * rsqrtf(vb) : 0.f;
-              oa = __ffma2_rn(make_float2(sa, sa), make_float2(z.x, z.y), oa);
-              ob = __ffma2_rn(make_float2(sb, sb), make_float2(z.z, z.w), ob);
+              WignerDraw<float>::add(fmaf(k.noise_b, na, k.noise_a), r2a, sna, csa, oa.x, oa.y);
+              WignerDraw<float>::add(fmaf(k.noise_b, nb, k.noise_a), r2b, snb, csb, ob.x, ob.y);
             }
             *reinterpret_cast<float4*>(out_psi_m + o) = make_float4(oa.x, oa.y, ob.x, ob.y);
             *reinterpret_cast<float2*>(out_n_m + o) = make_float2(na, nb);
@@ -249,9 +253,13 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
           xo[2 * HALF + t] = make_float4(q3[jc].a.x, q3[jc].a.y, q3[jc].b.x, q3[jc].b.y);
         }
         row_out = row_out + 1 == ny ? 0 : row_out + 1;
-        __syncthreads();
-        // Slot of row r+3 held row r-5, last read by stage 4 of the previous iteration.
-        if (t == 0 && i + 3 < n_iter) issue(i + 3);
+        if (kSplit) {
+          mbar_arrive(xbar);
+        } else {
+          __syncthreads();
+          // Slot of row r+3 held row r-5, last read by stage 4 of the previous iteration.
+          if (t == 0 && i + 3 < n_iter) issue(i + 3);
+        }
       }
     }
     it += n_iter;
@@ -266,8 +274,8 @@ bool wide_rk4_supported(int nx, int ny) {
 }
 
 size_t wide_rk4_smem(int nx) {
-  return static_cast<size_t>(kRing) * nx * 16 + static_cast<size_t>(10) * (nx / 2) * 16 +
-         kRing * sizeof(uint64_t);
+  return static_cast<size_t>(kRing) * nx * 16 + static_cast<size_t>(6) * (nx / 2) * 16 +
+         (kRing + 1) * sizeof(uint64_t);
 }
 
 namespace {
