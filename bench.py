@@ -189,6 +189,18 @@ def profiled_traffic(members):
     return float(per_site) * members * NX * NY
 
 
+def profiled_sweep_traffic(tiling, sites):
+    """DRAM bytes per launch of the sweep kernel from the committed ncu summary, when the
+    tile shape in use is the profiled one (the strips' pipeline fill depends on it)."""
+    path = ROOT / "profiles" / "rk4_sweep_traffic.json"
+    if not path.exists():
+        return None
+    data = json.loads(path.read_text())
+    if [int(tiling["lanes"]), int(tiling["strip_rows"])] != list(data.get("tiling", [])):
+        return None
+    return float(data["dram_bytes_per_site"]) * sites
+
+
 # ----------------------------------------------------------------------------- CPU legs
 def _cpu_member_steps(args):
     """Worker: FP64 oracle RK4 steps on one member (used by the CPU legs)."""
@@ -483,7 +495,9 @@ def run_sweep_bench(args):
                    "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "frac": achieved / peak,
+                     "traffic": profiled_sweep_traffic(eng.tiling, sites),
+                     "peak_source": peak_kind,
                      "algorithmic_bytes_per_site": BYTES_PER_SITE},
         "e2e": {"value": sites * chunk * calls / e2e_s, "unit": "site-updates/s",
                 "h2d_bytes_per_step": sites * 12, "d2h_bytes_per_step": sites * 12,
