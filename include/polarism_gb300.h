@@ -173,6 +173,28 @@ int pg_norms(pg_solver* s, double* out);
  * per member ||rho - rho_prev|| / ||rho_prev||, |N - N_prev| / N_prev (infinite on the first call)
  * and the norms N; the current density becomes the reference for the next call. */
 int pg_steady_check(pg_solver* s, double* rel_density, double* rel_norm, double* norms);
+/* Device-resident steady-state monitor: the sampling path of SimulationController.run
+ * (polarism/simulation_controller.py:1063-1130 with _check_steady_state and _record_stops,
+ * :698-734) without a host round trip per check.
+ * pg_steady_update enqueues one check on the solver's stream and returns at once: the
+ * comparison of pg_steady_check, and, when `record` is non-zero (the caller's t >= min_time),
+ * `step` becomes the stop step of every member not yet stopped whose norm is below 1e-30 or
+ * whose relative density and norm changes are both below rtol (no decision on the first check
+ * after a reset).  With halt_when_all_stopped, the check that finds every member stopped sets
+ * the solver's halt word: RK4 steps queued after it return without changing the state.
+ * pg_steady_poll reads, without waiting for the device, the number of stopped members and the
+ * index (1, 2, ...) of the newest check the device has finished.
+ * pg_steady_results waits for the stream and copies the newest check's values and the stop
+ * steps (-1: not stopped; any output may be NULL); if the run halted it returns the halt step
+ * (else -1), makes the state of that step the current one and clears the halt.
+ * pg_steady_reset forgets the previous density, the stop steps and the halt.
+ * pg_steady_check shares the previous density with these calls. */
+int pg_steady_update(pg_solver* s, int64_t step, int32_t record, double rtol,
+                     int32_t halt_when_all_stopped);
+int pg_steady_poll(pg_solver* s, int32_t* stopped, int64_t* updates_done);
+int pg_steady_results(pg_solver* s, double* rel_density, double* rel_norm, double* norms,
+                      int64_t* stop_steps, int64_t* halt_step);
+int pg_steady_reset(pg_solver* s);
 /* FP64 norms (sum |psi|^2 * cell per member) of caller-owned device fields psi
  * (members * sites_per_member complex values of the given precision) into the device array
  * norms_out, on `stream` (a cudaStream_t, NULL for the default stream); per-block partial sums

@@ -8,6 +8,14 @@
 // * Per-member norm sum |psi|^2 dV (polarism/simulation_controller.py:92-103) and the
 //   steady-state comparison of simulation_controller.py:710-734 (relative density and norm
 //   changes against the previous check), reduced in FP64 through per-block partial sums.
+// * The device-resident steady-state monitor (pg_steady_update / _poll / _results): the
+//   comparison, the per-member stop decision and the first stop step of
+//   simulation_controller.py:698-734 are made by a one-block kernel after the partial sums, so
+//   the chunk loop of simulation_controller.py:1063-1130 needs no host round trip per check.
+//   The kernel publishes (update index, members stopped) in one 64-bit word of mapped host
+//   memory that the host reads without waiting, and, when asked, sets the solver's halt word
+//   once every member has stopped: RK4 launches queued after that return at once, so the run
+//   ends on the step of the deciding check as the reference's loop does.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -97,8 +105,10 @@ __global__ void finalize_partials_kernel(const double* __restrict__ partials, in
 template <typename T>
 __global__ void steady_partials_kernel(const typename C2T<T>::type* __restrict__ psi,
                                        T* __restrict__ rho_old, long long sites, int comps,
-                                       int have_old, double* __restrict__ partials) {
+                                       int have_old, double* __restrict__ partials,
+                                       const int* __restrict__ halt) {
   __shared__ double red[3][32];
+  if (halt != nullptr && __ldcg(halt) != 0) return;  // the state no longer advances
   const int member = blockIdx.y;
   const long long base = static_cast<long long>(member) * sites;
   double d2 = 0.0, o2 = 0.0, n = 0.0;
@@ -135,6 +145,55 @@ __global__ void steady_partials_kernel(const typename C2T<T>::type* __restrict__
   }
 }
 
+// Per-member decision of one steady-state check from the partial sums (one block): relative
+// density and norm changes, the stop criterion of simulation_controller.py:728-729 and the
+// first stop step (_record_stops, :698-708).  results = [rel_density | rel_norm | norm].
+__global__ void steady_decide_kernel(const double* __restrict__ partials, int blocks, int members,
+                                     double cell, int have_old, int record, double rtol,
+                                     long long step, int halt_when_all, double* __restrict__ norm_old,
+                                     long long* __restrict__ stop_step, double* __restrict__ results,
+                                     int* __restrict__ halt, long long* __restrict__ halt_step,
+                                     unsigned long long* __restrict__ host_word,
+                                     unsigned int update_index) {
+  __shared__ int stopped;
+  if (halt != nullptr && __ldcg(halt) != 0) return;  // already halted: nothing has changed
+  if (threadIdx.x == 0) stopped = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  for (int m = warp; m < members; m += warps) {
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int b = lane; b < blocks; b += 32)
+      for (int q = 0; q < 3; ++q) v[q] += partials[(static_cast<long long>(m) * blocks + b) * 3 + q];
+    for (int q = 0; q < 3; ++q)
+      for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+    if (lane == 0) {
+      const double norm = v[2] * cell;
+      double rd = INFINITY, rn = INFINITY;
+      if (have_old) {
+        rd = sqrt(v[0]) / fmax(sqrt(v[1]), 1e-30);
+        rn = fabs(norm - norm_old[m]) / fmax(norm_old[m], 1e-30);
+        const bool reached = norm < 1e-30 || (rn < rtol && rd < rtol);
+        if (record && reached && stop_step[m] < 0) stop_step[m] = step;
+      }
+      results[m] = rd;
+      results[members + m] = rn;
+      results[2 * members + m] = norm;
+      norm_old[m] = norm;
+      if (stop_step[m] >= 0) atomicAdd(&stopped, 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (halt_when_all && stopped == members && halt != nullptr) {
+      *halt = 1;
+      *halt_step = step;
+    }
+    *reinterpret_cast<volatile unsigned long long*>(host_word) =
+        (static_cast<unsigned long long>(update_index) << 32) | static_cast<unsigned int>(stopped);
+    __threadfence_system();
+  }
+}
+
 struct AccumBuffers {
   double* sum_rho = nullptr;
   double* sum_rho2 = nullptr;
@@ -146,7 +205,14 @@ struct AccumBuffers {
   int partial_blocks = 0;    // per member
   double* out = nullptr;     // device results (members)
   long long samples_rho = 0, samples_k = 0;
-  std::vector<double> host_norm_old;
+  // Device steady-state monitor.
+  double* norm_old = nullptr;        // device, members
+  long long* stop_step = nullptr;    // device, members (-1: not stopped)
+  double* results = nullptr;         // device, 3 * members
+  long long* halt_step = nullptr;    // device
+  unsigned long long* host_word = nullptr;  // mapped host memory: (update index << 32) | stopped
+  unsigned long long* dev_word = nullptr;   // its device alias
+  unsigned int updates = 0;          // checks enqueued since the last reset
 };
 
 constexpr int kReduceThreads = 256;
@@ -190,6 +256,11 @@ void accum_release(pg_solver* s) {
   cudaFree(a->rho_old);
   cudaFree(a->partials);
   cudaFree(a->out);
+  cudaFree(a->norm_old);
+  cudaFree(a->stop_step);
+  cudaFree(a->results);
+  cudaFree(a->halt_step);
+  if (a->host_word) cudaFreeHost(a->host_word);
   delete a;
   s->accum = nullptr;
 }
@@ -343,50 +414,121 @@ int pg_norms(pg_solver* s, double* out) {
   return PG_OK;
 }
 
-int pg_steady_check(pg_solver* s, double* rel_density, double* rel_norm, double* norms) {
-  PG_CHECK(s && rel_density && rel_norm && norms, PG_ERR_INVALID, "pg_steady_check: null argument");
-  PG_CHECK(!s->spectral, PG_ERR_INVALID, "pg_steady_check: the state holds a spectrum");
+int pg_steady_reset(pg_solver* s) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_steady_reset: null solver");
   int rc = pg::ensure_accum(s);
   if (rc != PG_OK) return rc;
   pg::AccumBuffers& a = pg::acc(s);
+  const int m = s->cfg.members;
+  if (!a.norm_old) {
+    PG_CUDA(cudaMalloc(&a.norm_old, sizeof(double) * m));
+    PG_CUDA(cudaMalloc(&a.stop_step, sizeof(long long) * m));
+    PG_CUDA(cudaMalloc(&a.results, sizeof(double) * 3 * m));
+    PG_CUDA(cudaMalloc(&a.halt_step, sizeof(long long)));
+    PG_CUDA(cudaHostAlloc(&a.host_word, sizeof(unsigned long long), cudaHostAllocMapped));
+    PG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&a.dev_word), a.host_word, 0));
+  }
   if (!a.rho_old) PG_CUDA(cudaMalloc(&a.rho_old, static_cast<size_t>(s->sites) * s->real_size));
+  PG_CUDA(cudaStreamSynchronize(s->stream));  // no check of an earlier run is still in flight
+  PG_CUDA(cudaMemsetAsync(a.norm_old, 0, sizeof(double) * m, s->stream));
+  PG_CUDA(cudaMemsetAsync(a.stop_step, 0xff, sizeof(long long) * m, s->stream));  // -1
+  PG_CUDA(cudaMemsetAsync(a.halt_step, 0xff, sizeof(long long), s->stream));
+  PG_CUDA(cudaMemsetAsync(s->halt, 0, sizeof(int), s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  *reinterpret_cast<volatile unsigned long long*>(a.host_word) = 0ull;
+  a.have_old = false;
+  a.updates = 0;
+  return PG_OK;
+}
+
+int pg_steady_update(pg_solver* s, int64_t step, int32_t record, double rtol,
+                     int32_t halt_when_all_stopped) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_steady_update: null solver");
+  PG_CHECK(!s->spectral, PG_ERR_INVALID, "pg_steady_update: the state holds a spectrum");
+  PG_CHECK(rtol >= 0.0, PG_ERR_INVALID, "pg_steady_update: negative rtol");
+  int rc = pg::ensure_accum(s);
+  if (rc != PG_OK) return rc;
+  pg::AccumBuffers& a = pg::acc(s);
+  if (!a.norm_old) {
+    rc = pg_steady_reset(s);
+    if (rc != PG_OK) return rc;
+  }
   const int blocks = a.partial_blocks;
   const int m = s->cfg.members;
   if (s->cfg.precision == PG_DOUBLE)
     pg::steady_partials_kernel<double><<<dim3(blocks, m), 256, 0, s->stream>>>(
         static_cast<const double2*>(s->psi[s->cur]), static_cast<double*>(a.rho_old), s->plane,
-        s->comps, a.have_old ? 1 : 0, a.partials);
+        s->comps, a.have_old ? 1 : 0, a.partials, s->halt);
   else
     pg::steady_partials_kernel<float><<<dim3(blocks, m), 256, 0, s->stream>>>(
         static_cast<const float2*>(s->psi[s->cur]), static_cast<float*>(a.rho_old), s->plane,
-        s->comps, a.have_old ? 1 : 0, a.partials);
+        s->comps, a.have_old ? 1 : 0, a.partials, s->halt);
   PG_CUDA(cudaGetLastError());
-  std::vector<double> host(static_cast<size_t>(3) * blocks * m);
-  PG_CUDA(cudaMemcpyAsync(host.data(), a.partials, host.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                          s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
-  const double cell = s->cfg.dx * s->cfg.dy;
-  if (a.host_norm_old.size() != static_cast<size_t>(m)) a.host_norm_old.assign(m, 0.0);
-  for (int mm = 0; mm < m; ++mm) {
-    double d2 = 0, o2 = 0, n = 0;
-    for (int b = 0; b < blocks; ++b) {
-      const double* p = &host[(static_cast<size_t>(mm) * blocks + b) * 3];
-      d2 += p[0];
-      o2 += p[1];
-      n += p[2];
-    }
-    const double norm = n * cell;
-    norms[mm] = norm;
-    if (a.have_old) {
-      rel_density[mm] = std::sqrt(d2) / std::max(std::sqrt(o2), 1e-30);
-      rel_norm[mm] = std::fabs(norm - a.host_norm_old[mm]) / std::max(a.host_norm_old[mm], 1e-30);
-    } else {
-      rel_density[mm] = rel_norm[mm] = INFINITY;
-    }
-    a.host_norm_old[mm] = norm;
-  }
+  a.updates += 1;
+  pg::steady_decide_kernel<<<1, 256, 0, s->stream>>>(
+      a.partials, blocks, m, s->cfg.dx * s->cfg.dy, a.have_old ? 1 : 0, record ? 1 : 0, rtol,
+      static_cast<long long>(step), halt_when_all_stopped ? 1 : 0, a.norm_old, a.stop_step,
+      a.results, s->halt, a.halt_step, a.dev_word, a.updates);
+  PG_CUDA(cudaGetLastError());
   a.have_old = true;
   return PG_OK;
+}
+
+int pg_steady_poll(pg_solver* s, int32_t* stopped, int64_t* updates_done) {
+  PG_CHECK(s && stopped && updates_done, PG_ERR_INVALID, "pg_steady_poll: null argument");
+  if (!s->accum || !pg::acc(s).host_word) {
+    *stopped = 0;
+    *updates_done = 0;
+    return PG_OK;
+  }
+  const unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(pg::acc(s).host_word);
+  *stopped = static_cast<int32_t>(w & 0xffffffffull);
+  *updates_done = static_cast<int64_t>(w >> 32);
+  return PG_OK;
+}
+
+int pg_steady_results(pg_solver* s, double* rel_density, double* rel_norm, double* norms,
+                      int64_t* stop_steps, int64_t* halt_step) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_steady_results: null solver");
+  PG_CHECK(s->accum && pg::acc(s).norm_old, PG_ERR_INVALID,
+           "pg_steady_results: no steady-state check has been made");
+  pg::AccumBuffers& a = pg::acc(s);
+  const int m = s->cfg.members;
+  std::vector<double> res(static_cast<size_t>(3) * m);
+  std::vector<long long> stops(m);
+  long long hs = -1;
+  int halted = 0;
+  PG_CUDA(cudaMemcpyAsync(res.data(), a.results, res.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                          s->stream));
+  PG_CUDA(cudaMemcpyAsync(stops.data(), a.stop_step, stops.size() * sizeof(long long),
+                          cudaMemcpyDeviceToHost, s->stream));
+  PG_CUDA(cudaMemcpyAsync(&halted, s->halt, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  PG_CUDA(cudaMemcpyAsync(&hs, a.halt_step, sizeof(long long), cudaMemcpyDeviceToHost, s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  for (int mm = 0; mm < m; ++mm) {
+    if (rel_density) rel_density[mm] = res[mm];
+    if (rel_norm) rel_norm[mm] = res[m + mm];
+    if (norms) norms[mm] = res[2 * m + mm];
+    if (stop_steps) stop_steps[mm] = stops[mm];
+  }
+  if (halted) {
+    // RK4 launches after the halt returned without writing, yet the host swapped the
+    // ping-pong buffers for each of them: the state of the halt step is under the parity it
+    // had then.  Clear the halt so that the solver steps again.
+    s->cur ^= static_cast<int>((s->parity_step - hs) & 1);
+    s->parity_step = hs;
+    PG_CUDA(cudaMemsetAsync(s->halt, 0, sizeof(int), s->stream));
+    PG_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  if (halt_step) *halt_step = halted ? hs : -1;
+  return PG_OK;
+}
+
+int pg_steady_check(pg_solver* s, double* rel_density, double* rel_norm, double* norms) {
+  PG_CHECK(s && rel_density && rel_norm && norms, PG_ERR_INVALID, "pg_steady_check: null argument");
+  int rc = pg_steady_update(s, -1, 0, 0.0, 0);
+  if (rc != PG_OK) return rc;
+  return pg_steady_results(s, rel_density, rel_norm, norms, nullptr, nullptr);
 }
 
 // Stand-alone FP64 norms of caller-owned device fields; scratch for the per-block partial

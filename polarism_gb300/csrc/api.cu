@@ -188,6 +188,7 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
     w.members = s->cfg.members;
     w.blocks = s->wide_blocks;
     w.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
+    w.halt = s->halt;
     return pg::launch_rk4_wide(static_cast<const float*>(s->psi[from]),
                                static_cast<const float*>(s->res[from]),
                                static_cast<const float*>(s->pump), static_cast<float*>(s->psi[to]),
@@ -199,6 +200,7 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
   pg::RK4Geom g = s->geom;
   g.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
   g.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
+  g.halt = s->halt;
   if (s->cfg.precision == PG_DOUBLE) {
     return pg::launch_rk4_step<double>(
         static_cast<const double*>(s->psi[from]), static_cast<const double*>(s->res[from]),
@@ -266,6 +268,7 @@ void release(pg_solver* s) {
   cudaFree(s->scales);
   cudaFree(s->step_base);
   cudaFree(s->err_flag);
+  cudaFree(s->halt);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -359,6 +362,8 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   cudaMemsetAsync(s->step_base, 0, sizeof(unsigned long long), s->stream);
   if ((e = cudaMalloc(&s->err_flag, sizeof(int))) != cudaSuccess) return fail(e, "error flag");
   cudaMemsetAsync(s->err_flag, 0, sizeof(int), s->stream);
+  if ((e = cudaMalloc(&s->halt, sizeof(int))) != cudaSuccess) return fail(e, "halt word");
+  cudaMemsetAsync(s->halt, 0, sizeof(int), s->stream);
   if (cfg->precision == PG_SINGLE && pg::wide_rk4_supported(cfg->nx, cfg->ny)) {
     if ((e = pg::configure_wide_rk4()) != cudaSuccess) return fail(e, "wide kernel attributes");
     const long long rows = static_cast<long long>(cfg->members) * cfg->ny;
@@ -577,6 +582,7 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
     s->last_launches += len;
     done += len;
   }
+  s->parity_step = start_step + n_steps;
   return PG_OK;
 }
 

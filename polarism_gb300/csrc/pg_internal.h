@@ -57,6 +57,7 @@ struct RK4Geom {
   int wrap;          // 1: the block spans the full periodic row (no x halo)
   long long pump_stride;   // 0: shared envelope; nx*ny: one envelope per member
   long long pot_stride;    // 0: shared potential; nx*ny: per member
+  const int* halt = nullptr;  // when non-null and set, the launch returns at once
 };
 
 struct RK4Features {

@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
                       const T* __restrict__ scales, const unsigned long long* __restrict__ step_base,
                       const int step_offset, const T dt, const RK4Geom g, const RK4Features f) {
   using C2 = typename Cplx<T>::type;
+  if (g.halt != nullptr && __ldcg(g.halt) != 0) return;  // steady-state monitor halted the run
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C2* xbuf = reinterpret_cast<C2*>(smem_raw);  // [2 parities][4 stage rows][blockDim]
 

@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
   // apart by up to a row, which measured faster; with several blocks per SM the blocks
   // already interleave and a block-wide barrier is cheaper.
   constexpr bool kSplit = NX >= 1024;
+  if (g.halt != nullptr && __ldcg(g.halt) != 0) return;  // steady-state monitor halted the run
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][NX]
   float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * NX); // [kRing][NX]

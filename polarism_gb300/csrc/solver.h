@@ -47,6 +47,10 @@ struct pg_solver {
   int next_slot = 0;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (length, parity) -> graph
   int* err_flag = nullptr;   // set by kernels whose bounded waits gave up
+  // Device halt word of the steady-state monitor: once it is set every RK4 launch returns
+  // at once, so steps queued after the last member stopped leave the state as it was.
+  int* halt = nullptr;
+  long long parity_step = 0;  // absolute step whose state sits under `cur` after pg_rk4_advance
   int rk4_kernel = 0;        // 0 auto, 1 tiled streaming kernel, 2 full-width kernel
   int wide_blocks = 0;       // persistent grid of the full-width kernel
   // Split-step state.

@@ -10,6 +10,7 @@ struct WideGeom {
   int nx, ny, members;
   int blocks;              // persistent grid size
   long long pump_stride;   // 0: shared envelope; nx*ny: one per member
+  const int* halt = nullptr;  // when non-null and set, the launch returns at once
 };
 
 bool wide_rk4_supported(int nx, int ny);

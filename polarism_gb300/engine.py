@@ -303,6 +303,35 @@ class RK4Engine:
                                             nm.ctypes.data), "pg_steady_check")
         return rd, rn, nm
 
+    # -- device-resident steady-state monitor -----------------------------------------
+    def steady_reset(self):
+        _lib.check(self.lib.pg_steady_reset(self.handle), "pg_steady_reset")
+
+    def steady_update(self, step, record=True, rtol=1e-6, halt=False):
+        """Enqueue one steady-state check (no wait); see ``pg_steady_update``."""
+        _lib.check(self.lib.pg_steady_update(self.handle, int(step), int(bool(record)), float(rtol),
+                                             int(bool(halt))), "pg_steady_update")
+
+    def steady_poll(self):
+        """(members stopped, index of the newest finished check), read without waiting."""
+        stopped = C.c_int32()
+        done = C.c_int64()
+        _lib.check(self.lib.pg_steady_poll(self.handle, C.byref(stopped), C.byref(done)),
+                   "pg_steady_poll")
+        return int(stopped.value), int(done.value)
+
+    def steady_results(self):
+        """Waits; returns (rel_density, rel_norm, norms, stop_steps, halt_step or None)."""
+        rd = np.empty(self.members)
+        rn = np.empty(self.members)
+        nm = np.empty(self.members)
+        stops = np.empty(self.members, dtype=np.int64)
+        halt = C.c_int64()
+        _lib.check(self.lib.pg_steady_results(self.handle, rd.ctypes.data, rn.ctypes.data,
+                                              nm.ctypes.data, stops.ctypes.data, C.byref(halt)),
+                   "pg_steady_results")
+        return rd, rn, nm, stops, (None if halt.value < 0 else int(halt.value))
+
     def set_state_kind(self, spectral: bool):
         _lib.check(self.lib.pg_set_state_kind(self.handle, int(bool(spectral))), "pg_set_state_kind")
 

@@ -28,7 +28,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from polarism_gb300 import host
+from polarism_gb300 import host, sampling
 
 
 def threshold(physics) -> float:
@@ -201,23 +201,15 @@ def run_uniform(cfgs, initial=None, total_time=None):
             n0 = np.ascontiguousarray(np.asarray(initial[1], np.float32).reshape(m, 1, *grid.shape))
         eng.set_state(psi0, n0)
         p0 = np.asarray([c.laser.P0 for c in cfgs])
-        scales = np.broadcast_to(p0, (interval, 3, m)).copy()
-        stop = np.full(m, np.nan)
-        step, n_total = 0, int(round(total / dt))
-        import time as _time
-
-        t0 = _time.perf_counter()
-        norms = np.zeros(m)
-        while step < n_total and not np.isfinite(stop).all():
-            eng.advance(step, interval, scales)
-            step += interval
-            rd, rn, norms = eng.steady_check()
-            reached = (norms < 1e-30) | ((rn < rtol) & (rd < rtol))
-            stop[reached & np.isnan(stop)] = step * dt
-        eng.synchronize()
-        wall = _time.perf_counter() - t0
+        n_total = int(round(total / dt))
+        t0 = time.perf_counter()
+        run = sampling.run_to_steady(
+            eng, 0, n_total, lambda a, b: np.broadcast_to(p0, (b - a, 3, m)), dt, interval, rtol,
+            min_time=float(getattr(c0.stop, "min_time", 0.0)))
+        wall = time.perf_counter() - t0
         psi, res = eng.get_state()
-        return UniformResult(psi[:, 0].copy(), res[:, 0].copy(), stop, norms, step * dt, wall)
+        return UniformResult(psi[:, 0].copy(), res[:, 0].copy(), run.stop_times, run.norms,
+                             run.final_step * dt, wall)
     finally:
         eng.close()
 
