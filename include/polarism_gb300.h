@@ -167,6 +167,10 @@ int pg_ifrk_trial(pg_solver* s, int32_t tableau, double h, const double* stage_s
 int pg_accumulate(pg_solver* s, int32_t kinds);
 int pg_accumulator_sums(pg_solver* s, int32_t kind, double* out, int64_t* samples);
 int pg_accumulator_reset(pg_solver* s);
+/* Restore one accumulator (kind as pg_accumulator_sums) and its sample count, as
+ * Accumulator.load_state_dict does on a checkpoint resume (polarism/results/accumulators.py:
+ * 83-87,117-119,155-158). */
+int pg_accumulator_load(pg_solver* s, int32_t kind, const double* sums, int64_t samples);
 /* Per-member norm sum |psi|^2 dx dy in FP64 (polarism/simulation_controller.py:92-103). */
 int pg_norms(pg_solver* s, double* out);
 /* Steady-state comparison against the previous call (polarism/simulation_controller.py:710-734):
@@ -195,6 +199,16 @@ int pg_steady_poll(pg_solver* s, int32_t* stopped, int64_t* updates_done);
 int pg_steady_results(pg_solver* s, double* rel_density, double* rel_norm, double* norms,
                       int64_t* stop_steps, int64_t* halt_step);
 int pg_steady_reset(pg_solver* s);
+/* The monitor's state in checkpoint form (the steady_density / steady_norm / stop_time entries
+ * of checkpoint format 2, polarism/simulation_controller.py:771-774,851-864): the previous
+ * check's density (members * nx * ny reals of the solver's precision, summed over components),
+ * its norms and the stop steps (-1: not stopped).  have_reference is 0 before the first check
+ * (density and norms are then left untouched).  pg_steady_import restores them (a reset
+ * first); any of density / norms / stop_steps may be NULL on export, stop_steps on import. */
+int pg_steady_export(pg_solver* s, void* density, double* norms, int64_t* stop_steps,
+                     int32_t* have_reference);
+int pg_steady_import(pg_solver* s, const void* density, const double* norms,
+                     const int64_t* stop_steps, int32_t have_reference);
 /* FP64 norms (sum |psi|^2 * cell per member) of caller-owned device fields psi
  * (members * sites_per_member complex values of the given precision) into the device array
  * norms_out, on `stream` (a cudaStream_t, NULL for the default stream); per-block partial sums

@@ -80,6 +80,9 @@ SIGNATURES = {
     "pg_steady_poll": (C.c_int, [_vp, _vp, _vp]),
     "pg_steady_results": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "pg_steady_reset": (C.c_int, [_vp]),
+    "pg_steady_export": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "pg_steady_import": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32]),
+    "pg_accumulator_load": (C.c_int, [_vp, C.c_int32, _vp, C.c_int64]),
     "pg_field_norms": (C.c_int, [_vp, _i32, _i32, _i64, _f64, _vp, _vp]),
     "pg_field_norms_noalloc": (C.c_int, [_vp, _i32, _i32, _i64, _f64, _vp, _vp]),
     "pg_rk4_set_kernel": (C.c_int, [_vp, _i32]),

@@ -306,8 +306,8 @@ int pg_accumulate(pg_solver* s, int32_t kinds) {
     if (!a.sum_k) {
       PG_CUDA(cudaMalloc(&a.sum_k, dbytes));
       PG_CUDA(cudaMemsetAsync(a.sum_k, 0, dbytes, s->stream));
-      PG_CUDA(cudaMalloc(&a.half, cbytes));
     }
+    if (!a.half) PG_CUDA(cudaMalloc(&a.half, cbytes));
     PG_CUDA(cudaMemcpyAsync(a.half, s->psi[s->cur], cbytes, cudaMemcpyDeviceToDevice, s->stream));
     // Column pass F_y (in place on the scratch copy), then the squaring row pass.
     pg::IfrkColArgs c{};
@@ -378,6 +378,75 @@ int pg_accumulator_sums(pg_solver* s, int32_t kind, double* out, int64_t* sample
   PG_CUDA(cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, s->stream));
   PG_CUDA(cudaStreamSynchronize(s->stream));
   *samples = kind == 2 ? a.samples_k : a.samples_rho;
+  return PG_OK;
+}
+
+int pg_accumulator_load(pg_solver* s, int32_t kind, const double* sums, int64_t samples) {
+  PG_CHECK(s && sums && samples >= 0, PG_ERR_INVALID, "pg_accumulator_load: bad argument");
+  PG_CHECK(kind >= 0 && kind <= 2, PG_ERR_INVALID,
+           "pg_accumulator_load: kind 0 sum rho, 1 sum rho^2, 2 sum |psi_k|^2");
+  int rc = pg::ensure_accum(s);
+  if (rc != PG_OK) return rc;
+  pg::AccumBuffers& a = pg::acc(s);
+  const size_t bytes = static_cast<size_t>(s->field_values) * sizeof(double);
+  double** dst = kind == 0 ? &a.sum_rho : kind == 1 ? &a.sum_rho2 : &a.sum_k;
+  if (kind < 2 && !a.sum_rho) {  // the two density sums live and die together
+    PG_CUDA(cudaMalloc(&a.sum_rho, bytes));
+    PG_CUDA(cudaMalloc(&a.sum_rho2, bytes));
+    PG_CUDA(cudaMemsetAsync(a.sum_rho, 0, bytes, s->stream));
+    PG_CUDA(cudaMemsetAsync(a.sum_rho2, 0, bytes, s->stream));
+  }
+  if (!*dst) PG_CUDA(cudaMalloc(dst, bytes));
+  PG_CUDA(cudaMemcpyAsync(*dst, sums, bytes, cudaMemcpyHostToDevice, s->stream));
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  if (kind == 2)
+    a.samples_k = samples;
+  else
+    a.samples_rho = samples;
+  return PG_OK;
+}
+
+int pg_steady_export(pg_solver* s, void* density, double* norms, int64_t* stop_steps,
+                     int32_t* have_reference) {
+  PG_CHECK(s && have_reference, PG_ERR_INVALID, "pg_steady_export: null argument");
+  *have_reference = 0;
+  if (!s->accum || !pg::acc(s).norm_old) {
+    if (stop_steps)
+      for (int m = 0; m < s->cfg.members; ++m) stop_steps[m] = -1;
+    return PG_OK;
+  }
+  pg::AccumBuffers& a = pg::acc(s);
+  const int m = s->cfg.members;
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  if (a.have_old) {
+    if (density)
+      PG_CUDA(cudaMemcpy(density, a.rho_old, static_cast<size_t>(s->sites) * s->real_size,
+                         cudaMemcpyDeviceToHost));
+    if (norms) PG_CUDA(cudaMemcpy(norms, a.norm_old, sizeof(double) * m, cudaMemcpyDeviceToHost));
+    *have_reference = 1;
+  }
+  if (stop_steps)
+    PG_CUDA(cudaMemcpy(stop_steps, a.stop_step, sizeof(long long) * m, cudaMemcpyDeviceToHost));
+  return PG_OK;
+}
+
+int pg_steady_import(pg_solver* s, const void* density, const double* norms,
+                     const int64_t* stop_steps, int32_t have_reference) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_steady_import: null solver");
+  PG_CHECK(!have_reference || (density && norms), PG_ERR_INVALID,
+           "pg_steady_import: a reference needs the density and the norms");
+  int rc = pg_steady_reset(s);
+  if (rc != PG_OK) return rc;
+  pg::AccumBuffers& a = pg::acc(s);
+  const int m = s->cfg.members;
+  if (have_reference) {
+    PG_CUDA(cudaMemcpy(a.rho_old, density, static_cast<size_t>(s->sites) * s->real_size,
+                       cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(a.norm_old, norms, sizeof(double) * m, cudaMemcpyHostToDevice));
+    a.have_old = true;
+  }
+  if (stop_steps)
+    PG_CUDA(cudaMemcpy(a.stop_step, stop_steps, sizeof(long long) * m, cudaMemcpyHostToDevice));
   return PG_OK;
 }
 

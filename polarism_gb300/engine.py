@@ -289,6 +289,39 @@ class RK4Engine:
     def accumulator_reset(self):
         _lib.check(self.lib.pg_accumulator_reset(self.handle), "pg_accumulator_reset")
 
+    def accumulator_load(self, kind, sums, samples):
+        """Restore one accumulator (kind "rho", "rho2" or "k") and its sample count."""
+        index = {"rho": 0, "rho2": 1, "k": 2}[kind]
+        arr = np.ascontiguousarray(np.broadcast_to(np.asarray(sums, dtype=np.float64), self.shape))
+        _lib.check(self.lib.pg_accumulator_load(self.handle, index, arr.ctypes.data, int(samples)),
+                   "pg_accumulator_load")
+
+    def steady_export(self):
+        """(density (B, ny, nx) or None, norms or None, stop_steps) of the steady monitor."""
+        density = np.empty((self.members, self.ny, self.nx), dtype=self.real)
+        norms = np.empty(self.members)
+        stops = np.empty(self.members, dtype=np.int64)
+        have = C.c_int32()
+        _lib.check(self.lib.pg_steady_export(self.handle, density.ctypes.data, norms.ctypes.data,
+                                             stops.ctypes.data, C.byref(have)), "pg_steady_export")
+        if not have.value:
+            return None, None, stops
+        return density, norms, stops
+
+    def steady_import(self, density, norms, stop_steps=None):
+        """Restore the monitor from :meth:`steady_export`'s values (density None: no reference)."""
+        have = density is not None
+        d = n = None
+        if have:
+            d = np.ascontiguousarray(np.asarray(density, dtype=self.real).reshape(self.members, self.ny,
+                                                                                   self.nx))
+            n = np.ascontiguousarray(np.asarray(norms, dtype=np.float64).reshape(self.members))
+        st = None if stop_steps is None else np.ascontiguousarray(np.asarray(stop_steps, dtype=np.int64))
+        _lib.check(self.lib.pg_steady_import(self.handle, None if d is None else d.ctypes.data,
+                                             None if n is None else n.ctypes.data,
+                                             None if st is None else st.ctypes.data, int(have)),
+                   "pg_steady_import")
+
     def norms(self):
         out = np.empty(self.members, dtype=np.float64)
         _lib.check(self.lib.pg_norms(self.handle, out.ctypes.data), "pg_norms")
