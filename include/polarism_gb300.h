@@ -81,6 +81,14 @@ typedef struct pg_config {
   int32_t components;           /* 1 scalar field, 2 circular-basis spinor (0 means 1) */
   int32_t reservoir_components; /* reservoir fields per component set: 1 shared or = components
                                    (0 means = components) */
+  /* Separable pump terms L (lasers, polarism/laser/pump_field.py:81-89; 0 means 1):
+   * P(x, t) = sum_l c_l(t) E_l(x), each product and each partial sum rounded separately as in
+   * the reference's combiner (polarism/solver/cuda_pump.py:7-19).  With L > 1 pg_set_pump
+   * takes L envelopes one after another and every coefficient array below gains a term axis
+   * before the member axis ([step][stage][term][member]); the full-width RK4 kernel then gives
+   * way to the general one. */
+  int32_t pump_terms;
+  int32_t reserved_;
 } pg_config;
 
 typedef struct pg_solver pg_solver;
@@ -105,7 +113,7 @@ int pg_get_state(pg_solver* s, void* psi, void* res, int on_device);
 /* Device addresses of the current state buffers (valid until the next advance). */
 int pg_state_pointers(pg_solver* s, void** psi, void** res);
 
-/* Pump envelope (nx*ny reals, or B*nx*ny with pump_per_member) and potential
+/* Pump envelopes (L times nx*ny reals, or L times B*nx*ny with pump_per_member) and potential
  * (nx*ny reals or complex, or B*nx*ny with potential_per_member). */
 int pg_set_pump(pg_solver* s, const void* envelope, int on_device);
 int pg_set_potential(pg_solver* s, const void* potential, int on_device);

@@ -36,7 +36,8 @@ class PgConfig(C.Structure):
                 ("precision", C.c_int32), ("reservoir", C.c_int32), ("potential", C.c_int32),
                 ("pump_per_member", C.c_int32), ("potential_per_member", C.c_int32),
                 ("dx", C.c_double), ("dy", C.c_double), ("dt", C.c_double),
-                ("components", C.c_int32), ("reservoir_components", C.c_int32)]
+                ("components", C.c_int32), ("reservoir_components", C.c_int32),
+                ("pump_terms", C.c_int32), ("reserved_", C.c_int32)]
 
 
 class PgSweepGrid(C.Structure):

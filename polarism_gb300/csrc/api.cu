@@ -83,7 +83,7 @@ int stage_coefficients(pg_solver* s, const double* coeffs, int len, int per_step
     for (size_t i = 0; i < count; ++i) h[i] = static_cast<float>(coeffs[i]);
   }
   const size_t bytes = count * s->real_size;
-  const size_t base_off = static_cast<size_t>(kChunk) * 3 * m * 8;
+  const size_t base_off = static_cast<size_t>(kChunk) * 3 * s->pump_terms * m * 8;
   unsigned long long b = static_cast<unsigned long long>(step);
   std::memcpy(host + base_off, &b, sizeof(b));
   if (bytes) PG_CUDA(cudaMemcpyAsync(s->scales, host, bytes, cudaMemcpyHostToDevice, s->stream));
@@ -163,6 +163,7 @@ pg::RK4Features features(const pg_solver* s) {
   pg::RK4Features f{};
   f.potential = s->cfg.potential;
   f.reservoir = s->cfg.reservoir;
+  f.pump_terms = s->pump_terms;
   f.relax = 0;
   for (const auto& p : s->physics)
     if (p.kinetic_relaxation_eta != 0.0) f.relax = 1;
@@ -172,7 +173,8 @@ pg::RK4Features features(const pg_solver* s) {
 bool use_wide(const pg_solver* s) {
   const pg::RK4Features f = features(s);
   const bool eligible = s->cfg.precision == PG_SINGLE && f.potential == 0 && f.relax == 0 &&
-                        f.reservoir == 1 && pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny);
+                        f.reservoir == 1 && f.pump_terms == 1 &&
+                        pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny);
   if (s->rk4_kernel == 1) return false;
   return eligible;
 }
@@ -201,6 +203,7 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
   g.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
   g.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
   g.halt = s->halt;
+  g.pump_term_stride = s->pump_term_stride;
   if (s->cfg.precision == PG_DOUBLE) {
     return pg::launch_rk4_step<double>(
         static_cast<const double*>(s->psi[from]), static_cast<const double*>(s->res[from]),
@@ -298,6 +301,8 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
            "pg_create: precision must be PG_SINGLE or PG_DOUBLE");
   PG_CHECK(cfg->reservoir >= PG_RES_NONE && cfg->reservoir <= PG_RES_QDOUBLE, PG_ERR_UNSUPPORTED,
            "pg_create: reservoir must be PG_RES_NONE, PG_RES_SINGLE, PG_RES_DOUBLE or PG_RES_QDOUBLE");
+  PG_CHECK(cfg->pump_terms >= 0 && cfg->pump_terms <= 16, PG_ERR_INVALID,
+           "pg_create: pump_terms must be between 1 and 16 (0 means 1)");
   PG_CHECK(cfg->components >= 0 && cfg->components <= 2, PG_ERR_INVALID,
            "pg_create: components must be 1 or 2");
   const int comps = cfg->components == 0 ? 1 : cfg->components;
@@ -321,6 +326,8 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   s->res_fields = cfg->reservoir >= PG_RES_DOUBLE ? 2 : cfg->reservoir;
   s->res_comps = res_comps;
   s->field_values = s->sites * comps;
+  s->pump_terms = cfg->pump_terms <= 0 ? 1 : cfg->pump_terms;
+  s->pump_term_stride = cfg->pump_per_member ? s->sites : s->plane;
   s->res_values = s->sites * s->res_fields * res_comps;
   int dev = 0;
   auto fail = [&](cudaError_t e, const char* what) {
@@ -342,7 +349,7 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
     cudaMemsetAsync(s->psi[i], 0, field_bytes, s->stream);
     cudaMemsetAsync(s->res[i], 0, res_bytes, s->stream);
   }
-  const size_t pump_bytes = static_cast<size_t>(cfg->pump_per_member ? s->sites : s->plane) * s->real_size;
+  const size_t pump_bytes = static_cast<size_t>(s->pump_term_stride) * s->pump_terms * s->real_size;
   if ((e = cudaMalloc(&s->pump, pump_bytes)) != cudaSuccess) return fail(e, "pump buffer");
   cudaMemsetAsync(s->pump, 0, pump_bytes, s->stream);
   if (cfg->potential != PG_POT_NONE) {
@@ -355,7 +362,8 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
                              (cfg->precision == PG_DOUBLE ? sizeof(pg::RhsConst<double>)
                                                           : sizeof(pg::RhsConst<float>));
   if ((e = cudaMalloc(&s->consts, const_bytes)) != cudaSuccess) return fail(e, "constants");
-  const size_t scale_bytes = static_cast<size_t>(kChunk) * 3 * cfg->members * s->real_size;
+  const size_t scale_bytes =
+      static_cast<size_t>(kChunk) * 3 * s->pump_terms * cfg->members * s->real_size;
   if ((e = cudaMalloc(&s->scales, scale_bytes)) != cudaSuccess) return fail(e, "scales");
   if ((e = cudaMalloc(&s->step_base, sizeof(unsigned long long))) != cudaSuccess)
     return fail(e, "step base");
@@ -372,7 +380,7 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
     const long long by_rows = std::max<long long>(1, rows / 16);
     s->wide_blocks = static_cast<int>(std::min(blocks, by_rows));
   }
-  const size_t staging_bytes = static_cast<size_t>(kChunk) * 3 * cfg->members * 8 + 64;
+  const size_t staging_bytes = static_cast<size_t>(kChunk) * 3 * s->pump_terms * cfg->members * 8 + 64;
   for (auto& slot : s->staging) {
     if ((e = cudaMallocHost(&slot.host, staging_bytes)) != cudaSuccess) return fail(e, "staging");
     if ((e = cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming)) != cudaSuccess)
@@ -475,8 +483,7 @@ int pg_state_pointers(pg_solver* s, void** psi, void** res) {
 
 int pg_set_pump(pg_solver* s, const void* envelope, int on_device) {
   PG_CHECK(s && envelope, PG_ERR_INVALID, "pg_set_pump: null argument");
-  const size_t bytes =
-      static_cast<size_t>(s->cfg.pump_per_member ? s->sites : s->plane) * s->real_size;
+  const size_t bytes = static_cast<size_t>(s->pump_term_stride) * s->pump_terms * s->real_size;
   PG_CUDA(cudaMemcpyAsync(s->pump, envelope, bytes,
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream));
   PG_CUDA(cudaStreamSynchronize(s->stream));
@@ -564,7 +571,8 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
     int len = std::min(kChunk, remaining);
     const bool graph = use_graphs && len >= 2;
     if (graph && (len & 1)) len -= 1;
-    int rc = pg::stage_coefficients(s, stage_scales + static_cast<size_t>(done) * 3 * m, len, 3,
+    int rc = pg::stage_coefficients(s, stage_scales + static_cast<size_t>(done) * 3 * s->pump_terms * m, len,
+                                    3 * s->pump_terms,
                                     start_step + done);
     if (rc != PG_OK) return rc;
     if (graph) {

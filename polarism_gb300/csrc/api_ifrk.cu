@@ -238,6 +238,8 @@ Plan make_plan(const pg_solver* s) {
   k.reservoir = s->res_fields > 0;
   k.potential = c.potential;
   k.pump_stride = c.pump_per_member ? s->plane : 0;
+  k.pump_terms = s->pump_terms;
+  k.pump_term_stride = s->pump_term_stride;
   k.pot_stride = c.potential_per_member ? s->plane : 0;
   return p;
 }
@@ -455,7 +457,8 @@ int ifrk_advance_t(pg_solver* s, int tab, int64_t start_step, int n_steps, const
   int done = 0;
   while (done < n_steps) {
     const int len = std::min(per_chunk, n_steps - done);
-    rc = stage_coefficients(s, scales + static_cast<size_t>(done) * tb.stages * m, len, tb.stages,
+    rc = stage_coefficients(s, scales + static_cast<size_t>(done) * tb.stages * s->pump_terms * m, len,
+                            tb.stages * s->pump_terms,
                             start_step + done);
     if (rc != PG_OK) return rc;
     for (int k = 0; k < len; ++k) {
@@ -477,7 +480,7 @@ int ifrk_trial_t(pg_solver* s, int tab, double h, const double* scales, double r
   StepTables st = build_tables(tb, h);
   int rc = s->comps == 1 ? upload_tables<T>(s, st.taus) : PG_OK;
   if (rc != PG_OK) return rc;
-  rc = stage_coefficients(s, scales, 1, tb.stages, 0);
+  rc = stage_coefficients(s, scales, 1, tb.stages * s->pump_terms, 0);
   if (rc != PG_OK) return rc;
   s->last_launches = 0;
   rc = run_step<T>(s, p, tb, st, h, 0, 0, false, true, rtol, atol, err);

@@ -192,6 +192,8 @@ PassPlan plan(const pg_solver* s) {
   k.potential = c.potential;
   k.noise = s->noise ? 1 : 0;
   k.pump_stride = c.pump_per_member ? s->plane : 0;
+  k.pump_terms = s->pump_terms;
+  k.pump_term_stride = s->pump_term_stride;
   k.pot_stride = c.potential_per_member ? s->plane : 0;
   k.dt_d = c.dt;
   k.dt_f = static_cast<float>(c.dt);
@@ -278,8 +280,8 @@ int split_advance_t(pg_solver* s, int ordering, int64_t start_step, int n_steps,
   int done = 0;
   while (done < n_steps) {
     const int len = std::min(kChunk, n_steps - done);
-    int rc = stage_coefficients(s, scales + static_cast<size_t>(done) * 2 * m, len, 2,
-                                start_step + done);
+    int rc = stage_coefficients(s, scales + static_cast<size_t>(done) * 2 * s->pump_terms * m, len,
+                                2 * s->pump_terms, start_step + done);
     if (rc != PG_OK) return rc;
     if (use_graphs && len >= 2) {
       auto key = std::make_tuple(ordering, len, 0);

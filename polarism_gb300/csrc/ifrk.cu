@@ -201,7 +201,10 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
   double local = 0.0;
   if (a.mode != 3) {
     const SplitConst<T> k = consts[member];
-    const T s0 = scales ? scales[a.scale_index * a.members + member] : T(0);
+    const int L = a.pump_terms > 1 ? a.pump_terms : 1;
+    const T* cs = scales ? scales + static_cast<long long>(a.scale_index * L) * a.members + member
+                         : nullptr;
+    const T s0 = cs ? cs[0] : T(0);
     const T* pm = pump + member * a.pump_stride;
     const T* vm = potential ? potential + member * a.pot_stride * (a.potential == 2 ? 2 : 1) : nullptr;
     const unsigned long long step = a.noise ? step_base[0] + a.step_offset : 0ull;
@@ -260,7 +263,8 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
           buf[i * CC + comp * C + c] = C2{g * v[comp].x + e_over * v[comp].y, g * v[comp].y - e_over * v[comp].x};
         }
         if (F >= 1) {
-          const T p_site = mul_rn_i(s0, pm[o]);
+          const T p_site = L > 1 && cs ? pump_terms_value(pm, a.pump_term_stride, cs, a.members, L, o)
+                                       : mul_rn_i(s0, pm[o]);
 #pragma unroll
           for (int cr = 0; cr < 2; ++cr) {
             if (cr >= Cr) break;

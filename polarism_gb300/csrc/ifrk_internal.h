@@ -54,7 +54,9 @@ struct IfrkColArgs {
   const void* dn[kIfrkMaxStages];   // stage reservoir derivatives
   double coef[kIfrkMaxStages];      // h a_ij (stage) or h b_j (step end) or h (b_j - bhat_j)
   long long pump_stride, pot_stride;
-  int scale_index;             // pump coefficient index into `scales` ([k][member])
+  int scale_index;             // pump coefficient sample of `scales` ([k][term][member])
+  int pump_terms;              // separable pump terms L
+  long long pump_term_stride;  // reals between consecutive terms' envelopes
   int step_offset;
   double rtol, atol;
 };

@@ -58,13 +58,31 @@ struct RK4Geom {
   long long pump_stride;   // 0: shared envelope; nx*ny: one envelope per member
   long long pot_stride;    // 0: shared potential; nx*ny: per member
   const int* halt = nullptr;  // when non-null and set, the launch returns at once
+  long long pump_term_stride = 0;  // reals between consecutive pump terms' envelopes
 };
 
 struct RK4Features {
   int potential;     // 0 none, 1 real, 2 complex
   int relax;         // kinetic relaxation term on
   int reservoir;     // PG_RES_*: 0 none, 1 single, 2 double, 3 quadratic-double
+  int pump_terms;    // separable pump terms L (> 1 only on the general variant)
 };
+
+// Pump value of L separable terms at element o of the member's first envelope:
+// sum_t c[t * cstride] E_t[o], each product and each partial sum rounded separately (the
+// reference's combiner is compiled without FMA contraction, polarism/solver/cuda_pump.py:7-19).
+__device__ __forceinline__ float pump_mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double pump_mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float pump_add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double pump_add_rn(double a, double b) { return __dadd_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T pump_terms_value(const T* env, long long term_stride, const T* c,
+                                              int cstride, int terms, long long o) {
+  T v = pump_mul_rn(c[0], env[o]);
+  for (int t = 1; t < terms; ++t)
+    v = pump_add_rn(v, pump_mul_rn(c[static_cast<long long>(t) * cstride], env[t * term_stride + o]));
+  return v;
+}
 
 // Launch one fused whole-step RK4 update; scales points at [3][members] pump
 // coefficients (device memory) and step_base at the global step counter (device).

@@ -135,9 +135,13 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
 
   const RhsConst<T> k = consts[member];
   const int m_count = g.members;
-  const T s0 = scales[(step_offset * 3 + 0) * m_count + member];
-  const T s1 = scales[(step_offset * 3 + 1) * m_count + member];
-  const T s2 = scales[(step_offset * 3 + 2) * m_count + member];
+  // Coefficients [step][stage][term][member]; the term axis exists only with several lasers.
+  const int L = GENERAL ? f.pump_terms : 1;
+  const T* c0 = scales + static_cast<long long>((step_offset * 3 + 0) * L) * m_count + member;
+  const T* c1 = scales + static_cast<long long>((step_offset * 3 + 1) * L) * m_count + member;
+  const T* c2 = scales + static_cast<long long>((step_offset * 3 + 2) * L) * m_count + member;
+  const T s0 = c0[0], s1 = c1[0], s2 = c2[0];
+  const bool multi = GENERAL && L > 1;  // several separable lasers: sum the terms per site
   const T hh = dt * T(0.5), h6 = dt / T(6), h3 = dt / T(3);
 
   const C2* psi_m = psi_in + member * plane;
@@ -228,8 +232,11 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
           vim = f.potential == 2 ? pot_m[2 * o + 1] : T(0);
         }
         T dre, dim, dnr, du;
+        const T sP = multi ? pump_terms_value(pump_m, g.pump_term_stride, c0, m_count, L,
+                                              static_cast<long long>(ra) * nx + gx)
+                           : mul_rn(s0, P[sa]);
         site_rhs<T, GENERAL, TWO>(p0[sa], xin[lt_i], xin[rt_i], p0[sb], p0[j], n0[sa],
-                             mul_rn(s0, P[sa]), k, vre, vim, f, dre, dim, dnr, u0[sa], du);
+                             sP, k, vre, vim, f, dre, dim, dnr, u0[sa], du);
         q1[sa] = C2{p0[sa].x + hh * dre, p0[sa].y + hh * dim};
         m1[sa] = n0[sa] + hh * dnr;
         acc[sa] = C2{p0[sa].x + h6 * dre, p0[sa].y + h6 * dim};
@@ -250,8 +257,15 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
         }
         T dre, dim, dnr, du;
         const C2* xr = xin + nthreads;
+        T sP = mul_rn(s1, P[sb]);
+        if (multi) {
+          int rb = row_load - 2;
+          if (rb < 0) rb += ny;
+          sP = pump_terms_value(pump_m, g.pump_term_stride, c1, m_count, L,
+                                static_cast<long long>(rb) * nx + gx);
+        }
         site_rhs<T, GENERAL, TWO>(q1[sb], xr[lt_i], xr[rt_i], q1[sc], q1[sa], m1[sb],
-                             mul_rn(s1, P[sb]), k, vre, vim, f, dre, dim, dnr, v1[sb], du);
+                             sP, k, vre, vim, f, dre, dim, dnr, v1[sb], du);
         q2[sb] = C2{p0[sb].x + hh * dre, p0[sb].y + hh * dim};
         m2[sb] = n0[sb] + hh * dnr;
         acc[sb] = C2{acc[sb].x + h3 * dre, acc[sb].y + h3 * dim};
@@ -272,8 +286,15 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
         }
         T dre, dim, dnr, du;
         const C2* xr = xin + 2 * nthreads;
+        T sP = mul_rn(s1, P[sc]);
+        if (multi) {
+          int rc = row_load - 3;
+          if (rc < 0) rc += ny;
+          sP = pump_terms_value(pump_m, g.pump_term_stride, c1, m_count, L,
+                                static_cast<long long>(rc) * nx + gx);
+        }
         site_rhs<T, GENERAL, TWO>(q2[sc], xr[lt_i], xr[rt_i], q2[sd], q2[sb], m2[sc],
-                             mul_rn(s1, P[sc]), k, vre, vim, f, dre, dim, dnr, v2[sc], du);
+                             sP, k, vre, vim, f, dre, dim, dnr, v2[sc], du);
         q3[sc] = C2{p0[sc].x + dt * dre, p0[sc].y + dt * dim};
         m3[sc] = n0[sc] + dt * dnr;
         acc[sc] = C2{acc[sc].x + h3 * dre, acc[sc].y + h3 * dim};
@@ -292,8 +313,11 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
         }
         T dre, dim, dnr, du;
         const C2* xr = xin + 3 * nthreads;
+        const T sP = multi ? pump_terms_value(pump_m, g.pump_term_stride, c2, m_count, L,
+                                              static_cast<long long>(row_out) * nx + gx)
+                           : mul_rn(s2, P[sd]);
         site_rhs<T, GENERAL, TWO>(q3[sd], xr[lt_i], xr[rt_i], q3[sa], q3[sc], m3[sd],
-                             mul_rn(s2, P[sd]), k, vre, vim, f, dre, dim, dnr, v3[sd], du);
+                             sP, k, vre, vim, f, dre, dim, dnr, v3[sd], du);
         T ore = acc[sd].x + h6 * dre;
         T oim = acc[sd].y + h6 * dim;
         T on = accn[sd] + h6 * dnr;
@@ -351,7 +375,7 @@ cudaError_t launch_rk4_step(const T* psi_in, const T* n_in, const T* pump, const
                             T* psi_out, T* n_out, const RhsConst<T>* consts, const T* scales,
                             const unsigned long long* step_base, int step_offset, T dt, bool noise,
                             const RK4Geom& g, const RK4Features& f, cudaStream_t stream) {
-  const bool general = f.potential != 0 || f.relax != 0 || f.reservoir != 1;
+  const bool general = f.potential != 0 || f.relax != 0 || f.reservoir != 1 || f.pump_terms > 1;
   const bool two = f.reservoir >= 2;
 #define PG_RK4_VARIANT(N, G, W)                                                                  \
   launch_variant<T, N, G, W>(psi_in, n_in, pump, potential, psi_out, n_out, consts, scales,     \

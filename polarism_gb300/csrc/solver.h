@@ -31,7 +31,9 @@ struct pg_solver {
   void* pump = nullptr;
   void* potential = nullptr;
   void* consts = nullptr;
-  void* scales = nullptr;  // kChunk * 3 * members reals
+  void* scales = nullptr;  // kChunk * 3 * pump_terms * members reals
+  int pump_terms = 1;      // separable pump terms L
+  long long pump_term_stride = 0;  // reals between consecutive terms' envelopes
   unsigned long long* step_base = nullptr;
   int cur = 0;
   bool noise = false;

@@ -172,8 +172,11 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
   if (a.op != SPLIT_OP_NONE) {
     const SplitConst<T> k = consts[member];
     const int m_count = a.members;
-    const T s0 = scales[(a.scale_offset + 0) * m_count + member];
-    const T s1 = scales[(a.scale_offset + 1) * m_count + member];
+    // Coefficients [k][sample][term][member]; the term axis exists only with several lasers.
+    const int L = a.pump_terms > 1 ? a.pump_terms : 1;
+    const T* c0 = scales + static_cast<long long>((a.scale_offset + 0) * L) * m_count + member;
+    const T* c1 = scales + static_cast<long long>((a.scale_offset + 1) * L) * m_count + member;
+    const T s0 = c0[0], s1 = c1[0];
     const T* pm = pump + member * a.pump_stride;
     const T* vm = potential ? potential + member * a.pot_stride * (a.potential == 2 ? 2 : 1) : nullptr;
     T* rm = res + member * plane;
@@ -198,7 +201,15 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
       C2 v = buf[i * C + c];
       T n = (a.reservoir || two) ? rm[o] : T(0);
       T n2 = two ? rm2[o] : T(0);
-      const T P = pm[o];
+      T Pa, Pb;  // pump at the first and the second coefficient sample
+      if (L > 1) {
+        Pa = pump_terms_value(pm, a.pump_term_stride, c0, m_count, L, o);
+        Pb = pump_terms_value(pm, a.pump_term_stride, c1, m_count, L, o);
+      } else {
+        const T P = pm[o];
+        Pa = mul_rn_t(s0, P);
+        Pb = mul_rn_t(s1, P);
+      }
       T vre = T(0), vim = T(0);
       if (vm) {
         vre = a.potential == 2 ? vm[2 * o] : vm[o];
@@ -207,18 +218,18 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
       bool add_noise = false;
       switch (a.op) {
         case SPLIT_OP_KOUTER:
-          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s0, P));
+          res_half(n, n2, v.x * v.x + v.y * v.y, Pa);
           nonlinear(v.x, v.y, n, n2, two, vre, vim, dt, k);
-          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s1, P));
+          res_half(n, n2, v.x * v.x + v.y * v.y, Pb);
           add_noise = a.noise != 0;
           break;
         case SPLIT_OP_RES_START:
-          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s0, P));
+          res_half(n, n2, v.x * v.x + v.y * v.y, Pa);
           break;
         case SPLIT_OP_RES_END_START: {
           const T rho = v.x * v.x + v.y * v.y;
-          res_half(n, n2, rho, mul_rn_t(s0, P));
-          res_half(n, n2, rho, mul_rn_t(s1, P));
+          res_half(n, n2, rho, Pa);
+          res_half(n, n2, rho, Pb);
           break;
         }
         case SPLIT_OP_NONLINEAR:
@@ -226,7 +237,7 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
           add_noise = a.noise != 0;
           break;
         case SPLIT_OP_RES_END:
-          res_half(n, n2, v.x * v.x + v.y * v.y, mul_rn_t(s0, P));
+          res_half(n, n2, v.x * v.x + v.y * v.y, Pa);
           break;
         default:
           break;

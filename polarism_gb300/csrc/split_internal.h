@@ -47,7 +47,9 @@ struct ColPassArgs {
   int potential;        // 0 none, 1 real, 2 complex
   int noise;
   long long pump_stride, pot_stride;
-  int scale_offset;     // index into scales ([k][member]) of the first coefficient
+  int pump_terms;       // separable pump terms L
+  long long pump_term_stride;  // reals between consecutive terms' envelopes
+  int scale_offset;     // coefficient sample ([k][sample][term][member]) of the first coefficient
   int step_offset;      // noise step = step_base[0] + step_offset
   double dt_d;
   float dt_f;

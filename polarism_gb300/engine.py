@@ -95,10 +95,12 @@ class RK4Engine:
 
     def __init__(self, nx, ny, members, dx, dy, dt, physics, precision="single", reservoir=True,
                  potential=_lib.PG_POT_NONE, pump_per_member=False, potential_per_member=False,
-                 components=1, reservoir_components=None):
-        """``reservoir``: True/"single", False/"none" or "double" (active + inactive, IFRK only);
+                 components=1, reservoir_components=None, pump_terms=1):
+        """``reservoir``: True/"single", False/"none", "double" or "quadratic-double";
         ``components``: 1, or 2 for a circular-basis spinor (IFRK only);
-        ``reservoir_components``: reservoir planes per field, 1 (shared) or ``components``."""
+        ``reservoir_components``: reservoir planes per field, 1 (shared) or ``components``;
+        ``pump_terms``: separable lasers L (envelopes (L, ...) and coefficients with a term
+        axis before the member axis when L > 1)."""
         self.lib = _lib.load()
         self.nx, self.ny, self.members = int(nx), int(ny), int(members)
         self.precision = precision
@@ -120,7 +122,9 @@ class RK4Engine:
                             potential_per_member=int(potential_per_member),
                             dx=float(dx), dy=float(dy), dt=float(dt),
                             components=self.components,
-                            reservoir_components=self.res_components)
+                            reservoir_components=self.res_components,
+                            pump_terms=int(pump_terms))
+        self.pump_terms = max(1, int(pump_terms))
         if isinstance(physics, (list, tuple)):
             plist = list(physics)
         else:
@@ -234,10 +238,15 @@ class RK4Engine:
         return t.value, h.value
 
     # -- stepping ----------------------------------------------------------------
+    def _coefficients(self, values, *lead):
+        """Pump coefficients as a C-contiguous (*lead, [L,] members) FP64 array."""
+        shape = tuple(int(v) for v in lead) + ((self.pump_terms,) if self.pump_terms > 1 else ()) \
+            + (self.members,)
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64), shape))
+
     def advance(self, start_step, n_steps, stage_scales, use_graphs=True):
-        """``stage_scales``: array (n_steps, 3, members) of pump coefficients."""
-        scales = np.ascontiguousarray(np.broadcast_to(
-            np.asarray(stage_scales, dtype=np.float64), (int(n_steps), 3, self.members)))
+        """``stage_scales``: array (n_steps, 3, [L,] members) of pump coefficients."""
+        scales = self._coefficients(stage_scales, n_steps, 3)
         _lib.check(self.lib.pg_rk4_advance(self.handle, int(start_step), int(n_steps),
                                            scales.ctypes.data, int(bool(use_graphs))),
                    "pg_rk4_advance")
@@ -246,8 +255,7 @@ class RK4Engine:
         """Split-step Fourier steps; ``half_scales`` is (n_steps, 2, members): the pump
         coefficients at t + dt/4 and t + 3 dt/4.  ordering 0 = R/2 K/2 N K/2 R/2 (real-space
         state), 1 = K/2 [R/2 N R/2] K/2 (leaves the unnormalised spectrum)."""
-        scales = np.ascontiguousarray(np.broadcast_to(
-            np.asarray(half_scales, dtype=np.float64), (int(n_steps), 2, self.members)))
+        scales = self._coefficients(half_scales, n_steps, 2)
         _lib.check(self.lib.pg_split_advance(self.handle, int(ordering), int(start_step),
                                              int(n_steps), scales.ctypes.data,
                                              int(bool(use_graphs))), "pg_split_advance")
@@ -256,16 +264,14 @@ class RK4Engine:
         """Fixed-step Lawson IFRK steps; tableau "rk4" or "dp5"; ``stage_scales`` is
         (n_steps, stages, members): pump coefficients at t + c_i dt."""
         tab, stages = _TABLEAUS[tableau]
-        scales = np.ascontiguousarray(np.broadcast_to(
-            np.asarray(stage_scales, dtype=np.float64), (int(n_steps), stages, self.members)))
+        scales = self._coefficients(stage_scales, n_steps, stages)
         _lib.check(self.lib.pg_ifrk_advance(self.handle, tab, int(start_step), int(n_steps),
                                             scales.ctypes.data), "pg_ifrk_advance")
 
     def ifrk_trial(self, h, stage_scales, rtol, atol):
         """One adaptive Dormand-Prince trial; returns (error, accepted).  Accepted trials
         become the state."""
-        scales = np.ascontiguousarray(np.broadcast_to(
-            np.asarray(stage_scales, dtype=np.float64), (7, self.members)))
+        scales = self._coefficients(stage_scales, 7)
         err = C.c_double()
         acc = C.c_int32()
         _lib.check(self.lib.pg_ifrk_trial(self.handle, 1, float(h), scales.ctypes.data, float(rtol),

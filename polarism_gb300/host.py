@@ -86,6 +86,16 @@ class LaserParameters:
     delay: float = 0.0
     circular_polarization: float = 0.0
     profile: dict = field(default_factory=dict)
+    # pulse-gaussian (polarism/laser/pulse_gaussian.py, peak-amplitude definition)
+    Pmax: float = 1.2
+    sigma_time: float = 0.1
+    pulse_separation: float = 0.6
+    cutoff_sigma: float = 3.0
+    n_pulses: int = 0
+    # mode "multiple": the lasers listed here (the reference reads them from a YAML file,
+    # polarism/laser/laser_factory.py:28-34,55-80)
+    mode: str = "single"
+    lasers: list = field(default_factory=list)
 
 
 @dataclass
@@ -235,11 +245,55 @@ def square_lattice(X, Y, constant, width, x0=0.0, y0=0.0):
     return out
 
 
+class PulseGaussian:
+    """Gaussian spot with a train of Gaussian pulses in time, peak-amplitude definition
+    (``polarism/laser/pulse_gaussian.py:34-55,101-135``): pulse n is centred at
+    delay + phase + n * separation with phase = cutoff * sigma_t, cut at cutoff * sigma_t, its
+    amplitude min(P0 + n (Pmax - P0), Pmax); n_pulses <= 0 means an endless train."""
+
+    time_independent = False
+
+    def __init__(self, cfg: LaserParameters, X, Y, precision="double"):
+        self.P0, self.Pmax = float(cfg.P0), float(cfg.Pmax)
+        self.x0, self.y0 = float(cfg.x0), float(cfg.y0)
+        self.delay, self.sigma_space = float(cfg.delay), float(cfg.sigma_space)
+        self.sigma_time, self.cutoff_sigma = float(cfg.sigma_time), float(cfg.cutoff_sigma)
+        self.pulse_separation, self.n_pulses = float(cfg.pulse_separation), int(cfg.n_pulses)
+        self.phase = self.cutoff_sigma * self.sigma_time
+        r2 = (X - self.x0) ** 2 + (Y - self.y0) ** 2
+        self._spatial_envelope = np.exp(-0.5 * r2 / self.sigma_space ** 2).astype(
+            real_dtype(precision), copy=False)
+
+    def power_coefficient(self, t: float) -> float:
+        if t < self.delay:
+            return 0.0
+        t_eff = t - self.delay
+        n = max(0, round((t_eff - self.phase) / self.pulse_separation))
+        if self.n_pulses > 0 and n >= self.n_pulses:
+            return 0.0
+        offset = t_eff - n * self.pulse_separation - self.phase
+        if abs(offset) > self.cutoff_sigma * self.sigma_time:
+            return 0.0
+        amplitude = min(self.P0 + n * (self.Pmax - self.P0), self.Pmax)
+        return amplitude * math.exp(-0.5 * (offset / self.sigma_time) ** 2)
+
+
+def make_lasers(cfg: LaserParameters, X, Y, precision="double"):
+    """The lasers of one config: one, or every entry of ``lasers`` in mode "multiple"."""
+    if cfg.mode == "multiple":
+        if not cfg.lasers:
+            raise ValueError("laser mode 'multiple' needs a non-empty lasers list")
+        return [make_laser(item, X, Y, precision) for item in cfg.lasers]
+    return [make_laser(cfg, X, Y, precision)]
+
+
 def make_laser(cfg: LaserParameters, X, Y, precision="double"):
     if cfg.laser_type == "profile":
         return ProfileLaser(cfg, X, Y, precision)
     if cfg.laser_type == "continuous-gaussian":
         return ContinuousGaussian(cfg, X, Y, precision)
+    if cfg.laser_type == "pulse-gaussian":
+        return PulseGaussian(cfg, X, Y, precision)
     raise ValueError(f"unsupported laser_type {cfg.laser_type!r}")
 
 
@@ -268,33 +322,42 @@ class PumpField:
 
 
 class BatchedPumpField:
-    """One laser per member: stacked envelopes and member-vector coefficients
-    (``polarism/laser/pump_field.py:92-152``)."""
+    """Laser slots matched across members (``polarism/laser/pump_field.py:92-152``): slot l
+    holds every member's l-th laser, its envelope shared when all are equal (else stacked per
+    member) and its coefficient a member vector."""
 
     def __init__(self, member_lasers, grid, precision):
         self.member_lasers = [list(lasers) for lasers in member_lasers]
+        if len({len(lasers) for lasers in self.member_lasers}) != 1:
+            raise ValueError("every member needs the same number of lasers")
         self.lasers = self.member_lasers[0]
         self.grid = grid
         self.precision = precision
-        slot = [lasers[0] for lasers in self.member_lasers]
-        envelopes = [laser._spatial_envelope for laser in slot]
-        shared = all(np.array_equal(envelopes[0], e) for e in envelopes[1:])
-        self._envelope = envelopes[0] if shared else np.stack(envelopes)[:, None]
-        self._slot = slot
+        self._terms = []
+        for slot in zip(*self.member_lasers):
+            envelopes = [laser._spatial_envelope for laser in slot]
+            shared = all(np.array_equal(envelopes[0], e) for e in envelopes[1:])
+            envelope = envelopes[0] if shared else np.stack(envelopes)[:, None]
+            self._terms.append((envelope, self._slot_coefficient(slot)))
 
-    def _coefficient(self, t):
-        return np.asarray([laser.power_coefficient(t) for laser in self._slot],
-                          dtype=real_dtype(self.precision))
+    def _slot_coefficient(self, slot):
+        dtype = real_dtype(self.precision)
+
+        def coefficient(t):
+            return np.asarray([laser.power_coefficient(t) for laser in slot], dtype=dtype)
+        return coefficient
 
     def separable_terms(self):
-        return [(self._envelope, self._coefficient)]
+        return list(self._terms)
 
     def separable_term(self):
         return None
 
     def __call__(self, t):
-        value = self._coefficient(t).reshape(-1, 1, 1, 1)
-        return self._envelope * value
+        total = 0
+        for envelope, coefficient in self._terms:
+            total = total + envelope * coefficient(t).reshape(-1, 1, 1, 1)
+        return total
 
 
 # --------------------------------------------------------------------------- reservoir
@@ -534,7 +597,7 @@ def build_simulation(cfg: Config, members: list[Config] | None = None):
             m.noise.seed = cfg.noise.seed if cfg.noise.seed is not None else 0
     components = 2 if cfg.physics.spin == "spinor" else 1
     res_components = cfg.reservoir.components or components
-    lasers = [[make_laser(m.laser, grid.X, grid.Y, precision)] for m in member_cfgs]
+    lasers = [make_lasers(m.laser, grid.X, grid.Y, precision) for m in member_cfgs]
     pump = BatchedPumpField(lasers, grid, precision) if batched else PumpField(lasers[0], grid, precision)
     res_cls = {"single": SingleReservoir, "double": DoubleReservoir,
                "quadratic-double": QuadraticDoubleReservoir,

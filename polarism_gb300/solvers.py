@@ -85,14 +85,15 @@ class _GB300Solver(AbstractSolver):
                 phys.pump_weight_plus, phys.pump_weight_minus = (float(v) for v in w[m if len(w) > 1 else 0])
         return out
 
-    def _ensure_engine(self, model, members, pump_env, potential):
-        pump_per_member = np.ndim(pump_env) == 4 and pump_env.shape[0] > 1
+    def _ensure_engine(self, model, members, pump_envs, potential):
+        pump_per_member = any(np.ndim(e) == 4 and e.shape[0] > 1 for e in pump_envs)
+        pump_terms = len(pump_envs)
         pot_kind = _lib.PG_POT_NONE
         pot_per_member = False
         if potential is not None and np.ndim(potential) > 0 and np.any(potential != 0):
             pot_kind = _lib.PG_POT_COMPLEX if np.iscomplexobj(potential) else _lib.PG_POT_REAL
             pot_per_member = np.ndim(potential) == 4 and potential.shape[0] > 1
-        key = (members, pump_per_member, pot_kind, pot_per_member)
+        key = (members, pump_per_member, pot_kind, pot_per_member, pump_terms)
         if self._engine is None or self._engine_key != key:
             if self._engine is not None:
                 self._engine.close()
@@ -103,27 +104,40 @@ class _GB300Solver(AbstractSolver):
                                      pump_per_member=pump_per_member,
                                      potential_per_member=pot_per_member,
                                      components=self._components,
-                                     reservoir_components=self._res_components)
+                                     reservoir_components=self._res_components,
+                                     pump_terms=pump_terms)
             self._engine_key = key
             self._pump_key = self._noise_key = self._potential_key = None
         return self._engine
 
     @staticmethod
-    def _pump_term(pump):
+    def _pump_terms(pump):
+        """Every laser's (envelope, coefficient(t)) (``pump_field.py:81-89``): the kernels sum
+        the terms per site, so any number of separable lasers runs on the GPU."""
         terms = pump.separable_terms() if hasattr(pump, "separable_terms") else None
         if terms is None and hasattr(pump, "separable_term"):
             term = pump.separable_term()
             terms = [term] if term is not None else None
-        if not terms or len(terms) != 1:
-            raise ValueError("rk4-cuda (GB300) needs a single separable pump term "
-                             "(envelope x coefficient(t))")
-        return terms[0]
+        if not terms:
+            raise ValueError("rk4-cuda (GB300) needs separable pump terms "
+                             "(envelope x coefficient(t) per laser)")
+        return list(terms)
 
-    def _upload_inputs(self, engine, model, envelope, potential):
-        env = _host(envelope)
-        key = (id(envelope), env.shape)
+    def _upload_inputs(self, engine, model, envelopes, potential):
+        envs = [_host(e) for e in envelopes]
+        key = tuple((id(e), h.shape) for e, h in zip(envelopes, envs))
         if self._pump_key != key:
-            engine.set_pump(np.ascontiguousarray(env, dtype=engine.real))
+            if len(envs) == 1:
+                env = np.ascontiguousarray(envs[0], dtype=engine.real)
+            else:
+                per_member = engine.members > 1 and any(np.ndim(h) == 4 and h.shape[0] > 1
+                                                        for h in envs)
+                shape = (engine.members, 1, engine.ny, engine.nx) if per_member else (engine.ny, engine.nx)
+                env = np.ascontiguousarray(np.stack([
+                    np.broadcast_to(np.asarray(h).reshape(shape if np.size(h) == np.prod(shape)
+                                                          else (engine.ny, engine.nx)), shape)
+                    for h in envs]), dtype=engine.real)
+            engine.set_pump(env)
             self._pump_key = key
         if engine.potential_kind != _lib.PG_POT_NONE:
             pkey = id(potential)
@@ -141,16 +155,31 @@ class _GB300Solver(AbstractSolver):
                 engine.set_noise(None)
             self._noise_key = nkey
 
-    def stage_scales(self, coefficient, t0, start_step, n_steps, members):
-        """Pump coefficients at t, t + dt/2, t + dt of each step (shape (n, 3, B))."""
+    @staticmethod
+    def _coefficient_row(coefficients, time, members):
+        """(L, B) coefficients of the L lasers at ``time`` (scalar or per-member values)."""
+        row = np.empty((len(coefficients), members), dtype=np.float64)
+        for term, coefficient in enumerate(coefficients):
+            value = np.asarray(coefficient(time), dtype=np.float64).reshape(-1)
+            row[term] = value if value.size == members else value[0]
+        return row
+
+    def _sampled(self, coefficients, times, members):
+        """Coefficients at each (step, sample) time: (n, S, B), or (n, S, L, B) with several
+        lasers (the layout of ``pg_rk4_advance`` / ``pg_split_advance`` / ``pg_ifrk_*``)."""
+        if callable(coefficients):  # one laser given as its coefficient function
+            coefficients = [coefficients]
+        times = np.asarray(times, dtype=np.float64)
+        out = np.empty(times.shape + (len(coefficients), members), dtype=np.float64)
+        for index in np.ndindex(times.shape):
+            out[index] = self._coefficient_row(coefficients, float(times[index]), members)
+        return out[..., 0, :] if len(coefficients) == 1 else out
+
+    def stage_scales(self, coefficients, t0, start_step, n_steps, members):
+        """Pump coefficients at t, t + dt/2, t + dt of each step (shape (n, 3, [L,] B))."""
         dt = self._dt
-        out = np.empty((n_steps, 3, members), dtype=np.float64)
-        for k in range(n_steps):
-            t = t0 + (start_step + k) * dt
-            for s, time in enumerate((t, t + 0.5 * dt, t + dt)):
-                value = np.asarray(coefficient(time), dtype=np.float64).reshape(-1)
-                out[k, s] = value if value.size == members else value[0]
-        return out
+        t = t0 + (start_step + np.arange(n_steps, dtype=np.float64)) * dt
+        return self._sampled(coefficients, t[:, None] + np.array([0.0, 0.5, 1.0]) * dt, members)
 
     #: Write results back into the caller's host arrays (for example pinned buffers)
     #: instead of returning fresh arrays each call.
@@ -161,16 +190,11 @@ class _GB300Solver(AbstractSolver):
         return (isinstance(array, np.ndarray) and array.dtype == dtype
                 and array.flags.c_contiguous and array.flags.writeable)
 
-    def half_scales(self, coefficient, t0, start_step, n_steps, members):
-        """Pump coefficients at t + dt/4 and t + 3 dt/4 of each step (shape (n, 2, B))."""
+    def half_scales(self, coefficients, t0, start_step, n_steps, members):
+        """Pump coefficients at t + dt/4 and t + 3 dt/4 of each step (shape (n, 2, [L,] B))."""
         dt = self._dt
-        out = np.empty((n_steps, 2, members), dtype=np.float64)
-        for k in range(n_steps):
-            t = t0 + (start_step + k) * dt
-            for s, time in enumerate((t + 0.25 * dt, t + 0.75 * dt)):
-                value = np.asarray(coefficient(time), dtype=np.float64).reshape(-1)
-                out[k, s] = value if value.size == members else value[0]
-        return out
+        t = t0 + (start_step + np.arange(n_steps, dtype=np.float64)) * dt
+        return self._sampled(coefficients, t[:, None] + np.array([0.25, 0.75]) * dt, members)
 
     # ------------------------------------------------------------------ contract
     def step(self, model, state, dt):
@@ -182,12 +206,13 @@ class _GB300Solver(AbstractSolver):
         field = state.field if state.field_k is None or getattr(state, "_field", None) is not None \
             else state.field_k
         members = int(field.shape[0])
-        envelope, coefficient = self._pump_term(model.pump)
+        terms = self._pump_terms(model.pump)
+        envelopes = [e for e, _ in terms]
         potential = getattr(model, "potential", None)
-        engine = self._ensure_engine(model, members, np.asarray(_host(envelope)),
+        engine = self._ensure_engine(model, members, [np.asarray(_host(e)) for e in envelopes],
                                      None if potential is None else _host(potential))
-        self._upload_inputs(engine, model, envelope, potential)
-        return engine, members, coefficient
+        self._upload_inputs(engine, model, envelopes, potential)
+        return engine, members, [c for _, c in terms]
 
     def _upload_state(self, engine, model, array):
         res_state = model.reservoir.get_state()
@@ -380,12 +405,8 @@ class IFRKFFTCudaSolver(_GB300Solver):
                 getattr(model.noise, "active", True):
             raise ValueError("solver.adaptive requires stochastic noise off")
 
-    def _stage_scales(self, coefficient, times, members):
-        out = np.empty((len(times), members), dtype=np.float64)
-        for i, time in enumerate(times):
-            value = np.asarray(coefficient(time), dtype=np.float64).reshape(-1)
-            out[i] = value if value.size == members else value[0]
-        return out
+    def _stage_scales(self, coefficients, times, members):
+        return self._sampled(coefficients, times, members)
 
     def advance(self, model, state, n_steps: int) -> None:
         from polarism_gb300.engine import TABLEAU_NODES

@@ -14,6 +14,7 @@ fresh run so the recorded vectors are pinned to it.
 """
 from __future__ import annotations
 
+import copy
 import importlib.abc
 import importlib.machinery
 import json
@@ -179,6 +180,47 @@ def trajectory_case(out, name, method, steps, **kw):
         seed=np.uint64(kw["seed"]), wigner=np.bool_(kw["wigner"]),
         physics=_physics_json(ctl.cfg), psi=np.asarray(ctl.state.field),
         res=np.stack([np.asarray(f) for f in ctl.reservoir.get_state()]),
+        norms=np.asarray(norms))
+
+
+def two_laser_case(out, name, method, steps, **kw):
+    """Two separable lasers (``pump_field.py:81-89``): the controller's continuous Gaussian plus
+    a pulsed Gaussian off centre, built directly (the reference's multiple-laser mode reads a
+    YAML file).  Stores both envelopes and every stage-time coefficient the reference used."""
+    from polarism.laser.laser_registry import available_lasers
+
+    ctl = _controller(method, **kw)
+    grid = ctl.grid
+    pulse = copy.deepcopy(ctl.cfg.laser)
+    pulse.laser_type, pulse.mode = "pulse-gaussian", "single"
+    pulse.x0, pulse.y0, pulse.sigma_space = 6.0, -3.0, 5.0
+    pulse.P0 = pulse.Pmax = 0.4
+    pulse.sigma_time, pulse.cutoff_sigma, pulse.pulse_separation, pulse.n_pulses = 0.01, 3.0, 0.05, 0
+    pulse.delay = 0.002
+    second = available_lasers.lookup("pulse-gaussian")(pulse, grid.X, grid.Y, ctl.cfg.solver.precision)
+    ctl.lasers = [ctl.lasers[0], second]
+    ctl.pump_field.lasers = ctl.lasers
+    assert len(ctl.pump_field.separable_terms()) == 2
+    psi0 = np.array(ctl.state.field, copy=True)
+    res0 = tuple(np.array(f, copy=True) for f in ctl.reservoir.get_state())
+    dt = kw["dt"]
+    nodes = (0.0, 0.5, 1.0) if method == "rk4-fdm" else (0.25, 0.75)
+    coeffs = np.asarray([[[laser.power_coefficient(k * dt + c * dt) for laser in ctl.lasers]
+                          for c in nodes] for k in range(steps)])
+    norms = []
+    for _ in range(steps):
+        ctl.solver.advance(ctl.model, ctl.state, 1)
+        norms.append(float(np.sum(np.abs(ctl.state.field) ** 2) * grid.dx * grid.dy))
+    np.savez_compressed(
+        out / f"{name}.npz", psi0=psi0, res0=np.stack(res0),
+        envelopes=np.stack([np.asarray(l._spatial_envelope) for l in ctl.lasers]),
+        coefficients=coeffs, nodes=np.asarray(nodes), dt=np.float64(dt), dx=np.float64(grid.dx),
+        dy=np.float64(grid.dy), k_squared=np.asarray(grid.k_squared), steps=np.int64(steps),
+        seed=np.uint64(kw["seed"]), wigner=np.bool_(kw["wigner"]), physics=_physics_json(ctl.cfg),
+        pulse=json.dumps({k: getattr(pulse, k) for k in ("P0", "Pmax", "x0", "y0", "sigma_space",
+                                                         "sigma_time", "cutoff_sigma",
+                                                         "pulse_separation", "n_pulses", "delay")}),
+        psi=np.asarray(ctl.state.field), res=np.stack([np.asarray(f) for f in ctl.reservoir.get_state()]),
         norms=np.asarray(norms))
 
 
@@ -372,6 +414,9 @@ def main(root):
                         **dict(common, reservoir=res, p0=0.3))
         trajectory_case(HERE, "split_cpu_p2_" + res.replace("-", "_"), "split-step-fft", 12,
                         **dict(common, nx=32, ny=16, lx=40.0, ly=20.0, reservoir=res, p0=0.3))
+    two_laser_case(HERE, "rk4_fdm_two_lasers", "rk4-fdm", 20, **dict(common, nx=32, ny=16, ly=20.0))
+    two_laser_case(HERE, "split_cpu_two_lasers", "split-step-fft", 20,
+                   **dict(common, nx=32, ny=16, ly=20.0))
     kouter_case(HERE)
     ifrk4_cases(HERE, root)
     dp5_case(HERE)

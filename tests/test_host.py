@@ -88,6 +88,12 @@ def test_stage_scales_follow_stage_times():
     assert np.allclose(scales[:, :, 0], [[0.3, 0.35, 0.4], [0.4, 0.45, 0.5]])
     member = solver.stage_scales(lambda t: np.asarray([t, 2 * t]), 0.0, 0, 1, 2)
     assert np.allclose(member[0], [[0.0, 0.0], [0.05, 0.1], [0.1, 0.2]])
+    two = solver.stage_scales([lambda t: t, lambda t: np.asarray([1.0, 2.0])], 0.0, 1, 1, 2)
+    assert two.shape == (1, 3, 2, 2)  # [step][stage][laser][member]
+    assert np.allclose(two[0, :, 0], [[0.1, 0.1], [0.15, 0.15], [0.2, 0.2]])
+    assert np.allclose(two[0, :, 1], [[1.0, 2.0]] * 3)
+    half = solver.half_scales([lambda t: t, lambda t: 3.0], 0.0, 0, 2, 1)
+    assert half.shape == (2, 2, 2, 1) and np.allclose(half[1, :, 0, 0], [0.125, 0.175])
     grid, model, state = build_simulation(cfg)
     assert state.field.shape == (1, 1, cfg.grid.ny, cfg.grid.nx)
 
@@ -135,3 +141,25 @@ def test_registers_as_drop_in_for_reference_solver_names():
     assert available_solvers.lookup("rk4-cuda") is registered["rk4-cuda"]
     caps = solver_capabilities("rk4-cuda")
     assert "wigner" in caps.noise and 1 in caps.components
+
+
+def test_pulse_gaussian_coefficient_matches_reference_fixture():
+    """The host mirror's pulsed-laser time envelope reproduces the coefficients the reference
+    computed for the two-laser fixtures (``polarism/laser/pulse_gaussian.py:101-135``)."""
+    import json
+
+    from polarism_gb300.host import GridParameters, LaserParameters, PeriodicGrid, make_lasers
+    from tests.conftest import load_golden
+
+    for case in ("rk4_fdm_two_lasers", "split_cpu_two_lasers"):
+        g = load_golden(case)
+        pulse = json.loads(str(g["pulse"]))
+        cw = LaserParameters(laser_type="continuous-gaussian", P0=0.05, sigma_space=8.0)
+        pl = LaserParameters(laser_type="pulse-gaussian", **pulse)
+        grid = PeriodicGrid(GridParameters(nx=32, ny=16, lx=40.0, ly=20.0))
+        lasers = make_lasers(LaserParameters(mode="multiple", lasers=[cw, pl]), grid.X, grid.Y)
+        assert np.allclose(lasers[1]._spatial_envelope, g["envelopes"][1], rtol=1e-15, atol=0)
+        dt = float(g["dt"])
+        got = np.asarray([[[laser.power_coefficient(k * dt + c * dt) for laser in lasers]
+                           for c in g["nodes"]] for k in range(int(g["steps"]))])
+        np.testing.assert_allclose(got, g["coefficients"], rtol=1e-13, atol=1e-15)

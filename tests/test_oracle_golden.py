@@ -220,3 +220,38 @@ def test_config1_smoke_values():
     norm = float(gpe.norm(psi, grid.dx, grid.dy)[0])
     assert abs(norm - 0.009835377212841102) < 1e-12
     assert abs(float(fields[0].max()) - 0.003993766474840784) < 1e-12
+
+
+def two_laser_pump(g):
+    """P(t) = E_0 c_0(t) + E_1 c_1(t) from the fixture's recorded stage coefficients, keyed by
+    quarter steps (the RK4 and split-step stage times are multiples of dt / 4)."""
+    dt = float(g["dt"])
+    table = {}
+    for k in range(int(g["steps"])):
+        for s, node in enumerate(g["nodes"]):
+            table[int(round(4 * (k + node)))] = g["coefficients"][k, s]
+    env = g["envelopes"]
+
+    def pump_at(t):
+        c = table[int(round(4 * t / dt))]
+        return env[0] * c[0] + env[1] * c[1]
+    return pump_at
+
+
+@pytest.mark.parametrize("case", ["rk4_fdm_two_lasers", "split_cpu_two_lasers"])
+def test_two_laser_trajectories_match_reference(golden, case):
+    g = golden(case)
+    p = g["physics"]
+    dx, dy, dt = float(g["dx"]), float(g["dy"]), float(g["dt"])
+    noise = gpe.Noise([int(g["seed"])], [p["gamma_C"]], [p["R"]], [1.0], dt, dx * dy, "double")
+    norms = []
+    if case.startswith("rk4"):
+        psi, fields = gpe.rk4_advance(g["psi0"].copy(), tuple(g["res0"]), two_laser_pump(g), 0.0, p,
+                                      dx, dy, dt, 0, int(g["steps"]), noise=noise, norm_trace=norms)
+    else:
+        psi, fields = gpe.split_advance("cpu", g["psi0"].copy(), tuple(g["res0"]), two_laser_pump(g),
+                                        0.0, p, g["k_squared"], dx, dy, dt, 0, int(g["steps"]),
+                                        noise=noise, norm_trace=norms)
+    assert rel_l2(psi, g["psi"]) < 1e-12
+    assert rel_l2(fields[0], g["res"][0]) < 1e-12
+    assert rel_l2(np.asarray(norms).ravel(), g["norms"]) < 1e-12
