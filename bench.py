@@ -389,6 +389,138 @@ def run_e2e(args, w, members, torch):
             "calls": calls}
 
 
+# ----------------------------------------------------------------------------- split-step leg
+SPLIT_BYTES = {"kouter": 44, "cpu": 76}  # FP32 algorithmic bytes per site-update
+
+
+def run_split_bench(args):
+    """Split-step Fourier throughput at 1024^2 (the precision-check configuration stepped by
+    split-step-fft-cuda, or split-step-fft with --split-ordering cpu): members x 1024^2 FP32,
+    Wigner noise on, site-updates/s against the HBM roofline at 44 B/site (K-outer: one column
+    pass and one row pass per step, each reading and writing psi, plus the reservoir and the
+    pump in the column pass) or 76 B/site (CPU ordering: two of each pass)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from polarism_gb300 import build as _build
+
+    _build.build()
+    from polarism_gb300.engine import MemberPhysics, RK4Engine
+
+    ordering = args.split_ordering
+    members = args.members
+    w = workload(members, first=rank_members(rank, world, members)[0])
+    eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**PHYSICS), "single",
+                    pump_per_member=True)
+    eng.set_pump(w["env"])
+    eng.set_noise(w["seeds"], PHYSICS["gamma_C"], PHYSICS["R"], 1.0, DT / (4 * w["dx"] * w["dy"]))
+    eng.set_state(w["psi"], w["n"])
+    stream = torch.cuda.ExternalStream(eng.stream)
+    code = 1 if ordering == "kouter" else 0
+    half = np.full((args.warmup + args.steps, 2, members), P0)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    eng.split_advance(code, 0, args.warmup, half[:args.warmup])
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    start.record(stream)
+    eng.split_advance(code, args.warmup, args.steps, half[args.warmup:])
+    stop.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    launches = eng.last_launch_count
+    elapsed_ms = max_over_ranks(start.elapsed_time(stop), world, "cuda")
+    sites = members * NX * NY
+    value = world * sites * args.steps / (elapsed_ms / 1e3)
+    bytes_per_site = SPLIT_BYTES[ordering]
+    achieved = bytes_per_site * sites / (elapsed_ms / 1e3 / args.steps) / 1e9
+    peak, peak_kind = measured_peak()
+
+    # End to end: host state in (pinned), 64 steps, host state out, every call.
+    psi_host = torch.empty(w["psi"].shape, dtype=torch.complex64, pin_memory=True).numpy()
+    n_host = torch.empty(w["n"].shape, dtype=torch.float32, pin_memory=True).numpy()
+    psi_host[...] = w["psi"]
+    n_host[...] = w["n"]
+    chunk = 64
+    calls = max(1, min(args.e2e_calls, 1 + args.steps // chunk))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c in range(calls):
+        eng.set_state(psi_host, n_host)
+        eng.set_state_kind(False)
+        eng.split_advance(code, c * chunk, chunk, np.full((chunk, 2, members), P0))
+        eng.get_state(psi_host, n_host)  # K-outer leaves the spectrum, read back as it is
+    e2e_s = time.perf_counter() - t0
+    eng.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": f"split-step site-updates/s at 1024^2 ({ordering} ordering)", "value": value,
+        "unit": "site-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": ("split-step-fft-cuda (K/2 [R/2 N R/2] K/2)" if code == 1 else
+                                "split-step-fft (R/2 K/2 N K/2 R/2)") +
+                               ", 1024^2 periodic, lx=ly=400, dt=5e-4, single reservoir, "
+                               "Wigner noise on, complex64",
+                   "members": members, "global_members": members * world, "grid": [NY, NX],
+                   "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_site": bytes_per_site},
+        "e2e": {"value": sites * chunk * calls / e2e_s, "unit": "site-updates/s",
+                "h2d_bytes_per_step": sites * 12, "d2h_bytes_per_step": sites * 12,
+                "step": f"set_state + {chunk} split steps + get_state from pinned host arrays",
+                "calls": calls},
+        "clocks": clocks,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = split_cpu_baseline(ordering)
+    print(json.dumps(line), flush=True)
+
+
+def split_cpu_baseline(ordering, sample_steps=4):
+    """Oracle port, one core: sample_steps split steps of one 1024^2 member (FP64 NumPy)."""
+    from oracle import gpe
+
+    w = workload(1, "double")
+    p = dict(PHYSICS)
+    env = w["env"][0, 0].astype(np.float64) * P0
+    kx = 2 * np.pi * np.fft.fftfreq(NX, d=w["dx"])
+    ky = 2 * np.pi * np.fft.fftfreq(NY, d=w["dy"])
+    k2 = kx[None, :] ** 2 + ky[:, None] ** 2
+    psi, fields = w["psi"].astype(np.complex128), (w["n"].astype(np.float64),)
+    noise = gpe.Noise([42], [p["gamma_C"]], [p["R"]], [1.0], DT, w["dx"] * w["dy"])
+    gpe.split_advance(ordering, psi.copy(), fields, lambda t: env, 0.0, p, k2, w["dx"], w["dy"],
+                      DT, 0, 1, noise=noise)
+    t0 = time.perf_counter()
+    gpe.split_advance(ordering, psi, fields, lambda t: env, 0.0, p, k2, w["dx"], w["dy"], DT, 0,
+                      sample_steps, noise=noise)
+    elapsed = time.perf_counter() - t0
+    return {"value": sample_steps * NX * NY / elapsed, "unit": "site-updates/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{sample_steps} split steps ({ordering} ordering) of one 1024^2 member, "
+                      "FP64 NumPy oracle, 1 thread"}
+
+
 # ----------------------------------------------------------------------------- sweep leg
 SWEEP_SIZES = (128, 256, 512)
 SWEEP_DX = 100.0 / 128  # lx scaled with nx so every member has the same cell
@@ -712,7 +844,9 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=8)
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["rk4", "sweep", "spinor", "fno"], default="rk4",
+    ap.add_argument("--split-ordering", choices=["kouter", "cpu"], default="kouter",
+                    help="split workload: K-outer (split-step-fft-cuda) or CPU ordering")
+    ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno"], default="rk4",
                     help="rk4: the 1024^2 fused-step benchmark; sweep: the uneven-size sweep; "
                          "spinor: the adaptive two-component IFRK run")
     ap.add_argument("--spinor-time", type=float, default=500.0)
@@ -735,6 +869,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.workload == "split":
+        run_split_bench(args)
+        return
     if args.workload == "spinor":
         run_spinor_bench(args)
         return

@@ -63,19 +63,11 @@ __global__ void __launch_bounds__(1024) row_pass_kernel(typename C2T<T>::type* _
 
 // ------------------------------------------------------------------ local operations
 template <typename T>
-__device__ __forceinline__ T expm1_t(T x);
-template <>
-__device__ __forceinline__ float expm1_t<float>(float x) { return expm1f(x); }
-template <>
-__device__ __forceinline__ double expm1_t<double>(double x) { return expm1(x); }
-template <typename T>
 __device__ __forceinline__ T exp_t(T x);
 template <>
 __device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
 template <>
 __device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
-__device__ __forceinline__ void sincos_t(float x, float* s, float* c) { sincosf(x, s, c); }
-__device__ __forceinline__ void sincos_t(double x, double* s, double* c) { sincos(x, s, c); }
 __device__ __forceinline__ float mul_rn_t(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn_t(double a, double b) { return __dmul_rn(a, b); }
 
@@ -120,6 +112,31 @@ __device__ __forceinline__ void reservoir_half2(T& a, T& b, T rho, T pump, T h, 
   b = nb > T(0) ? nb : T(0);
 }
 
+// (exp(x) - 1) / x and (sin, cos) of the local step.  FP64 follows the reference (expm1 with its
+// three-term series below 1e-6, library sincos).  FP32 uses a five-term series for |x| < 2^-5
+// (truncation x^5/720 < 5e-11 relative) and Taylor polynomials for |phi| < 1/8 (truncation
+// below 1e-13), the library functions outside: the per-step arguments are that small at the
+// time steps the split-step solvers run with, and the polynomials are cheaper than the
+// library's range reduction.
+__device__ __forceinline__ double phase_time_factor(double x) {
+  return fabs(x) < 1e-6 ? 1.0 + x * 0.5 + x * x / 6.0 : expm1(x) / x;
+}
+__device__ __forceinline__ float phase_time_factor(float x) {
+  if (fabsf(x) < 0.03125f)
+    return 1.0f + x * (0.5f + x * (1.0f / 6.0f + x * (1.0f / 24.0f + x * (1.0f / 120.0f))));
+  return expm1f(x) / x;
+}
+__device__ __forceinline__ void local_sincos(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void local_sincos(float x, float* s, float* c) {
+  if (fabsf(x) < 0.125f) {
+    const float x2 = x * x;
+    *s = x * (1.0f - x2 * (1.0f / 6.0f) * (1.0f - x2 * (1.0f / 20.0f) * (1.0f - x2 * (1.0f / 42.0f))));
+    *c = 1.0f - x2 * 0.5f * (1.0f - x2 * (1.0f / 12.0f) * (1.0f - x2 * (1.0f / 30.0f) * (1.0f - x2 * (1.0f / 56.0f))));
+  } else {
+    sincosf(x, s, c);
+  }
+}
+
 // Exact local step psi * exp(g dt - i phi) (split_step_fft_solver.py:121-139); n2 is the
 // inactive reservoir (0 without one), which enters the phase through g_I.
 template <typename T>
@@ -128,14 +145,13 @@ __device__ __forceinline__ void nonlinear(T& re, T& im, T n, T n2, bool two, T v
   const T rho = re * re + im * im;
   const T gain = (k.R * n - k.gamma_C) * T(0.5) + vim * k.inv_hbar;
   const T x = T(2) * gain * dt;
-  const T phase_time =
-      fabs(x) < T(1e-6) ? dt * (T(1) + x * T(0.5) + x * x / T(6)) : dt * expm1_t(x) / x;
+  const T phase_time = dt * phase_time_factor(x);
   T pot = vre + k.g_R * n;
   if (two) pot += k.g_I * n2;
   const T phase = (pot * dt + k.g_C * rho * phase_time) * k.inv_hbar;
   const T amp = exp_t(gain * dt);
   T s, c;
-  sincos_t(phase, &s, &c);
+  local_sincos(phase, &s, &c);
   const T r = re, i = im;
   re = amp * (r * c + i * s);
   im = amp * (i * c - r * s);
@@ -187,6 +203,10 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
     const T dt = a.template dt_of<T>();
     const T h = dt * T(0.5);
     const unsigned long long step = a.noise ? step_base[0] + a.step_offset : 0ull;
+    // Philox rounds that depend only on (step, stream, key), formed once for the block.
+    const PhiloxCellPrefix prefix =
+        philox_cell_prefix(static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32), 1u,
+                           static_cast<uint32_t>(k.seed), static_cast<uint32_t>(k.seed >> 32));
     // One reservoir half step at the given pump coefficient on the chosen model.
     auto res_half = [&](T& n, T& n2, T rho, T pump_value) {
       if (two) {
@@ -243,8 +263,10 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
           break;
       }
       if (add_noise) {
-        const Words4 w = wigner_words(static_cast<uint32_t>(o), step, 1u, k.seed);
-        WignerDraw<T>::apply(w, k.noise_a + k.noise_b * n, v.x, v.y);
+        const uint32_t cell[1] = {static_cast<uint32_t>(o)};
+        Words4 w[1];
+        philox_cells(cell, prefix, w);
+        WignerDraw<T>::apply(w[0], k.noise_a + k.noise_b * n, v.x, v.y);
       }
       buf[i * C + c] = v;
       if (a.reservoir || two) rm[o] = n;
