@@ -26,6 +26,10 @@
 namespace pg {
 namespace {
 
+// Element loops are unrolled so several global loads are in flight per thread.
+constexpr int kUnrollIO = 4;
+constexpr int kUnrollLocal = 2;
+
 // ------------------------------------------------------------------ row pass
 template <typename T>
 __global__ void __launch_bounds__(1024) row_pass_kernel(typename C2T<T>::type* __restrict__ data,
@@ -44,6 +48,7 @@ __global__ void __launch_bounds__(1024) row_pass_kernel(typename C2T<T>::type* _
   C2* d = data + member * plane + static_cast<long long>(row0) * a.nx;
   for (int k = threadIdx.x; k < a.nx; k += blockDim.x) tws[k] = tw[k];
   const int count = rows * a.nx;
+  #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) buf[e] = d[e];
   __syncthreads();
   if (a.forward) smem_fft<T, false, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
@@ -58,6 +63,7 @@ __global__ void __launch_bounds__(1024) row_pass_kernel(typename C2T<T>::type* _
     __syncthreads();
   }
   if (a.inverse) smem_fft<T, true, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
+  #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) d[e] = buf[e];
 }
 
@@ -179,6 +185,7 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
   C2* d = data + member * plane;
   for (int k = threadIdx.x; k < a.ny; k += blockDim.x) tws[k] = tw[k];
   const int count = C * a.ny;
+  #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) {
     const int c = e & (C - 1), i = e >> a.log2cols;
     buf[i * C + c] = d[static_cast<long long>(i) * a.nx + x0 + c];
@@ -215,6 +222,7 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
         n = reservoir_half(n, rho, pump_value, h, k);
       }
     };
+    #pragma unroll kUnrollLocal
     for (int e = threadIdx.x; e < count; e += blockDim.x) {
       const int c = e & (C - 1), i = e >> a.log2cols;
       const long long o = static_cast<long long>(i) * a.nx + x0 + c;
@@ -275,6 +283,7 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
     __syncthreads();
   }
   if (a.forward) smem_fft<T, false, true>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
+  #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) {
     const int c = e & (C - 1), i = e >> a.log2cols;
     d[static_cast<long long>(i) * a.nx + x0 + c] = buf[i * C + c];
