@@ -87,6 +87,7 @@ struct IfrkBuffers {
   std::vector<double> host_partials;
   bool w_valid = false;  // W holds F_y of the current state
   SpinorConst* spin = nullptr;  // two-component Lawson constants per member
+  float* spin_modes = nullptr;  // FP32 state: per-mode table of the two-component factor
 };
 
 IfrkBuffers& bufs(pg_solver* s) { return *static_cast<IfrkBuffers*>(s->ifrk); }
@@ -129,6 +130,14 @@ int ensure_ifrk(pg_solver* s) {
     }
     PG_CUDA(cudaMalloc(&b->spin, host.size() * sizeof(SpinorConst)));
     PG_CUDA(cudaMemcpy(b->spin, host.data(), host.size() * sizeof(SpinorConst), cudaMemcpyHostToDevice));
+    if (c.precision == PG_SINGLE) {
+      PG_CUDA(cudaMalloc(&b->spin_modes, sizeof(float) * kSpinModeFields * static_cast<size_t>(s->plane) *
+                                             c.members));
+      PG_CUDA(launch_spin_mode_table(b->spin_modes, b->spin, c.nx, c.ny, c.members,
+                                     2.0 * kPi2 / (static_cast<double>(c.nx) * c.dx),
+                                     2.0 * kPi2 / (static_cast<double>(c.ny) * c.dy), s->stream));
+      PG_CUDA(cudaStreamSynchronize(s->stream));
+    }
   }
   const size_t esize = s->real_size;
   if (c.precision == PG_DOUBLE)
@@ -205,8 +214,17 @@ Plan make_plan(const pg_solver* s) {
     rows *= 2;
   r.rows = rows;
   r.log2rows = ilog2i(rows);
-  int threads = (rows * c.nx * comps + mv - 1) / mv;
-  r.threads = std::max(32, ((threads + 31) / 32) * 32);
+  // Threads per block: mv values each, unless the whole grid would then hold fewer threads
+  // than the GPU runs at once (a single 512^2 spinor gives about 7 warps per SM); then down to
+  // four values a thread, which the Stockham passes handle with one butterfly per thread.
+  const long long resident = 1024LL * std::max(1, s->sm_count);
+  auto block_threads = [&](long long blocks, int values) {
+    int th = (values + mv - 1) / mv;
+    if (blocks * th < resident) th = std::min(1024, std::max(th, (values + 3) / 4));
+    return std::max(32, ((th + 31) / 32) * 32);
+  };
+  int threads = block_threads(static_cast<long long>(c.ny / rows) * c.members, rows * c.nx * comps);
+  r.threads = threads;
   r.members = c.members;
   r.comps = comps;
   r.member_stride = s->plane * comps;
@@ -215,6 +233,7 @@ Plan make_plan(const pg_solver* s) {
   r.ky_unit = 2.0 * kPi2 / (static_cast<double>(c.ny) * c.dy);
   r.inv_n = 1.0 / (static_cast<double>(c.nx) * c.ny);
   r.spin = s->ifrk ? static_cast<const void*>(static_cast<IfrkBuffers*>(s->ifrk)->spin) : nullptr;
+  r.modes = s->ifrk ? static_cast<IfrkBuffers*>(s->ifrk)->spin_modes : nullptr;
   IfrkColArgs& k = p.col;
   k.nx = c.nx;
   k.ny = c.ny;
@@ -227,8 +246,7 @@ Plan make_plan(const pg_solver* s) {
     cols *= 2;
   k.cols = cols;
   k.log2cols = ilog2i(cols);
-  threads = (cols * comps * c.ny + mv - 1) / mv;
-  k.threads = std::max(32, ((threads + 31) / 32) * 32);
+  k.threads = block_threads(static_cast<long long>(c.nx / cols) * c.members, cols * comps * c.ny);
   k.members = c.members;
   k.comps = comps;
   k.log2comps = comps == 2 ? 1 : 0;
@@ -276,7 +294,11 @@ StepTables build_tables(const Tableau& tb, double h) {
 
 // The spinor row pass evaluates its Lawson factors from tau instead of the tables.
 void set_taus(IfrkRowArgs& r, const StepTables& st) {
-  for (int t = 0; t < r.terms; ++t) r.tau[t] = st.taus[r.table[t]];
+  for (int t = 0; t < r.terms; ++t) {
+    r.tau[t] = st.taus[r.table[t]];
+    r.tau_hi[t] = static_cast<float>(r.tau[t]);
+    r.tau_lo[t] = static_cast<float>(r.tau[t] - static_cast<double>(r.tau_hi[t]));
+  }
 }
 
 template <typename T>
@@ -514,6 +536,7 @@ void ifrk_release(pg_solver* s) {
   cudaFree(b->tables);
   cudaFree(b->partials);
   cudaFree(b->spin);
+  cudaFree(b->spin_modes);
   delete b;
   s->ifrk = nullptr;
 }

@@ -169,9 +169,15 @@ PassPlan plan(const pg_solver* s) {
   while (rows * 2 <= c.ny && rows * 2 * c.nx <= 4096) rows *= 2;
   r.rows = rows;
   r.log2rows = ilog2(rows);
-  int threads = (rows * c.nx + mv - 1) / mv;
-  threads = ((threads + 31) / 32) * 32;
-  r.threads = threads < 32 ? 32 : threads;
+  // mv values a thread, or down to four when the grid would not fill the GPU otherwise.
+  const long long resident = 1024LL * std::max(1, s->sm_count);
+  auto block_threads = [&](long long blocks, int values) {
+    int th = (values + mv - 1) / mv;
+    if (blocks * th < resident) th = std::min(1024, std::max(th, (values + 3) / 4));
+    return std::max(32, ((th + 31) / 32) * 32);
+  };
+  int threads = block_threads(static_cast<long long>(c.ny / rows) * c.members, rows * c.nx);
+  r.threads = threads;
   r.table_stride = c.nx + c.ny;
   ColPassArgs& k = p.col;
   k.nx = c.nx;
@@ -183,9 +189,7 @@ PassPlan plan(const pg_solver* s) {
     cols *= 2;
   k.cols = cols;
   k.log2cols = ilog2(cols);
-  threads = (cols * c.ny + mv - 1) / mv;
-  threads = ((threads + 31) / 32) * 32;
-  k.threads = threads < 32 ? 32 : threads;
+  k.threads = block_threads(static_cast<long long>(c.nx / cols) * c.members, cols * c.ny);
   k.members = c.members;
   k.reservoir = c.reservoir == PG_RES_SINGLE;
   k.res_kind = c.reservoir;

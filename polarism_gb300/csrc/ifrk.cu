@@ -8,6 +8,8 @@
 // condensate and the reservoir, accumulated here in FP64).  The fused kernels of
 // polarism/solver/ifrk_cuda_fused.py:10-108 (combine_k / stage_rhs / finish_res) map onto
 // one row pass and one column pass per stage.
+#include <algorithm>
+
 #include "fft.cuh"
 #include "ifrk_internal.h"
 #include "philox.cuh"
@@ -25,6 +27,52 @@ __device__ __forceinline__ void sincos_angle(double a, float* s, float* c) {
   sincosf(static_cast<float>(fma(-n, kTwoPi, a)), s, c);
 }
 __device__ __forceinline__ void sincos_angle(double a, double* s, double* c) { sincos(a, s, c); }
+
+// sin and cos of (r_hi + r_lo)(t_hi + t_lo): the product is formed as p + t with the exact
+// rounding error of p = r_hi t_hi (an FMA) and the cross terms, reduced by 2 pi split into two
+// floats (Cody and Waite's method), so the reduced angle carries an absolute error of a few
+// 1e-7 for any angle below 2^24 turns -- the accuracy of the FP64 reduction rounded to FP32.
+__device__ __forceinline__ void sincos_product(float r_hi, float r_lo, float t_hi, float t_lo,
+                                               float* s, float* c) {
+  constexpr float kTwoPiHi = 6.28318548202514648f;        // float(2 pi)
+  constexpr float kTwoPiLo = -1.74845553146951617e-07f;   // 2 pi - kTwoPiHi
+  constexpr float kInvTwoPi = 0.159154943091895336f;
+  const float p = r_hi * t_hi;
+  const float e = fmaf(r_hi, t_hi, -p);
+  const float t = fmaf(r_hi, t_lo, fmaf(r_lo, t_hi, e));
+  const float n = rintf(p * kInvTwoPi);
+  const float d = fmaf(-n, kTwoPiLo, fmaf(-n, kTwoPiHi, p)) + t;
+  sincosf(d, s, c);
+}
+
+// Per-mode FP32 table of the two-component Lawson factor, formed once in FP64.
+__global__ void spin_mode_table_kernel(float* __restrict__ table, const SpinorConst* __restrict__ consts,
+                                       int nx, int ny, double kx_unit, double ky_unit) {
+  const int member = blockIdx.y;
+  const long long plane = static_cast<long long>(nx) * ny;
+  const SpinorConst sc = consts[member];
+  float* tm = table + static_cast<long long>(member) * kSpinModeFields * plane;
+  for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < plane;
+       e += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int j = static_cast<int>(e % nx);
+    const int i = static_cast<int>(e / nx);
+    const double kx = kx_unit * static_cast<double>(j < (nx >> 1) ? j : j - nx);
+    const double ky = ky_unit * static_cast<double>(i < (ny >> 1) ? i : i - ny);
+    const double k2 = kx * kx + ky * ky;
+    const double rate_e = sc.rate * k2;
+    const double bk2 = sc.beta * k2;
+    const double omega = sqrt(sc.half_z * sc.half_z + bk2 * bk2);
+    const double rate_w = omega * sc.inv_hbar;
+    const float re_hi = static_cast<float>(rate_e), rw_hi = static_cast<float>(rate_w);
+    tm[0 * plane + e] = re_hi;
+    tm[1 * plane + e] = static_cast<float>(rate_e - static_cast<double>(re_hi));
+    tm[2 * plane + e] = rw_hi;
+    tm[3 * plane + e] = static_cast<float>(rate_w - static_cast<double>(rw_hi));
+    tm[4 * plane + e] = static_cast<float>(sc.beta * (kx * kx - ky * ky));
+    tm[5 * plane + e] = static_cast<float>(-2.0 * sc.beta * kx * ky);
+    tm[6 * plane + e] = omega > 0.0 ? static_cast<float>(1.0 / omega) : 0.0f;
+  }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(1024) ifrk_row_kernel(const typename C2T<T>::type* __restrict__ in,
@@ -86,6 +134,49 @@ __global__ void __launch_bounds__(1024) ifrk_row_kernel(const typename C2T<T>::t
     // s = sin(w t) / w, w = sqrt(z^2 + |u|^2), u = beta (kx - i ky)^2 (dispersion.py:66-83).
     const SpinorConst sc = static_cast<const SpinorConst*>(a.spin)[member];
     const T zf = static_cast<T>(sc.half_z);
+    if constexpr (sizeof(T) == 4) {
+      // FP32 state: the per-mode quantities come from the table and the angles are formed in
+      // compensated FP32 (sincos_product); the arithmetic after the angles is the same.
+      const float inv_hbar_f = static_cast<float>(sc.inv_hbar);
+      const long long mplane = static_cast<long long>(a.nx) * a.ny;
+      const float* tm = a.modes + static_cast<long long>(member) * kSpinModeFields * mplane +
+                        static_cast<long long>(row0) * a.nx;
+      for (int e = threadIdx.x; e < count; e += blockDim.x) {
+        const float re_hi = tm[e], re_lo = tm[mplane + e];
+        const float rw_hi = tm[2 * mplane + e], rw_lo = tm[3 * mplane + e];
+        const float ure = tm[4 * mplane + e], uim = tm[5 * mplane + e];
+        const float inv_om = tm[6 * mplane + e];
+        C2 acc0{T(0), T(0)}, acc1{T(0), T(0)};
+#pragma unroll 1
+        for (int t = 0; t < a.terms; ++t) {
+          T se, ce, sw, cw;
+          sincos_product(re_hi, re_lo, a.tau_hi[t], a.tau_lo[t], &se, &ce);
+          sincos_product(rw_hi, rw_lo, a.tau_hi[t], a.tau_lo[t], &sw, &cw);
+          const T so = inv_om > 0.0f ? sw * inv_om : a.tau_hi[t] * inv_hbar_f;
+          C2 s0, s1;
+          if (a.src[t]) {
+            const C2* src = static_cast<const C2*>(a.src[t]) + moff;
+            s0 = src[e];
+            s1 = src[plane + e];
+          } else {
+            s0 = buf[e];
+            s1 = buf[count + e];
+          }
+          const T sz = so * zf;
+          const C2 a0{cw * s0.x + sz * s0.y + so * (uim * s1.x + ure * s1.y),
+                      cw * s0.y - sz * s0.x + so * (uim * s1.y - ure * s1.x)};
+          const C2 a1{cw * s1.x - sz * s1.y + so * (ure * s0.y - uim * s0.x),
+                      cw * s1.y + sz * s1.x - so * (ure * s0.x + uim * s0.y)};
+          const T w = static_cast<T>(a.coef[t] * a.inv_n);
+          acc0.x += w * (ce * a0.x + se * a0.y);
+          acc0.y += w * (ce * a0.y - se * a0.x);
+          acc1.x += w * (ce * a1.x + se * a1.y);
+          acc1.y += w * (ce * a1.y - se * a1.x);
+        }
+        buf[e] = acc0;
+        buf[count + e] = acc1;
+      }
+    } else
     for (int e = threadIdx.x; e < count; e += blockDim.x) {
       const int j = e & (a.nx - 1);
       const int i = row0 + (e >> a.log2nx);
@@ -404,5 +495,14 @@ template cudaError_t launch_ifrk_col<double>(double*, const double*, double*, do
                                              const IfrkColArgs&, cudaStream_t);
 template cudaError_t configure_ifrk_kernels<float>(size_t);
 template cudaError_t configure_ifrk_kernels<double>(size_t);
+
+cudaError_t launch_spin_mode_table(float* table, const SpinorConst* consts, int nx, int ny,
+                                   int members, double kx_unit, double ky_unit, cudaStream_t stream) {
+  const long long plane = static_cast<long long>(nx) * ny;
+  const int blocks = static_cast<int>(std::min<long long>(1024, (plane + 255) / 256));
+  spin_mode_table_kernel<<<dim3(blocks, members), 256, 0, stream>>>(table, consts, nx, ny, kx_unit,
+                                                                     ky_unit);
+  return cudaGetLastError();
+}
 
 }  // namespace pg

@@ -28,7 +28,12 @@ struct IfrkRowArgs {
   double kx_unit, ky_unit;          // 2 pi / (n d) along x and y
   double inv_n;                     // 1 / (nx ny): normalisation of the inverse transforms
   const void* spin;                 // SpinorConst per member
+  // FP32 state: per-mode table (see kSpinModeFields) and each tau as a float pair
+  // tau_hi + tau_lo, so the phase angles are formed in compensated FP32 instead of FP64.
+  const float* modes;
+  float tau_hi[kIfrkMaxTerms], tau_lo[kIfrkMaxTerms];
 };
+
 
 // Per-member constants of the two-component Lawson factor (polarism/dispersion.py:34-83).
 struct SpinorConst {
@@ -37,6 +42,13 @@ struct SpinorConst {
   double beta;      // TE-TM coefficient
   double inv_hbar;
 };
+
+// Per-mode fields of the FP32 spinor table, [member][field][mode]: E(k)/hbar and w(k)/hbar as
+// float pairs (hi + lo of the FP64 value), Re u and Im u of u = beta (kx - i ky)^2, and 1 / w
+// (0 where w = 0).
+constexpr int kSpinModeFields = 7;
+cudaError_t launch_spin_mode_table(float* table, const SpinorConst* consts, int nx, int ny,
+                                   int members, double kx_unit, double ky_unit, cudaStream_t stream);
 
 // Column pass of one stage: F_y^-1 -> psi_i; n_i = n0 + sum coef_j dn_j; rhs_i; dn_i -> F_y.
 struct IfrkColArgs {
