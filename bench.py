@@ -178,9 +178,10 @@ def measured_peak():
 
 
 def profiled_traffic(members):
-    """DRAM bytes per launch of the RK4 kernel from the committed ncu summary, if any."""
+    """DRAM bytes per launch of the RK4 kernel from the committed ncu summary (profiled at
+    1024^2), if any."""
     path = ROOT / "profiles" / "rk4_stream_traffic.json"
-    if not path.exists():
+    if not path.exists() or NX != 1024:
         return None
     data = json.loads(path.read_text())
     per_site = data.get("dram_bytes_per_site")
@@ -225,7 +226,7 @@ def cpu_baseline(sample_steps=12):
     elapsed = _cpu_member_steps((0, sample_steps, "double"))
     return {"value": sample_steps * NX * NY / elapsed, "unit": "site-updates/s", "cores": 1,
             "kind": "port",
-            "sample": f"{sample_steps} RK4 steps of one 1024^2 member, FP64 NumPy oracle "
+            "sample": f"{sample_steps} RK4 steps of one {NX}^2 member, FP64 NumPy oracle "
                       "(restatement of the reference rk4-fdm + Wigner), 1 thread"}
 
 
@@ -253,9 +254,9 @@ def run_reference(args):
         "steps": budget_steps, "warmup": 1, "ms_per_step": 1e3 * elapsed / budget_steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"rk4 1024^2 x {args.members} members, Wigner on", "members": args.members},
+        "config": {"workload": f"rk4 {NX}^2 x {args.members} members, Wigner on", "members": args.members},
         "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": workers, "kind": "port",
-                         "sample": f"{budget_steps} RK4 steps of {args.members} members at 1024^2, "
+                         "sample": f"{budget_steps} RK4 steps of {args.members} members at {NX}^2, "
                                    f"FP64 NumPy oracle port, {workers} worker processes"},
         "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -328,7 +329,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "rk4-cuda fused step, 1024^2 periodic, lx=ly=400, dt=5e-4, "
+        "config": {"workload": f"rk4-cuda fused step, {NX}^2 periodic, lx=ly={LX:g}, dt=5e-4, "
                                "single reservoir, Wigner noise on, complex64",
                    "members": members, "global_members": members * world, "grid": [NY, NX],
                    "parallelism": f"replicas{world}",
@@ -471,13 +472,13 @@ def run_split_bench(args):
     if rank != 0:
         return
     line = {
-        "metric": f"split-step site-updates/s at 1024^2 ({ordering} ordering)", "value": value,
+        "metric": f"split-step site-updates/s at {NX}^2 ({ordering} ordering)", "value": value,
         "unit": "site-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": ("split-step-fft-cuda (K/2 [R/2 N R/2] K/2)" if code == 1 else
                                 "split-step-fft (R/2 K/2 N K/2 R/2)") +
-                               ", 1024^2 periodic, lx=ly=400, dt=5e-4, single reservoir, "
+                               f", {NX}^2 periodic, lx=ly={LX:g}, dt=5e-4, single reservoir, "
                                "Wigner noise on, complex64",
                    "members": members, "global_members": members * world, "grid": [NY, NX],
                    "parallelism": f"replicas{world}",
@@ -844,6 +845,9 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=8)
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=1024,
+                    help="rk4 / split workloads: grid size n (n^2 sites, lx = ly = 400 n / 1024, the same "
+                         "cell); members default to keep 32 x 1024^2 sites")
     ap.add_argument("--split-ordering", choices=["kouter", "cpu"], default="kouter",
                     help="split workload: K-outer (split-step-fft-cuda) or CPU ordering")
     ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno"], default="rk4",
@@ -869,6 +873,13 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.grid != 1024:
+        global NX, NY, LX, LY, METRIC
+        NX = NY = int(args.grid)
+        LX = LY = 400.0 * NX / 1024
+        METRIC = f"RK4 site-updates/s at {NX}^2"
+        if "--members" not in sys.argv:
+            args.members = max(1, 32 * 1024 * 1024 // (NX * NY))
     if args.workload == "split":
         run_split_bench(args)
         return
