@@ -197,6 +197,10 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
   __syncthreads();
 
   const unsigned long long noise_step = NOISE ? step_base[0] + step_offset : 0ull;
+  // Philox rounds that depend only on (step, stream, key), formed once for the block.
+  const PhiloxCellPrefix prefix =
+      philox_cell_prefix(static_cast<uint32_t>(noise_step), static_cast<uint32_t>(noise_step >> 32),
+                         1u, static_cast<uint32_t>(k.seed), static_cast<uint32_t>(k.seed >> 32));
 
   for (int i0 = 0; i0 < n_iter; i0 += 4) {
 #pragma unroll
@@ -222,6 +226,15 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
       }
       const C2* xin = xbuf + ((j + 1) & 1) * 4 * nthreads;
       T vre = T(0), vim = T(0);
+      // The Philox words of this iteration's output site, drawn in the straight-line code of
+      // the four stages so the integer work fills their issue gaps.
+      Words4 wz{0u, 0u, 0u, 0u};
+      if (NOISE) {
+        const uint32_t cell[1] = {static_cast<uint32_t>(static_cast<long long>(row_out) * nx + gx)};
+        Words4 w1[1];
+        philox_cells(cell, prefix, w1);
+        wz = w1[0];
+      }
 
       // Stage 1 at row r-1: k1 = f(psi0).
       {
@@ -327,8 +340,7 @@ __global__ void __launch_bounds__(MaxThreads<T>::value, 1)
         if (i >= 8 && i - 8 < h_eff && col_writes) {
           const long long o = static_cast<long long>(row_out) * nx + gx;
           if (NOISE) {
-            const Words4 w = wigner_words(static_cast<uint32_t>(o), noise_step, 1u, k.seed);
-            WignerDraw<T>::apply(w, k.noise_a + k.noise_b * on, ore, oim);
+            WignerDraw<T>::apply(wz, k.noise_a + k.noise_b * on, ore, oim);
           }
           psi_out[member * plane + o] = C2{ore, oim};
           if (!GENERAL || f.reservoir) n_out[member * plane + o] = on;
