@@ -29,6 +29,7 @@ struct GemmArgs {
   long long sA, sB, sC;       // outer batch strides
   int inner;                  // inner batch count: blockIdx.z = outer * inner + inner index
   long long sA2, sB2, sC2;    // inner batch strides
+  int vecA, vecB;             // operand rows start on 16-byte boundaries: stage 8 values at once
 };
 
 __device__ __forceinline__ void batch_offsets(const GemmArgs& g, long long& oa, long long& ob, long long& oc) {
@@ -198,6 +199,91 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
                : "memory");
 }
 
+// One K slab of an operand into the canonical K-major layout: ROWS rows (M or N) x 64 k.
+// kmajor: element (r, k) at X[r * ld + k], else at X[k * ld + r].  With vec, rows start on
+// 16-byte boundaries and eight consecutive values along the contiguous index load at once:
+// along k they are one 16-byte chunk of the layout, along r they go to eight chunks.
+template <int ROWS>
+__device__ __forceinline__ void stage_slab(__nv_bfloat16* S, const __nv_bfloat16* X, int ld, int kmajor,
+                                           int vec, int r0, int R, int k0, int K, int tid) {
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  if (vec) {
+    if (kmajor) {
+      for (int e = tid; e < ROWS * (kTcK / 8); e += 128) {
+        const int r = e >> 3, kv = (e & 7) * 8;
+        const int gr = r0 + r, gk = k0 + kv;
+        uint4 val = make_uint4(0u, 0u, 0u, 0u);
+        if (gr < R) {
+          const __nv_bfloat16* src = X + static_cast<long long>(gr) * ld + gk;
+          if (gk + 8 <= K) {
+            val = *reinterpret_cast<const uint4*>(src);
+          } else {
+            __nv_bfloat16 t[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) t[q] = gk + q < K ? src[q] : zero;
+            val = *reinterpret_cast<const uint4*>(t);
+          }
+        }
+        *reinterpret_cast<uint4*>(S + ((r >> 3) * 8 + (kv >> 3)) * 64 + (r & 7) * 8) = val;
+      }
+    } else {
+      // Eight k rows x eight contiguous r values per thread: eight 16-byte loads, a transpose
+      // in registers (byte permutes pairing the 16-bit halves of two k rows), eight 16-byte
+      // stores, one per r, each the k-contiguous row of a core matrix.
+      for (int blk = tid; blk < (ROWS / 8) * (kTcK / 8); blk += 128) {
+        const int rb = blk % (ROWS / 8), kb = blk / (ROWS / 8);
+        const int gr = r0 + rb * 8, gk0 = k0 + kb * 8;
+        uint32_t w[8][4];
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+          const int gk = gk0 + kk;
+          uint4 val = make_uint4(0u, 0u, 0u, 0u);
+          if (gk < K) {
+            const __nv_bfloat16* src = X + static_cast<long long>(gk) * ld + gr;
+            if (gr + 8 <= R) {
+              val = *reinterpret_cast<const uint4*>(src);
+            } else {
+              __nv_bfloat16 t[8];
+#pragma unroll
+              for (int q = 0; q < 8; ++q) t[q] = gr + q < R ? src[q] : zero;
+              val = *reinterpret_cast<const uint4*>(t);
+            }
+          }
+          w[kk][0] = val.x;
+          w[kk][1] = val.y;
+          w[kk][2] = val.z;
+          w[kk][3] = val.w;
+        }
+        __nv_bfloat16* dst = S + (rb * 8 + kb) * 64;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          uint4 lo, hi;  // r = 2j and 2j + 1: k pairs (2i, 2i + 1) in word i
+          lo.x = __byte_perm(w[0][j], w[1][j], 0x5410);
+          hi.x = __byte_perm(w[0][j], w[1][j], 0x7632);
+          lo.y = __byte_perm(w[2][j], w[3][j], 0x5410);
+          hi.y = __byte_perm(w[2][j], w[3][j], 0x7632);
+          lo.z = __byte_perm(w[4][j], w[5][j], 0x5410);
+          hi.z = __byte_perm(w[4][j], w[5][j], 0x7632);
+          lo.w = __byte_perm(w[6][j], w[7][j], 0x5410);
+          hi.w = __byte_perm(w[6][j], w[7][j], 0x7632);
+          *reinterpret_cast<uint4*>(dst + (2 * j) * 8) = lo;
+          *reinterpret_cast<uint4*>(dst + (2 * j + 1) * 8) = hi;
+        }
+      }
+    }
+    return;
+  }
+  for (int e = tid; e < ROWS * kTcK; e += 128) {
+    int r, k;
+    if (kmajor) { r = e / kTcK; k = e % kTcK; } else { k = e / ROWS; r = e % ROWS; }
+    const int gr = r0 + r, gk = k0 + k;
+    __nv_bfloat16 v = zero;
+    if (gr < R && gk < K)
+      v = kmajor ? X[static_cast<long long>(gr) * ld + gk] : X[static_cast<long long>(gk) * ld + gr];
+    S[((r >> 3) * 8 + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
+  }
+}
+
 __global__ void __launch_bounds__(128, 1) gemm_bf16_tc05_kernel(const GemmArgs g, int* err_flag) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(tc_smem);
@@ -211,7 +297,6 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16_tc05_kernel(const GemmArgs g
   float* C = g.C + oc;
   const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(taddr_slot)),
@@ -234,24 +319,8 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16_tc05_kernel(const GemmArgs g
   for (int k0 = 0; k0 < g.K; k0 += kTcK, ++slab) {
     // Stage the slabs in the canonical layout: element (r, k) of a [rows][64] slab lives at
     // ((r / 8) * 8 + k / 8) * 64 + (r % 8) * 8 + k % 8 (elements).
-    for (int e = tid; e < kTcM * kTcK; e += 128) {
-      int r, k;
-      if (!g.transA) { r = e / kTcK; k = e % kTcK; } else { k = e / kTcM; r = e % kTcM; }
-      const int gm = m0 + r, gk = k0 + k;
-      __nv_bfloat16 v = zero;
-      if (gm < g.M && gk < g.K)
-        v = g.transA ? A[static_cast<long long>(gk) * g.lda + gm] : A[static_cast<long long>(gm) * g.lda + gk];
-      As[((r >> 3) * 8 + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7)] = v;
-    }
-    for (int e = tid; e < kTcN * kTcK; e += 128) {
-      int n, k;
-      if (g.transB) { n = e / kTcK; k = e % kTcK; } else { k = e / kTcN; n = e % kTcN; }
-      const int gn = n0 + n, gk = k0 + k;
-      __nv_bfloat16 v = zero;
-      if (gn < g.N && gk < g.K)
-        v = g.transB ? B[static_cast<long long>(gn) * g.ldb + gk] : B[static_cast<long long>(gk) * g.ldb + gn];
-      Bs[((n >> 3) * 8 + (k >> 3)) * 64 + (n & 7) * 8 + (k & 7)] = v;
-    }
+    stage_slab<kTcM>(As, A, g.lda, !g.transA, g.vecA, m0, g.M, k0, g.K, tid);  // A is M x K unless transA
+    stage_slab<kTcN>(Bs, B, g.ldb, g.transB, g.vecB, n0, g.N, k0, g.K, tid);   // B is K x N unless transB
     // Make the generic-proxy stores visible to the tensor core's async proxy.
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -287,15 +356,30 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16_tc05_kernel(const GemmArgs g
         "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
       : "r"(lane_addr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-  const int row = m0 + tid;
-  if (ok && row < g.M && g.K > 0) {
-    float* dst = C + static_cast<long long>(row) * g.ldc;
+  // Write the tile through shared memory (the slab area; every MMA has completed) so each warp
+  // stores whole 128-byte row segments: 64 rows at a time, row stride 65 floats (no bank
+  // conflicts on either side).
+  float* stage = reinterpret_cast<float*>(tc_smem);
+#pragma unroll 1
+  for (int half = 0; half < 2; ++half) {
+    __syncthreads();
+    if ((warp >> 1) == half) {
+      const int r = tid - 64 * half;
 #pragma unroll
-    for (int j = 0; j < 64; ++j) {
-      const int c = n0 + j;
-      if (c < g.N) {
-        const float x = g.alpha * __uint_as_float(v[j]);
-        dst[c] = g.beta == 0.f ? x : x + g.beta * dst[c];
+      for (int j = 0; j < 64; ++j) stage[r * 65 + j] = __uint_as_float(v[j]);
+    }
+    __syncthreads();
+    const int c = n0 + (tid & 63);
+    if (ok && g.K > 0 && c < g.N) {
+#pragma unroll 4
+      for (int q = 0; q < 32; ++q) {
+        const int r = 2 * q + (tid >> 6);
+        const int row = m0 + 64 * half + r;
+        if (row < g.M) {
+          float* dst = C + static_cast<long long>(row) * g.ldc + c;
+          const float x = g.alpha * stage[r * 65 + (tid & 63)];
+          *dst = g.beta == 0.f ? x : x + g.beta * *dst;
+        }
       }
     }
   }
@@ -532,9 +616,14 @@ int pg_gemm_bf16_2d(const void* A, const void* B, float* C, int32_t M, int32_t N
            PG_ERR_INVALID, "pg_gemm_bf16: grid too large");
   if (M == 0 || N == 0) return PG_OK;
   batch *= inner;
+  // Vector staging needs every operand row (and batch slice) to start on a 16-byte boundary.
+  auto aligned = [](const void* p, long long ld, long long s1, long long s2) {
+    return (reinterpret_cast<uintptr_t>(p) & 15u) == 0 && ld % 8 == 0 && s1 % 8 == 0 && s2 % 8 == 0;
+  };
   pg::GemmArgs g{static_cast<const __nv_bfloat16*>(A), static_cast<const __nv_bfloat16*>(B), C, M, N, K,
                  lda, ldb, ldc, transA ? 1 : 0, transB ? 1 : 0, alpha, beta, strideA, strideB, strideC,
-                 inner, strideA2, strideB2, strideC2};
+                 inner, strideA2, strideB2, strideC2, aligned(A, lda, strideA, strideA2) ? 1 : 0,
+                 aligned(B, ldb, strideB, strideB2) ? 1 : 0};
   if (pg::g_gemm_engine == 0 && K > 0) {
     PG_CHECK((M + pg::kTcM - 1) / pg::kTcM <= 65535, PG_ERR_INVALID, "pg_gemm_bf16: grid too large");
     int* flag = nullptr;

@@ -38,7 +38,8 @@ def test_gemm_bf16_matches_numpy(cuda_lib, ta, tb, engine):
     lib = _lib.load()
     _lib.check(lib.pg_gemm_set_engine(engine), "pg_gemm_set_engine")
     rng = np.random.default_rng(ta * 2 + tb)
-    for M, N, K, batch in [(70, 45, 33, 3), (128, 64, 256, 1), (5, 130, 7, 2), (300, 200, 96, 1)]:
+    for M, N, K, batch in [(70, 45, 33, 3), (128, 64, 256, 1), (5, 130, 7, 2), (300, 200, 96, 1),
+                           (136, 72, 40, 2)]:
         a_shape = (batch, K, M) if ta else (batch, M, K)
         b_shape = (batch, N, K) if tb else (batch, K, N)
         a = _bf16_round(rng.standard_normal(a_shape))
