@@ -281,9 +281,25 @@ def run_ours(args):
 
     members = args.members
     w = workload(members, first=rank_members(rank, world, members)[0])
-    eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**PHYSICS), "single",
-                    pump_per_member=True)
+    from polarism_gb300 import _lib
+
+    pot_kind = {"none": _lib.PG_POT_NONE, "real": _lib.PG_POT_REAL,
+                "complex": _lib.PG_POT_COMPLEX}[args.potential]
+    physics = dict(PHYSICS, kinetic_relaxation_eta=args.eta)
+    eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**physics), "single",
+                    pump_per_member=True, potential=pot_kind)
     eng.set_pump(w["env"])
+    if args.potential != "none":
+        # A harmonic trap (real part) and an absorbing rim (imaginary part), shared by members.
+        x = (np.arange(NX) - (NX - 1) * 0.5) * w["dx"]
+        y = (np.arange(NY) - (NY - 1) * 0.5) * w["dy"]
+        r2 = x[None, :] ** 2 + y[:, None] ** 2
+        trap = 1e-4 * r2
+        if args.potential == "complex":
+            rim = -0.5 * np.clip(np.sqrt(r2) / (0.5 * LX) - 0.9, 0.0, None)
+            eng.set_potential((trap + 1j * rim).astype(np.complex64))
+        else:
+            eng.set_potential(trap.astype(np.float32))
     eng.set_noise(w["seeds"], PHYSICS["gamma_C"], PHYSICS["R"], 1.0, DT / (4 * w["dx"] * w["dy"]))
     eng.set_state(w["psi"], w["n"])
     stream = torch.cuda.ExternalStream(eng.stream)
@@ -315,12 +331,15 @@ def run_ours(args):
     sites = members * NX * NY
     value = world * sites * args.steps / (elapsed_ms / 1e3)
     kernel_s = elapsed_ms / 1e3 / args.steps
-    achieved = BYTES_PER_SITE * sites / kernel_s / 1e9
+    bytes_per_site = BYTES_PER_SITE + {"none": 0, "real": 4, "complex": 8}[args.potential]
+    achieved = bytes_per_site * sites / kernel_s / 1e9
     peak, peak_kind = measured_peak()
-    traffic = profiled_traffic(members)
+    traffic = profiled_traffic(members) if args.potential == "none" and args.eta == 0.0 else None
 
     # End to end through the public solver API on pinned host state.
     e2e = run_e2e(args, w, members, torch)
+    if args.potential != "none" or args.eta:
+        e2e["step"] += " (without the potential / relaxation: the host mirror's configs have none)"
     eng.close()
     if rank != 0:
         return
@@ -330,14 +349,16 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": f"rk4-cuda fused step, {NX}^2 periodic, lx=ly={LX:g}, dt=5e-4, "
-                               "single reservoir, Wigner noise on, complex64",
+                               "single reservoir, Wigner noise on, complex64" +
+                               (f", {args.potential} potential" if args.potential != "none" else "") +
+                               (f", kinetic relaxation eta={args.eta:g}" if args.eta else ""),
                    "members": members, "global_members": members * world, "grid": [NY, NX],
                    "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "algorithmic_bytes_per_site": BYTES_PER_SITE},
+                     "algorithmic_bytes_per_site": bytes_per_site},
         "e2e": e2e,
         "clocks": clocks,
     }
@@ -848,6 +869,10 @@ def main():
     ap.add_argument("--grid", type=int, default=1024,
                     help="rk4 / split workloads: grid size n (n^2 sites, lx = ly = 400 n / 1024, the same "
                          "cell); members default to keep 32 x 1024^2 sites")
+    ap.add_argument("--potential", choices=["none", "real", "complex"], default="none",
+                    help="rk4 workload: add a trap (and an absorbing rim) potential")
+    ap.add_argument("--eta", type=float, default=0.0,
+                    help="rk4 workload: kinetic relaxation eta (the general kernel variant)")
     ap.add_argument("--split-ordering", choices=["kouter", "cpu"], default="kouter",
                     help="split workload: K-outer (split-step-fft-cuda) or CPU ordering")
     ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno"], default="rk4",

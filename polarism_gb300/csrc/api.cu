@@ -172,8 +172,9 @@ pg::RK4Features features(const pg_solver* s) {
 
 bool use_wide(const pg_solver* s) {
   const pg::RK4Features f = features(s);
-  const bool eligible = s->cfg.precision == PG_SINGLE && f.potential == 0 && f.relax == 0 &&
-                        f.reservoir == 1 && f.pump_terms == 1 &&
+  // FP32, single reservoir and one laser; a potential or kinetic relaxation selects the
+  // full-width kernel's general variant.
+  const bool eligible = s->cfg.precision == PG_SINGLE && f.reservoir == 1 && f.pump_terms == 1 &&
                         pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny);
   if (s->rk4_kernel == 1) return false;
   return eligible;
@@ -191,6 +192,10 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
     w.blocks = s->wide_blocks;
     w.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
     w.halt = s->halt;
+    w.pot = static_cast<const float*>(s->potential);
+    w.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
+    w.pot_kind = f.potential;
+    w.relax = f.relax;
     return pg::launch_rk4_wide(static_cast<const float*>(s->psi[from]),
                                static_cast<const float*>(s->res[from]),
                                static_cast<const float*>(s->pump), static_cast<float*>(s->psi[to]),
@@ -457,11 +462,11 @@ int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
   PG_CHECK(kind >= 0 && kind <= 2, PG_ERR_INVALID, "pg_rk4_set_kernel: kind must be 0, 1 or 2");
   if (kind == 2) {
     const pg::RK4Features f = features(s);
-    PG_CHECK(s->cfg.precision == PG_SINGLE && f.potential == 0 && f.relax == 0 &&
-                 f.reservoir == 1 && pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny),
+    PG_CHECK(s->cfg.precision == PG_SINGLE && f.reservoir == 1 && f.pump_terms == 1 &&
+                 pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny),
              PG_ERR_UNSUPPORTED,
-             "pg_rk4_set_kernel: the full-width kernel needs FP32, a single reservoir, no "
-             "potential or relaxation term, and nx in {128, 256, 512, 1024}");
+             "pg_rk4_set_kernel: the full-width kernel needs FP32, a single reservoir, one laser "
+             "and nx in {128, 256, 512, 1024}");
   }
   s->rk4_kernel = kind;
   free_graphs(s);

@@ -17,6 +17,7 @@ struct Pair {
 struct WideConst {
   float2 nax, nay;      // (-ax, -ax), (-ay, -ay)
   float w0, gc, gr, half_R, half_gC, R, gamma_R, noise_a, noise_b;
+  float inv_hbar, eta;  // potential scale and kinetic relaxation (general variant)
   uint64_t seed;
 };
 
@@ -33,6 +34,8 @@ __device__ __forceinline__ WideConst wide_const(const RhsConst<float>& kk) {
   k.gamma_R = kk.gamma_R;
   k.noise_a = kk.noise_a;
   k.noise_b = kk.noise_b;
+  k.inv_hbar = kk.inv_hbar;
+  k.eta = kk.eta_a;
   k.seed = kk.seed;
   return k;
 }
@@ -50,6 +53,30 @@ __device__ __forceinline__ float site_rhs(float2 c, float2 lt, float2 rt, float2
   const float2 u = __ffma2_rn(make_float2(w, w), c, nl);  // w c - a lap_neighbours
   d.x = fmaf(gl, c.x, u.y);
   d.y = fmaf(gl, c.y, -u.x);
+  return fmaf(-fmaf(k.R, rho, k.gamma_R), n, sP);
+}
+
+// site_rhs with a potential V = vre + i vim (polarism/model.py:89-127: -i V psi / hbar) and,
+// when relax, the kinetic-relaxation term + eta n_A (hbar / 2m) Laplacian psi of the general
+// right-hand side; the Laplacian with its centre weight is -(w0 c + nl).
+__device__ __forceinline__ float site_rhs_general(float2 c, float2 lt, float2 rt, float2 up,
+                                                  float2 dn, float n, float sP, const WideConst& k,
+                                                  float vre, float vim, bool relax, float2& d) {
+  const float2 sx = __fadd2_rn(lt, rt);
+  const float2 sy = __fadd2_rn(up, dn);
+  const float2 nl = __ffma2_rn(k.nay, sy, __fmul2_rn(k.nax, sx));
+  const float rho = fmaf(c.x, c.x, c.y * c.y);
+  const float w = fmaf(vre, k.inv_hbar, fmaf(k.gr, n, fmaf(k.gc, rho, k.w0)));
+  const float gl = fmaf(vim, k.inv_hbar, fmaf(k.half_R, n, -k.half_gC));
+  const float2 u = __ffma2_rn(make_float2(w, w), c, nl);
+  d.x = fmaf(gl, c.x, u.y);
+  d.y = fmaf(gl, c.y, -u.x);
+  if (relax) {
+    const float en = k.eta * n;
+    const float2 t = __ffma2_rn(make_float2(k.w0, k.w0), c, nl);
+    d.x = fmaf(-en, t.x, d.x);
+    d.y = fmaf(-en, t.y, d.y);
+  }
   return fmaf(-fmaf(k.R, rho, k.gamma_R), n, sP);
 }
 

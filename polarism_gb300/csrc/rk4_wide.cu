@@ -30,7 +30,7 @@ constexpr int kRing = 8;          // rows resident: r-4..r plus three in flight
 constexpr int kWaitLimit = 100000;
 
 // At least 512 resident threads per SM for every row width (128 registers a thread).
-template <int NX, bool NOISE>
+template <int NX, bool NOISE, bool GENERAL>
 __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
     rk4_wide_kernel(const float2* __restrict__ psi_in, const float* __restrict__ n_in,
                     const float* __restrict__ pump, float2* __restrict__ psi_out,
@@ -98,6 +98,30 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
     const float2* psi_m = psi_in + member * plane;
     const float* n_m = n_in + member * plane;
     const float* p_m = pump + member * g.pump_stride;
+    const float* pot_m = GENERAL && g.pot_kind != 0
+                             ? g.pot + member * g.pot_stride * (g.pot_kind == 2 ? 2 : 1)
+                             : nullptr;
+    // General variant: the potential of the thread's two sites on `row` as (Re, Im) pairs.
+    auto pot_at = [&](int row, float2& va, float2& vb) {
+      va = vb = make_float2(0.f, 0.f);
+      if (GENERAL && pot_m != nullptr) {
+        const long long o = static_cast<long long>(row) * NX + col0;
+        if (g.pot_kind == 2) {
+          const float4 v = *reinterpret_cast<const float4*>(pot_m + 2 * o);
+          va = make_float2(v.x, v.y);
+          vb = make_float2(v.z, v.w);
+        } else {
+          const float2 v = *reinterpret_cast<const float2*>(pot_m + o);
+          va.x = v.x;
+          vb.x = v.y;
+        }
+      }
+    };
+    auto rhs = [&](float2 c, float2 lt, float2 rt, float2 up, float2 dn, float n, float sP,
+                   float2 v, float2& d) -> float {
+      if (GENERAL) return site_rhs_general(c, lt, rt, up, dn, n, sP, k, v.x, v.y, g.relax != 0, d);
+      return site_rhs(c, lt, rt, up, dn, n, sP, k, d);
+    };
     float2* out_psi_m = psi_out + member * plane + col0;
     float* out_n_m = n_out + member * plane + col0;
     int row_first = (ya - 4) % ny;
@@ -165,10 +189,18 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
         const float2 dn0 = make_float2(d4.x, d4.y), dn1 = make_float2(d4.z, d4.w);
         const float2 n1v = *reinterpret_cast<const float2*>(ring_n + slot1 * NX + col0);
         const float2 P1 = *reinterpret_cast<const float2*>(ring_p + slot1 * NX + col0);
+        // Rows of the four stages (general variant only: the potential is read per stage).
+        int srow[4] = {0, 0, 0, 0};
+        if (GENERAL) {
+          srow[3] = row_out;
+#pragma unroll
+          for (int q = 2; q >= 0; --q) srow[q] = srow[q + 1] + 1 == ny ? 0 : srow[q + 1] + 1;
+        }
         {
-          float2 da, db;
-          const float dna = site_rhs(c0, lt, c1, up0, dn0, n1v.x, __fmul_rn(s0, P1.x), k, da);
-          const float dnb = site_rhs(c1, c0, rt, up1, dn1, n1v.y, __fmul_rn(s0, P1.y), k, db);
+          float2 da, db, va, vb;
+          pot_at(srow[0], va, vb);
+          const float dna = rhs(c0, lt, c1, up0, dn0, n1v.x, __fmul_rn(s0, P1.x), va, da);
+          const float dnb = rhs(c1, c0, rt, up1, dn1, n1v.y, __fmul_rn(s0, P1.y), vb, db);
           q1[ja] = Pair{axpy2(hh, da, c0), axpy2(hh, db, c1)};
           acc[ja] = Pair{axpy2(h6, da, c0), axpy2(h6, db, c1)};
           m1[ja] = make_float2(fmaf(hh, dna, n1v.x), fmaf(hh, dnb, n1v.y));
@@ -191,11 +223,12 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
           const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * NX + col0);
           const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * NX + col0);
           const Pair c = q1[jb];
-          float2 da, db;
-          const float dna = site_rhs(c.a, lt2, c.b, q1[jc].a, q1[ja].a, m1[jb].x,
-                                     __fmul_rn(s1, P2.x), k, da);
-          const float dnb = site_rhs(c.b, c.a, rt2, q1[jc].b, q1[ja].b, m1[jb].y,
-                                     __fmul_rn(s1, P2.y), k, db);
+          float2 da, db, va, vb;
+          pot_at(srow[1], va, vb);
+          const float dna = rhs(c.a, lt2, c.b, q1[jc].a, q1[ja].a, m1[jb].x,
+                                __fmul_rn(s1, P2.x), va, da);
+          const float dnb = rhs(c.b, c.a, rt2, q1[jc].b, q1[ja].b, m1[jb].y,
+                                __fmul_rn(s1, P2.y), vb, db);
           q2[jb] = Pair{axpy2(hh, da, up0), axpy2(hh, db, up1)};  // psi0 at row r-2
           m2[jb] = make_float2(fmaf(hh, dna, n0.x), fmaf(hh, dnb, n0.y));
           acc[jb] = Pair{axpy2(h3, da, acc[jb].a), axpy2(h3, db, acc[jb].b)};
@@ -209,11 +242,12 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
           const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * NX + col0);
           const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * NX + col0);
           const Pair c = q2[jc];
-          float2 da, db;
-          const float dna = site_rhs(c.a, lt3, c.b, q2[jd].a, q2[jb].a, m2[jc].x,
-                                     __fmul_rn(s1, P3.x), k, da);
-          const float dnb = site_rhs(c.b, c.a, rt3, q2[jd].b, q2[jb].b, m2[jc].y,
-                                     __fmul_rn(s1, P3.y), k, db);
+          float2 da, db, va, vb;
+          pot_at(srow[2], va, vb);
+          const float dna = rhs(c.a, lt3, c.b, q2[jd].a, q2[jb].a, m2[jc].x,
+                                __fmul_rn(s1, P3.x), va, da);
+          const float dnb = rhs(c.b, c.a, rt3, q2[jd].b, q2[jb].b, m2[jc].y,
+                                __fmul_rn(s1, P3.y), vb, db);
           q3[jc] = Pair{axpy2(dt, da, make_float2(p4.x, p4.y)), axpy2(dt, db, make_float2(p4.z, p4.w))};
           m3[jc] = make_float2(fmaf(dt, dna, n0.x), fmaf(dt, dnb, n0.y));
           acc[jc] = Pair{axpy2(h3, da, acc[jc].a), axpy2(h3, db, acc[jc].b)};
@@ -225,11 +259,12 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
           const float2 lt4 = make_float2(L.z, L.w), rt4 = make_float2(Rr.x, Rr.y);
           const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * NX + col0);
           const Pair c = q3[jd];
-          float2 da, db;
-          const float dna = site_rhs(c.a, lt4, c.b, q3[ja].a, q3[jc].a, m3[jd].x,
-                                     __fmul_rn(s2, P4.x), k, da);
-          const float dnb = site_rhs(c.b, c.a, rt4, q3[ja].b, q3[jc].b, m3[jd].y,
-                                     __fmul_rn(s2, P4.y), k, db);
+          float2 da, db, va, vb;
+          pot_at(srow[3], va, vb);
+          const float dna = rhs(c.a, lt4, c.b, q3[ja].a, q3[jc].a, m3[jd].x,
+                                __fmul_rn(s2, P4.x), va, da);
+          const float dnb = rhs(c.b, c.a, rt4, q3[ja].b, q3[jc].b, m3[jd].y,
+                                __fmul_rn(s2, P4.y), vb, db);
           float2 oa = axpy2(h6, da, acc[jd].a);
           float2 ob = axpy2(h6, db, acc[jd].b);
           float na = fmaf(h6, dna, accn[jd].x);
@@ -283,22 +318,28 @@ namespace {
 
 template <int NX>
 cudaError_t configure_nx() {
-  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(wide_rk4_smem(NX)));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(rk4_wide_kernel<NX, false>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(wide_rk4_smem(NX)));
+  const int smem = static_cast<int>(wide_rk4_smem(NX));
+  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
 }
 
 template <int NX>
 int blocks_nx(bool noise) {
   int blocks = 0;
   cudaError_t e = noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &blocks, rk4_wide_kernel<NX, true>, NX / 2, wide_rk4_smem(NX))
+                              &blocks, rk4_wide_kernel<NX, true, false>, NX / 2, wide_rk4_smem(NX))
                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &blocks, rk4_wide_kernel<NX, false>, NX / 2, wide_rk4_smem(NX));
+                              &blocks, rk4_wide_kernel<NX, false, false>, NX / 2, wide_rk4_smem(NX));
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -312,14 +353,21 @@ cudaError_t launch_nx(const float* psi_in, const float* n_in, const float* pump,
                       const unsigned long long* step_base, int step_offset, float dt, bool noise,
                       const WideGeom& g, int* err_flag, cudaStream_t stream) {
   const size_t smem = wide_rk4_smem(NX);
-  if (noise) {
-    rk4_wide_kernel<NX, true><<<g.blocks, NX / 2, smem, stream>>>(
-        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
-        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  const float2* pin = reinterpret_cast<const float2*>(psi_in);
+  float2* pout = reinterpret_cast<float2*>(psi_out);
+  const bool general = wide_general(g);
+  if (noise && general) {
+    rk4_wide_kernel<NX, true, true><<<g.blocks, NX / 2, smem, stream>>>(
+        pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  } else if (noise) {
+    rk4_wide_kernel<NX, true, false><<<g.blocks, NX / 2, smem, stream>>>(
+        pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  } else if (general) {
+    rk4_wide_kernel<NX, false, true><<<g.blocks, NX / 2, smem, stream>>>(
+        pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
   } else {
-    rk4_wide_kernel<NX, false><<<g.blocks, NX / 2, smem, stream>>>(
-        reinterpret_cast<const float2*>(psi_in), n_in, pump, reinterpret_cast<float2*>(psi_out),
-        n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+    rk4_wide_kernel<NX, false, false><<<g.blocks, NX / 2, smem, stream>>>(
+        pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
   }
   return cudaGetLastError();
 }

@@ -11,6 +11,12 @@ struct WideGeom {
   int blocks;              // persistent grid size
   long long pump_stride;   // 0: shared envelope; nx*ny: one per member
   const int* halt = nullptr;  // when non-null and set, the launch returns at once
+  // General variant: potential (0 none, 1 real, 2 complex; shared or per member) and the
+  // kinetic-relaxation term.
+  const float* pot = nullptr;
+  long long pot_stride = 0;
+  int pot_kind = 0;
+  int relax = 0;
 };
 
 bool wide_rk4_supported(int nx, int ny);
@@ -22,5 +28,7 @@ cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float*
                             const float* scales, const unsigned long long* step_base,
                             int step_offset, float dt, bool noise, const WideGeom& g,
                             int* err_flag, cudaStream_t stream);
+// The general variant runs when the geometry asks for a potential or kinetic relaxation.
+inline bool wide_general(const WideGeom& g) { return g.pot_kind != 0 || g.relax != 0; }
 
 }  // namespace pg

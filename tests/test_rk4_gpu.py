@@ -293,3 +293,49 @@ def test_device_normals_within_error_bound(cuda_lib, precision):
     assert np.all(np.abs(got[0] - re) <= bound)
     assert np.all(np.abs(got[1] - im) <= bound)
     assert rel_l2(got[0], re) < 1e-6 and rel_l2(got[1], im) < 1e-6
+
+
+@pytest.mark.parametrize("pot_kind,per_member", [("complex", True), ("real", False), ("none", False)])
+@pytest.mark.parametrize("nx,ny,members", [(256, 24, 2), (1024, 12, 1)])
+def test_full_width_general_variant_matches_oracle_and_tiled(cuda_lib, pot_kind, per_member, nx, ny,
+                                                             members):
+    """The full-width kernel's general variant (potential and kinetic relaxation, Wigner noise
+    on): within 1e-4 of the FP64 oracle on the same noise and 1e-5 of the tiled kernel."""
+    from polarism_gb300 import _lib
+    from polarism_gb300.engine import MemberPhysics, RK4Engine
+
+    rng = np.random.default_rng(nx + members)
+    p = dict(hbar=0.6582119514, m_eff=0.284, g_C=0.003, g_R=0.002, g_I=0.0, R=0.02,
+             gamma_C=0.083, gamma_R=0.005, kinetic_relaxation_eta=0.05)
+    dx, dy, dt = 0.5, 0.6, 1e-3
+    psi0 = 0.1 * (rng.standard_normal((members, 1, ny, nx)) + 1j * rng.standard_normal((members, 1, ny, nx)))
+    res0 = np.abs(rng.standard_normal((members, 1, ny, nx))) * 0.05
+    env = np.abs(rng.standard_normal((members, 1, ny, nx)))
+    shape = (members, 1, ny, nx) if per_member else (ny, nx)
+    kind = {"complex": _lib.PG_POT_COMPLEX, "real": _lib.PG_POT_REAL, "none": _lib.PG_POT_NONE}[pot_kind]
+    pot = 0.02 * rng.standard_normal(shape)
+    if pot_kind == "complex":
+        pot = pot - 0.003j * np.abs(rng.standard_normal(shape))
+    seeds = [9 + m for m in range(members)]
+    steps = 6
+    outs = {}
+    for kernel in (2, 1):
+        eng = RK4Engine(nx, ny, members, dx, dy, dt, MemberPhysics(**p), "single", pump_per_member=True,
+                        potential=kind, potential_per_member=per_member)
+        eng.set_kernel(kernel)
+        assert eng.kernel() == kernel
+        eng.set_pump(env.astype(np.float32))
+        if pot_kind != "none":
+            eng.set_potential(pot.astype(np.complex64 if pot_kind == "complex" else np.float32))
+        eng.set_noise(seeds, p["gamma_C"], p["R"], 1.0, dt / (4 * dx * dy))
+        eng.set_state(psi0.astype(np.complex64), res0.astype(np.float32))
+        eng.advance(0, steps, np.full((steps, 3, members), 0.05))
+        outs[kernel] = eng.get_state()
+        eng.close()
+    noise = gpe.Noise(seeds, [p["gamma_C"]] * members, [p["R"]] * members, [1.0] * members, dt,
+                      dx * dy, "double", normals_precision="single")
+    psi_o, f_o = gpe.rk4_advance(psi0.copy(), (res0.copy(),), lambda t: env * 0.05,
+                                 0.0 if pot_kind == "none" else pot, p, dx, dy, dt, 0, steps, noise=noise)
+    (psi_w, res_w), (psi_t, res_t) = outs[2], outs[1]
+    assert rel_l2(psi_w, psi_o) < 1e-4 and rel_l2(res_w, f_o[0]) < 1e-4
+    assert rel_l2(psi_w, psi_t) < 1e-5 and rel_l2(res_w, res_t) < 1e-5
