@@ -299,6 +299,12 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
     const T* pm = pump + member * a.pump_stride;
     const T* vm = potential ? potential + member * a.pot_stride * (a.potential == 2 ? 2 : 1) : nullptr;
     const unsigned long long step = a.noise ? step_base[0] + a.step_offset : 0ull;
+    // Philox rounds that depend only on (step, stream, key), per component stream 1 + comp.
+    const PhiloxCellPrefix prefix[2] = {
+        philox_cell_prefix(static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32), 1u,
+                           static_cast<uint32_t>(k.seed), static_cast<uint32_t>(k.seed >> 32)),
+        philox_cell_prefix(static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32), 2u,
+                           static_cast<uint32_t>(k.seed), static_cast<uint32_t>(k.seed >> 32))};
     const int F = a.res_fields, Cr = a.res_comps;
     const int NQ = F * Cr;
     const long long qstride = static_cast<long long>(Cr) * plane;      // reservoir member stride
@@ -389,7 +395,10 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
           C2 w = v[comp];
           if (a.noise) {
             const T nA = F >= 1 ? nval[Cr == comps ? comp : 0] : T(0);
-            const Words4 words = wigner_words(static_cast<uint32_t>(o), step, 1u + comp, k.seed);
+            const uint32_t cell[1] = {static_cast<uint32_t>(o)};
+            Words4 w1[1];
+            philox_cells(cell, prefix[comp], w1);
+            const Words4 words = w1[0];
             WignerDraw<T>::apply(words, k.noise_a + k.noise_b * nA, w.x, w.y);
             buf[i * CC + comp * C + c] = w;
           }
