@@ -203,13 +203,25 @@ def profiled_sweep_traffic(tiling, sites):
 
 
 # ----------------------------------------------------------------------------- CPU legs
+_CPU_WORK = {}
+
+
 def _cpu_member_steps(args):
-    """Worker: FP64 oracle RK4 steps on one member (used by the CPU legs)."""
-    member, steps, precision = args
+    """Worker: FP64 oracle RK4 steps on one member (used by the CPU legs).  Returns the time of
+    the steps alone; the inputs (member 0's field and envelope; the member's own noise seed) are
+    built once per worker process, so the timed region holds the stepping only."""
+    member, steps, precision, n = args
+    global NX, NY, LX, LY
+    if NX != n:
+        NX = NY = n
+        LX = LY = 400.0 * n / 1024
+        _CPU_WORK.clear()
     sys.path.insert(0, str(ROOT))
     from oracle import gpe
 
-    w = workload(1, "double")
+    if "w" not in _CPU_WORK:
+        _CPU_WORK["w"] = workload(1, "double")
+    w = _CPU_WORK["w"]
     p = dict(PHYSICS)
     env = w["env"][0, 0].astype(np.float64) * P0
     psi, fields = w["psi"].astype(np.complex128), (w["n"].astype(np.float64),)
@@ -222,8 +234,8 @@ def _cpu_member_steps(args):
 
 def cpu_baseline(sample_steps=12):
     """Oracle port, one core, a bounded sample (sample_steps RK4 steps of one 1024^2 member)."""
-    _cpu_member_steps((0, 1, "double"))  # warm-up
-    elapsed = _cpu_member_steps((0, sample_steps, "double"))
+    _cpu_member_steps((0, 1, "double", NX))  # warm-up
+    elapsed = _cpu_member_steps((0, sample_steps, "double", NX))
     return {"value": sample_steps * NX * NY / elapsed, "unit": "site-updates/s", "cores": 1,
             "kind": "port",
             "sample": f"{sample_steps} RK4 steps of one {NX}^2 member, FP64 NumPy oracle "
@@ -241,12 +253,15 @@ def run_reference(args):
     workers = max(1, min(args.members, cores))
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
-        pool.map(_cpu_member_steps, [(m, 1, "double") for m in range(workers)])  # warm-up
+        # Warm-up: every worker builds its inputs and runs one step.
+        tasks = [(m, 1, "double", NX) for m in range(args.members)]
+        chunk = max(1, args.members // workers)
+        pool.map(_cpu_member_steps, [(m, 1, "double", NX) for m in range(workers)], chunksize=1)
         # Each timed step: one RK4 step of every member, members spread over the workers.
         budget_steps = max(1, min(args.steps, 3))
         t0 = time.perf_counter()
         for _ in range(budget_steps):
-            pool.map(_cpu_member_steps, [(m, 1, "double") for m in range(args.members)])
+            pool.map(_cpu_member_steps, tasks, chunksize=chunk)
         elapsed = time.perf_counter() - t0
     value = budget_steps * args.members * NX * NY / elapsed
     line = {
