@@ -303,6 +303,10 @@ def run_ours(args):
     physics = dict(PHYSICS, kinetic_relaxation_eta=args.eta)
     eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**physics), "single",
                     pump_per_member=True, potential=pot_kind)
+    if args.rk4_kernel != "auto":
+        eng.set_kernel(2 if args.rk4_kernel == "wide" else 1)
+    kernel_name = ("tiled" if eng.kernel() == 1 else
+                   "full-width" if NX <= 1024 else "full-width, 1024-site bands")
     eng.set_pump(w["env"])
     if args.potential != "none":
         # A harmonic trap (real part) and an absorbing rim (imaginary part), shared by members.
@@ -368,7 +372,7 @@ def run_ours(args):
                                (f", {args.potential} potential" if args.potential != "none" else "") +
                                (f", kinetic relaxation eta={args.eta:g}" if args.eta else ""),
                    "members": members, "global_members": members * world, "grid": [NY, NX],
-                   "parallelism": f"replicas{world}",
+                   "parallelism": f"replicas{world}", "kernel": kernel_name,
                    "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -888,6 +892,9 @@ def main():
                     help="rk4 workload: add a trap (and an absorbing rim) potential")
     ap.add_argument("--eta", type=float, default=0.0,
                     help="rk4 workload: kinetic relaxation eta (the general kernel variant)")
+    ap.add_argument("--rk4-kernel", choices=["auto", "wide", "tiled"], default="auto",
+                    help="rk4 workload: the full-width TMA kernel, the tiled kernel, or the "
+                         "engine's choice")
     ap.add_argument("--split-ordering", choices=["kouter", "cpu"], default="kouter",
                     help="split workload: K-outer (split-step-fft-cuda) or CPU ordering")
     ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno"], default="rk4",

@@ -30,37 +30,55 @@ constexpr int kRing = 8;          // rows resident: r-4..r plus three in flight
 constexpr int kWaitLimit = 100000;
 
 // At least 512 resident threads per SM for every row width (128 registers a thread).
-template <int NX, bool NOISE, bool GENERAL>
-__global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
+// Threads of a block: two sites each over the shared-memory row (BAND: a 1024-column band of a
+// wider row plus four halo columns on each side, rounded up to whole warps).
+template <int NX, bool BAND>
+struct WideShape {
+  static constexpr int W = BAND ? NX + 8 : NX;  // sites per shared-memory row
+  static constexpr int ACTIVE = W / 2;          // threads that own two sites
+  static constexpr int THREADS = BAND ? ((ACTIVE + 31) / 32) * 32 : NX / 2;
+};
+
+template <int NX, bool NOISE, bool GENERAL, bool BAND>
+__global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 : 1024 / NX))
     rk4_wide_kernel(const float2* __restrict__ psi_in, const float* __restrict__ n_in,
                     const float* __restrict__ pump, float2* __restrict__ psi_out,
                     float* __restrict__ n_out, const RhsConst<float>* __restrict__ consts,
                     const float* __restrict__ scales,
                     const unsigned long long* __restrict__ step_base, const int step_offset,
                     const float dt, const WideGeom g, int* __restrict__ err_flag) {
-  constexpr int HALF = NX / 2;
+  constexpr int W = WideShape<NX, BAND>::W;
+  constexpr int ACTIVE = WideShape<NX, BAND>::ACTIVE;
+  constexpr int HALF = WideShape<NX, BAND>::THREADS;  // exchange-buffer stride (every thread)
   // One block per SM (1024-site rows): a split arrive/wait barrier lets its warps drift
   // apart by up to a row, which measured faster; with several blocks per SM the blocks
   // already interleave and a block-wide barrier is cheaper.
   constexpr bool kSplit = NX >= 1024;
   if (g.halt != nullptr && __ldcg(g.halt) != 0) return;  // steady-state monitor halted the run
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][NX]
-  float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * NX); // [kRing][NX]
-  float* ring_p = ring_n + kRing * NX;                             // [kRing][NX]
-  float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * NX);   // [2][3][HALF]
+  float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][W]
+  float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * W);  // [kRing][W]
+  float* ring_p = ring_n + kRing * W;                              // [kRing][W]
+  float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * W);    // [2][3][HALF]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kRing] + exchange barrier
   const uint32_t xbar = smem_u32(&mbar[kRing]);
 
   const int ny = g.ny;
   const int t = threadIdx.x;
-  const int col0 = 2 * t;
-  const int lcol = col0 == 0 ? NX - 1 : col0 - 1;   // left neighbour of column 2t
-  const int rcol = col0 + 2 == NX ? 0 : col0 + 2;   // right neighbour of column 2t+1
-  const int lthr = t == 0 ? HALF - 1 : t - 1;       // thread owning lcol
-  const int rthr = t + 1 == HALF ? 0 : t + 1;       // thread owning rcol
-  const long long plane = static_cast<long long>(NX) * ny;
-  constexpr uint32_t kRowBytes = NX * 16u;
+  // BAND: threads past the band's sites repeat the last active thread's work and write
+  // nothing; the halo columns have no left / right neighbour in the band (their results are
+  // not written either).
+  const int tc = BAND ? min(t, ACTIVE - 1) : t;
+  const bool owner = !BAND || t < ACTIVE;
+  const int col0 = 2 * tc;
+  const int lcol = BAND ? (col0 == 0 ? 0 : col0 - 1) : (col0 == 0 ? NX - 1 : col0 - 1);
+  const int rcol = BAND ? (col0 + 2 >= W ? col0 + 1 : col0 + 2) : (col0 + 2 == NX ? 0 : col0 + 2);
+  const int lthr = BAND ? max(tc - 1, 0) : (t == 0 ? HALF - 1 : t - 1);          // owns lcol
+  const int rthr = BAND ? min(tc + 1, ACTIVE - 1) : (t + 1 == HALF ? 0 : t + 1);  // owns rcol
+  const int gnx = BAND ? g.nx : NX;       // sites per grid row
+  const int bands = BAND ? g.nx / NX : 1;
+  const long long plane = static_cast<long long>(gnx) * ny;
+  constexpr uint32_t kRowBytes = W * 16u;
 
   if (t == 0) {
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
@@ -69,7 +87,7 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
   }
   __syncthreads();
 
-  const long long total_rows = static_cast<long long>(g.members) * ny;
+  const long long total_rows = static_cast<long long>(g.members) * bands * ny;
   const long long r_begin = total_rows * blockIdx.x / gridDim.x;
   const long long r_end = total_rows * (blockIdx.x + 1) / gridDim.x;
   const float hh = 0.5f * dt, h6 = dt / 6.0f, h3 = dt / 3.0f;
@@ -78,8 +96,11 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
 
   long long gr = r_begin;
   while (gr < r_end) {
-    const int member = static_cast<int>(gr / ny);
-    const int ya = static_cast<int>(gr - static_cast<long long>(member) * ny);
+    // Row space [member][band][row]; a segment stays within one (member, band).
+    const long long unit = gr / ny;
+    const int member = static_cast<int>(unit / bands);
+    const int band = static_cast<int>(unit % bands);
+    const int ya = static_cast<int>(gr - unit * ny);
     const int yb = static_cast<int>(min(static_cast<long long>(ny), ya + (r_end - gr)));
     gr += yb - ya;
     const int h_rows = yb - ya;
@@ -95,6 +116,12 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
     const PhiloxCellPrefix prefix =
         philox_cell_prefix(static_cast<uint32_t>(noise_step), static_cast<uint32_t>(noise_step >> 32),
                            1u, key0, key1);
+    // Grid column of shared-memory column c: the band starts four columns left of its first
+    // written column.
+    const int gc0 = BAND ? band * NX - 4 : 0;
+    const int gcol0 = gc0 + col0;                                    // may lie outside [0, gnx)
+    const int gcol0w = gcol0 < 0 ? gcol0 + gnx : (gcol0 >= gnx ? gcol0 - gnx : gcol0);
+    const bool writes = owner && (!BAND || (col0 >= 4 && col0 < 4 + NX));
     const float2* psi_m = psi_in + member * plane;
     const float* n_m = n_in + member * plane;
     const float* p_m = pump + member * g.pump_stride;
@@ -105,7 +132,7 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
     auto pot_at = [&](int row, float2& va, float2& vb) {
       va = vb = make_float2(0.f, 0.f);
       if (GENERAL && pot_m != nullptr) {
-        const long long o = static_cast<long long>(row) * NX + col0;
+        const long long o = static_cast<long long>(row) * gnx + gcol0w;
         if (g.pot_kind == 2) {
           const float4 v = *reinterpret_cast<const float4*>(pot_m + 2 * o);
           va = make_float2(v.x, v.y);
@@ -122,8 +149,8 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
       if (GENERAL) return site_rhs_general(c, lt, rt, up, dn, n, sP, k, v.x, v.y, g.relax != 0, d);
       return site_rhs(c, lt, rt, up, dn, n, sP, k, d);
     };
-    float2* out_psi_m = psi_out + member * plane + col0;
-    float* out_n_m = n_out + member * plane + col0;
+    float2* out_psi_m = psi_out + member * plane + gcol0w;
+    float* out_n_m = n_out + member * plane + gcol0w;
     int row_first = (ya - 4) % ny;
     if (row_first < 0) row_first += ny;
 
@@ -134,9 +161,26 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
       while (row >= ny) row -= ny;
       const uint32_t bar = smem_u32(&mbar[slot]);
       mbar_arrive_expect_tx(bar, kRowBytes);
-      bulk_g2s(smem_u32(ring_psi + slot * NX), psi_m + static_cast<long long>(row) * NX, NX * 8u, bar);
-      bulk_g2s(smem_u32(ring_n + slot * NX), n_m + static_cast<long long>(row) * NX, NX * 4u, bar);
-      bulk_g2s(smem_u32(ring_p + slot * NX), p_m + static_cast<long long>(row) * NX, NX * 4u, bar);
+      const long long ro = static_cast<long long>(row) * gnx;
+      if (!BAND) {
+        bulk_g2s(smem_u32(ring_psi + slot * W), psi_m + ro, NX * 8u, bar);
+        bulk_g2s(smem_u32(ring_n + slot * W), n_m + ro, NX * 4u, bar);
+        bulk_g2s(smem_u32(ring_p + slot * W), p_m + ro, NX * 4u, bar);
+      } else {
+        // Columns [gc0, gc0 + W) of the periodic row: one copy, or two where the band wraps
+        // (the first band starts at gnx - 4, the last one ends past gnx).  Every piece is a
+        // multiple of four columns, so every copy starts and ends on 16 bytes.
+        const int first = gc0 < 0 ? 4 : (gc0 + W > gnx ? gnx - gc0 : W);
+        const int src0 = gc0 < 0 ? gnx - 4 : gc0;
+        bulk_g2s(smem_u32(ring_psi + slot * W), psi_m + ro + src0, first * 8u, bar);
+        bulk_g2s(smem_u32(ring_n + slot * W), n_m + ro + src0, first * 4u, bar);
+        bulk_g2s(smem_u32(ring_p + slot * W), p_m + ro + src0, first * 4u, bar);
+        if (first < W) {  // the rest continues from column 0 of the row
+          bulk_g2s(smem_u32(ring_psi + slot * W + first), psi_m + ro, (W - first) * 8u, bar);
+          bulk_g2s(smem_u32(ring_n + slot * W + first), n_m + ro, (W - first) * 4u, bar);
+          bulk_g2s(smem_u32(ring_p + slot * W + first), p_m + ro, (W - first) * 4u, bar);
+        }
+      }
     };
     if (t == 0) {
       for (int i = 0; i < 3 && i < n_iter; ++i) issue(i);
@@ -169,7 +213,7 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
         // that the integer and SFU work fills the stencil's issue gaps.
         float r2a = 0.f, sna = 0.f, csa = 0.f, r2b = 0.f, snb = 0.f, csb = 0.f;
         if (NOISE) {
-          const uint32_t cell = static_cast<uint32_t>(row_out * NX + col0);
+          const uint32_t cell = static_cast<uint32_t>(row_out * gnx + gcol0w);
           const uint32_t cells[2] = {cell, cell + 1u};
           Words4 w[2];
           philox_cells(cells, prefix, w);
@@ -179,16 +223,16 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
         const float4* xin = xbuf + ((j + 1) & 1) * 3 * HALF;
 
         // Stage 1 at row r-1 from the ring: k1 = f(psi0).
-        const float2* R1 = ring_psi + slot1 * NX;
+        const float2* R1 = ring_psi + slot1 * W;
         const float4 c4 = *reinterpret_cast<const float4*>(R1 + col0);
-        const float4 u4 = *reinterpret_cast<const float4*>(ring_psi + slot2 * NX + col0);
-        const float4 d4 = *reinterpret_cast<const float4*>(ring_psi + slot0 * NX + col0);
+        const float4 u4 = *reinterpret_cast<const float4*>(ring_psi + slot2 * W + col0);
+        const float4 d4 = *reinterpret_cast<const float4*>(ring_psi + slot0 * W + col0);
         const float2 lt = R1[lcol], rt = R1[rcol];
         const float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
         const float2 up0 = make_float2(u4.x, u4.y), up1 = make_float2(u4.z, u4.w);
         const float2 dn0 = make_float2(d4.x, d4.y), dn1 = make_float2(d4.z, d4.w);
-        const float2 n1v = *reinterpret_cast<const float2*>(ring_n + slot1 * NX + col0);
-        const float2 P1 = *reinterpret_cast<const float2*>(ring_p + slot1 * NX + col0);
+        const float2 n1v = *reinterpret_cast<const float2*>(ring_n + slot1 * W + col0);
+        const float2 P1 = *reinterpret_cast<const float2*>(ring_p + slot1 * W + col0);
         // Rows of the four stages (general variant only: the potential is read per stage).
         int srow[4] = {0, 0, 0, 0};
         if (GENERAL) {
@@ -220,8 +264,8 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
         {
           const float4 L = xin[lthr], Rr = xin[rthr];
           const float2 lt2 = make_float2(L.z, L.w), rt2 = make_float2(Rr.x, Rr.y);
-          const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * NX + col0);
-          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * NX + col0);
+          const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * W + col0);
+          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * W + col0);
           const Pair c = q1[jb];
           float2 da, db, va, vb;
           pot_at(srow[1], va, vb);
@@ -238,9 +282,9 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
         {
           const float4 L = xin[HALF + lthr], Rr = xin[HALF + rthr];
           const float2 lt3 = make_float2(L.z, L.w), rt3 = make_float2(Rr.x, Rr.y);
-          const float2 P3 = *reinterpret_cast<const float2*>(ring_p + slot3 * NX + col0);
-          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * NX + col0);
-          const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * NX + col0);
+          const float2 P3 = *reinterpret_cast<const float2*>(ring_p + slot3 * W + col0);
+          const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * W + col0);
+          const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * W + col0);
           const Pair c = q2[jc];
           float2 da, db, va, vb;
           pot_at(srow[2], va, vb);
@@ -257,7 +301,7 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
         {
           const float4 L = xin[2 * HALF + lthr], Rr = xin[2 * HALF + rthr];
           const float2 lt4 = make_float2(L.z, L.w), rt4 = make_float2(Rr.x, Rr.y);
-          const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * NX + col0);
+          const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * W + col0);
           const Pair c = q3[jd];
           float2 da, db, va, vb;
           pot_at(srow[3], va, vb);
@@ -271,8 +315,8 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
           float nb = fmaf(h6, dnb, accn[jd].y);
           na = na < 0.f ? 0.f : na;
           nb = nb < 0.f ? 0.f : nb;
-          if (i >= 8 && i - 8 < h_rows) {
-            const int o = row_out * NX;
+          if (writes && i >= 8 && i - 8 < h_rows) {
+            const long long o = static_cast<long long>(row_out) * gnx;
             if (NOISE) {
               WignerDraw<float>::add(fmaf(k.noise_b, na, k.noise_a), r2a, sna, csa, oa.x, oa.y);
               WignerDraw<float>::add(fmaf(k.noise_b, nb, k.noise_a), r2b, snb, csb, ob.x, ob.y);
@@ -306,40 +350,45 @@ __global__ void __launch_bounds__(NX / 2, (NX >= 1024 ? 1 : 1024 / NX))
 }  // namespace
 
 bool wide_rk4_supported(int nx, int ny) {
-  return (nx == 128 || nx == 256 || nx == 512 || nx == 1024) && ny >= 4;
-}
-
-size_t wide_rk4_smem(int nx) {
-  return static_cast<size_t>(kRing) * nx * 16 + static_cast<size_t>(6) * (nx / 2) * 16 +
-         (kRing + 1) * sizeof(uint64_t);
+  const bool full = nx == 128 || nx == 256 || nx == 512 || nx == 1024;
+  const bool band = nx > 1024 && nx % 1024 == 0 && nx <= 16384;
+  return (full || band) && ny >= 4;
 }
 
 namespace {
 
-template <int NX>
-cudaError_t configure_nx() {
-  const int smem = static_cast<int>(wide_rk4_smem(NX));
-  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, false>,
+template <int NX, bool BAND>
+size_t smem_for() {
+  using S = WideShape<NX, BAND>;
+  return static_cast<size_t>(kRing) * S::W * 16 + static_cast<size_t>(6) * S::THREADS * 16 +
+         (kRing + 1) * sizeof(uint64_t);
+}
+
+template <int NX, bool BAND>
+cudaError_t configure_shape() {
+  const int smem = static_cast<int>(smem_for<NX, BAND>());
+  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, false, BAND>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, false>,
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, false, BAND>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, true>,
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, true, BAND>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, true>,
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, true, BAND>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   return e;
 }
 
-template <int NX>
-int blocks_nx(bool noise) {
+template <int NX, bool BAND>
+int blocks_shape(bool noise) {
   int blocks = 0;
+  const int threads = WideShape<NX, BAND>::THREADS;
   cudaError_t e = noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &blocks, rk4_wide_kernel<NX, true, false>, NX / 2, wide_rk4_smem(NX))
+                              &blocks, rk4_wide_kernel<NX, true, false, BAND>, threads, smem_for<NX, BAND>())
                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &blocks, rk4_wide_kernel<NX, false, false>, NX / 2, wide_rk4_smem(NX));
+                              &blocks, rk4_wide_kernel<NX, false, false, BAND>, threads, smem_for<NX, BAND>());
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -347,26 +396,27 @@ int blocks_nx(bool noise) {
   return blocks < 1 ? 1 : blocks;
 }
 
-template <int NX>
-cudaError_t launch_nx(const float* psi_in, const float* n_in, const float* pump, float* psi_out,
-                      float* n_out, const RhsConst<float>* consts, const float* scales,
-                      const unsigned long long* step_base, int step_offset, float dt, bool noise,
-                      const WideGeom& g, int* err_flag, cudaStream_t stream) {
-  const size_t smem = wide_rk4_smem(NX);
+template <int NX, bool BAND>
+cudaError_t launch_shape(const float* psi_in, const float* n_in, const float* pump, float* psi_out,
+                         float* n_out, const RhsConst<float>* consts, const float* scales,
+                         const unsigned long long* step_base, int step_offset, float dt, bool noise,
+                         const WideGeom& g, int* err_flag, cudaStream_t stream) {
+  const size_t smem = smem_for<NX, BAND>();
+  const int threads = WideShape<NX, BAND>::THREADS;
   const float2* pin = reinterpret_cast<const float2*>(psi_in);
   float2* pout = reinterpret_cast<float2*>(psi_out);
   const bool general = wide_general(g);
   if (noise && general) {
-    rk4_wide_kernel<NX, true, true><<<g.blocks, NX / 2, smem, stream>>>(
+    rk4_wide_kernel<NX, true, true, BAND><<<g.blocks, threads, smem, stream>>>(
         pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
   } else if (noise) {
-    rk4_wide_kernel<NX, true, false><<<g.blocks, NX / 2, smem, stream>>>(
+    rk4_wide_kernel<NX, true, false, BAND><<<g.blocks, threads, smem, stream>>>(
         pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
   } else if (general) {
-    rk4_wide_kernel<NX, false, true><<<g.blocks, NX / 2, smem, stream>>>(
+    rk4_wide_kernel<NX, false, true, BAND><<<g.blocks, threads, smem, stream>>>(
         pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
   } else {
-    rk4_wide_kernel<NX, false, false><<<g.blocks, NX / 2, smem, stream>>>(
+    rk4_wide_kernel<NX, false, false, BAND><<<g.blocks, threads, smem, stream>>>(
         pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
   }
   return cudaGetLastError();
@@ -374,20 +424,32 @@ cudaError_t launch_nx(const float* psi_in, const float* n_in, const float* pump,
 
 }  // namespace
 
+size_t wide_rk4_smem(int nx) {
+  switch (nx) {
+    case 128: return smem_for<128, false>();
+    case 256: return smem_for<256, false>();
+    case 512: return smem_for<512, false>();
+    case 1024: return smem_for<1024, false>();
+    default: return smem_for<1024, true>();
+  }
+}
+
 cudaError_t configure_wide_rk4() {
-  cudaError_t e = configure_nx<128>();
-  if (e == cudaSuccess) e = configure_nx<256>();
-  if (e == cudaSuccess) e = configure_nx<512>();
-  if (e == cudaSuccess) e = configure_nx<1024>();
+  cudaError_t e = configure_shape<128, false>();
+  if (e == cudaSuccess) e = configure_shape<256, false>();
+  if (e == cudaSuccess) e = configure_shape<512, false>();
+  if (e == cudaSuccess) e = configure_shape<1024, false>();
+  if (e == cudaSuccess) e = configure_shape<1024, true>();
   return e;
 }
 
 int wide_rk4_blocks_per_sm(int nx, bool noise) {
   switch (nx) {
-    case 128: return blocks_nx<128>(noise);
-    case 256: return blocks_nx<256>(noise);
-    case 512: return blocks_nx<512>(noise);
-    default: return blocks_nx<1024>(noise);
+    case 128: return blocks_shape<128, false>(noise);
+    case 256: return blocks_shape<256, false>(noise);
+    case 512: return blocks_shape<512, false>(noise);
+    case 1024: return blocks_shape<1024, false>(noise);
+    default: return blocks_shape<1024, true>(noise);
   }
 }
 
@@ -398,18 +460,21 @@ cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float*
                             int* err_flag, cudaStream_t stream) {
   switch (g.nx) {
     case 128:
-      return launch_nx<128>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
-                            step_offset, dt, noise, g, err_flag, stream);
+      return launch_shape<128, false>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                                      step_offset, dt, noise, g, err_flag, stream);
     case 256:
-      return launch_nx<256>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
-                            step_offset, dt, noise, g, err_flag, stream);
+      return launch_shape<256, false>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                                      step_offset, dt, noise, g, err_flag, stream);
     case 512:
-      return launch_nx<512>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
-                            step_offset, dt, noise, g, err_flag, stream);
+      return launch_shape<512, false>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                                      step_offset, dt, noise, g, err_flag, stream);
     case 1024:
-      return launch_nx<1024>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
-                             step_offset, dt, noise, g, err_flag, stream);
+      return launch_shape<1024, false>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                                       step_offset, dt, noise, g, err_flag, stream);
     default:
+      if (g.nx > 1024 && g.nx % 1024 == 0)
+        return launch_shape<1024, true>(psi_in, n_in, pump, psi_out, n_out, consts, scales,
+                                        step_base, step_offset, dt, noise, g, err_flag, stream);
       return cudaErrorInvalidValue;
   }
 }

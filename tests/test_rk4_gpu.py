@@ -225,9 +225,14 @@ def test_launch_count_and_error_status(cuda_lib):
         eng.set_geometry(8, 6)
 
 
-@pytest.mark.parametrize("nx,ny,members", [(128, 48, 3), (256, 20, 2), (512, 12, 2), (1024, 8, 1)])
+@pytest.mark.parametrize("nx,ny,members", [(128, 48, 3), (256, 20, 2), (512, 12, 2), (1024, 8, 1),
+                                            (2048, 40, 1), (3072, 10, 1), (4096, 6, 2)])
 def test_full_width_kernel_matches_oracle_and_tiled(cuda_lib, nx, ny, members):
-    """The TMA full-width FP32 kernel against the oracle (1e-4) and the tiled kernel (1e-5)."""
+    """The TMA full-width FP32 kernel against the oracle (1e-4) and the tiled kernel (1e-5).
+
+    Rows wider than 1024 sites run as 1024-site bands with four recomputed halo columns on
+    each side; the cases cover the periodic wrap of the first and last band, several bands
+    per member, and blocks whose row range crosses from one band into the next."""
     from polarism_gb300.engine import MemberPhysics, RK4Engine
 
     rng = np.random.default_rng(nx + ny)
@@ -296,7 +301,7 @@ def test_device_normals_within_error_bound(cuda_lib, precision):
 
 
 @pytest.mark.parametrize("pot_kind,per_member", [("complex", True), ("real", False), ("none", False)])
-@pytest.mark.parametrize("nx,ny,members", [(256, 24, 2), (1024, 12, 1)])
+@pytest.mark.parametrize("nx,ny,members", [(256, 24, 2), (1024, 12, 1), (2048, 12, 2)])
 def test_full_width_general_variant_matches_oracle_and_tiled(cuda_lib, pot_kind, per_member, nx, ny,
                                                              members):
     """The full-width kernel's general variant (potential and kinetic relaxation, Wigner noise
