@@ -1,0 +1,26 @@
+"""Host logic of the full-size precision check, on a small grid without a GPU: the oracle leg
+reads a device leg's files and reports relative L2 errors (zero for an oracle-made file)."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def test_oracle_leg_reports_errors_of_a_device_file(tmp_path):
+    from tests import precision_check as pc
+
+    n, steps = 16, 3
+    for method, precision in pc.CASES:
+        psi, res, norms, fp = pc.oracle_case(method, precision, steps, n)
+        env = pc.inputs(n)[3]
+        np.savez(tmp_path / f"{pc.case_name(method, precision)}.npz", psi=psi, res=res,
+                 norms=norms, wall=0.0, inputs=fp, env=env, steps=steps, n=n)
+    results = pc.oracle_leg(tmp_path, tmp_path / "r.json", jobs=1)
+    assert set(results) == {pc.case_name(m, p) for m, p in pc.CASES}
+    for r in results.values():
+        assert r["psi_rel_l2"] == 0.0 and r["n_R_rel_l2"] == 0.0 and r["pass"]
+    # A perturbed device state is reported, not hidden.
+    g = dict(np.load(tmp_path / "rk4_fp32.npz"))
+    g["psi"] = g["psi"] * (1 + 1e-3)
+    np.savez(tmp_path / "rk4_fp32.npz", **g)
+    r = pc.oracle_leg(tmp_path, tmp_path / "r.json", jobs=1)["rk4_fp32"]
+    assert abs(r["psi_rel_l2"] - 1e-3) < 1e-9 and not r["pass"]
