@@ -306,7 +306,9 @@ def run_ours(args):
     if args.rk4_kernel != "auto":
         eng.set_kernel(2 if args.rk4_kernel == "wide" else 1)
     kernel_name = ("tiled" if eng.kernel() == 1 else
-                   "full-width" if NX <= 1024 else "full-width, 1024-site bands")
+                   "full-width" if NX <= 1024 else
+                   f"full-width, clusters of {NX // 1024} CTAs (1024-site bands)" if NX <= 8192 else
+                   "full-width, 1024-site bands with recomputed halo")
     eng.set_pump(w["env"])
     if args.potential != "none":
         # A harmonic trap (real part) and an absorbing rim (imaginary part), shared by members.

@@ -379,13 +379,7 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   cudaMemsetAsync(s->halt, 0, sizeof(int), s->stream);
   if (cfg->precision == PG_SINGLE && pg::wide_rk4_supported(cfg->nx, cfg->ny)) {
     if ((e = pg::configure_wide_rk4()) != cudaSuccess) return fail(e, "wide kernel attributes");
-    // Rows wider than 1024 sites run as 1024-site bands, each its own row stream.
-    const long long bands = cfg->nx > 1024 ? cfg->nx / 1024 : 1;
-    const long long rows = static_cast<long long>(cfg->members) * bands * cfg->ny;
-    const long long per_sm = pg::wide_rk4_blocks_per_sm(cfg->nx, true);
-    long long blocks = per_sm * s->sm_count;
-    const long long by_rows = std::max<long long>(1, rows / 16);
-    s->wide_blocks = static_cast<int>(std::min(blocks, by_rows));
+    s->wide_blocks = pg::wide_rk4_grid(cfg->nx, cfg->ny, cfg->members, s->sm_count);
   }
   const size_t staging_bytes = static_cast<size_t>(kChunk) * 3 * s->pump_terms * cfg->members * 8 + 64;
   for (auto& slot : s->staging) {

@@ -17,6 +17,8 @@
 // * Blocks are persistent: block c advances rows [c R / G, (c+1) R / G) of the
 //   member-major row space (R = members * ny rows), restarting the 4-row pipeline
 //   fill whenever it crosses into the next member.
+#include <algorithm>
+
 #include "philox.cuh"
 #include "pg_internal.h"
 #include "rk4_site.cuh"
@@ -30,26 +32,37 @@ constexpr int kRing = 8;          // rows resident: r-4..r plus three in flight
 constexpr int kWaitLimit = 100000;
 
 // At least 512 resident threads per SM for every row width (128 registers a thread).
-// Threads of a block: two sites each over the shared-memory row (BAND: a 1024-column band of a
-// wider row plus four halo columns on each side, rounded up to whole warps).
-template <int NX, bool BAND>
+// Threads of a block: two sites each over the shared-memory row.  Rows wider than NX = 1024
+// sites go in 1024-column bands whose shared-memory rows carry four halo columns on each side:
+// BAND recomputes the halo (a block owns the band alone; the four stages each reach one
+// column further, so 516 threads rounded up to whole warps), CLUSTER gives each band of a row
+// to one CTA of a thread-block cluster (NX / 2 threads) and exchanges the two edge columns of
+// each stage through distributed shared memory.
+template <int NX, bool BAND, bool CLUSTER = false>
 struct WideShape {
-  static constexpr int W = BAND ? NX + 8 : NX;  // sites per shared-memory row
-  static constexpr int ACTIVE = W / 2;          // threads that own two sites
+  static constexpr int W = (BAND || CLUSTER) ? NX + 8 : NX;  // sites per shared-memory row
+  static constexpr int ACTIVE = BAND ? W / 2 : NX / 2;      // threads that own two sites
   static constexpr int THREADS = BAND ? ((ACTIVE + 31) / 32) * 32 : NX / 2;
 };
+// Barriers after the ring's: the row exchange, then (CLUSTER) the left and right
+// neighbours' edge deliveries, two of each by iteration parity.
+constexpr int kBars = kRing + 5;
+// CLUSTER inboxes after the barriers: [from left, from right][parity][stage] edge values.
+constexpr int kInbox = 2 * 2 * 3;
+constexpr uint32_t kEdgeBytes = 3 * 8;  // one iteration's delivery: three stage values
 
-template <int NX, bool NOISE, bool GENERAL, bool BAND>
-__global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 : 1024 / NX))
+template <int NX, bool NOISE, bool GENERAL, bool BAND, bool CLUSTER = false>
+__global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 1024 ? 1 : 1024 / NX))
     rk4_wide_kernel(const float2* __restrict__ psi_in, const float* __restrict__ n_in,
                     const float* __restrict__ pump, float2* __restrict__ psi_out,
                     float* __restrict__ n_out, const RhsConst<float>* __restrict__ consts,
                     const float* __restrict__ scales,
                     const unsigned long long* __restrict__ step_base, const int step_offset,
                     const float dt, const WideGeom g, int* __restrict__ err_flag) {
-  constexpr int W = WideShape<NX, BAND>::W;
-  constexpr int ACTIVE = WideShape<NX, BAND>::ACTIVE;
-  constexpr int HALF = WideShape<NX, BAND>::THREADS;  // exchange-buffer stride (every thread)
+  constexpr int W = WideShape<NX, BAND, CLUSTER>::W;
+  constexpr int ACTIVE = WideShape<NX, BAND, CLUSTER>::ACTIVE;
+  constexpr int HALF = WideShape<NX, BAND, CLUSTER>::THREADS;  // exchange-buffer stride
+  constexpr bool HALO = BAND || CLUSTER;  // shared-memory rows carry the band's halo
   // One block per SM (1024-site rows): a split arrive/wait barrier lets its warps drift
   // apart by up to a row, which measured faster; with several blocks per SM the blocks
   // already interleave and a block-wide barrier is cheaper.
@@ -60,8 +73,16 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
   float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * W);  // [kRing][W]
   float* ring_p = ring_n + kRing * W;                              // [kRing][W]
   float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * W);    // [2][3][HALF]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kRing] + exchange barrier
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kBars]
   const uint32_t xbar = smem_u32(&mbar[kRing]);
+  // CLUSTER: at the end of each iteration the left neighbour's thread HALF-1 pushes its
+  // right column's three stage values into in_left[parity] with st.async, completing on
+  // from_left[parity]; the right neighbour's thread 0 pushes its left column into in_right.
+  // Only this CTA's edge threads (0 and HALF-1) read them, after arming and waiting.
+  const uint32_t from_left = smem_u32(&mbar[kRing + 1]);
+  const uint32_t from_right = smem_u32(&mbar[kRing + 3]);
+  float2* in_left = reinterpret_cast<float2*>(mbar + kBars);  // [2][3]
+  float2* in_right = in_left + 6;                              // [2][3]
 
   const int ny = g.ny;
   const int t = threadIdx.x;
@@ -70,26 +91,78 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
   // not written either).
   const int tc = BAND ? min(t, ACTIVE - 1) : t;
   const bool owner = !BAND || t < ACTIVE;
-  const int col0 = 2 * tc;
-  const int lcol = BAND ? (col0 == 0 ? 0 : col0 - 1) : (col0 == 0 ? NX - 1 : col0 - 1);
-  const int rcol = BAND ? (col0 + 2 >= W ? col0 + 1 : col0 + 2) : (col0 + 2 == NX ? 0 : col0 + 2);
-  const int lthr = BAND ? max(tc - 1, 0) : (t == 0 ? HALF - 1 : t - 1);          // owns lcol
-  const int rthr = BAND ? min(tc + 1, ACTIVE - 1) : (t + 1 == HALF ? 0 : t + 1);  // owns rcol
-  const int gnx = BAND ? g.nx : NX;       // sites per grid row
-  const int bands = BAND ? g.nx / NX : 1;
+  // Shared-memory column of the thread's first site (CLUSTER: past the left halo).
+  const int col0 = CLUSTER ? 2 * tc + 4 : 2 * tc;
+  const int lcol = CLUSTER ? col0 - 1
+                 : BAND    ? (col0 == 0 ? 0 : col0 - 1)
+                           : (col0 == 0 ? NX - 1 : col0 - 1);
+  const int rcol = CLUSTER ? col0 + 2
+                 : BAND    ? (col0 + 2 >= W ? col0 + 1 : col0 + 2)
+                           : (col0 + 2 == NX ? 0 : col0 + 2);
+  // Owners of lcol / rcol in the exchange (CLUSTER: the edge threads' neighbours are the
+  // neighbouring CTAs' edge threads, read through distributed shared memory).
+  const int lthr = BAND ? max(tc - 1, 0) : (t == 0 ? HALF - 1 : t - 1);
+  const int rthr = BAND ? min(tc + 1, ACTIVE - 1) : (t + 1 == HALF ? 0 : t + 1);
+  const int gnx = HALO ? g.nx : NX;  // sites per grid row
+  const int bands = HALO ? g.nx / NX : 1;
+  // CLUSTER: the CTA's band is its rank; clusters share out the rows.
+  const int rank = CLUSTER ? static_cast<int>(cluster_ctarank()) : 0;
+  const int unit_id = CLUSTER ? static_cast<int>(blockIdx.x) / bands : static_cast<int>(blockIdx.x);
+  const int units = CLUSTER ? static_cast<int>(gridDim.x) / bands : static_cast<int>(gridDim.x);
+  const uint32_t left_rank = CLUSTER ? static_cast<uint32_t>((rank + bands - 1) % bands) : 0u;
+  const uint32_t right_rank = CLUSTER ? static_cast<uint32_t>((rank + 1) % bands) : 0u;
   const long long plane = static_cast<long long>(gnx) * ny;
   constexpr uint32_t kRowBytes = W * 16u;
 
   if (t == 0) {
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
     if (kSplit) mbar_init(xbar, HALF);
+    if (CLUSTER)
+      for (int s = kRing + 1; s < kBars; ++s) mbar_init(smem_u32(&mbar[s]), 1);
     fence_mbar_init();
   }
-  __syncthreads();
+  // CLUSTER: every CTA's barriers exist before any neighbour arrives on them.
+  if (CLUSTER) cluster_sync_all(); else __syncthreads();
+  // Neighbour addresses (CLUSTER): the inbox and barrier each edge thread delivers to.
+  const uint32_t left_inbox = CLUSTER ? map_shared_rank(smem_u32(in_right), left_rank) : 0u;
+  const uint32_t left_bar = CLUSTER ? map_shared_rank(from_right, left_rank) : 0u;
+  const uint32_t right_inbox = CLUSTER ? map_shared_rank(smem_u32(in_left), right_rank) : 0u;
+  const uint32_t right_bar = CLUSTER ? map_shared_rank(from_left, right_rank) : 0u;
+  // Horizontal neighbours of stage s (0..2) from the exchange of parity `xb`: the left
+  // neighbour's right column and the right neighbour's left column.
+  auto xchg = [&](int xb, int s, float2& lt, float2& rt) {
+    const float4* xin = xbuf + xb * 3 * HALF + s * HALF;
+    if (CLUSTER && t == 0) {
+      lt = in_left[xb * 3 + s];
+    } else {
+      const float4 L = xin[lthr];
+      lt = make_float2(L.z, L.w);
+    }
+    if (CLUSTER && t == HALF - 1) {
+      rt = in_right[xb * 3 + s];
+    } else {
+      const float4 Rr = xin[rthr];
+      rt = make_float2(Rr.x, Rr.y);
+    }
+  };
+  // CLUSTER edge threads: arm and wait for the neighbours' delivery of iteration g.
+  auto receive = [&](unsigned g) {
+    const uint32_t q = g & 1u, par = (g >> 1) & 1u;
+    bool ok = true;
+    if (t == 0) {
+      mbar_arrive_expect_tx(from_left + 8u * q, kEdgeBytes);
+      ok = mbar_wait_bounded(from_left + 8u * q, par, kWaitLimit);
+    }
+    if (t == HALF - 1) {
+      mbar_arrive_expect_tx(from_right + 8u * q, kEdgeBytes);
+      ok = mbar_wait_bounded(from_right + 8u * q, par, kWaitLimit);
+    }
+    return ok;
+  };
 
-  const long long total_rows = static_cast<long long>(g.members) * bands * ny;
-  const long long r_begin = total_rows * blockIdx.x / gridDim.x;
-  const long long r_end = total_rows * (blockIdx.x + 1) / gridDim.x;
+  const long long total_rows = static_cast<long long>(g.members) * (CLUSTER ? 1 : bands) * ny;
+  const long long r_begin = total_rows * unit_id / units;
+  const long long r_end = total_rows * (unit_id + 1) / units;
   const float hh = 0.5f * dt, h6 = dt / 6.0f, h3 = dt / 3.0f;
   unsigned it = 0;  // ring uses so far; always a multiple of kRing at a segment start
   bool timed_out = false;
@@ -98,8 +171,8 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
   while (gr < r_end) {
     // Row space [member][band][row]; a segment stays within one (member, band).
     const long long unit = gr / ny;
-    const int member = static_cast<int>(unit / bands);
-    const int band = static_cast<int>(unit % bands);
+    const int member = CLUSTER ? static_cast<int>(unit) : static_cast<int>(unit / bands);
+    const int band = CLUSTER ? rank : static_cast<int>(unit % bands);
     const int ya = static_cast<int>(gr - unit * ny);
     const int yb = static_cast<int>(min(static_cast<long long>(ny), ya + (r_end - gr)));
     gr += yb - ya;
@@ -118,10 +191,10 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
                            1u, key0, key1);
     // Grid column of shared-memory column c: the band starts four columns left of its first
     // written column.
-    const int gc0 = BAND ? band * NX - 4 : 0;
+    const int gc0 = HALO ? band * NX - 4 : 0;
     const int gcol0 = gc0 + col0;                                    // may lie outside [0, gnx)
     const int gcol0w = gcol0 < 0 ? gcol0 + gnx : (gcol0 >= gnx ? gcol0 - gnx : gcol0);
-    const bool writes = owner && (!BAND || (col0 >= 4 && col0 < 4 + NX));
+    const bool writes = owner && (!HALO || (col0 >= 4 && col0 < 4 + NX));
     const float2* psi_m = psi_in + member * plane;
     const float* n_m = n_in + member * plane;
     const float* p_m = pump + member * g.pump_stride;
@@ -162,7 +235,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
       const uint32_t bar = smem_u32(&mbar[slot]);
       mbar_arrive_expect_tx(bar, kRowBytes);
       const long long ro = static_cast<long long>(row) * gnx;
-      if (!BAND) {
+      if (!HALO) {
         bulk_g2s(smem_u32(ring_psi + slot * W), psi_m + ro, NX * 8u, bar);
         bulk_g2s(smem_u32(ring_n + slot * W), n_m + ro, NX * 4u, bar);
         bulk_g2s(smem_u32(ring_p + slot * W), p_m + ro, NX * 4u, bar);
@@ -220,7 +293,6 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
           WignerDraw<float>::prepare(w[0], r2a, sna, csa);
           WignerDraw<float>::prepare(w[1], r2b, snb, csb);
         }
-        const float4* xin = xbuf + ((j + 1) & 1) * 3 * HALF;
 
         // Stage 1 at row r-1 from the ring: k1 = f(psi0).
         const float2* R1 = ring_psi + slot1 * W;
@@ -258,12 +330,16 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
           // the draw and stage 1 overlap with the slower warps of the previous row.
           const unsigned g = it + i;
           if (g > 0 && !mbar_wait_bounded(xbar, (g - 1) & 1u, kWaitLimit)) timed_out = true;
+          // The edge threads also wait for the neighbouring CTAs' edge values of iteration
+          // i-1.  A neighbour delivers into the same inbox again only at the end of iteration
+          // i+1, after it has received this thread's own delivery of iteration i.
+          if (CLUSTER && g > 0 && !receive(g - 1)) timed_out = true;
           if (t == 0 && i + 3 < n_iter) issue(i + 3);
         }
         // Stage 2 at row r-2: k2 = f(psi1).
         {
-          const float4 L = xin[lthr], Rr = xin[rthr];
-          const float2 lt2 = make_float2(L.z, L.w), rt2 = make_float2(Rr.x, Rr.y);
+          float2 lt2, rt2;
+          xchg((j + 1) & 1, 0, lt2, rt2);
           const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * W + col0);
           const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * W + col0);
           const Pair c = q1[jb];
@@ -280,8 +356,8 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
         }
         // Stage 3 at row r-3: k3 = f(psi2).
         {
-          const float4 L = xin[HALF + lthr], Rr = xin[HALF + rthr];
-          const float2 lt3 = make_float2(L.z, L.w), rt3 = make_float2(Rr.x, Rr.y);
+          float2 lt3, rt3;
+          xchg((j + 1) & 1, 1, lt3, rt3);
           const float2 P3 = *reinterpret_cast<const float2*>(ring_p + slot3 * W + col0);
           const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * W + col0);
           const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * W + col0);
@@ -299,8 +375,8 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
         }
         // Stage 4 at row r-4: k4 = f(psi3), final combine, clamp, Wigner increment.
         {
-          const float4 L = xin[2 * HALF + lthr], Rr = xin[2 * HALF + rthr];
-          const float2 lt4 = make_float2(L.z, L.w), rt4 = make_float2(Rr.x, Rr.y);
+          float2 lt4, rt4;
+          xchg((j + 1) & 1, 2, lt4, rt4);
           const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * W + col0);
           const Pair c = q3[jd];
           float2 da, db, va, vb;
@@ -333,6 +409,22 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
           xo[2 * HALF + t] = make_float4(q3[jc].a.x, q3[jc].a.y, q3[jc].b.x, q3[jc].b.y);
         }
         row_out = row_out + 1 == ny ? 0 : row_out + 1;
+        if (CLUSTER) {
+          // Deliver the edge column's three stage values to the neighbour that needs them.
+          const uint32_t q = (it + i) & 1u;
+          if (t == 0) {
+            const uint32_t dst = left_inbox + q * kEdgeBytes;
+            st_async_f2(dst, q1[ja].a, left_bar + 8u * q);
+            st_async_f2(dst + 8u, q2[jb].a, left_bar + 8u * q);
+            st_async_f2(dst + 16u, q3[jc].a, left_bar + 8u * q);
+          }
+          if (t == HALF - 1) {
+            const uint32_t dst = right_inbox + q * kEdgeBytes;
+            st_async_f2(dst, q1[ja].b, right_bar + 8u * q);
+            st_async_f2(dst + 8u, q2[jb].b, right_bar + 8u * q);
+            st_async_f2(dst + 16u, q3[jc].b, right_bar + 8u * q);
+          }
+        }
         if (kSplit) {
           mbar_arrive(xbar);
         } else {
@@ -344,7 +436,11 @@ __global__ void __launch_bounds__(WideShape<NX, BAND>::THREADS, (NX >= 1024 ? 1 
     }
     it += n_iter;
   }
+  // CLUSTER: take the neighbours' last deliveries, so that no store into this CTA's shared
+  // memory is still in flight when it exits, then leave together.
+  if (CLUSTER && it > 0 && !receive(it - 1)) timed_out = true;
   if (timed_out) atomicOr(err_flag, 1);
+  if (CLUSTER) cluster_sync_all();
 }
 
 }  // namespace
@@ -357,26 +453,30 @@ bool wide_rk4_supported(int nx, int ny) {
 
 namespace {
 
-template <int NX, bool BAND>
+// Rows of 2048 .. 8192 sites run as clusters of nx / 1024 CTAs (the portable cluster size
+// limit is 8); wider rows as independent bands.
+bool use_cluster(int nx) { return nx > 1024 && nx % 1024 == 0 && nx / 1024 <= 8; }
+
+template <int NX, bool BAND, bool CLUSTER>
 size_t smem_for() {
-  using S = WideShape<NX, BAND>;
+  using S = WideShape<NX, BAND, CLUSTER>;
   return static_cast<size_t>(kRing) * S::W * 16 + static_cast<size_t>(6) * S::THREADS * 16 +
-         (kRing + 1) * sizeof(uint64_t);
+         kBars * sizeof(uint64_t) + kInbox * sizeof(float2);
 }
 
-template <int NX, bool BAND>
+template <int NX, bool BAND, bool CLUSTER>
 cudaError_t configure_shape() {
-  const int smem = static_cast<int>(smem_for<NX, BAND>());
-  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, false, BAND>,
+  const int smem = static_cast<int>(smem_for<NX, BAND, CLUSTER>());
+  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, false, BAND, CLUSTER>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, false, BAND>,
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, false, BAND, CLUSTER>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, true, BAND>,
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, true, BAND, CLUSTER>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, true, BAND>,
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, true, BAND, CLUSTER>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   return e;
 }
@@ -385,10 +485,11 @@ template <int NX, bool BAND>
 int blocks_shape(bool noise) {
   int blocks = 0;
   const int threads = WideShape<NX, BAND>::THREADS;
-  cudaError_t e = noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &blocks, rk4_wide_kernel<NX, true, false, BAND>, threads, smem_for<NX, BAND>())
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                              &blocks, rk4_wide_kernel<NX, false, false, BAND>, threads, smem_for<NX, BAND>());
+  cudaError_t e =
+      noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                  &blocks, rk4_wide_kernel<NX, true, false, BAND>, threads, smem_for<NX, BAND, false>())
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                  &blocks, rk4_wide_kernel<NX, false, false, BAND>, threads, smem_for<NX, BAND, false>());
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -396,12 +497,36 @@ int blocks_shape(bool noise) {
   return blocks < 1 ? 1 : blocks;
 }
 
+// Clusters of `size` CTAs of the 1024-column cluster kernel that fit on the GPU at once.
+int active_clusters(int size, bool noise) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = size;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(size, 1, 1);
+  cfg.blockDim = dim3(WideShape<1024, false, true>::THREADS, 1, 1);
+  cfg.dynamicSmemBytes = smem_for<1024, false, true>();
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  const cudaError_t e =
+      noise ? cudaOccupancyMaxActiveClusters(&n, rk4_wide_kernel<1024, true, false, false, true>, &cfg)
+            : cudaOccupancyMaxActiveClusters(&n, rk4_wide_kernel<1024, false, false, false, true>, &cfg);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
 template <int NX, bool BAND>
 cudaError_t launch_shape(const float* psi_in, const float* n_in, const float* pump, float* psi_out,
                          float* n_out, const RhsConst<float>* consts, const float* scales,
                          const unsigned long long* step_base, int step_offset, float dt, bool noise,
                          const WideGeom& g, int* err_flag, cudaStream_t stream) {
-  const size_t smem = smem_for<NX, BAND>();
+  const size_t smem = smem_for<NX, BAND, false>();
   const int threads = WideShape<NX, BAND>::THREADS;
   const float2* pin = reinterpret_cast<const float2*>(psi_in);
   float2* pout = reinterpret_cast<float2*>(psi_out);
@@ -422,35 +547,88 @@ cudaError_t launch_shape(const float* psi_in, const float* n_in, const float* pu
   return cudaGetLastError();
 }
 
+// Cluster launch: g.blocks CTAs in clusters of nx / 1024.
+cudaError_t launch_cluster(const float* psi_in, const float* n_in, const float* pump,
+                           float* psi_out, float* n_out, const RhsConst<float>* consts,
+                           const float* scales, const unsigned long long* step_base,
+                           int step_offset, float dt, bool noise, const WideGeom& g, int* err_flag,
+                           cudaStream_t stream) {
+  const int size = g.nx / 1024;
+  if (g.blocks < size || g.blocks % size != 0) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = size;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(g.blocks, 1, 1);
+  cfg.blockDim = dim3(WideShape<1024, false, true>::THREADS, 1, 1);
+  cfg.dynamicSmemBytes = smem_for<1024, false, true>();
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const float2* pin = reinterpret_cast<const float2*>(psi_in);
+  float2* pout = reinterpret_cast<float2*>(psi_out);
+  const bool general = wide_general(g);
+  if (noise && general)
+    return cudaLaunchKernelEx(&cfg, rk4_wide_kernel<1024, true, true, false, true>, pin, n_in, pump,
+                              pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+  if (noise)
+    return cudaLaunchKernelEx(&cfg, rk4_wide_kernel<1024, true, false, false, true>, pin, n_in,
+                              pump, pout, n_out, consts, scales, step_base, step_offset, dt, g,
+                              err_flag);
+  if (general)
+    return cudaLaunchKernelEx(&cfg, rk4_wide_kernel<1024, false, true, false, true>, pin, n_in,
+                              pump, pout, n_out, consts, scales, step_base, step_offset, dt, g,
+                              err_flag);
+  return cudaLaunchKernelEx(&cfg, rk4_wide_kernel<1024, false, false, false, true>, pin, n_in, pump,
+                            pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+}
+
 }  // namespace
 
 size_t wide_rk4_smem(int nx) {
   switch (nx) {
-    case 128: return smem_for<128, false>();
-    case 256: return smem_for<256, false>();
-    case 512: return smem_for<512, false>();
-    case 1024: return smem_for<1024, false>();
-    default: return smem_for<1024, true>();
+    case 128: return smem_for<128, false, false>();
+    case 256: return smem_for<256, false, false>();
+    case 512: return smem_for<512, false, false>();
+    case 1024: return smem_for<1024, false, false>();
+    default: return use_cluster(nx) ? smem_for<1024, false, true>() : smem_for<1024, true, false>();
   }
 }
 
 cudaError_t configure_wide_rk4() {
-  cudaError_t e = configure_shape<128, false>();
-  if (e == cudaSuccess) e = configure_shape<256, false>();
-  if (e == cudaSuccess) e = configure_shape<512, false>();
-  if (e == cudaSuccess) e = configure_shape<1024, false>();
-  if (e == cudaSuccess) e = configure_shape<1024, true>();
+  cudaError_t e = configure_shape<128, false, false>();
+  if (e == cudaSuccess) e = configure_shape<256, false, false>();
+  if (e == cudaSuccess) e = configure_shape<512, false, false>();
+  if (e == cudaSuccess) e = configure_shape<1024, false, false>();
+  if (e == cudaSuccess) e = configure_shape<1024, true, false>();
+  if (e == cudaSuccess) e = configure_shape<1024, false, true>();
   return e;
 }
 
-int wide_rk4_blocks_per_sm(int nx, bool noise) {
-  switch (nx) {
-    case 128: return blocks_shape<128, false>(noise);
-    case 256: return blocks_shape<256, false>(noise);
-    case 512: return blocks_shape<512, false>(noise);
-    case 1024: return blocks_shape<1024, false>(noise);
-    default: return blocks_shape<1024, true>(noise);
+int wide_rk4_grid(int nx, int ny, int members, int sm_count) {
+  if (use_cluster(nx)) {
+    // Whole clusters, as many as fit at once, and at least 16 rows a cluster.
+    const int size = nx / 1024;
+    const long long rows = static_cast<long long>(members) * ny;
+    const long long fit = std::max(1, active_clusters(size, true));
+    const long long clusters = std::max<long long>(1, std::min(fit, rows / 16));
+    return static_cast<int>(clusters * size);
   }
+  int per_sm = 1;
+  switch (nx) {
+    case 128: per_sm = blocks_shape<128, false>(true); break;
+    case 256: per_sm = blocks_shape<256, false>(true); break;
+    case 512: per_sm = blocks_shape<512, false>(true); break;
+    case 1024: per_sm = blocks_shape<1024, false>(true); break;
+    default: per_sm = blocks_shape<1024, true>(true); break;
+  }
+  // Rows wider than 1024 sites (BAND) are separate 1024-site bands, each its own row stream.
+  const long long bands = nx > 1024 ? nx / 1024 : 1;
+  const long long rows = static_cast<long long>(members) * bands * ny;
+  const long long blocks = static_cast<long long>(per_sm) * std::max(1, sm_count);
+  return static_cast<int>(std::min(blocks, std::max<long long>(1, rows / 16)));
 }
 
 cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float* pump,
@@ -472,6 +650,9 @@ cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float*
       return launch_shape<1024, false>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
                                        step_offset, dt, noise, g, err_flag, stream);
     default:
+      if (use_cluster(g.nx))
+        return launch_cluster(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
+                              step_offset, dt, noise, g, err_flag, stream);
       if (g.nx > 1024 && g.nx % 1024 == 0)
         return launch_shape<1024, true>(psi_in, n_in, pump, psi_out, n_out, consts, scales,
                                         step_base, step_offset, dt, noise, g, err_flag, stream);

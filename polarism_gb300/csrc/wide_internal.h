@@ -22,7 +22,9 @@ struct WideGeom {
 bool wide_rk4_supported(int nx, int ny);
 size_t wide_rk4_smem(int nx);
 cudaError_t configure_wide_rk4();
-int wide_rk4_blocks_per_sm(int nx, bool noise);
+// Grid of the full-width kernel for this shape: persistent blocks (or, for rows of 2048 to
+// 8192 sites, whole clusters of nx / 1024 CTAs), at least 16 rows of work each.
+int wide_rk4_grid(int nx, int ny, int members, int sm_count);
 cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float* pump,
                             float* psi_out, float* n_out, const RhsConst<float>* consts,
                             const float* scales, const unsigned long long* step_base,
