@@ -1,4 +1,5 @@
-// Full-width fused RK4 step for FP32 rows up to 1024 sites (the common case).
+// Full-width fused RK4 step for FP32 rows of 128 to 1024 sites, and of multiples of 1024 sites
+// up to 16384 as 1024-site bands (2048-8192: one band per CTA of a thread-block cluster).
 //
 // Same mathematics and operation order as rk4.cu (polarism/model.py:89-127,
 // polarism/solver/rk4_fdm_solver.py:36-82, single_reservoir.py:70-98, Wigner

@@ -139,7 +139,7 @@ def _rel_l2(a, b):
 
 
 def _compare(job):
-    gpu_dir, method, precision = job
+    gpu_dir, method, precision, keep = job
     name = case_name(method, precision)
     g = np.load(Path(gpu_dir) / f"{name}.npz")
     steps, n = int(g["steps"]), int(g["n"])
@@ -147,6 +147,8 @@ def _compare(job):
     psi, res, norms, fp = oracle_case(method, precision, steps, n, env=g["env"])
     if fp != str(g["inputs"]):
         raise RuntimeError(f"{name}: the GPU leg started from a different initial field")
+    if keep:
+        np.savez(Path(gpu_dir) / f"{name}_oracle.npz", psi=psi, res=res, norms=norms)
     return name, {
         "method": "rk4-fdm" if method == "rk4" else "split-step-fft (CPU ordering)",
         "precision": "complex64" if precision == "single" else "complex128",
@@ -161,10 +163,12 @@ def _compare(job):
     }
 
 
-def oracle_leg(gpu_dir, out_json, jobs=4, cases=CASES):
+def oracle_leg(gpu_dir, out_json, jobs=4, cases=CASES, keep=False):
+    """Oracle runs for every device file in gpu_dir (``keep``: also save the oracle's final
+    state and norms beside it as <case>_oracle.npz)."""
     import multiprocessing as mp
 
-    work = [(str(gpu_dir), m, p) for m, p in cases
+    work = [(str(gpu_dir), m, p, keep) for m, p in cases
             if (Path(gpu_dir) / f"{case_name(m, p)}.npz").exists()]
     if jobs <= 1 or len(work) <= 1:
         results = dict(map(_compare, work))
@@ -194,11 +198,13 @@ def main(argv=None):
     o.add_argument("--gpu", required=True)
     o.add_argument("--out", required=True)
     o.add_argument("--jobs", type=int, default=int(os.environ.get("PG_ORACLE_JOBS", "4")))
+    o.add_argument("--cases", nargs="+", default=[case_name(m, p) for m, p in CASES])
+    o.add_argument("--keep", action="store_true", help="save the oracle states too")
     a = ap.parse_args(argv)
     if a.leg == "gpu":
         gpu_leg(a.out, a.steps, a.grid, [c for c in CASES if case_name(*c) in a.cases])
     else:
-        oracle_leg(a.gpu, a.out, a.jobs)
+        oracle_leg(a.gpu, a.out, a.jobs, [c for c in CASES if case_name(*c) in a.cases], a.keep)
 
 
 if __name__ == "__main__":
