@@ -246,7 +246,14 @@ class _GB300Solver(AbstractSolver):
         return engine.get_state()
 
     def _finish(self, model, state, res, n_steps):
-        if self._reservoir_type == "single":
+        # Every kernel leaves n_R clamped at zero at the end of a step, as the reservoir's
+        # set_state would.  When the result went in place into the reservoir's own host array
+        # (inplace_host), handing it back through set_state would only repeat that clamp over
+        # the whole array (for 32 x 1024^2 sites as long as 64 device steps), so it is skipped.
+        if (self.inplace_host and self._reservoir_type == "single" and isinstance(res, np.ndarray)
+                and res is model.reservoir.get_state()[0]):
+            pass
+        elif self._reservoir_type == "single":
             model.reservoir.set_state((res,))
         elif self._reservoir_type in ("double", "quadratic-double"):
             model.reservoir.set_state((res[0], res[1]))
