@@ -6,7 +6,11 @@
 // increment of rk4_cuda_solver.py:518-532), mapped differently onto the SM:
 //
 // * A block spans the whole periodic row (2 columns per thread, nx/2 threads), so
-//   there is no horizontal halo and 1024-wide rows use 16 balanced warps.
+//   there is no horizontal halo and 1024-wide rows use 16 balanced warps.  Wider rows
+//   split into 1024-column bands: a cluster of CTAs per row range (one band each, the two
+//   edge columns of stages 2-4 pushed to the neighbouring CTA's shared memory with
+//   st.async), or past the portable cluster size, independent blocks that recompute a
+//   four-column halo.
 // * Rows of psi0, n0 and the pump envelope stream into an 8-row shared-memory ring
 //   through 1-D bulk copies (TMA) that complete on per-slot mbarriers, three rows
 //   ahead of use.  Stage 1 reads its whole stencil straight from the ring; stages 2-4
@@ -16,8 +20,9 @@
 //   by up to a row.
 // * Complex arithmetic uses packed FP32x2 instructions (__ffma2_rn and friends).
 // * Blocks are persistent: block c advances rows [c R / G, (c+1) R / G) of the
-//   member-major row space (R = members * ny rows), restarting the 4-row pipeline
-//   fill whenever it crosses into the next member.
+//   member-major row space (R = members * ny rows; BAND: members * bands * ny; CLUSTER:
+//   c and G count clusters), restarting the 4-row pipeline fill whenever it crosses into
+//   the next member (or band).
 #include <algorithm>
 
 #include "philox.cuh"
