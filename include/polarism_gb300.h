@@ -238,7 +238,9 @@ int pg_field_norms_noalloc(const void* psi, int32_t precision, int32_t members,
 
 /* Choose the RK4 kernel: 0 automatic, 1 the tiled streaming kernel (any size, FP32/FP64,
  * potential and relaxation terms), 2 the full-width FP32 kernel (nx in {128, 256, 512, 1024},
- * single reservoir, no potential).  pg_rk4_get_kernel reports the one in use (1 or 2). */
+ * or a multiple of 1024 up to 16384 in 1024-site bands; single reservoir, one laser; real or
+ * complex potential and kinetic relaxation in its general variant).  pg_rk4_get_kernel
+ * reports the one in use (1 or 2). */
 int pg_rk4_set_kernel(pg_solver* s, int32_t kind);
 int pg_rk4_get_kernel(pg_solver* s, int32_t* kind);
 

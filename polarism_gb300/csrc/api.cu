@@ -462,7 +462,7 @@ int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
                  pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny),
              PG_ERR_UNSUPPORTED,
              "pg_rk4_set_kernel: the full-width kernel needs FP32, a single reservoir, one laser "
-             "and nx in {128, 256, 512, 1024}");
+             "and nx in {128, 256, 512, 1024} or a multiple of 1024 up to 16384");
   }
   s->rk4_kernel = kind;
   free_graphs(s);
