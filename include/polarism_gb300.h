@@ -73,7 +73,7 @@ typedef struct pg_config {
   int32_t nx, ny;          /* periodic grid */
   int32_t members;         /* batch size B */
   int32_t precision;       /* PG_SINGLE (complex64) or PG_DOUBLE (complex128) */
-  int32_t reservoir;       /* PG_RES_NONE or PG_RES_SINGLE */
+  int32_t reservoir;       /* PG_RES_NONE, PG_RES_SINGLE, PG_RES_DOUBLE or PG_RES_QDOUBLE */
   int32_t potential;       /* PG_POT_* */
   int32_t pump_per_member; /* 0: one envelope shared by all members; 1: one per member */
   int32_t potential_per_member;
