@@ -145,3 +145,28 @@ def test_device_resident_state(cuda_lib):
     assert state2.field.is_cuda
     assert np.array_equal(state2.field.cpu().numpy(), expect_psi)
     assert np.array_equal(model2.reservoir.nR.cpu().numpy(), expect_n)
+
+
+@pytest.mark.parametrize("solver_name", ["RK4CudaSolver", "SplitStepFFTSolver"])
+def test_in_place_host_results_match_default_path(cuda_lib, solver_name):
+    """``inplace_host``: results land in the caller's own psi and n_R arrays (no new arrays, no
+    second host clamp of n_R) and equal the default path's bit for bit across several calls."""
+    from polarism_gb300 import solvers
+    from polarism_gb300.host import build_simulation
+
+    cfg = _config("single")
+    members = _members(cfg, 2)
+    outs = []
+    for inplace in (False, True):
+        grid, model, state = build_simulation(cfg, members)
+        solver = getattr(solvers, solver_name)(cfg, grid, model)
+        solver.inplace_host = inplace
+        psi_buf, n_buf = state.field, model.reservoir.get_state()[0]
+        for _ in range(3):
+            solver.advance(model, state, 4)
+        if inplace:
+            assert state.field is psi_buf and model.reservoir.get_state()[0] is n_buf
+        assert np.all(model.reservoir.get_state()[0] >= 0)
+        outs.append((state.field.copy(), model.reservoir.get_state()[0].copy()))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
