@@ -303,7 +303,7 @@ def test_device_normals_within_error_bound(cuda_lib, precision):
 
 
 @pytest.mark.parametrize("pot_kind,per_member", [("complex", True), ("real", False), ("none", False)])
-@pytest.mark.parametrize("nx,ny,members", [(256, 24, 2), (1024, 12, 1), (2048, 12, 2)])
+@pytest.mark.parametrize("nx,ny,members", [(256, 24, 2), (1024, 12, 1), (2048, 12, 2), (4096, 6, 1)])
 def test_full_width_general_variant_matches_oracle_and_tiled(cuda_lib, pot_kind, per_member, nx, ny,
                                                              members):
     """The full-width kernel's general variant (potential and kinetic relaxation, Wigner noise
