@@ -242,6 +242,16 @@ def cpu_baseline(sample_steps=12):
                       "(restatement of the reference rk4-fdm + Wigner), 1 thread"}
 
 
+def rk4_workload_config(args, members, world):
+    """The RK4 workload's config keys, the same on both arms."""
+    return {"workload": f"rk4-cuda fused step, {NX}^2 periodic, lx=ly={LX:g}, dt=5e-4, "
+                        "single reservoir, Wigner noise on, complex64" +
+                        (f", {args.potential} potential" if args.potential != "none" else "") +
+                        (f", kinetic relaxation eta={args.eta:g}" if args.eta else ""),
+            "members": members, "global_members": members * world, "grid": [NY, NX],
+            "parallelism": f"replicas{world}"}
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm's CPU implementation on all host cores."""
     import multiprocessing as mp
@@ -253,11 +263,15 @@ def run_reference(args):
     workers = max(1, min(args.members, cores))
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
-        # Warm-up: every worker builds its inputs and runs one step.
+        # Warm-up: min(W, 3) rounds in which every worker (inputs built on its first round)
+        # runs one member's step; the full workload per step would take minutes per round.
         tasks = [(m, 1, "double", NX) for m in range(args.members)]
         chunk = max(1, args.members // workers)
-        pool.map(_cpu_member_steps, [(m, 1, "double", NX) for m in range(workers)], chunksize=1)
-        # Each timed step: one RK4 step of every member, members spread over the workers.
+        warm = max(1, min(args.warmup, 3))
+        for _ in range(warm):
+            pool.map(_cpu_member_steps, [(m, 1, "double", NX) for m in range(workers)], chunksize=1)
+        # Each timed step: one RK4 step of every member, members spread over the workers; at
+        # most three, so that the arm ends within a few minutes (the line reports the count).
         budget_steps = max(1, min(args.steps, 3))
         t0 = time.perf_counter()
         for _ in range(budget_steps):
@@ -266,10 +280,11 @@ def run_reference(args):
     value = budget_steps * args.members * NX * NY / elapsed
     line = {
         "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world,
-        "steps": budget_steps, "warmup": 1, "ms_per_step": 1e3 * elapsed / budget_steps,
+        "steps": budget_steps, "warmup": warm, "ms_per_step": 1e3 * elapsed / budget_steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": f"rk4 {NX}^2 x {args.members} members, Wigner on", "members": args.members},
+        "config": dict(rk4_workload_config(args, args.members, world),
+                       kernel="reference CPU path (FP64 NumPy port of rk4-fdm + Wigner)"),
         "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": workers, "kind": "port",
                          "sample": f"{budget_steps} RK4 steps of {args.members} members at {NX}^2, "
                                    f"FP64 NumPy oracle port, {workers} worker processes"},
@@ -369,13 +384,8 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"rk4-cuda fused step, {NX}^2 periodic, lx=ly={LX:g}, dt=5e-4, "
-                               "single reservoir, Wigner noise on, complex64" +
-                               (f", {args.potential} potential" if args.potential != "none" else "") +
-                               (f", kinetic relaxation eta={args.eta:g}" if args.eta else ""),
-                   "members": members, "global_members": members * world, "grid": [NY, NX],
-                   "parallelism": f"replicas{world}", "kernel": kernel_name,
-                   "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
+        "config": dict(rk4_workload_config(args, members, world), kernel=kernel_name,
+                       l2="inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)),
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,

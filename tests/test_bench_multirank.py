@@ -62,3 +62,26 @@ def test_uneven_members_are_balanced_by_sites():
     assert sorted(m for p in parts for m in p) == list(range(len(sites)))
     loads = [sum(sites[m] for m in p) for p in parts]
     assert max(loads) - min(loads) <= 512 ** 2
+
+
+def test_reference_arm_line_on_cpu():
+    """``--impl reference`` on CPU: one JSON line with the same metric, unit and config keys as
+    the GPU arm, a cpu_baseline describing the run and an e2e entry without host copies."""
+    import json
+    import subprocess
+    import sys
+
+    from tests.conftest import ROOT
+
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--grid", "64",
+                          "--members", "2", "--steps", "1", "--warmup", "3"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"].startswith("RK4 site-updates/s")
+    assert line["unit"] == "site-updates/s" and line["higher_is_better"] is True
+    assert line["warmup"] == 3 and line["steps"] == 1 and line["value"] > 0
+    assert line["config"]["grid"] == [64, 64] and line["config"]["members"] == 2
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "site-updates/s",
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
