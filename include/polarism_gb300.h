@@ -38,7 +38,7 @@ extern "C" {
 #define PG_OK 0
 #define PG_ERR_INVALID 1     /* bad argument or unsupported configuration */
 #define PG_ERR_CUDA 2        /* a CUDA runtime call failed */
-#define PG_ERR_UNSUPPORTED 3 /* feature not available in this build */
+#define PG_ERR_UNSUPPORTED 3 /* configuration the kernels do not support */
 #define PG_ERR_TIMEOUT 4     /* a bounded device wait gave up */
 
 #define PG_SINGLE 0
