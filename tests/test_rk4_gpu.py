@@ -226,13 +226,14 @@ def test_launch_count_and_error_status(cuda_lib):
 
 
 @pytest.mark.parametrize("nx,ny,members", [(128, 48, 3), (256, 20, 2), (512, 12, 2), (1024, 8, 1),
-                                            (2048, 40, 1), (3072, 10, 1), (4096, 6, 2), (9216, 6, 1)])
+                                            (2048, 40, 1), (3072, 10, 1), (4096, 6, 2), (8192, 4, 1),
+                                            (9216, 6, 1)])
 def test_full_width_kernel_matches_oracle_and_tiled(cuda_lib, nx, ny, members):
     """The TMA full-width FP32 kernel against the oracle (1e-4) and the tiled kernel (1e-5).
 
     Rows of 2048 to 8192 sites run as clusters of 1024-site bands exchanging edge columns
-    through distributed shared memory (clusters of 2, 3 and 4 here, with row ranges that cross
-    members); wider rows (9216) as independent bands with four recomputed halo columns on each
+    through distributed shared memory (clusters of 2, 3, 4 and 8 here, with row ranges that
+    cross members); wider rows (9216) as independent bands with four recomputed halo columns on each
     side, whose row ranges cross from one band into the next.  Both cover the periodic wrap
     of the first and last band."""
     from polarism_gb300.engine import MemberPhysics, RK4Engine
