@@ -252,8 +252,16 @@ def rk4_workload_config(args, members, world):
             "parallelism": f"replicas{world}"}
 
 
+REFERENCE_ARM_BUDGET_S = 240.0  # longest the reference arm's timed steps may take
+
+
 def run_reference(args):
-    """--impl reference: the reference algorithm's CPU implementation on all host cores."""
+    """--impl reference: the reference algorithm's CPU implementation on all host cores.
+
+    A step is one RK4 step of every member (the GPU arm's step), the members spread over one
+    worker process per core.  W warm-up steps and K timed steps run as asked; only when K
+    steps would take longer than REFERENCE_ARM_BUDGET_S (estimated from the warm-up) does the
+    arm time fewer, and the line's ``steps`` and ``same_steps`` say so."""
     import multiprocessing as mp
 
     rank, world, _ = dist_info()
@@ -262,32 +270,37 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     workers = max(1, min(args.members, cores))
     ctx = mp.get_context("spawn")
+    tasks = [(m, 1, "double", NX) for m in range(args.members)]
+    chunk = max(1, math.ceil(args.members / workers))
     with ctx.Pool(workers) as pool:
-        # Warm-up: min(W, 3) rounds in which every worker (inputs built on its first round)
-        # runs one member's step; the full workload per step would take minutes per round.
-        tasks = [(m, 1, "double", NX) for m in range(args.members)]
-        chunk = max(1, args.members // workers)
-        warm = max(1, min(args.warmup, 3))
-        for _ in range(warm):
-            pool.map(_cpu_member_steps, [(m, 1, "double", NX) for m in range(workers)], chunksize=1)
-        # Each timed step: one RK4 step of every member, members spread over the workers; at
-        # most three, so that the arm ends within a few minutes (the line reports the count).
-        budget_steps = max(1, min(args.steps, 3))
+        # Every worker builds its inputs on its first task, outside any timed step.
+        pool.map(_cpu_member_steps, [(m, 1, "double", NX) for m in range(workers)], chunksize=1)
+        warm = max(1, args.warmup)
         t0 = time.perf_counter()
-        for _ in range(budget_steps):
+        for k in range(warm):
+            pool.map(_cpu_member_steps, tasks, chunksize=chunk)
+            if time.perf_counter() - t0 > REFERENCE_ARM_BUDGET_S / 4:
+                warm = k + 1
+                break
+        per_step = (time.perf_counter() - t0) / warm
+        steps = max(1, min(args.steps, int(REFERENCE_ARM_BUDGET_S // max(per_step, 1e-9))))
+        t0 = time.perf_counter()
+        for _ in range(steps):
             pool.map(_cpu_member_steps, tasks, chunksize=chunk)
         elapsed = time.perf_counter() - t0
-    value = budget_steps * args.members * NX * NY / elapsed
+    value = steps * args.members * NX * NY / elapsed
     line = {
         "metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world,
-        "steps": budget_steps, "warmup": warm, "ms_per_step": 1e3 * elapsed / budget_steps,
+        "steps": steps, "warmup": warm, "same_steps": steps == args.steps and warm == args.warmup,
+        "ms_per_step": 1e3 * elapsed / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
         "config": dict(rk4_workload_config(args, args.members, world),
                        kernel="reference CPU path (FP64 NumPy port of rk4-fdm + Wigner)"),
         "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": workers, "kind": "port",
-                         "sample": f"{budget_steps} RK4 steps of {args.members} members at {NX}^2, "
-                                   f"FP64 NumPy oracle port, {workers} worker processes"},
+                         "sample": f"{steps} RK4 steps of {args.members} members at {NX}^2 after "
+                                   f"{warm} warm-up steps, FP64 NumPy oracle port, {workers} "
+                                   "worker processes"},
         "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -319,8 +332,10 @@ def run_ours(args):
     eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**physics), "single",
                     pump_per_member=True, potential=pot_kind)
     if args.rk4_kernel != "auto":
-        eng.set_kernel(2 if args.rk4_kernel == "wide" else 1)
+        eng.set_kernel({"wide": 2, "tiled": 1, "wide2": 3}[args.rk4_kernel])
     kernel_name = ("tiled" if eng.kernel() == 1 else
+                   "full-width, four sites a thread" if NX in (512, 1024) and eng.kernel() == 2
+                   and args.potential == "none" and not args.eta else
                    "full-width" if NX <= 1024 else
                    f"full-width, clusters of {NX // 1024} CTAs (1024-site bands)" if NX <= 8192 else
                    "full-width, 1024-site bands with recomputed halo")
@@ -428,18 +443,20 @@ def run_e2e(args, w, members, torch):
     chunk = 64
     solver.advance(model, state, chunk)  # warm-up: uploads pump/noise, captures graphs
 
-    calls = max(1, min(args.e2e_calls, 1 + args.steps // chunk))
+    calls = max(2, args.e2e_calls)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(calls):
         solver.advance(model, state, chunk)
     elapsed = time.perf_counter() - t0
     sites = members * NX * NY
-    h2d = sites * (8 + 4)
+    per_call = sites * (8 + 4)  # psi (complex64) and n_R (float32), each way, every call
     return {"value": sites * chunk * calls / elapsed, "unit": "site-updates/s",
-            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-            "step": f"one RK4CudaSolver.advance call of {chunk} steps on pinned host state",
-            "calls": calls}
+            "h2d_bytes_per_step": per_call / chunk, "d2h_bytes_per_step": per_call / chunk,
+            "h2d_bytes_per_call": per_call, "d2h_bytes_per_call": per_call,
+            "step": f"{calls} RK4CudaSolver.advance calls of {chunk} RK4 steps each on pinned "
+                    "host state (bytes per step = bytes per call / steps per call)",
+            "calls": calls, "steps_per_call": chunk}
 
 
 # ----------------------------------------------------------------------------- split-step leg
@@ -511,7 +528,7 @@ def run_split_bench(args):
     psi_host[...] = w["psi"]
     n_host[...] = w["n"]
     chunk = 64
-    calls = max(1, min(args.e2e_calls, 1 + args.steps // chunk))
+    calls = max(2, args.e2e_calls)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for c in range(calls):
@@ -540,9 +557,11 @@ def run_split_bench(args):
                      "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                      "algorithmic_bytes_per_site": bytes_per_site},
         "e2e": {"value": sites * chunk * calls / e2e_s, "unit": "site-updates/s",
-                "h2d_bytes_per_step": sites * 12, "d2h_bytes_per_step": sites * 12,
-                "step": f"set_state + {chunk} split steps + get_state from pinned host arrays",
-                "calls": calls},
+                "h2d_bytes_per_step": sites * 12 / chunk, "d2h_bytes_per_step": sites * 12 / chunk,
+                "h2d_bytes_per_call": sites * 12, "d2h_bytes_per_call": sites * 12,
+                "step": f"{calls} calls of set_state + {chunk} split steps + get_state from pinned "
+                        "host arrays (bytes per step = bytes per call / steps per call)",
+                "calls": calls, "steps_per_call": chunk},
         "clocks": clocks,
     }
     if world == 1 and not args.no_cpu_baseline:
@@ -904,9 +923,10 @@ def main():
                     help="rk4 workload: add a trap (and an absorbing rim) potential")
     ap.add_argument("--eta", type=float, default=0.0,
                     help="rk4 workload: kinetic relaxation eta (the general kernel variant)")
-    ap.add_argument("--rk4-kernel", choices=["auto", "wide", "tiled"], default="auto",
-                    help="rk4 workload: the full-width TMA kernel, the tiled kernel, or the "
-                         "engine's choice")
+    ap.add_argument("--rk4-kernel", choices=["auto", "wide", "tiled", "wide2"], default="auto",
+                    help="rk4 workload: the full-width TMA kernel (wide; four sites a thread on "
+                         "512- and 1024-site rows), the same with two sites a thread (wide2), "
+                         "the tiled kernel, or the engine's choice")
     ap.add_argument("--split-ordering", choices=["kouter", "cpu"], default="kouter",
                     help="split workload: K-outer (split-step-fft-cuda) or CPU ordering")
     ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno"], default="rk4",

@@ -30,6 +30,33 @@ ACCUMULATORS = {
     "momentum-distribution": (("k", "sum_k"),),
 }
 
+#: reservoir type -> the reservoir's ``state_names``, the order of its fields in the engine
+#: (``single_reservoir.py:24``, ``double_reservoir.py:24``, ``quadratic_double_reservoir.py:43``,
+#: ``no_reservoir.py:12``)
+STATE_NAMES = {
+    "single": ("nR",),
+    "double": ("nA", "nI"),
+    "quadratic-double": ("nR", "nI"),
+    "none": (),
+}
+
+
+def reservoir_fields(ckpt):
+    """The checkpoint's reservoir fields in the engine's order.
+
+    A file stores them by name and HDF5 lists a group's members alphabetically, so the order
+    comes from the reservoir type's ``state_names``; as ``load_checkpoint`` does
+    (``simulation_controller.py:858-861``), a name set other than that type's is an error."""
+    stored = ckpt["reservoir"]
+    kind = str(ckpt["attrs"].get("reservoir_type", ""))
+    names = STATE_NAMES.get(kind)
+    if names is None:  # a reservoir this library does not model: keep the stored order
+        return [np.asarray(v) for v in stored.values()]
+    if set(stored) != set(names):
+        raise ValueError(f"checkpoint reservoir names mismatch: {sorted(stored)} stored, "
+                         f"{list(names)} expected for reservoir type {kind!r}")
+    return [np.asarray(stored[n]) for n in names]
+
 
 def _public(array, batched, components):
     """(B, C, ...) engine layout -> the reference's public shape."""
@@ -97,8 +124,8 @@ def restore(engine, ckpt):
     if step < 0 or not math.isclose(t, t0 + step * dt, rel_tol=0.0, abs_tol=1e-9 * max(1.0, abs(t))):
         raise ValueError("checkpoint time and step mismatch")
     field = np.asarray(ckpt["data"]["field"])
-    fields = [np.asarray(v) for v in ckpt["reservoir"].values()]
-    res = fields[0] if len(fields) == 1 else np.stack(fields)
+    fields = reservoir_fields(ckpt)
+    res = fields[0] if len(fields) == 1 else np.stack(fields) if fields else None
     engine.set_state(np.ascontiguousarray(field, dtype=engine.complex),
                      np.ascontiguousarray(res, dtype=engine.real) if fields else None)
     stop_time = np.asarray(attrs.get("stop_time", np.full(engine.members, np.nan)), dtype=float)

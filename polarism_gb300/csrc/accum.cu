@@ -644,7 +644,11 @@ int pg_field_norms(const void* psi, int32_t precision, int32_t members, int64_t 
 // the GPU (different streams or host threads) race on it and must be serialised by the
 // caller.  The first call on each device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call before any stream
-// capture.
+// capture.  The address is cached per device for the life of the process: after
+// cudaDeviceReset (which unloads this module's device copy) the cache is stale, so a process
+// that resets a device must not call this entry point on it again.  Two host threads making
+// their first call on the same device at once both look the address up and store the same
+// value, so the unsynchronised cache write is harmless.
 namespace pg {
 namespace {
 

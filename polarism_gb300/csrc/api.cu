@@ -180,6 +180,13 @@ bool use_wide(const pg_solver* s) {
   return eligible;
 }
 
+// The full-width kernel's four-sites-a-thread form: rows of 512 or 1024 sites, no potential
+// or relaxation, unless the two-site form was chosen (kernel kind 3).
+bool use_quad(const pg_solver* s, const pg::WideGeom& w) {
+  return s->rk4_kernel != 3 && s->quad_blocks > 0 && !pg::wide_general(w) &&
+         pg::quad_rk4_supported(s->cfg.nx, s->cfg.ny);
+}
+
 // Launch one RK4 step reading buffers of parity `from`; step_offset indexes the chunk scales.
 cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
   const int to = 1 - from;
@@ -196,6 +203,16 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
     w.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
     w.pot_kind = f.potential;
     w.relax = f.relax;
+    if (use_quad(s, w)) {
+      w.blocks = s->quad_blocks;
+      return pg::launch_rk4_quad(static_cast<const float*>(s->psi[from]),
+                                 static_cast<const float*>(s->res[from]),
+                                 static_cast<const float*>(s->pump), static_cast<float*>(s->psi[to]),
+                                 static_cast<float*>(s->res[to]),
+                                 static_cast<const pg::RhsConst<float>*>(s->consts),
+                                 static_cast<const float*>(s->scales), s->step_base, step_offset,
+                                 static_cast<float>(s->cfg.dt), s->noise, w, s->err_flag, s->stream);
+    }
     return pg::launch_rk4_wide(static_cast<const float*>(s->psi[from]),
                                static_cast<const float*>(s->res[from]),
                                static_cast<const float*>(s->pump), static_cast<float*>(s->psi[to]),
@@ -380,6 +397,10 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   if (cfg->precision == PG_SINGLE && pg::wide_rk4_supported(cfg->nx, cfg->ny)) {
     if ((e = pg::configure_wide_rk4()) != cudaSuccess) return fail(e, "wide kernel attributes");
     s->wide_blocks = pg::wide_rk4_grid(cfg->nx, cfg->ny, cfg->members, s->sm_count);
+    if (pg::quad_rk4_supported(cfg->nx, cfg->ny)) {
+      if ((e = pg::configure_quad_rk4()) != cudaSuccess) return fail(e, "quad kernel attributes");
+      s->quad_blocks = pg::quad_rk4_grid(cfg->nx, cfg->ny, cfg->members, s->sm_count);
+    }
   }
   const size_t staging_bytes = static_cast<size_t>(kChunk) * 3 * s->pump_terms * cfg->members * 8 + 64;
   for (auto& slot : s->staging) {
@@ -455,8 +476,9 @@ int pg_get_state(pg_solver* s, void* psi, void* res, int on_device) {
 
 int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
   PG_CHECK(s, PG_ERR_INVALID, "pg_rk4_set_kernel: null solver");
-  PG_CHECK(kind >= 0 && kind <= 2, PG_ERR_INVALID, "pg_rk4_set_kernel: kind must be 0, 1 or 2");
-  if (kind == 2) {
+  PG_CHECK(kind >= 0 && kind <= 3, PG_ERR_INVALID,
+           "pg_rk4_set_kernel: kind must be 0, 1, 2 or 3");
+  if (kind >= 2) {
     const pg::RK4Features f = features(s);
     PG_CHECK(s->cfg.precision == PG_SINGLE && f.reservoir == 1 && f.pump_terms == 1 &&
                  pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny),
@@ -471,7 +493,7 @@ int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
 
 int pg_rk4_get_kernel(pg_solver* s, int32_t* kind) {
   PG_CHECK(s && kind, PG_ERR_INVALID, "pg_rk4_get_kernel: null argument");
-  *kind = use_wide(s) ? 2 : 1;
+  *kind = !use_wide(s) ? 1 : s->rk4_kernel == 3 ? 3 : 2;
   return PG_OK;
 }
 

@@ -53,8 +53,10 @@ struct pg_solver {
   // at once, so steps queued after the last member stopped leave the state as it was.
   int* halt = nullptr;
   long long parity_step = 0;  // absolute step whose state sits under `cur` after pg_rk4_advance
-  int rk4_kernel = 0;        // 0 auto, 1 tiled streaming kernel, 2 full-width kernel
+  int rk4_kernel = 0;        // 0 auto, 1 tiled streaming kernel, 2 full-width kernel,
+                             // 3 full-width kernel in its two-sites-a-thread form
   int wide_blocks = 0;       // persistent grid of the full-width kernel
+  int quad_blocks = 0;       // persistent grid of its four-sites-a-thread form
   // Split-step state.
   bool spectral = false;      // psi holds the unnormalised 2-D spectrum instead of psi(x, y)
   bool split_ready = false;

@@ -30,6 +30,16 @@ cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float*
                             const float* scales, const unsigned long long* step_base,
                             int step_offset, float dt, bool noise, const WideGeom& g,
                             int* err_flag, cudaStream_t stream);
+// Four sites a thread (rk4_quad.cu): rows of 512 or 1024 sites without a potential or
+// kinetic relaxation; bitwise the same results as launch_rk4_wide.
+bool quad_rk4_supported(int nx, int ny);
+cudaError_t configure_quad_rk4();
+int quad_rk4_grid(int nx, int ny, int members, int sm_count);
+cudaError_t launch_rk4_quad(const float* psi_in, const float* n_in, const float* pump,
+                            float* psi_out, float* n_out, const RhsConst<float>* consts,
+                            const float* scales, const unsigned long long* step_base,
+                            int step_offset, float dt, bool noise, const WideGeom& g,
+                            int* err_flag, cudaStream_t stream);
 // The general variant runs when the geometry asks for a potential or kinetic relaxation.
 inline bool wide_general(const WideGeom& g) { return g.pot_kind != 0 || g.relax != 0; }
 

@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this folder by running the reference itself.
 
-Run in a container that has the Polarism reference source tree::
+Run where the Polarism v0.9.2 source tree is available, naming it::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py PATH/TO/POLARISM     # or set POLARISM_REFERENCE
 
 Every fixture records both the inputs (initial fields, pump arrays at the
 stage times, physics constants) and the reference's outputs, so the tests can
@@ -46,11 +46,15 @@ class _InertModules(importlib.abc.MetaPathFinder, importlib.abc.Loader):
         return None
 
 
-def reference_root() -> str:
-    """Location of the Polarism source tree (``POLARISM_REFERENCE`` overrides it)."""
+def reference_root() -> str | None:
+    """Location of the Polarism source tree: ``POLARISM_REFERENCE`` when set, else a checkout
+    named ``reference`` beside this repository's directory, else None."""
     import os
 
-    return os.environ.get("POLARISM_REFERENCE", "/root/reference")
+    if os.environ.get("POLARISM_REFERENCE"):
+        return os.environ["POLARISM_REFERENCE"]
+    beside = Path(__file__).resolve().parents[3] / "reference"
+    return str(beside) if (beside / "polarism" / "__init__.py").exists() else None
 
 
 def _import_reference(root: str):
@@ -429,4 +433,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else reference_root())
+    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if root is None:
+        sys.exit("usage: make_golden.py PATH/TO/POLARISM (or set POLARISM_REFERENCE)")
+    main(root)

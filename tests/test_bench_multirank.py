@@ -74,13 +74,14 @@ def test_reference_arm_line_on_cpu():
     from tests.conftest import ROOT
 
     out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--grid", "64",
-                          "--members", "2", "--steps", "1", "--warmup", "3"],
+                          "--members", "2", "--steps", "2", "--warmup", "3"],
                          cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     line = json.loads(out.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["metric"].startswith("RK4 site-updates/s")
     assert line["unit"] == "site-updates/s" and line["higher_is_better"] is True
-    assert line["warmup"] == 3 and line["steps"] == 1 and line["value"] > 0
+    assert line["warmup"] == 3 and line["steps"] == 2 and line["same_steps"] is True
+    assert line["value"] > 0
     assert line["config"]["grid"] == [64, 64] and line["config"]["members"] == 2
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": "site-updates/s",

@@ -59,3 +59,42 @@ def test_h5_layout_matches_save_checkpoint(tmp_path):
 def test_accumulator_names_follow_the_reference():
     assert set(checkpoint.ACCUMULATORS) == {"g2", "momentum-distribution"}
     assert [k for _, k in checkpoint.ACCUMULATORS["g2"]] == ["sum_density", "sum_density_squared"]
+
+
+class _RecordingEngine:
+    """Stands in for an engine: records what restore() hands it."""
+
+    members, ny, nx = 3, 4, 8
+    complex, real = np.complex128, np.float64
+
+    def set_state(self, psi, res):
+        self.psi, self.res = psi, res
+
+    def steady_import(self, density, norms, stops):
+        self.stops = stops
+
+    def accumulator_load(self, kind, sums, samples):
+        pass
+
+
+def test_restore_orders_quadratic_double_fields_by_state_names():
+    """A quadratic-double reservoir's state_names are ('nR', 'nI'); an HDF5 group lists them
+    alphabetically ('nI', 'nR'), so restore must take the order from the reservoir type."""
+    ck = _ckpt()
+    ck["attrs"]["reservoir_type"] = "quadratic-double"
+    n_r, n_i = ck["reservoir"]["nA"], ck["reservoir"]["nI"]
+    ck["reservoir"] = {"nI": n_i, "nR": n_r}  # the order h5py iterates a group in
+    eng = _RecordingEngine()
+    assert checkpoint.restore(eng, ck) == 40
+    assert np.array_equal(eng.res[0], n_r) and np.array_equal(eng.res[1], n_i)
+    ck["attrs"]["reservoir_type"] = "double"
+    ck["reservoir"] = {"nI": n_i, "nA": n_r}
+    checkpoint.restore(eng, ck)
+    assert np.array_equal(eng.res[0], n_r) and np.array_equal(eng.res[1], n_i)
+
+
+def test_restore_rejects_reservoir_names_of_another_type():
+    ck = _ckpt()
+    ck["attrs"]["reservoir_type"] = "quadratic-double"  # stored names are nA / nI
+    with pytest.raises(ValueError, match="reservoir names mismatch"):
+        checkpoint.restore(_RecordingEngine(), ck)

@@ -116,8 +116,9 @@ def _reference_importable():
         import make_golden  # noqa: F401
         from pathlib import Path
 
-        root = Path(make_golden.reference_root())
-        if not (root / "polarism" / "__init__.py").exists():
+        found = make_golden.reference_root()
+        root = Path(found) if found else None
+        if root is None or not (root / "polarism" / "__init__.py").exists():
             return None
         make_golden._import_reference(str(root))
         return root

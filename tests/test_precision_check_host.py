@@ -24,3 +24,22 @@ def test_oracle_leg_reports_errors_of_a_device_file(tmp_path):
     np.savez(tmp_path / "rk4_fp32.npz", **g)
     r = pc.oracle_leg(tmp_path, tmp_path / "r.json", jobs=1)["rk4_fp32"]
     assert abs(r["psi_rel_l2"] - 1e-3) < 1e-9 and not r["pass"]
+
+
+def test_committed_oracle_fixtures_start_from_the_workload_and_match_the_oracle():
+    """The full-size fixtures (tests/golden/precision_*.npz, written by
+    make_precision_golden.py) belong to this workload: same initial field (fingerprint),
+    1000 norms, 128^2 sampled sites, and the oracle's first two steps reproduce their first
+    two norms."""
+    from tests import precision_check as pc
+    from tests.conftest import load_golden
+
+    fp = pc.fingerprint(pc.inputs(pc.N)[4])
+    for method, precision in pc.CASES:
+        g = load_golden(f"precision_{pc.case_name(method, precision)}")
+        assert str(g["inputs"]) == fp
+        assert g["norms"].shape == (pc.STEPS,) and int(g["steps"]) == pc.STEPS
+        assert g["psi"].shape == (128, 128) and g["res"].shape == (128, 128)
+        assert np.all(g["res"] >= 0) and np.all(np.isfinite(g["psi"]))
+        _, _, norms, _ = pc.oracle_case(method, precision, 2, pc.N)
+        np.testing.assert_allclose(norms, g["norms"][:2], rtol=1e-13)

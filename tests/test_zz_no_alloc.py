@@ -44,6 +44,29 @@ def test_noalloc_norms_match_allocating_entry_point_twice():
         np.testing.assert_allclose(got, expect, rtol=1e-12, atol=0)
 
 
+def test_noalloc_norms_with_fewer_blocks_than_the_allocating_call_match_fp64_numpy():
+    """48 members of 512 x 1024 sites: the allocating call uses 256 blocks a member, the
+    fixed array holds only 8192 / 48 = 170, so this case runs the clamped block count.  Both
+    calls are checked against FP64 NumPy sums of the same values, twice in a row."""
+    import torch
+
+    from polarism_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(7)
+    members, ny, nx, cell = 48, 512, 1024, 0.25
+    host = (rng.standard_normal((members, 1, ny, nx)) +
+            1j * rng.standard_normal((members, 1, ny, nx))).astype(np.complex64)
+    psi = torch.as_tensor(host, device="cuda")
+    h64 = host.astype(np.complex128)
+    expect = (np.abs(h64) ** 2).reshape(members, -1).sum(axis=1) * cell
+    for _ in range(2):
+        got = _norms(lib, "pg_field_norms_noalloc", psi, _lib.PG_SINGLE, members, ny * nx, cell)
+        np.testing.assert_allclose(got, expect, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(_norms(lib, "pg_field_norms", psi, _lib.PG_SINGLE, members, ny * nx, cell),
+                               expect, rtol=1e-12, atol=0)
+
+
 def test_noalloc_rejects_more_members_than_the_scratch_holds():
     import torch
 
