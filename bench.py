@@ -332,10 +332,9 @@ def run_ours(args):
     eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**physics), "single",
                     pump_per_member=True, potential=pot_kind)
     if args.rk4_kernel != "auto":
-        eng.set_kernel({"wide": 2, "tiled": 1, "wide2": 3}[args.rk4_kernel])
+        eng.set_kernel({"wide": 2, "tiled": 1, "wide4": 3}[args.rk4_kernel])
     kernel_name = ("tiled" if eng.kernel() == 1 else
-                   "full-width, four sites a thread" if NX in (512, 1024) and eng.kernel() == 2
-                   and args.potential == "none" and not args.eta else
+                   "full-width, four sites a thread" if eng.kernel() == 3 else
                    "full-width" if NX <= 1024 else
                    f"full-width, clusters of {NX // 1024} CTAs (1024-site bands)" if NX <= 8192 else
                    "full-width, 1024-site bands with recomputed halo")
@@ -923,10 +922,9 @@ def main():
                     help="rk4 workload: add a trap (and an absorbing rim) potential")
     ap.add_argument("--eta", type=float, default=0.0,
                     help="rk4 workload: kinetic relaxation eta (the general kernel variant)")
-    ap.add_argument("--rk4-kernel", choices=["auto", "wide", "tiled", "wide2"], default="auto",
-                    help="rk4 workload: the full-width TMA kernel (wide; four sites a thread on "
-                         "512- and 1024-site rows), the same with two sites a thread (wide2), "
-                         "the tiled kernel, or the engine's choice")
+    ap.add_argument("--rk4-kernel", choices=["auto", "wide", "tiled", "wide4"], default="auto",
+                    help="rk4 workload: the full-width TMA kernel (wide), the same with four "
+                         "sites a thread (wide4), the tiled kernel, or the engine's choice")
     ap.add_argument("--split-ordering", choices=["kouter", "cpu"], default="kouter",
                     help="split workload: K-outer (split-step-fft-cuda) or CPU ordering")
     ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno"], default="rk4",

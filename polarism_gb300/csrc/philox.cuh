@@ -134,12 +134,26 @@ __device__ __forceinline__ Words4 wigner_words(uint32_t cell, uint64_t step, uin
 template <typename T>
 struct WignerDraw;
 
-// Single precision uses the SFU approximations: -2 ln u1 = -2 ln2 log2(u1) (absolute
-// error of log2 below 2^-22 on [0.5, 2]), sqrt(x) = x rsqrt(x), and sin/cos of the angle
-// reduced exactly to (-pi, pi] (u2 - 1 is exact for u2 > 1/2; absolute error of the SFU
-// sine/cosine about 2^-21 there).  The resulting normals stay within a few 1e-6 of the
-// correctly rounded Box-Muller transform except at radii below ~1e-3 (u1 within 2^-20
-// of 1), where the error is bounded in absolute terms by ~1e-4 * sqrt(variance).
+// Single precision uses the SFU approximations.  With m1 = (a >> 8) + 1 and
+// m2 = (b >> 8) + 1 (integers in [1, 2^24], so u = m 2^-24):
+// * -2 ln u1 = -2 ln2 log2(u1) with the SFU log2 (absolute error below 2^-22 on [0.5, 2]; taken
+//   of u1 itself, not of m1, so that radii near 0 keep the fine absolute resolution of values
+//   near 1);
+// * the angle 2 pi u2 is reduced to (-pi, pi] in integers: m2 - 2^24 when bit 23 of m2 is
+//   set (u2 >= 1/2), which is the 24-bit sign extension of m2, then one multiply by
+//   2 pi 2^-24 (u2 = 1/2 maps to -pi instead of pi: the same cosine, a sine of the same tiny
+//   magnitude); SFU sine and cosine (absolute error about 2^-21 there);
+// * sqrt(variance (-2 ln u1)) by the SFU square root (relative error about 2^-23; exact 0
+//   at 0).
+// The normals stay within a few 1e-6 of the correctly rounded Box-Muller transform except at
+// radii below ~1e-3 (u1 within 2^-20 of 1), where the error is bounded in absolute terms by
+// ~1e-4 * sqrt(variance).
+__device__ __forceinline__ float sqrt_sfu(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 template <>
 struct WignerDraw<float> {
   static __device__ __forceinline__ float radius2(uint32_t a) {
@@ -147,14 +161,13 @@ struct WignerDraw<float> {
     return -1.3862943611198906f * __log2f(u1);  // -2 ln(u1)
   }
   static __device__ __forceinline__ void angle(uint32_t b, float* s, float* c) {
-    float u2 = static_cast<float>((b >> 8) + 1u) * 5.9604644775390625e-08f;
-    u2 = u2 > 0.5f ? u2 - 1.0f : u2;
-    __sincosf(6.283185307179586f * u2, s, c);
+    // ((b >> 8) + 1) << 8, reinterpreted as signed and shifted back: the 24-bit sign extension.
+    const int32_t m2 = static_cast<int32_t>((b & 0xFFFFFF00u) + 256u) >> 8;
+    __sincosf(static_cast<float>(m2) * 3.7450702829239286e-07f, s, c);  // 2 pi 2^-24
   }
   // Unit-variance normals (r cos theta, r sin theta) of one word quadruple.
   static __device__ __forceinline__ float2 unit(const Words4& w) {
-    const float r2 = radius2(w.a);
-    const float r = r2 > 0.0f ? r2 * rsqrtf(r2) : 0.0f;
+    const float r = sqrt_sfu(radius2(w.a));
     float s, c;
     angle(w.b, &s, &c);
     return make_float2(r * c, r * s);
@@ -167,8 +180,7 @@ struct WignerDraw<float> {
   // Adds sqrt(variance * r2) (cos, sin) to (re, im).
   static __device__ __forceinline__ void add(float variance, float r2, float s, float c, float& re,
                                              float& im) {
-    const float x = variance * r2;
-    const float amp = x > 0.0f ? x * rsqrtf(x) : 0.0f;
+    const float amp = sqrt_sfu(variance * r2);
     re = fmaf(amp, c, re);
     im = fmaf(amp, s, im);
   }

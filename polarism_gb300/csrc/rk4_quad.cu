@@ -1,5 +1,9 @@
 // Full-width fused RK4 step for FP32 rows of 512 or 1024 sites with four adjacent sites per
-// thread (the quad form of the full-width kernel in rk4_wide.cu).
+// thread: the four-site form of the full-width kernel in rk4_wide.cu, chosen with RK4 kernel
+// kind 3.  It executes about 27% fewer instructions per site than the two-site form but keeps
+// only eight warps on an SM (four sites need ~230 registers a thread), which leaves the stage
+// chains' latencies exposed: 124.7 against 130.8 G site-updates/s at 1024^2 x 32 with Wigner
+// noise, so the two-site form is the default.
 //
 // Same mathematics and, site by site, the same operation order as rk4_wide.cu and rk4.cu
 // (polarism/model.py:89-127, polarism/solver/rk4_fdm_solver.py:36-82,
@@ -214,6 +218,18 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
         const uint32_t parity = ((it + i) / kQRing) & 1u;
         if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kQWaitLimit)) timed_out = true;
 
+        // Philox words and the variance-free part of the Box-Muller draw of this
+        // iteration's output row (four cells), interleaved with the stages by the compiler.
+        float r2[4] = {0.f, 0.f, 0.f, 0.f}, sn[4] = {0.f, 0.f, 0.f, 0.f}, cs[4] = {0.f, 0.f, 0.f, 0.f};
+        if (NOISE) {
+          const uint32_t cell = static_cast<uint32_t>(row_out * NX + col0);
+          const uint32_t cells[4] = {cell, cell + 1u, cell + 2u, cell + 3u};
+          Words4 w[4];
+          philox_cells(cells, prefix, w);
+#pragma unroll
+          for (int s = 0; s < 4; ++s) WignerDraw<float>::prepare(w[s], r2[s], sn[s], cs[s]);
+        }
+
         // Stage 1 at row r-1 from the ring: k1 = f(psi0).
         float2 c[4], u[4], dv[4], d[4];
         load4(ring_psi + slot1 * NX + col0, c);
@@ -245,18 +261,6 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
           if (t == 0 && i + 3 < n_iter) issue(i + 3);
         }
         const float4* xin = xbuf + ((j + 1) & 1) * 3 * T;
-        // Philox words and the variance-free part of the Box-Muller draw of this iteration's
-        // output row (four cells), after the exchange wait: in the same straight-line code as
-        // stages 2-4, its integer and SFU work fills their dependency gaps.
-        float r2[4] = {0.f, 0.f, 0.f, 0.f}, sn[4] = {0.f, 0.f, 0.f, 0.f}, cs[4] = {0.f, 0.f, 0.f, 0.f};
-        if (NOISE) {
-          const uint32_t cell = static_cast<uint32_t>(row_out * NX + col0);
-          const uint32_t cells[4] = {cell, cell + 1u, cell + 2u, cell + 3u};
-          Words4 w[4];
-          philox_cells(cells, prefix, w);
-#pragma unroll
-          for (int s = 0; s < 4; ++s) WignerDraw<float>::prepare(w[s], r2[s], sn[s], cs[s]);
-        }
         // Stage 2 at row r-2: k2 = f(psi1).
         {
           const float2 L = make_float2(xin[lthr].z, xin[lthr].w);

@@ -84,4 +84,31 @@ __device__ __forceinline__ float2 axpy2(float h, float2 d, float2 y) {
   return __ffma2_rn(make_float2(h, h), d, y);
 }
 
+// site_rhs at two adjacent sites a (left) and b (right) of one row: L is a's left neighbour,
+// R is b's right neighbour.  The per-site scalars (nonlinear frequency, gain, reservoir
+// derivative) of the two sites run as packed FP32x2 instructions, each lane the same FP32
+// operation with the same rounding as site_rhs, so the results are bitwise those of two
+// site_rhs calls.  n2 and sp2 hold (a, b) reservoir values and pump products; returns the
+// (a, b) reservoir derivatives.
+__device__ __forceinline__ float2 pair_rhs(float2 ca, float2 cb, float2 L, float2 R, float2 upa,
+                                           float2 upb, float2 dna, float2 dnb, float2 n2,
+                                           float2 sp2, const WideConst& k, float2& da, float2& db) {
+  const float2 nla = __ffma2_rn(k.nay, __fadd2_rn(upa, dna), __fmul2_rn(k.nax, __fadd2_rn(L, cb)));
+  const float2 nlb = __ffma2_rn(k.nay, __fadd2_rn(upb, dnb), __fmul2_rn(k.nax, __fadd2_rn(ca, R)));
+  const float2 rho = make_float2(fmaf(ca.x, ca.x, ca.y * ca.y), fmaf(cb.x, cb.x, cb.y * cb.y));
+  const float2 w = __ffma2_rn(make_float2(k.gr, k.gr), n2,
+                              __ffma2_rn(make_float2(k.gc, k.gc), rho, make_float2(k.w0, k.w0)));
+  const float2 gl = __ffma2_rn(make_float2(k.half_R, k.half_R), n2,
+                               make_float2(-k.half_gC, -k.half_gC));
+  const float2 ua = __ffma2_rn(make_float2(w.x, w.x), ca, nla);
+  const float2 ub = __ffma2_rn(make_float2(w.y, w.y), cb, nlb);
+  da.x = fmaf(gl.x, ca.x, ua.y);
+  da.y = fmaf(gl.x, ca.y, -ua.x);
+  db.x = fmaf(gl.y, cb.x, ub.y);
+  db.y = fmaf(gl.y, cb.y, -ub.x);
+  // -(R rho + gamma_R) n + sP with the negation folded into the constants (exact).
+  return __ffma2_rn(__ffma2_rn(make_float2(-k.R, -k.R), rho, make_float2(-k.gamma_R, -k.gamma_R)),
+                    n2, sp2);
+}
+
 }  // namespace pg

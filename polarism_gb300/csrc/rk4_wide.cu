@@ -18,7 +18,11 @@
 //   one double-buffered shared exchange per row, ordered (for 1024-site rows) by a
 //   split arrive/wait mbarrier rather than a block-wide barrier, so warps drift apart
 //   by up to a row.
-// * Complex arithmetic uses packed FP32x2 instructions (__ffma2_rn and friends).
+// * Complex arithmetic uses packed FP32x2 instructions (__ffma2_rn and friends), and so do the
+//   per-site scalars of a thread's two sites (pair_rhs: density terms, gain, reservoir
+//   derivative, pump products, reservoir stage updates), lane for lane the scalar operations.
+// * The exchange holds each thread's two columns in two arrays, so a stage is published with
+//   two 8-byte stores straight from the register pairs the packed arithmetic produced.
 // * Blocks are persistent: block c advances rows [c R / G, (c+1) R / G) of the
 //   member-major row space (R = members * ny rows; BAND: members * bands * ny; CLUSTER:
 //   c and G count clusters), restarting the 4-row pipeline fill whenever it crosses into
@@ -78,8 +82,12 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
   float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][W]
   float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * W);  // [kRing][W]
   float* ring_p = ring_n + kRing * W;                              // [kRing][W]
-  float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * W);    // [2][3][HALF]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kBars]
+  // Exchange: each thread's first (xa) and second (xb) column of the three stage inputs,
+  // [parity][stage][thread]; two 8-byte stores a stage keep the values in the register pairs
+  // the packed arithmetic produced them in.
+  float2* xa = reinterpret_cast<float2*>(ring_p + kRing * W);  // [2][3][HALF]
+  float2* xb = xa + 6 * HALF;                                  // [2][3][HALF]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(xb + 6 * HALF);  // [kBars]
   const uint32_t xbar = smem_u32(&mbar[kRing]);
   // CLUSTER: at the end of each iteration the left neighbour's thread HALF-1 pushes its
   // right column's three stage values into in_left[parity] with st.async, completing on
@@ -136,20 +144,10 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
   const uint32_t right_bar = CLUSTER ? map_shared_rank(from_left, right_rank) : 0u;
   // Horizontal neighbours of stage s (0..2) from the exchange of parity `xb`: the left
   // neighbour's right column and the right neighbour's left column.
-  auto xchg = [&](int xb, int s, float2& lt, float2& rt) {
-    const float4* xin = xbuf + xb * 3 * HALF + s * HALF;
-    if (CLUSTER && t == 0) {
-      lt = in_left[xb * 3 + s];
-    } else {
-      const float4 L = xin[lthr];
-      lt = make_float2(L.z, L.w);
-    }
-    if (CLUSTER && t == HALF - 1) {
-      rt = in_right[xb * 3 + s];
-    } else {
-      const float4 Rr = xin[rthr];
-      rt = make_float2(Rr.x, Rr.y);
-    }
+  auto xchg = [&](int par, int s, float2& lt, float2& rt) {
+    const int o = (par * 3 + s) * HALF;
+    lt = CLUSTER && t == 0 ? in_left[par * 3 + s] : xb[o + lthr];
+    rt = CLUSTER && t == HALF - 1 ? in_right[par * 3 + s] : xa[o + rthr];
   };
   // CLUSTER edge threads: arm and wait for the neighbours' delivery of iteration g.
   auto receive = [&](unsigned g) {
@@ -223,10 +221,22 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         }
       }
     };
-    auto rhs = [&](float2 c, float2 lt, float2 rt, float2 up, float2 dn, float n, float sP,
-                   float2 v, float2& d) -> float {
-      if (GENERAL) return site_rhs_general(c, lt, rt, up, dn, n, sP, k, v.x, v.y, g.relax != 0, d);
-      return site_rhs(c, lt, rt, up, dn, n, sP, k, d);
+    // Right-hand side at the thread's two sites (a, b): L / R the outer neighbours, up / dn
+    // the rows above and below, n2 the reservoir pair, sP = s P the pump products, va / vb the
+    // potential (general variant); returns the reservoir derivatives.
+    auto rhs2 = [&](float2 ca, float2 cb, float2 L, float2 R, float2 upa, float2 upb, float2 dna,
+                    float2 dnb, float2 n2, float s, float2 P, float2 va, float2 vb, float2& da,
+                    float2& db) -> float2 {
+      if (GENERAL) {
+        const bool rl = g.relax != 0;
+        const float x = site_rhs_general(ca, L, cb, upa, dna, n2.x, __fmul_rn(s, P.x), k, va.x,
+                                         va.y, rl, da);
+        const float y = site_rhs_general(cb, ca, R, upb, dnb, n2.y, __fmul_rn(s, P.y), k, vb.x,
+                                         vb.y, rl, db);
+        return make_float2(x, y);
+      }
+      return pair_rhs(ca, cb, L, R, upa, upb, dna, dnb, n2, __fmul2_rn(make_float2(s, s), P), k,
+                      da, db);
     };
     float2* out_psi_m = psi_out + member * plane + gcol0w;
     float* out_n_m = n_out + member * plane + gcol0w;
@@ -287,19 +297,6 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         const int slot3 = (j + kRing - 3) % kRing;  // row r-3
         const int slot4 = (j + kRing - 4) % kRing;  // row r-4
         if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitLimit)) timed_out = true;
-        // Philox words and the variance-free part of the Box-Muller draw for this
-        // iteration's output row, in the same straight-line code as the four stages so
-        // that the integer and SFU work fills the stencil's issue gaps.
-        float r2a = 0.f, sna = 0.f, csa = 0.f, r2b = 0.f, snb = 0.f, csb = 0.f;
-        if (NOISE) {
-          const uint32_t cell = static_cast<uint32_t>(row_out * gnx + gcol0w);
-          const uint32_t cells[2] = {cell, cell + 1u};
-          Words4 w[2];
-          philox_cells(cells, prefix, w);
-          WignerDraw<float>::prepare(w[0], r2a, sna, csa);
-          WignerDraw<float>::prepare(w[1], r2b, snb, csb);
-        }
-
         // Stage 1 at row r-1 from the ring: k1 = f(psi0).
         const float2* R1 = ring_psi + slot1 * W;
         const float4 c4 = *reinterpret_cast<const float4*>(R1 + col0);
@@ -321,12 +318,11 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         {
           float2 da, db, va, vb;
           pot_at(srow[0], va, vb);
-          const float dna = rhs(c0, lt, c1, up0, dn0, n1v.x, __fmul_rn(s0, P1.x), va, da);
-          const float dnb = rhs(c1, c0, rt, up1, dn1, n1v.y, __fmul_rn(s0, P1.y), vb, db);
+          const float2 dn2 = rhs2(c0, c1, lt, rt, up0, up1, dn0, dn1, n1v, s0, P1, va, vb, da, db);
           q1[ja] = Pair{axpy2(hh, da, c0), axpy2(hh, db, c1)};
           acc[ja] = Pair{axpy2(h6, da, c0), axpy2(h6, db, c1)};
-          m1[ja] = make_float2(fmaf(hh, dna, n1v.x), fmaf(hh, dnb, n1v.y));
-          accn[ja] = make_float2(fmaf(h6, dna, n1v.x), fmaf(h6, dnb, n1v.y));
+          m1[ja] = axpy2(hh, dn2, n1v);
+          accn[ja] = axpy2(h6, dn2, n1v);
         }
         if (kSplit) {
           // Split barrier: wait until every thread has arrived at the end of iteration
@@ -342,6 +338,19 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
           if (CLUSTER && g > 0 && !receive(g - 1)) timed_out = true;
           if (t == 0 && i + 3 < n_iter) issue(i + 3);
         }
+        // Philox words and the variance-free part of the Box-Muller draw for this
+        // iteration's output row, in the same straight-line code as stages 2-4 (after the
+        // exchange wait) so that the integer and SFU work fills their issue gaps.
+        float r2a = 0.f, sna = 0.f, csa = 0.f, r2b = 0.f, snb = 0.f, csb = 0.f;
+        if (NOISE) {
+          const uint32_t cell = static_cast<uint32_t>(row_out * gnx + gcol0w);
+          const uint32_t cells[2] = {cell, cell + 1u};
+          Words4 w[2];
+          philox_cells(cells, prefix, w);
+          WignerDraw<float>::prepare(w[0], r2a, sna, csa);
+          WignerDraw<float>::prepare(w[1], r2b, snb, csb);
+        }
+
         // Stage 2 at row r-2: k2 = f(psi1).
         {
           float2 lt2, rt2;
@@ -351,14 +360,12 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
           const Pair c = q1[jb];
           float2 da, db, va, vb;
           pot_at(srow[1], va, vb);
-          const float dna = rhs(c.a, lt2, c.b, q1[jc].a, q1[ja].a, m1[jb].x,
-                                __fmul_rn(s1, P2.x), va, da);
-          const float dnb = rhs(c.b, c.a, rt2, q1[jc].b, q1[ja].b, m1[jb].y,
-                                __fmul_rn(s1, P2.y), vb, db);
+          const float2 dn2 = rhs2(c.a, c.b, lt2, rt2, q1[jc].a, q1[jc].b, q1[ja].a, q1[ja].b,
+                                  m1[jb], s1, P2, va, vb, da, db);
           q2[jb] = Pair{axpy2(hh, da, up0), axpy2(hh, db, up1)};  // psi0 at row r-2
-          m2[jb] = make_float2(fmaf(hh, dna, n0.x), fmaf(hh, dnb, n0.y));
+          m2[jb] = axpy2(hh, dn2, n0);
           acc[jb] = Pair{axpy2(h3, da, acc[jb].a), axpy2(h3, db, acc[jb].b)};
-          accn[jb] = make_float2(fmaf(h3, dna, accn[jb].x), fmaf(h3, dnb, accn[jb].y));
+          accn[jb] = axpy2(h3, dn2, accn[jb]);
         }
         // Stage 3 at row r-3: k3 = f(psi2).
         {
@@ -370,14 +377,12 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
           const Pair c = q2[jc];
           float2 da, db, va, vb;
           pot_at(srow[2], va, vb);
-          const float dna = rhs(c.a, lt3, c.b, q2[jd].a, q2[jb].a, m2[jc].x,
-                                __fmul_rn(s1, P3.x), va, da);
-          const float dnb = rhs(c.b, c.a, rt3, q2[jd].b, q2[jb].b, m2[jc].y,
-                                __fmul_rn(s1, P3.y), vb, db);
+          const float2 dn2 = rhs2(c.a, c.b, lt3, rt3, q2[jd].a, q2[jd].b, q2[jb].a, q2[jb].b,
+                                  m2[jc], s1, P3, va, vb, da, db);
           q3[jc] = Pair{axpy2(dt, da, make_float2(p4.x, p4.y)), axpy2(dt, db, make_float2(p4.z, p4.w))};
-          m3[jc] = make_float2(fmaf(dt, dna, n0.x), fmaf(dt, dnb, n0.y));
+          m3[jc] = axpy2(dt, dn2, n0);
           acc[jc] = Pair{axpy2(h3, da, acc[jc].a), axpy2(h3, db, acc[jc].b)};
-          accn[jc] = make_float2(fmaf(h3, dna, accn[jc].x), fmaf(h3, dnb, accn[jc].y));
+          accn[jc] = axpy2(h3, dn2, accn[jc]);
         }
         // Stage 4 at row r-4: k4 = f(psi3), final combine, clamp, Wigner increment.
         {
@@ -387,14 +392,12 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
           const Pair c = q3[jd];
           float2 da, db, va, vb;
           pot_at(srow[3], va, vb);
-          const float dna = rhs(c.a, lt4, c.b, q3[ja].a, q3[jc].a, m3[jd].x,
-                                __fmul_rn(s2, P4.x), va, da);
-          const float dnb = rhs(c.b, c.a, rt4, q3[ja].b, q3[jc].b, m3[jd].y,
-                                __fmul_rn(s2, P4.y), vb, db);
+          const float2 dn2 = rhs2(c.a, c.b, lt4, rt4, q3[ja].a, q3[ja].b, q3[jc].a, q3[jc].b,
+                                  m3[jd], s2, P4, va, vb, da, db);
           float2 oa = axpy2(h6, da, acc[jd].a);
           float2 ob = axpy2(h6, db, acc[jd].b);
-          float na = fmaf(h6, dna, accn[jd].x);
-          float nb = fmaf(h6, dnb, accn[jd].y);
+          const float2 nab = axpy2(h6, dn2, accn[jd]);
+          float na = nab.x, nb = nab.y;
           na = na < 0.f ? 0.f : na;
           nb = nb < 0.f ? 0.f : nb;
           if (writes && i >= 8 && i - 8 < h_rows) {
@@ -409,10 +412,13 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         }
         // Publish stage inputs for the horizontal neighbours.
         {
-          float4* xo = xbuf + (j & 1) * 3 * HALF;
-          xo[t] = make_float4(q1[ja].a.x, q1[ja].a.y, q1[ja].b.x, q1[ja].b.y);
-          xo[HALF + t] = make_float4(q2[jb].a.x, q2[jb].a.y, q2[jb].b.x, q2[jb].b.y);
-          xo[2 * HALF + t] = make_float4(q3[jc].a.x, q3[jc].a.y, q3[jc].b.x, q3[jc].b.y);
+          const int o = (j & 1) * 3 * HALF + t;
+          xa[o] = q1[ja].a;
+          xb[o] = q1[ja].b;
+          xa[o + HALF] = q2[jb].a;
+          xb[o + HALF] = q2[jb].b;
+          xa[o + 2 * HALF] = q3[jc].a;
+          xb[o + 2 * HALF] = q3[jc].b;
         }
         row_out = row_out + 1 == ny ? 0 : row_out + 1;
         if (CLUSTER) {

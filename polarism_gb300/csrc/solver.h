@@ -54,7 +54,7 @@ struct pg_solver {
   int* halt = nullptr;
   long long parity_step = 0;  // absolute step whose state sits under `cur` after pg_rk4_advance
   int rk4_kernel = 0;        // 0 auto, 1 tiled streaming kernel, 2 full-width kernel,
-                             // 3 full-width kernel in its two-sites-a-thread form
+                             // 3 full-width kernel with four sites a thread
   int wide_blocks = 0;       // persistent grid of the full-width kernel
   int quad_blocks = 0;       // persistent grid of its four-sites-a-thread form
   // Split-step state.

@@ -223,8 +223,8 @@ class RK4Engine:
                    "pg_rk4_set_geometry")
 
     def set_kernel(self, kind):
-        """0 automatic, 1 tiled streaming kernel, 2 full-width FP32 kernel (four sites a thread
-        on 512- and 1024-site rows), 3 full-width kernel with two sites a thread throughout."""
+        """0 automatic, 1 tiled streaming kernel, 2 full-width FP32 kernel, 3 full-width kernel
+        with four sites a thread (rows of 512 or 1024 sites)."""
         _lib.check(self.lib.pg_rk4_set_kernel(self.handle, int(kind)), "pg_rk4_set_kernel")
 
     def kernel(self) -> int:

@@ -352,10 +352,10 @@ def test_full_width_general_variant_matches_oracle_and_tiled(cuda_lib, pot_kind,
 @pytest.mark.parametrize("nx,ny,members,noise", [(1024, 40, 3, True), (1024, 8, 1, False),
                                                   (512, 36, 5, True), (512, 12, 2, False)])
 def test_four_site_form_is_bitwise_the_two_site_form(cuda_lib, nx, ny, members, noise):
-    """Rows of 512 and 1024 sites run four sites a thread by default (kernel kind 2); the same
-    kernel with two sites a thread (kind 3) does the same operations site by site, so the
-    results are identical bit for bit -- over member boundaries inside a block's row range,
-    the periodic seams and several graph-captured steps -- and within 1e-4 of the oracle."""
+    """The full-width kernel's four-sites-a-thread form (kernel kind 3) does the same operations
+    site by site as the default two-site form (kind 2), so the results are identical bit for
+    bit -- over member boundaries inside a block's row range, the periodic seams and several
+    graph-captured steps -- and within 1e-4 of the oracle."""
     from polarism_gb300.engine import MemberPhysics, RK4Engine
 
     rng = np.random.default_rng(nx * 7 + ny)
