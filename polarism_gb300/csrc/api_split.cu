@@ -42,52 +42,49 @@ template <typename T>
 int setup_tables(pg_solver* s) {
   const pg_config& c = s->cfg;
   const int nx = c.nx, ny = c.ny, m = c.members;
-  const double N = static_cast<double>(nx) * ny;
-  // Twiddles w_N^k = exp(-2 pi i k / N), computed in double precision.
-  std::vector<T> twx(2 * nx), twy(2 * ny);
-  for (int k = 0; k < nx; ++k) {
-    const double a = -2.0 * kPi * k / nx;
-    twx[2 * k] = static_cast<T>(std::cos(a));
-    twx[2 * k + 1] = static_cast<T>(std::sin(a));
-  }
-  for (int k = 0; k < ny; ++k) {
-    const double a = -2.0 * kPi * k / ny;
-    twy[2 * k] = static_cast<T>(std::cos(a));
-    twy[2 * k + 1] = static_cast<T>(std::sin(a));
-  }
-  // Separable propagators exp(-i hbar k^2 tau / 2m) = px[j] py[i], scale folded into px.
+  // Twiddles w_N^k = exp(-2 pi i k / N), computed in double precision.  FP32 tables hold a
+  // second block of N values after the first: the remainder w - round(w), so that the
+  // split-step passes multiply by hi + lo.  A rounded table alone misses |w| = 1 by ~3e-8
+  // with a non-zero mean; applied ~15 times a site and step, always with the same rounding,
+  // that bias drifts the norm by ~1e-4 over 1000 steps.  Other passes read the first block.
+  const int tw_blocks = sizeof(T) == 4 ? 2 : 1;
+  std::vector<T> twx(2 * nx * tw_blocks), twy(2 * ny * tw_blocks);
+  auto fill_twiddles = [&](std::vector<T>& tw, int n) {
+    for (int k = 0; k < n; ++k) {
+      const double a = -2.0 * kPi * k / n;
+      const double cr = std::cos(a), ci = std::sin(a);
+      tw[2 * k] = static_cast<T>(cr);
+      tw[2 * k + 1] = static_cast<T>(ci);
+      if (tw_blocks == 2) {
+        tw[2 * (n + k)] = static_cast<T>(cr - static_cast<double>(tw[2 * k]));
+        tw[2 * (n + k) + 1] = static_cast<T>(ci - static_cast<double>(tw[2 * k + 1]));
+      }
+    }
+  };
+  fill_twiddles(twx, nx);
+  fill_twiddles(twy, ny);
+  // Separable propagators exp(-i hbar k^2 tau / 2m) = (1 + dx[j]) (1 + dy[i]), stored as the
+  // differences d = exp(-i theta) - 1 = (-2 sin^2(theta / 2), -sin theta), which keep their
+  // relative precision at small theta (a rounded exp(-i theta) there has |f| > 1: its cosine
+  // rounds to 1).  The power-of-two scale of each table is applied apart (row_scale).
   const size_t per = static_cast<size_t>(nx + ny);
   std::vector<T> prop(static_cast<size_t>(PROP_COUNT) * m * per * 2);
   for (int table = 0; table < PROP_COUNT; ++table) {
     for (int mm = 0; mm < m; ++mm) {
       const pg_physics& p = s->physics[mm];
-      double tau = 0.0, scale = 1.0;
-      if (table == PROP_HALF_N) {
-        tau = 0.5 * c.dt;
-        scale = 1.0 / N;
-      } else if (table == PROP_FULL_N) {
-        tau = c.dt;
-        scale = 1.0 / N;
-      } else {
-        // The last row pass left F_x^-1 (Psi full / N); F_x of it is nx Psi full / N, so
-        // ny conj(half) turns it into Psi half.
-        tau = -0.5 * c.dt;
-        scale = static_cast<double>(ny);
-      }
+      // The last row pass left F_x^-1 (Psi full / N); F_x of it is nx Psi full / N, so
+      // ny conj(half) turns it into Psi half.
+      const double tau = table == PROP_HALF_N ? 0.5 * c.dt : table == PROP_FULL_N ? c.dt : -0.5 * c.dt;
       const double cf = p.hbar * tau / (2.0 * p.m_eff);
       T* base = prop.data() + ((static_cast<size_t>(table) * m + mm) * per) * 2;
-      for (int j = 0; j < nx; ++j) {
-        const double k = fft_wavenumber(j, nx, c.dx);
-        const std::complex<double> v = scale * std::exp(std::complex<double>(0.0, -cf * k * k));
-        base[2 * j] = static_cast<T>(v.real());
-        base[2 * j + 1] = static_cast<T>(v.imag());
-      }
-      for (int i = 0; i < ny; ++i) {
-        const double k = fft_wavenumber(i, ny, c.dy);
-        const std::complex<double> v = std::exp(std::complex<double>(0.0, -cf * k * k));
-        base[2 * (nx + i)] = static_cast<T>(v.real());
-        base[2 * (nx + i) + 1] = static_cast<T>(v.imag());
-      }
+      auto store = [&](int idx, double k) {
+        const double theta = cf * k * k;
+        const double sh = std::sin(0.5 * theta);
+        base[2 * idx] = static_cast<T>(-2.0 * sh * sh);
+        base[2 * idx + 1] = static_cast<T>(-std::sin(theta));
+      };
+      for (int j = 0; j < nx; ++j) store(j, fft_wavenumber(j, nx, c.dx));
+      for (int i = 0; i < ny; ++i) store(nx + i, fft_wavenumber(i, ny, c.dy));
     }
   }
   PG_CUDA(cudaMalloc(&s->tw_x, twx.size() * sizeof(T)));
@@ -214,6 +211,10 @@ cudaError_t row_launch(pg_solver* s, const PassPlan& p, int forward, int table, 
   a.forward = forward;
   a.inverse = inverse;
   a.multiply = table >= 0;
+  // Scale of the table: 1/N for the kicks between transforms, ny for the exit half kick
+  // (powers of two, so applying it apart rounds nothing).
+  a.scale = table == PROP_EXIT ? static_cast<double>(s->cfg.ny)
+                               : 1.0 / (static_cast<double>(s->cfg.nx) * s->cfg.ny);
   const size_t per = static_cast<size_t>(s->cfg.nx + s->cfg.ny);
   const T* px = static_cast<const T*>(s->prop) +
                 (static_cast<size_t>(table < 0 ? 0 : table) * s->cfg.members * per) * 2;

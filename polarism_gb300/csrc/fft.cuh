@@ -31,6 +31,34 @@ __device__ __forceinline__ C2 cmulc(C2 a, C2 b) {  // a * conj(b)
   return C2{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
 }
 
+// a * (h + l) and a * conj(h + l) for a twiddle carried as a rounded value h and its remainder
+// l: the small product a * l is formed first and added inside the fused multiply-adds of a * h.
+__device__ __forceinline__ float2 cmul2f(float2 a, float2 h, float2 l) {
+  const float cr = fmaf(a.x, l.x, -a.y * l.y);
+  const float ci = fmaf(a.x, l.y, a.y * l.x);
+  return float2{fmaf(a.x, h.x, fmaf(-a.y, h.y, cr)), fmaf(a.x, h.y, fmaf(a.y, h.x, ci))};
+}
+__device__ __forceinline__ float2 cmulc2f(float2 a, float2 h, float2 l) {
+  const float cr = fmaf(a.x, l.x, a.y * l.y);
+  const float ci = fmaf(a.y, l.x, -a.x * l.y);
+  return float2{fmaf(a.x, h.x, fmaf(a.y, h.y, cr)), fmaf(a.y, h.x, fmaf(-a.x, h.y, ci))};
+}
+template <bool INVERSE, typename C2>
+__device__ __forceinline__ C2 twiddle_mul(C2 v, const C2* tw, int idx, int n, bool comp) {
+  const C2 w = tw[idx];
+  return INVERSE ? cmulc(v, w) : cmul(v, w);
+}
+template <bool INVERSE>
+__device__ __forceinline__ float2 twiddle_mul(float2 v, const float2* tw, int idx, int n,
+                                              bool comp) {
+  const float2 w = tw[idx];
+  if (comp) {
+    const float2 l = tw[n + idx];
+    return INVERSE ? cmulc2f(v, w, l) : cmul2f(v, w, l);
+  }
+  return INVERSE ? cmulc(v, w) : cmul(v, w);
+}
+
 // Complex values a thread stages per pass (keeps the 1024-thread blocks within 64 registers).
 template <typename T>
 struct MaxVals {
@@ -41,8 +69,10 @@ struct MaxVals {
 // Element (i, c) of the shared buffer sits at buf[i * si + c * sc].  COLS selects which
 // index varies fastest across threads (c for column panels, i within a row) so shared
 // memory accesses stay contiguous.  s = stride (product of the radices already done),
-// m = N / (R s).  Requires N * C <= MaxVals<T>::value * blockDim.x.
-template <typename T, bool INVERSE, bool COLS, int R>
+// m = N / (R s).  Requires N * C <= MaxVals<T>::value * blockDim.x.  COMP (FP32 only):
+// tw holds N rounded twiddles followed by their N remainders, and every twiddle product uses
+// both.
+template <typename T, bool INVERSE, bool COLS, int R, bool COMP = false>
 __device__ __forceinline__ void stockham_pass(typename C2T<T>::type* buf,
                                               const typename C2T<T>::type* tw, int log2n,
                                               int log2c, int si, int sc, int log2s, int m) {
@@ -103,10 +133,7 @@ __device__ __forceinline__ void stockham_pass(typename C2T<T>::type* buf,
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         C2 val = y[r];
-        if (r > 0) {
-          const C2 w = tw[p * r * s];
-          val = INVERSE ? cmulc(val, w) : cmul(val, w);
-        }
+        if (r > 0) val = twiddle_mul<INVERSE>(val, tw, p * r * s, 1 << log2n, COMP);
         buf[(out + s * r) * si + c * sc] = val;
       }
     }
@@ -115,18 +142,18 @@ __device__ __forceinline__ void stockham_pass(typename C2T<T>::type* buf,
 }
 
 // In-place Stockham FFT (radix 4, with one radix-2 pass first when log2 N is odd).
-template <typename T, bool INVERSE, bool COLS>
+template <typename T, bool INVERSE, bool COLS, bool COMP = false>
 __device__ void smem_fft(typename C2T<T>::type* buf, const typename C2T<T>::type* tw, int log2n,
                          int log2c, int si, int sc) {
   int log2s = 0;
   int log2m = log2n;
   if (log2n & 1) {
-    stockham_pass<T, INVERSE, COLS, 2>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 1));
+    stockham_pass<T, INVERSE, COLS, 2, COMP>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 1));
     log2s += 1;
     log2m -= 1;
   }
   while (log2m > 0) {
-    stockham_pass<T, INVERSE, COLS, 4>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 2));
+    stockham_pass<T, INVERSE, COLS, 4, COMP>(buf, tw, log2n, log2c, si, sc, log2s, 1 << (log2m - 2));
     log2s += 2;
     log2m -= 2;
   }

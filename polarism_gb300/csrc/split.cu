@@ -39,41 +39,44 @@ __global__ void __launch_bounds__(1024) row_pass_kernel(typename C2T<T>::type* _
                                                         const RowPassArgs a) {
   using C2 = typename C2T<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool COMP = sizeof(T) == 4;  // FP32: twiddles as rounded value + remainder
   C2* tws = reinterpret_cast<C2*>(smem_raw);
-  C2* buf = tws + a.nx;
+  C2* buf = tws + (COMP ? 2 : 1) * a.nx;
   const int member = blockIdx.z;
   const int row0 = blockIdx.x * a.rows;
   const int rows = a.rows;
   const long long plane = static_cast<long long>(a.nx) * a.ny;
   C2* d = data + member * plane + static_cast<long long>(row0) * a.nx;
-  for (int k = threadIdx.x; k < a.nx; k += blockDim.x) tws[k] = tw[k];
+  for (int k = threadIdx.x; k < (COMP ? 2 : 1) * a.nx; k += blockDim.x) tws[k] = tw[k];
   const int count = rows * a.nx;
   #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) buf[e] = d[e];
   __syncthreads();
-  if (a.forward) smem_fft<T, false, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
+  if (a.forward) smem_fft<T, false, false, COMP>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
   if (a.multiply) {
+    // psi (1 + dx[j]) (1 + dy[i]) scale = (psi + psi (dx + dy + dx dy)) scale, with the factor
+    // differences d stored in place of the factors (see setup_tables) and scale a power of two.
     const C2* pxm = px + static_cast<long long>(member) * a.table_stride;
     const C2* pym = py + static_cast<long long>(member) * a.table_stride;
+    const T scale = static_cast<T>(a.scale);
     for (int e = threadIdx.x; e < count; e += blockDim.x) {
       const int r = e >> a.log2nx;
       const int j = e & (a.nx - 1);
-      buf[e] = cmul(buf[e], cmul(pxm[j], pym[row0 + r]));
+      const C2 dx = pxm[j], dy = pym[row0 + r];
+      const C2 dxy = cmul(dx, dy);
+      const C2 f1{dx.x + dy.x + dxy.x, dx.y + dy.y + dxy.y};
+      const C2 v = buf[e];
+      const C2 vf = cmul(v, f1);
+      buf[e] = C2{(v.x + vf.x) * scale, (v.y + vf.y) * scale};
     }
     __syncthreads();
   }
-  if (a.inverse) smem_fft<T, true, false>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
+  if (a.inverse) smem_fft<T, true, false, COMP>(buf, tws, a.log2nx, a.log2rows, 1, a.nx);
   #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) d[e] = buf[e];
 }
 
 // ------------------------------------------------------------------ local operations
-template <typename T>
-__device__ __forceinline__ T exp_t(T x);
-template <>
-__device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
-template <>
-__device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
 __device__ __forceinline__ float mul_rn_t(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn_t(double a, double b) { return __dmul_rn(a, b); }
 
@@ -118,12 +121,12 @@ __device__ __forceinline__ void reservoir_half2(T& a, T& b, T rho, T pump, T h, 
   b = nb > T(0) ? nb : T(0);
 }
 
-// (exp(x) - 1) / x and (sin, cos) of the local step.  FP64 follows the reference (expm1 with its
-// three-term series below 1e-6, library sincos).  FP32 uses a five-term series for |x| < 2^-5
-// (truncation x^5/720 < 5e-11 relative) and Taylor polynomials for |phi| < 1/8 (truncation
-// below 1e-13), the library functions outside: the per-step arguments are that small at the
-// time steps the split-step solvers run with, and the polynomials are cheaper than the
-// library's range reduction.
+// (exp(x) - 1) / x, exp(x) - 1 and (sin, cos - 1) of the local step.  FP64 follows the
+// reference (expm1 with its three-term series below 1e-6, library sincos).  FP32 uses
+// five-term series for |x| < 2^-5 (truncation x^5/720 < 5e-11 relative) and Taylor
+// polynomials for |phi| < 1/8 (truncation below 1e-13), the library functions outside: the
+// per-step arguments are that small at the time steps the split-step solvers run with, and
+// the polynomials are cheaper than the library's range reduction.
 __device__ __forceinline__ double phase_time_factor(double x) {
   return fabs(x) < 1e-6 ? 1.0 + x * 0.5 + x * x / 6.0 : expm1(x) / x;
 }
@@ -132,19 +135,34 @@ __device__ __forceinline__ float phase_time_factor(float x) {
     return 1.0f + x * (0.5f + x * (1.0f / 6.0f + x * (1.0f / 24.0f + x * (1.0f / 120.0f))));
   return expm1f(x) / x;
 }
-__device__ __forceinline__ void local_sincos(double x, double* s, double* c) { sincos(x, s, c); }
-__device__ __forceinline__ void local_sincos(float x, float* s, float* c) {
+__device__ __forceinline__ double local_expm1(double x) { return expm1(x); }
+__device__ __forceinline__ float local_expm1(float x) {
+  if (fabsf(x) < 0.03125f)
+    return x * (1.0f + x * (0.5f + x * (1.0f / 6.0f + x * (1.0f / 24.0f + x * (1.0f / 120.0f)))));
+  return expm1f(x);
+}
+__device__ __forceinline__ void local_sincos_m1(double x, double* s, double* cm1) {
+  double c;
+  sincos(x, s, &c);
+  *cm1 = c - 1.0;
+}
+__device__ __forceinline__ void local_sincos_m1(float x, float* s, float* cm1) {
   if (fabsf(x) < 0.125f) {
     const float x2 = x * x;
     *s = x * (1.0f - x2 * (1.0f / 6.0f) * (1.0f - x2 * (1.0f / 20.0f) * (1.0f - x2 * (1.0f / 42.0f))));
-    *c = 1.0f - x2 * 0.5f * (1.0f - x2 * (1.0f / 12.0f) * (1.0f - x2 * (1.0f / 30.0f) * (1.0f - x2 * (1.0f / 56.0f))));
+    *cm1 = -x2 * 0.5f * (1.0f - x2 * (1.0f / 12.0f) * (1.0f - x2 * (1.0f / 30.0f) * (1.0f - x2 * (1.0f / 56.0f))));
   } else {
-    sincosf(x, s, c);
+    float c;
+    sincosf(x, s, &c);
+    *cm1 = c - 1.0f;  // |phi| >= 1/8: |c - 1| >= 0.0078, so c - 1 keeps c's precision
   }
 }
 
 // Exact local step psi * exp(g dt - i phi) (split_step_fft_solver.py:121-139); n2 is the
-// inactive reservoir (0 without one), which enters the phase through g_I.
+// inactive reservoir (0 without one), which enters the phase through g_I.  Applied as
+// psi + psi D with D = exp(g dt - i phi) - 1 = (e + c1 + e c1) - i (1 + e) s, e = exp(g dt) - 1,
+// c1 = cos phi - 1: the factor itself sits next to 1 at these step sizes, where its rounding
+// would repeat step after step (a rounded exp(g dt) there carries up to 6e-8 of bias a step).
 template <typename T>
 __device__ __forceinline__ void nonlinear(T& re, T& im, T n, T n2, bool two, T vre, T vim, T dt,
                                           const SplitConst<T>& k) {
@@ -155,12 +173,14 @@ __device__ __forceinline__ void nonlinear(T& re, T& im, T n, T n2, bool two, T v
   T pot = vre + k.g_R * n;
   if (two) pot += k.g_I * n2;
   const T phase = (pot * dt + k.g_C * rho * phase_time) * k.inv_hbar;
-  const T amp = exp_t(gain * dt);
-  T s, c;
-  local_sincos(phase, &s, &c);
+  const T e = local_expm1(gain * dt);
+  T s, c1;
+  local_sincos_m1(phase, &s, &c1);
+  const T dre = e + c1 + e * c1;
+  const T dim = -(s + e * s);
   const T r = re, i = im;
-  re = amp * (r * c + i * s);
-  im = amp * (i * c - r * s);
+  re = r + (r * dre - i * dim);
+  im = i + (r * dim + i * dre);
 }
 
 // ------------------------------------------------------------------ column pass
@@ -176,14 +196,15 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
                                                         const ColPassArgs a) {
   using C2 = typename C2T<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool COMP = sizeof(T) == 4;  // FP32: twiddles as rounded value + remainder
   C2* tws = reinterpret_cast<C2*>(smem_raw);
-  C2* buf = tws + a.ny;
+  C2* buf = tws + (COMP ? 2 : 1) * a.ny;
   const int member = blockIdx.z;
   const int x0 = blockIdx.x * a.cols;
   const int C = a.cols;
   const long long plane = static_cast<long long>(a.nx) * a.ny;
   C2* d = data + member * plane;
-  for (int k = threadIdx.x; k < a.ny; k += blockDim.x) tws[k] = tw[k];
+  for (int k = threadIdx.x; k < (COMP ? 2 : 1) * a.ny; k += blockDim.x) tws[k] = tw[k];
   const int count = C * a.ny;
   #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) {
@@ -191,7 +212,7 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
     buf[i * C + c] = d[static_cast<long long>(i) * a.nx + x0 + c];
   }
   __syncthreads();
-  if (a.inverse) smem_fft<T, true, true>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
+  if (a.inverse) smem_fft<T, true, true, COMP>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
   if (a.op != SPLIT_OP_NONE) {
     const SplitConst<T> k = consts[member];
     const int m_count = a.members;
@@ -282,7 +303,7 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
     }
     __syncthreads();
   }
-  if (a.forward) smem_fft<T, false, true>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
+  if (a.forward) smem_fft<T, false, true, COMP>(buf, tws, a.log2ny, a.log2cols, a.cols, 1);
   #pragma unroll kUnrollIO
   for (int e = threadIdx.x; e < count; e += blockDim.x) {
     const int c = e & (C - 1), i = e >> a.log2cols;
@@ -297,7 +318,8 @@ cudaError_t launch_row_pass(T* data, const T* tw, const T* px, const T* py, cons
                             int members, cudaStream_t stream) {
   using C2 = typename C2T<T>::type;
   const int blocks = (a.ny + a.rows - 1) / a.rows;
-  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.nx) + static_cast<size_t>(a.rows) * a.nx);
+  const size_t tw_values = static_cast<size_t>(a.nx) * (sizeof(T) == 4 ? 2 : 1);
+  const size_t smem = sizeof(C2) * (tw_values + static_cast<size_t>(a.rows) * a.nx);
   row_pass_kernel<T><<<dim3(blocks, 1, members), a.threads, smem, stream>>>(
       reinterpret_cast<C2*>(data), reinterpret_cast<const C2*>(tw), reinterpret_cast<const C2*>(px),
       reinterpret_cast<const C2*>(py), a);
@@ -311,7 +333,8 @@ cudaError_t launch_col_pass(T* data, T* res, const T* pump, const T* potential, 
                             cudaStream_t stream) {
   using C2 = typename C2T<T>::type;
   const int blocks = (a.nx + a.cols - 1) / a.cols;
-  const size_t smem = sizeof(C2) * (static_cast<size_t>(a.ny) + static_cast<size_t>(a.cols) * a.ny);
+  const size_t tw_values = static_cast<size_t>(a.ny) * (sizeof(T) == 4 ? 2 : 1);
+  const size_t smem = sizeof(C2) * (tw_values + static_cast<size_t>(a.cols) * a.ny);
   col_pass_kernel<T><<<dim3(blocks, 1, a.members), a.threads, smem, stream>>>(
       reinterpret_cast<C2*>(data), res, pump, potential, reinterpret_cast<const C2*>(tw), consts,
       scales, step_base, a);

@@ -33,6 +33,7 @@ struct RowPassArgs {
   int threads;
   int forward, inverse, multiply;
   int table_stride;     // complex values between consecutive members' propagator factors
+  double scale;         // power-of-two factor of the kick: psi (1 + d) * scale
 };
 
 struct ColPassArgs {
