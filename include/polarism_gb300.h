@@ -246,6 +246,20 @@ int pg_field_norms_noalloc(const void* psi, int32_t precision, int32_t members,
 int pg_rk4_set_kernel(pg_solver* s, int32_t kind);
 int pg_rk4_get_kernel(pg_solver* s, int32_t* kind);
 
+/* Failure detection of the TMA-fed RK4 kernels (full-width, four-sites-a-thread, cluster
+ * form; no counterpart in the reference, whose kernels wait on nothing).  Every wait of these
+ * kernels on an mbarrier -- a row copy, the block's row exchange, a neighbouring CTA's edge
+ * values -- gives up after 100000 polls, a bound compiled into the kernels.  Once a wait of
+ * the thread that feeds a block's row ring has given up, it completes later ring slots without
+ * copying into them, so the block's remaining waits pass at once and the kernel ends in about
+ * the time of one full wait; copies still in flight are waited for before the block exits.
+ * The next pg_synchronize or pg_get_state then returns PG_ERR_TIMEOUT, and the state is
+ * invalid until set again.  `polls` is 100000 (the default) or 0, the give-up setting: the
+ * kernels withhold each block's first row copy, so that a wait runs out on a healthy GPU and
+ * the failure path can be exercised (PG_ERR_INVALID for other values).  Changing it drops the
+ * captured CUDA graphs. */
+int pg_set_wait_limit(pg_solver* s, int32_t polls);
+
 /* Number of kernel launches the last advance call issued (graph nodes included). */
 int64_t pg_last_launch_count(pg_solver* s);
 
@@ -295,6 +309,8 @@ int pg_sweep_set_tiling(pg_sweep* w, int32_t lanes, int32_t strip_rows);
 int pg_sweep_get_tiling(pg_sweep* w, int32_t* lanes, int32_t* strip_rows, int32_t* items,
                         int32_t* blocks);
 /* Leave members whose entry is 0 out of the launch (their state is kept); NULL = all active. */
+/* The same bound for the uneven sweep's kernel (see pg_set_wait_limit). */
+int pg_sweep_set_wait_limit(pg_sweep* w, int32_t polls);
 int pg_sweep_set_active(pg_sweep* w, const uint8_t* active);
 /* n_steps RK4 steps (rk4_cuda_solver.py:3451-3642 semantics per member); stage_scales holds
  * [n_steps][3][members] pump coefficients at t, t + dt/2, t + dt. */

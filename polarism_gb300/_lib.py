@@ -88,6 +88,7 @@ SIGNATURES = {
     "pg_field_norms_noalloc": (C.c_int, [_vp, _i32, _i32, _i64, _f64, _vp, _vp]),
     "pg_rk4_set_kernel": (C.c_int, [_vp, _i32]),
     "pg_rk4_get_kernel": (C.c_int, [_vp, C.POINTER(_i32)]),
+    "pg_set_wait_limit": (C.c_int, [_vp, _i32]),
     "pg_last_launch_count": (_i64, [_vp]),
     "pg_philox_words": (C.c_int, [_vp, _u64, _vp, _i64]),
     "pg_wigner_normals": (C.c_int, [_vp, _u64, _i32, _vp, _i64]),
@@ -105,6 +106,7 @@ SIGNATURES = {
     "pg_sweep_set_tiling": (C.c_int, [_vp, _i32, _i32]),
     "pg_sweep_get_tiling": (C.c_int, [_vp, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32),
                                       C.POINTER(_i32)]),
+    "pg_sweep_set_wait_limit": (C.c_int, [_vp, _i32]),
     "pg_sweep_set_active": (C.c_int, [_vp, _vp]),
     "pg_sweep_advance": (C.c_int, [_vp, _i64, _i32, _vp, C.c_int]),
     "pg_sweep_last_time_ms": (C.c_int, [_vp, C.POINTER(C.c_float)]),

@@ -17,6 +17,7 @@
 #include "philox.cuh"
 #include "pg_internal.h"
 #include "solver.h"
+#include "tma.cuh"
 #include "wide_internal.h"
 
 namespace pg {
@@ -205,6 +206,7 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
     w.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
     w.pot_kind = f.potential;
     w.relax = f.relax;
+    w.wait_limit = s->wait_limit;
     if (use_quad(s, w)) {
       w.blocks = s->quad_blocks;
       return pg::launch_rk4_quad(static_cast<const float*>(s->psi[from]),
@@ -495,6 +497,17 @@ int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
   }
   s->rk4_kernel = kind;
   free_graphs(s);
+  return PG_OK;
+}
+
+int pg_set_wait_limit(pg_solver* s, int32_t polls) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_set_wait_limit: null solver");
+  PG_CHECK(polls == 0 || polls == pg::kWaitPolls, PG_ERR_INVALID,
+           "pg_set_wait_limit: polls must be 0 (the give-up setting: every wait gives up at once) "
+           "or 100000 (the kernels' compiled bound)");
+  PG_CUDA(cudaStreamSynchronize(s->stream));
+  s->wait_limit = polls;
+  free_graphs(s);  // captured launches carry the old limit
   return PG_OK;
 }
 

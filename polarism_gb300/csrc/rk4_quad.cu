@@ -36,16 +36,16 @@ namespace pg {
 namespace {
 
 constexpr int kQRing = 8;  // rows resident: r-4 .. r plus three in flight
-constexpr int kQWaitLimit = 100000;
 
 template <int NX>
 struct QuadShape {
   static constexpr int THREADS = NX / 4;
   // Ring (psi 8 B + n 4 B + pump 4 B per site and row), exchange [parity][stage][thread]
-  // of float4 (the thread's first and last site), the ring barriers and the exchange barrier.
+  // of float4 (the thread's first and last site), the ring barriers and the exchange barrier,
+  // and one word of thread 0's (its feed mode; see feed) with padding.
   static constexpr size_t SMEM = static_cast<size_t>(kQRing) * NX * 16 +
                                  static_cast<size_t>(2) * 3 * THREADS * 16 +
-                                 (kQRing + 1) * sizeof(uint64_t);
+                                 (kQRing + 2) * sizeof(uint64_t);
 };
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
@@ -121,6 +121,7 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
   float4* xbuf = reinterpret_cast<float4*>(ring_p + kQRing * NX);    // [2][3][T]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * T);        // [kQRing + 1]
   const uint32_t xbar = smem_u32(&mbar[kQRing]);
+  volatile int* feed_mode = reinterpret_cast<volatile int*>(&mbar[kQRing + 1]);
 
   const int ny = g.ny;
   const int t = threadIdx.x;
@@ -136,6 +137,7 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
     for (int s = 0; s < kQRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
     mbar_init(xbar, T);
     fence_mbar_init();
+    *feed_mode = 0;
   }
   __syncthreads();
 
@@ -185,8 +187,29 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
       bulk_g2s(smem_u32(ring_n + slot * NX), n_m + ro, NX * 4u, bar);
       bulk_g2s(smem_u32(ring_p + slot * NX), p_m + ro, NX * 4u, bar);
     };
+    // Thread 0 feeds ring use it + i: the row copies, or, once one of its own waits has given
+    // up (tested at the barrier of the use it has just waited for), an empty arrival; the
+    // give-up setting withholds and later settles the block's first use, as in rk4_wide.cu.
+    auto feed = [&](int i) {
+      const unsigned u = it + i;
+      int mode = *feed_mode;
+      if (mode == 0 && i >= 3) {
+        // the use thread 0 has just waited for: open means its wait gave up
+        const unsigned w = u - 3;
+        if (!mbar_test(smem_u32(&mbar[w & (kQRing - 1)]), (w / kQRing) & 1u)) *feed_mode = mode = 1;
+      }
+      if (g.wait_limit == 0) {
+        if (u == 0) return;
+        if (u == kQRing) mbar_arrive(smem_u32(&mbar[0]));
+      }
+      if (mode == 0) {
+        issue(i);
+        return;
+      }
+      mbar_fill_empty(smem_u32(&mbar[i & (kQRing - 1)]), u, kQRing);
+    };
     if (t == 0) {
-      for (int i = 0; i < 3 && i < n_iter; ++i) issue(i);
+      for (int i = 0; i < 3 && i < n_iter; ++i) feed(i);
     }
 
     // Register rings [row slot][site] (complex) and [row slot] of site pairs (reservoir).
@@ -216,7 +239,7 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
         const int slot3 = (base + j + kQRing - 3) & (kQRing - 1);  // row r-3
         const int slot4 = (base + j + kQRing - 4) & (kQRing - 1);  // row r-4
         const uint32_t parity = ((it + i) / kQRing) & 1u;
-        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kQWaitLimit)) timed_out = true;
+        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitPolls)) timed_out = true;
 
         // Philox words and the variance-free part of the Box-Muller draw of this
         // iteration's output row (four cells), interleaved with the stages by the compiler.
@@ -257,8 +280,8 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
         // row r-5 that the copy of row r+3 reuses).
         {
           const unsigned gi = it + i;
-          if (gi > 0 && !mbar_wait_bounded(xbar, (gi - 1) & 1u, kQWaitLimit)) timed_out = true;
-          if (t == 0 && i + 3 < n_iter) issue(i + 3);
+          if (gi > 0 && !mbar_wait_bounded(xbar, (gi - 1) & 1u, kWaitPolls)) timed_out = true;
+          if (t == 0 && i + 3 < n_iter) feed(i + 3);
         }
         const float4* xin = xbuf + ((j + 1) & 1) * 3 * T;
         // Stage 2 at row r-2: k2 = f(psi1).
@@ -343,6 +366,9 @@ __global__ void __launch_bounds__(QuadShape<NX>::THREADS, 1)
     }
     it += n_iter;
   }
+  // After a wait of thread 0's gave up: copies it issued may still be in flight in the last
+  // ring uses; a use it filled empty completes at once.
+  if (t == 0 && (timed_out || *feed_mode != 0)) drain_ring(mbar, kQRing, it >= kQRing ? it - kQRing : 0u, it);
   if (timed_out) atomicOr(err_flag, 1);
 }
 

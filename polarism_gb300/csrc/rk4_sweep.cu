@@ -37,7 +37,6 @@ namespace pg {
 namespace {
 
 constexpr int kRing = 8;
-constexpr int kWaitLimit = 100000;
 constexpr int kMaxStrips = 8;      // strips per item: LANES / W <= 8
 constexpr int kSweepChunk = 64;    // steps per staged chunk / CUDA graph
 constexpr int kSweepSlots = 4;     // pinned staging ring depth
@@ -67,7 +66,7 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
                      const SweepMember* __restrict__ members, const SweepItem* __restrict__ items,
                      const int n_items, const int n_members, const float* __restrict__ scales,
                      const unsigned long long* __restrict__ step_base, const int step_offset,
-                     const float dt, int* __restrict__ err_flag) {
+                     const float dt, const int wait_limit, int* __restrict__ err_flag) {
   constexpr int HALF = LANES / 2;
   // One block per SM (1024 lanes): a split arrive/wait barrier lets its warps drift apart
   // by up to a row, which measured faster; with two blocks per SM the blocks already
@@ -80,6 +79,10 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
   float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * LANES);   // [2][3][HALF]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kRing] + exchange barrier
   const uint32_t xbar = smem_u32(&mbar[kRing]);
+  // Thread 0's decisions for the strip leaders: whether ring slot s holds copies (0) or was
+  // completed empty (1); its arm mode (0 copies, 1 empty arrivals; see arm); padding.
+  volatile int* slot_empty = reinterpret_cast<volatile int*>(&mbar[kRing + 1]);  // [kRing]
+  volatile int* arm_mode = slot_empty + kRing;
 
   const int t = threadIdx.x;
   const int col0 = 2 * t;  // ring column of the thread's first site
@@ -87,6 +90,8 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
     if (kSplit) mbar_init(xbar, LANES / 2);
     fence_mbar_init();
+    for (int s = 0; s < kRing; ++s) slot_empty[s] = 0;
+    *arm_mode = 0;
   }
   __syncthreads();
 
@@ -135,11 +140,36 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
     // Thread 0 arms the slot's barrier for the whole row (LANES * 16 bytes) before the
     // strips' leaders issue their bulk copies, so the expected bytes are always registered
     // first.
+    // Thread 0 arms ring use it + i for the strips' copies, or, once one of its own waits has
+    // given up, completes it with an empty arrival and tells the leaders (slot_empty) to copy
+    // nothing into it (see tma.cuh).  It reads its timed_out flag once per work item, before
+    // the item's rows (within the rows, a flag read or a barrier test per row measured 4-8%
+    // slower on this kernel, whose block barrier waits for thread 0 every row); an item in
+    // which a wait gives up runs on with copies, each wait still bounded.  The give-up
+    // setting (wait_limit 0) withholds the block's first use (no arming, no copies) so that
+    // every thread's wait for it runs out, and settles it just before its slot is armed again.
     auto arm = [&](int i) {
-      mbar_arrive_expect_tx(smem_u32(&mbar[i & (kRing - 1)]), LANES * 16u);
+      const int slot = i & (kRing - 1);
+      const uint32_t bar = smem_u32(&mbar[slot]);
+      const unsigned u = it + i;
+      if (wait_limit == 0) {
+        if (u == 0) {
+          slot_empty[slot] = 1;
+          return;
+        }
+        if (u == kRing) mbar_arrive(smem_u32(&mbar[0]));
+      }
+      if (*arm_mode == 0) {
+        slot_empty[slot] = 0;
+        mbar_arrive_expect_tx(bar, LANES * 16u);
+        return;
+      }
+      slot_empty[slot] = 1;
+      mbar_fill_empty(bar, u, kRing);
     };
     auto issue = [&](int i) {
       const int slot = i & (kRing - 1);
+      if (slot_empty[slot] != 0) return;
       int row = row_first + i;
       while (row >= ny) row -= ny;
       const uint32_t bar = smem_u32(&mbar[slot]);
@@ -149,6 +179,7 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
       bulk_g2s(smem_u32(ring_p + slot * LANES + base), p_m + src, W * 4u, bar);
     };
     if (t == 0) {
+      if (timed_out) *arm_mode = 1;  // a wait of thread 0's gave up in an earlier item
       for (int i = 0; i < (kSplit ? 4 : 3) && i < n_iter; ++i) arm(i);
     }
     __syncthreads();
@@ -177,7 +208,11 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
         const int slot2 = (j + kRing - 2) % kRing;
         const int slot3 = (j + kRing - 3) % kRing;
         const int slot4 = (j + kRing - 4) % kRing;
-        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitLimit)) timed_out = true;
+        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitPolls)) timed_out = true;
+        // Thread 0 arms the slot of use i + 4 (split barrier) or i + 3 (block barrier) here,
+        // off the block barrier's path: that slot's previous use completed rows ago, and arming
+        // touches no data (its copies are issued after the barrier that frees the slot).
+        if (t == 0 && i + (kSplit ? 4 : 3) < n_iter) arm(i + (kSplit ? 4 : 3));
         // Philox words and the variance-free part of the Box-Muller draw for this
         // iteration's output row, in the same straight-line code as the four stages so
         // that the integer and SFU work fills the stencil's issue gaps.
@@ -218,7 +253,7 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
           // below and the ring slot of row r-5 that the copy of row r+3 reuses).  Thread 0
           // armed that slot's barrier before arriving, so the copies follow the arming.
           const unsigned g = it + i;
-          if (g > 0 && !mbar_wait_bounded(xbar, (g - 1) & 1u, kWaitLimit)) timed_out = true;
+          if (g > 0 && !mbar_wait_bounded(xbar, (g - 1) & 1u, kWaitPolls)) timed_out = true;
           if (lt == 0 && i + 3 < n_iter) issue(i + 3);
         }
         // Stage 2 at row r-2.
@@ -291,14 +326,10 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
         }
         row_out = row_out + 1 == ny ? 0 : row_out + 1;
         if (kSplit) {
-          // Arm the slot the next iteration's copies fill (its last phase, row r-4, has
-          // completed), then arrive on the exchange barrier.
-          if (t == 0 && i + 4 < n_iter) arm(i + 4);
           mbar_arrive(xbar);
         } else {
           // The slot of row r+3 held row r-5, last read by stage 4 of the previous
-          // iteration.
-          if (t == 0 && i + 3 < n_iter) arm(i + 3);
+          // iteration (thread 0 armed it at the top of this one).
           __syncthreads();
           if (lt == 0 && i + 3 < n_iter) issue(i + 3);
         }
@@ -306,12 +337,15 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
     }
     it += n_iter;
   }
+  // After a wait of thread 0's gave up: copies of the last ring uses may still be in flight
+  // (uses completed empty, or long landed, return at once).
+  if (t == 0 && (timed_out || *arm_mode != 0)) drain_ring(mbar, kRing, it >= kRing ? it - kRing : 0u, it);
   if (timed_out) atomicOr(err_flag, 1);
 }
 
 size_t sweep_smem(int lanes) {
   return static_cast<size_t>(kRing) * lanes * 16 + static_cast<size_t>(6) * (lanes / 2) * 16 +
-         (kRing + 1) * sizeof(uint64_t);
+         (kRing + 1) * sizeof(uint64_t) + (kRing + 2) * sizeof(int);  // + slot_empty, modes
 }
 
 template <int LANES>
@@ -407,6 +441,7 @@ struct pg_sweep {
   float* scales = nullptr;
   unsigned long long* step_base = nullptr;
   int* err_flag = nullptr;
+  int wait_limit = 100000;  // 0: the give-up setting (pg_sweep_set_wait_limit)
   int cur = 0;
   bool noise = false;
   std::vector<uint64_t> seeds;
@@ -613,7 +648,8 @@ cudaError_t launch_sweep_step(pg_sweep* w, int from, int step_offset) {
   pg::rk4_sweep_kernel<L, N><<<w->blocks, L / 2, smem, w->stream>>>(                            \
       reinterpret_cast<const float2*>(w->psi[from]), w->res[from], w->pump,                    \
       reinterpret_cast<float2*>(w->psi[to]), w->res[to], w->consts, w->dmembers, w->ditems,     \
-      w->n_items, w->members, w->scales, w->step_base, step_offset, dt, w->err_flag)
+      w->n_items, w->members, w->scales, w->step_base, step_offset, dt, w->wait_limit,           \
+      w->err_flag)
   if (w->lanes == 1024) {
     if (w->noise) PG_SWEEP_LAUNCH(1024, true); else PG_SWEEP_LAUNCH(1024, false);
   } else {
@@ -849,6 +885,17 @@ int pg_sweep_set_tiling(pg_sweep* w, int32_t lanes, int32_t strip_rows) {
   if (rc != PG_OK) return rc;
   PG_CUDA(cudaStreamSynchronize(w->stream));
   return build_items(w, lanes, strip_rows);
+}
+
+int pg_sweep_set_wait_limit(pg_sweep* w, int32_t polls) {
+  PG_CHECK(w, PG_ERR_INVALID, "pg_sweep_set_wait_limit: null sweep");
+  PG_CHECK(polls == 0 || polls == pg::kWaitPolls, PG_ERR_INVALID,
+           "pg_sweep_set_wait_limit: polls must be 0 (the give-up setting: every wait gives up at "
+           "once) or 100000 (the kernel's compiled bound)");
+  PG_CUDA(cudaStreamSynchronize(w->stream));
+  w->wait_limit = polls;
+  sweep_free_graphs(w);  // captured launches carry the old setting
+  return PG_OK;
 }
 
 int pg_sweep_get_tiling(pg_sweep* w, int32_t* lanes, int32_t* strip_rows, int32_t* items,

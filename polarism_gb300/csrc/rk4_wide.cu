@@ -39,7 +39,6 @@ namespace pg {
 namespace {
 
 constexpr int kRing = 8;          // rows resident: r-4..r plus three in flight
-constexpr int kWaitLimit = 100000;
 
 // At least 512 resident threads per SM for every row width (128 registers a thread).
 // Threads of a block: two sites each over the shared-memory row.  Rows wider than NX = 1024
@@ -57,8 +56,10 @@ struct WideShape {
 // Barriers after the ring's: the row exchange, then (CLUSTER) the left and right
 // neighbours' edge deliveries, two of each by iteration parity.
 constexpr int kBars = kRing + 5;
-// CLUSTER inboxes after the barriers: [from left, from right][parity][stage] edge values.
+// CLUSTER inboxes after the barriers: [from left, from right][parity][stage] edge values,
+// then thread 0's feed mode (0 copies, 1 empty arrivals; see feed) and padding.
 constexpr int kInbox = 2 * 2 * 3;
+constexpr int kFailWords = 2;
 constexpr uint32_t kEdgeBytes = 3 * 8;  // one iteration's delivery: three stage values
 
 template <int NX, bool NOISE, bool GENERAL, bool BAND, bool CLUSTER = false>
@@ -97,6 +98,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
   const uint32_t from_right = smem_u32(&mbar[kRing + 3]);
   float2* in_left = reinterpret_cast<float2*>(mbar + kBars);  // [2][3]
   float2* in_right = in_left + 6;                              // [2][3]
+  volatile int* feed_mode = reinterpret_cast<volatile int*>(in_right + 6);
 
   const int ny = g.ny;
   const int t = threadIdx.x;
@@ -134,6 +136,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
     if (CLUSTER)
       for (int s = kRing + 1; s < kBars; ++s) mbar_init(smem_u32(&mbar[s]), 1);
     fence_mbar_init();
+    *feed_mode = 0;
   }
   // CLUSTER: every CTA's barriers exist before any neighbour arrives on them.
   if (CLUSTER) cluster_sync_all(); else __syncthreads();
@@ -155,11 +158,11 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
     bool ok = true;
     if (t == 0) {
       mbar_arrive_expect_tx(from_left + 8u * q, kEdgeBytes);
-      ok = mbar_wait_bounded(from_left + 8u * q, par, kWaitLimit);
+      ok = mbar_wait_bounded(from_left + 8u * q, par, kWaitPolls);
     }
     if (t == HALF - 1) {
       mbar_arrive_expect_tx(from_right + 8u * q, kEdgeBytes);
-      ok = mbar_wait_bounded(from_right + 8u * q, par, kWaitLimit);
+      ok = mbar_wait_bounded(from_right + 8u * q, par, kWaitPolls);
     }
     return ok;
   };
@@ -271,8 +274,33 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         }
       }
     };
+    // Thread 0 feeds ring use it + i: the row copies, or, once one of its own waits has given
+    // up, an empty arrival (see tma.cuh).  It tells the two apart at the barrier: feeding use
+    // u (u >= it + 3) it tests, without waiting, the use it has just waited for, u - 3, whose
+    // slot is not yet fed again (so the test cannot mistake a later phase for it).  Reading
+    // timed_out in the loop instead, even once per kRing rows, measured 6% slower.  The give-up
+    // setting (wait_limit 0) withholds the block's first use, so that every thread's wait for
+    // it runs out, and settles it just before its slot is fed again.
+    auto feed = [&](int i) {
+      const unsigned u = it + i;
+      int mode = *feed_mode;
+      if (mode == 0 && i >= 3) {
+        // the use thread 0 has just waited for: open means its wait gave up
+        const unsigned w = u - 3;
+        if (!mbar_test(smem_u32(&mbar[w & (kRing - 1)]), (w / kRing) & 1u)) *feed_mode = mode = 1;
+      }
+      if (g.wait_limit == 0) {
+        if (u == 0) return;
+        if (u == kRing) mbar_arrive(smem_u32(&mbar[0]));
+      }
+      if (mode == 0) {
+        issue(i);
+        return;
+      }
+      mbar_fill_empty(smem_u32(&mbar[i & (kRing - 1)]), u, kRing);
+    };
     if (t == 0) {
-      for (int i = 0; i < 3 && i < n_iter; ++i) issue(i);
+      for (int i = 0; i < 3 && i < n_iter; ++i) feed(i);
     }
 
     Pair q1[4], q2[4], q3[4], acc[4];
@@ -296,7 +324,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         const int slot2 = (j + kRing - 2) % kRing;  // row r-2
         const int slot3 = (j + kRing - 3) % kRing;  // row r-3
         const int slot4 = (j + kRing - 4) % kRing;  // row r-4
-        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitLimit)) timed_out = true;
+        if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitPolls)) timed_out = true;
         // Stage 1 at row r-1 from the ring: k1 = f(psi0).
         const float2* R1 = ring_psi + slot1 * W;
         const float4 c4 = *reinterpret_cast<const float4*>(R1 + col0);
@@ -331,12 +359,12 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
           // r-5, which the copy of row r+3 reuses).  The wait sits after stage 1 so that
           // the draw and stage 1 overlap with the slower warps of the previous row.
           const unsigned g = it + i;
-          if (g > 0 && !mbar_wait_bounded(xbar, (g - 1) & 1u, kWaitLimit)) timed_out = true;
+          if (g > 0 && !mbar_wait_bounded(xbar, (g - 1) & 1u, kWaitPolls)) timed_out = true;
           // The edge threads also wait for the neighbouring CTAs' edge values of iteration
           // i-1.  A neighbour delivers into the same inbox again only at the end of iteration
           // i+1, after it has received this thread's own delivery of iteration i.
           if (CLUSTER && g > 0 && !receive(g - 1)) timed_out = true;
-          if (t == 0 && i + 3 < n_iter) issue(i + 3);
+          if (t == 0 && i + 3 < n_iter) feed(i + 3);
         }
         // Philox words and the variance-free part of the Box-Muller draw for this
         // iteration's output row, in the same straight-line code as stages 2-4 (after the
@@ -442,7 +470,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         } else {
           __syncthreads();
           // Slot of row r+3 held row r-5, last read by stage 4 of the previous iteration.
-          if (t == 0 && i + 3 < n_iter) issue(i + 3);
+          if (t == 0 && i + 3 < n_iter) feed(i + 3);
         }
       }
     }
@@ -451,6 +479,9 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
   // CLUSTER: take the neighbours' last deliveries, so that no store into this CTA's shared
   // memory is still in flight when it exits, then leave together.
   if (CLUSTER && it > 0 && !receive(it - 1)) timed_out = true;
+  // After a wait of thread 0's gave up: copies it issued may still be in flight in the last
+  // ring uses (every earlier one it waited for); a use it filled empty completes at once.
+  if (t == 0 && (timed_out || *feed_mode != 0)) drain_ring(mbar, kRing, it >= kRing ? it - kRing : 0u, it);
   if (timed_out) atomicOr(err_flag, 1);
   if (CLUSTER) cluster_sync_all();
 }
@@ -473,7 +504,7 @@ template <int NX, bool BAND, bool CLUSTER>
 size_t smem_for() {
   using S = WideShape<NX, BAND, CLUSTER>;
   return static_cast<size_t>(kRing) * S::W * 16 + static_cast<size_t>(6) * S::THREADS * 16 +
-         kBars * sizeof(uint64_t) + kInbox * sizeof(float2);
+         kBars * sizeof(uint64_t) + kInbox * sizeof(float2) + kFailWords * sizeof(int);
 }
 
 template <int NX, bool BAND, bool CLUSTER>

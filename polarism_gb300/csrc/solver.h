@@ -49,6 +49,7 @@ struct pg_solver {
   int next_slot = 0;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (length, parity) -> graph
   int* err_flag = nullptr;   // set by kernels whose bounded waits gave up
+  int wait_limit = 100000;   // 0: bounded waits give up at once (pg_set_wait_limit)
   // Device halt word of the steady-state monitor: once it is set every RK4 launch returns
   // at once, so steps queued after the last member stopped leave the state as it was.
   int* halt = nullptr;

@@ -32,6 +32,21 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
       : "memory");
 }
 
+// Non-blocking test: has the phase of parity `parity` completed?
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Plain arrival (release semantics at CTA scope).
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
@@ -81,12 +96,43 @@ __device__ __forceinline__ void st_async_f2(uint32_t cluster_addr, float2 v, uin
                : "memory");
 }
 
-// Bounded wait: gives up after `limit` polls and reports failure instead of spinning
-// forever.
+// Bounded wait: gives up after `limit` polls (none when limit is 0) and reports failure
+// instead of spinning forever.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int limit) {
   for (int k = 0; k < limit; ++k)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+
+// Failure handling of the streaming kernels' waits.  Each wait polls at most kWaitPolls
+// times, a bound compiled into the loop above: the wait sites keep exactly the shape
+// `if (!mbar_wait_bounded(...)) timed_out = true;`, because anything more at them (a flag
+// tested before the wait, a flag read between polls, a jump out of the row loop, even as a
+// cold branch) measured 4-7% slower on the full-width RK4 kernel, whose warps spend part of
+// every row in these polls.  What makes a failure end quickly lives in the one thread that
+// feeds the ring: once its own wait has given up, it completes each later ring slot with an
+// empty arrival instead of a copy (mbar_fill_empty), so every later wait on the ring passes at
+// once on whatever the slot holds, the kernel runs to its end in about the time of one full
+// wait, and the call reports the timeout.
+constexpr int kWaitPolls = 100000;
+// After a timeout, before the block exits, each ring use that may still have a copy in flight
+// is waited for with this fixed bound (a copy that was issued lands within microseconds; the
+// bound only keeps the exit from hanging should one never land).
+constexpr int kDrainPolls = 100000;
+
+// Completes ring use u of slot barrier `bar` (a ring of `ring` slots, count 1) with an empty
+// arrival -- once the slot's previous use has completed: a slot whose copy never landed is left
+// as it is (a second arrival in an open phase is not allowed), and its later waits give up.
+__device__ __forceinline__ void mbar_fill_empty(uint32_t bar, unsigned u, unsigned ring) {
+  if (u >= ring && !mbar_test(bar, ((u - ring) / ring) & 1u)) return;
+  mbar_arrive(bar);
+}
+
+// Waits, bounded by kDrainPolls each, for the ring copies of global ring uses [lo, hi) (use u
+// fills slot u % ring, phase parity (u / ring) & 1).
+__device__ __forceinline__ void drain_ring(const uint64_t* mbar, int ring, unsigned lo, unsigned hi) {
+  for (unsigned u = lo; u < hi; ++u)
+    mbar_wait_bounded(smem_u32(&mbar[u % ring]), (u / ring) & 1u, kDrainPolls);
 }
 
 }  // namespace pg

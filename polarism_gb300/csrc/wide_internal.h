@@ -17,6 +17,9 @@ struct WideGeom {
   long long pot_stride = 0;
   int pot_kind = 0;
   int relax = 0;
+  // 0: the give-up setting (each block's first row copy is withheld, so its waits run out);
+  // otherwise the normal path.  Every wait polls up to kWaitPolls (tma.cuh).
+  int wait_limit = 100000;
 };
 
 bool wide_rk4_supported(int nx, int ny);

@@ -227,6 +227,12 @@ class RK4Engine:
         with four sites a thread (rows of 512 or 1024 sites)."""
         _lib.check(self.lib.pg_rk4_set_kernel(self.handle, int(kind)), "pg_rk4_set_kernel")
 
+    def set_wait_limit(self, polls):
+        """100000 (the default: the polls each mbarrier wait of the TMA-fed kernels makes before it
+        gives up) or 0: the kernels withhold each block's first row copy, so that a wait runs
+        out on a healthy GPU and the next synchronising call reports PG_ERR_TIMEOUT."""
+        _lib.check(self.lib.pg_set_wait_limit(self.handle, int(polls)), "pg_set_wait_limit")
+
     def kernel(self) -> int:
         k = C.c_int32()
         _lib.check(self.lib.pg_rk4_get_kernel(self.handle, C.byref(k)), "pg_rk4_get_kernel")

@@ -157,6 +157,12 @@ class SweepEngine:
             raise ValueError("one active flag per member is required")
         _lib.check(self._lib.pg_sweep_set_active(self._h, mask.ctypes.data), "pg_sweep_set_active")
 
+    def set_wait_limit(self, polls: int):
+        """100000 (the default: the polls each mbarrier wait of the sweep kernel makes before it
+        gives up) or 0: the kernel withholds each block's first row copy, so that a wait runs
+        out and the next synchronising call reports PG_ERR_TIMEOUT."""
+        _lib.check(self._lib.pg_sweep_set_wait_limit(self._h, int(polls)), "pg_sweep_set_wait_limit")
+
     # ------------------------------------------------------------------ stepping
     def advance(self, start_step: int, n_steps: int, stage_scales, use_graphs: bool = True):
         scales = np.ascontiguousarray(stage_scales, dtype=np.float64)
