@@ -79,10 +79,6 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
   float4* xbuf = reinterpret_cast<float4*>(ring_p + kRing * LANES);   // [2][3][HALF]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(xbuf + 6 * HALF);  // [kRing] + exchange barrier
   const uint32_t xbar = smem_u32(&mbar[kRing]);
-  // Thread 0's decisions for the strip leaders: whether ring slot s holds copies (0) or was
-  // completed empty (1); its arm mode (0 copies, 1 empty arrivals; see arm); padding.
-  volatile int* slot_empty = reinterpret_cast<volatile int*>(&mbar[kRing + 1]);  // [kRing]
-  volatile int* arm_mode = slot_empty + kRing;
 
   const int t = threadIdx.x;
   const int col0 = 2 * t;  // ring column of the thread's first site
@@ -90,8 +86,6 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
     if (kSplit) mbar_init(xbar, LANES / 2);
     fence_mbar_init();
-    for (int s = 0; s < kRing; ++s) slot_empty[s] = 0;
-    *arm_mode = 0;
   }
   __syncthreads();
 
@@ -140,36 +134,23 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
     // Thread 0 arms the slot's barrier for the whole row (LANES * 16 bytes) before the
     // strips' leaders issue their bulk copies, so the expected bytes are always registered
     // first.
-    // Thread 0 arms ring use it + i for the strips' copies, or, once one of its own waits has
-    // given up, completes it with an empty arrival and tells the leaders (slot_empty) to copy
-    // nothing into it (see tma.cuh).  It reads its timed_out flag once per work item, before
-    // the item's rows (within the rows, a flag read or a barrier test per row measured 4-8%
-    // slower on this kernel, whose block barrier waits for thread 0 every row); an item in
-    // which a wait gives up runs on with copies, each wait still bounded.  The give-up
-    // setting (wait_limit 0) withholds the block's first use (no arming, no copies) so that
-    // every thread's wait for it runs out, and settles it just before its slot is armed again.
+    // The give-up setting (wait_limit 0) withholds the block's first ring use (no arming, no
+    // copies), so that every thread's wait for it runs out on a healthy GPU, and settles it with
+    // an arrival just before its slot is armed again.  This kernel keeps no other failure
+    // state in its rows: each wait is bounded (kWaitPolls), and the completion of later ring
+    // slots without copies that the full-width kernel uses after a failure measured 4-6%
+    // slower here, where the block barrier waits for thread 0 every row.
     auto arm = [&](int i) {
-      const int slot = i & (kRing - 1);
-      const uint32_t bar = smem_u32(&mbar[slot]);
       const unsigned u = it + i;
       if (wait_limit == 0) {
-        if (u == 0) {
-          slot_empty[slot] = 1;
-          return;
-        }
+        if (u == 0) return;
         if (u == kRing) mbar_arrive(smem_u32(&mbar[0]));
       }
-      if (*arm_mode == 0) {
-        slot_empty[slot] = 0;
-        mbar_arrive_expect_tx(bar, LANES * 16u);
-        return;
-      }
-      slot_empty[slot] = 1;
-      mbar_fill_empty(bar, u, kRing);
+      mbar_arrive_expect_tx(smem_u32(&mbar[i & (kRing - 1)]), LANES * 16u);
     };
     auto issue = [&](int i) {
+      if (wait_limit == 0 && it + i == 0) return;
       const int slot = i & (kRing - 1);
-      if (slot_empty[slot] != 0) return;
       int row = row_first + i;
       while (row >= ny) row -= ny;
       const uint32_t bar = smem_u32(&mbar[slot]);
@@ -179,7 +160,6 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
       bulk_g2s(smem_u32(ring_p + slot * LANES + base), p_m + src, W * 4u, bar);
     };
     if (t == 0) {
-      if (timed_out) *arm_mode = 1;  // a wait of thread 0's gave up in an earlier item
       for (int i = 0; i < (kSplit ? 4 : 3) && i < n_iter; ++i) arm(i);
     }
     __syncthreads();
@@ -209,10 +189,6 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
         const int slot3 = (j + kRing - 3) % kRing;
         const int slot4 = (j + kRing - 4) % kRing;
         if (!mbar_wait_bounded(smem_u32(&mbar[slot0]), parity, kWaitPolls)) timed_out = true;
-        // Thread 0 arms the slot of use i + 4 (split barrier) or i + 3 (block barrier) here,
-        // off the block barrier's path: that slot's previous use completed rows ago, and arming
-        // touches no data (its copies are issued after the barrier that frees the slot).
-        if (t == 0 && i + (kSplit ? 4 : 3) < n_iter) arm(i + (kSplit ? 4 : 3));
         // Philox words and the variance-free part of the Box-Muller draw for this
         // iteration's output row, in the same straight-line code as the four stages so
         // that the integer and SFU work fills the stencil's issue gaps.
@@ -326,10 +302,14 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
         }
         row_out = row_out + 1 == ny ? 0 : row_out + 1;
         if (kSplit) {
+          // Arm the slot the next iteration's copies fill (its last phase, row r-4, has
+          // completed), then arrive on the exchange barrier.
+          if (t == 0 && i + 4 < n_iter) arm(i + 4);
           mbar_arrive(xbar);
         } else {
           // The slot of row r+3 held row r-5, last read by stage 4 of the previous
-          // iteration (thread 0 armed it at the top of this one).
+          // iteration.
+          if (t == 0 && i + 3 < n_iter) arm(i + 3);
           __syncthreads();
           if (lt == 0 && i + 3 < n_iter) issue(i + 3);
         }
@@ -337,15 +317,15 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
     }
     it += n_iter;
   }
-  // After a wait of thread 0's gave up: copies of the last ring uses may still be in flight
-  // (uses completed empty, or long landed, return at once).
-  if (t == 0 && (timed_out || *arm_mode != 0)) drain_ring(mbar, kRing, it >= kRing ? it - kRing : 0u, it);
+  // After a timeout: copies of the last ring uses may still be in flight (a use whose copies
+  // landed returns at once).
+  if (t == 0 && timed_out) drain_ring(mbar, kRing, it >= kRing ? it - kRing : 0u, it);
   if (timed_out) atomicOr(err_flag, 1);
 }
 
 size_t sweep_smem(int lanes) {
   return static_cast<size_t>(kRing) * lanes * 16 + static_cast<size_t>(6) * (lanes / 2) * 16 +
-         (kRing + 1) * sizeof(uint64_t) + (kRing + 2) * sizeof(int);  // + slot_empty, modes
+         (kRing + 1) * sizeof(uint64_t);
 }
 
 template <int LANES>

@@ -159,8 +159,8 @@ class SweepEngine:
 
     def set_wait_limit(self, polls: int):
         """100000 (the default: the polls each mbarrier wait of the sweep kernel makes before it
-        gives up) or 0: the kernel withholds each block's first row copy, so that a wait runs
-        out and the next synchronising call reports PG_ERR_TIMEOUT."""
+        gives up, about two seconds) or 0: the kernel withholds each block's first row copy, so
+        that a wait runs out and the next synchronising call reports PG_ERR_TIMEOUT."""
         _lib.check(self._lib.pg_sweep_set_wait_limit(self._h, int(polls)), "pg_sweep_set_wait_limit")
 
     # ------------------------------------------------------------------ stepping
