@@ -3,6 +3,7 @@
 Run where the Polarism v0.9.2 source tree is available, naming it::
 
     python tests/golden/make_golden.py PATH/TO/POLARISM     # or set POLARISM_REFERENCE
+    python tests/golden/make_golden.py PATH/TO/POLARISM accumulators   # one case only
 
 Every fixture records both the inputs (initial fields, pump arrays at the
 stage times, physics constants) and the reference's outputs, so the tests can
@@ -401,9 +402,67 @@ def spinor_case(out, name, tableau="dp5", adaptive=True, reservoir="double", res
         t=np.float64(ctl.state.t))
 
 
-def main(root):
+def accumulator_case(out, name="accumulators", samples=6):
+    """The reference's own ``MomentumDistribution`` and ``G2Accumulator``
+    (``polarism/results/accumulators.py:95-172``) over a short noisy ``rk4-fdm`` run of two
+    members with different Wigner strengths, sampled after every step.  Stores the sampled
+    fields (so the sums can be formed again, on the host or the device) and the reference's
+    finalised results: n(k) with the s/2 vacuum subtraction, g1, the corrected density moments
+    and g2 (``polarism/analysis/correlations.py:11-29``)."""
+    from polarism.config.simulation_parameters import Config
+    from polarism.results.accumulators import available_accumulators
+    from polarism.simulation_controller import SimulationController
+
+    cfg = Config()
+    cfg.grid.nx, cfg.grid.ny, cfg.grid.lx, cfg.grid.ly = 16, 12, 20.0, 9.0
+    cfg.reservoir.reservoir_type = "single"
+    cfg.potential.potential_type = "zero"
+    cfg.laser.mode = "single"
+    cfg.laser.laser_type = "continuous-gaussian"
+    cfg.laser.P0, cfg.laser.sigma_space = 0.3, 4.0
+    cfg.solver.method = "rk4-fdm"
+    cfg.solver.dt = 2e-3
+    cfg.solver.precision = "double"
+    cfg.solver.total_time = 2e-3 * samples
+    cfg.noise.seed = 5
+    cfg.noise.stochastic = "wigner"
+    ctl = SimulationController(cfg, members=[{"noise.seed": 5, "noise.stochastic_strength": 1.0},
+                                             {"noise.seed": 6, "noise.stochastic_strength": 0.5}])
+    # A condensate well above the Wigner vacuum (|psi|^2 of order 2 against s / 2dV <= 0.53),
+    # so that the corrected moments and g2 are not dominated by the subtraction.
+    rng = np.random.default_rng(11)
+    g = ctl.grid
+    blob = 1.4 * np.exp(-0.5 * (g.X ** 2 + g.Y ** 2) / 5.0 ** 2)
+    shape = np.shape(ctl.state.field)
+    ctl.state.field = (blob + 0.3 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    mom = available_accumulators.lookup("momentum-distribution")(ctl)
+    g2acc = available_accumulators.lookup("g2")(ctl)
+    fields = []
+    for k in range(samples):
+        ctl.solver.advance(ctl.model, ctl.state, 1)
+        fields.append(np.array(ctl.state.field, copy=True))
+        mom.update(ctl.state, ctl.state.t)
+        g2acc.update(ctl.state, ctl.state.t)
+    results = {r.name: np.asarray(r.value) for r in mom.results() + g2acc.results()}
+    np.savez_compressed(
+        out / f"{name}.npz", fields=np.stack(fields), samples=np.int64(samples),
+        cell=np.float64(mom.cell), cells=np.int64(mom.cells),
+        strength=np.asarray(mom.strength).reshape(-1), delta=np.asarray(g2acc.delta).reshape(-1),
+        sum_k=np.asarray(mom.sum_k), sum_density=np.asarray(g2acc.sum_density),
+        sum_density_squared=np.asarray(g2acc.sum_density_squared), **results)
+
+
+CASES = {"accumulators": accumulator_case}
+
+
+def main(root, only=()):
     _import_reference(root)
     HERE.mkdir(exist_ok=True)
+    if only:
+        for name in only:
+            CASES[name](HERE)
+        print("golden fixtures written to", HERE, ":", ", ".join(only))
+        return
     philox_cases(HERE)
     wigner_cases(HERE)
     common = dict(nx=32, ny=24, lx=40.0, ly=30.0, dt=2e-3, p0=0.05, sigma=8.0, seed=42, wigner=True)
@@ -429,11 +488,15 @@ def main(root):
     spinor_case(HERE, "spinor_dp5_shared", reservoir="single", res_components=1, nx=16, ny=8, ticks=16,
                 polarization=0.3)
     spinor_case(HERE, "spinor_rk4_wigner", tableau="rk4", adaptive=False, wigner=True, ticks=4)
+    accumulator_case(HERE)
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    # make_golden.py [PATH/TO/POLARISM] [case ...]: every fixture, or only the named cases
+    # (of CASES); the path may come from POLARISM_REFERENCE instead.
+    args = sys.argv[1:]
+    root = args.pop(0) if args and args[0] not in CASES else reference_root()
     if root is None:
-        sys.exit("usage: make_golden.py PATH/TO/POLARISM (or set POLARISM_REFERENCE)")
-    main(root)
+        sys.exit("usage: make_golden.py PATH/TO/POLARISM [case ...] (or set POLARISM_REFERENCE)")
+    main(root, tuple(args))

@@ -109,3 +109,29 @@ def test_field_norms_on_caller_device_arrays(cuda_lib):
                    "pg_field_norms")
         expect = (np.abs(dev.cpu().numpy().astype(np.complex128)) ** 2).reshape(3, -1).sum(1) * 0.25
         assert np.allclose(out.cpu().numpy(), expect, rtol=1e-12)
+
+
+def test_device_sums_finalise_to_the_reference_accumulators(cuda_lib):
+    """The sampled fields of ``tests/golden/accumulators.npz`` through the device's FP64
+    accumulation (``pg_accumulate``), finalised on the host, against the reference's own
+    MomentumDistribution / G2Accumulator results at 1e-12."""
+    from polarism_gb300 import observables as obs
+    from polarism_gb300.engine import Engine, MemberPhysics
+    from tests.conftest import load_golden
+
+    g = load_golden("accumulators")
+    fields = g["fields"]  # (samples, members, 1, ny, nx) complex128
+    members, ny, nx = fields.shape[1], fields.shape[-2], fields.shape[-1]
+    eng = Engine(nx, ny, members, 1.25, 0.75, 1e-3, MemberPhysics(), "double")
+    res = np.zeros((members, 1, ny, nx))
+    for f in fields:
+        eng.set_state(np.ascontiguousarray(f), res)
+        eng.accumulate(density=True, momentum=True)
+    (s_rho, n), (s_rho2, _), (s_k, _) = (eng.accumulator_sums(k) for k in ("rho", "rho2", "k"))
+    assert n == int(g["samples"])
+    n_k = obs.momentum_distribution(s_k[:, 0], n, float(g["cell"]), int(g["cells"]), g["strength"])
+    mean, squared = obs.density_moments(s_rho[:, 0], s_rho2[:, 0], n, g["delta"])
+    for name, value in (("momentum_distribution", n_k), ("g1", obs.g1(n_k)),
+                        ("density_mean", mean), ("density_squared_mean", squared),
+                        ("g2", obs.g2(mean, squared))):
+        assert rel_l2(value, g[name]) < 1e-12, name

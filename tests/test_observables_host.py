@@ -44,3 +44,32 @@ def test_momentum_distribution_normalisation():
     sum_k = np.full((1, 4, 4), 8.0)
     value = obs.momentum_distribution(sum_k, 2, cell=0.5, cells=16, strength=np.asarray([1.0]))
     assert np.allclose(value, 8.0 * 0.5 / (16 * 2) - 0.5)
+
+
+def test_finalisation_matches_the_reference_accumulators():
+    """The reference's own MomentumDistribution and G2Accumulator results
+    (``polarism/results/accumulators.py:95-172``; two members with Wigner strengths 1 and 0.5,
+    cell 0.9375, six samples of a noisy rk4-fdm run, ``tests/golden/accumulators.npz``):
+    the sums formed again from the sampled fields, then n(k), g1, the corrected density
+    moments and g2 from this module, agree to 1e-12."""
+    from polarism_gb300 import observables as obs
+    from tests.conftest import load_golden
+
+    g = load_golden("accumulators")
+    fields = g["fields"][:, :, 0]  # (samples, members, ny, nx)
+    samples = int(g["samples"])
+    rho = np.abs(fields) ** 2
+    fk = np.fft.fft2(fields, axes=(-2, -1))
+    sums = {"sum_density": rho.sum(0), "sum_density_squared": (rho * rho).sum(0),
+            "sum_k": (fk.real ** 2 + fk.imag ** 2).sum(0)}
+    for name, value in sums.items():
+        np.testing.assert_allclose(value, g[name], rtol=1e-13, atol=0)
+    n_k = obs.momentum_distribution(sums["sum_k"], samples, float(g["cell"]), int(g["cells"]),
+                                    g["strength"])
+    mean, squared = obs.density_moments(sums["sum_density"], sums["sum_density_squared"], samples,
+                                        g["delta"])
+    for name, value in (("momentum_distribution", n_k), ("g1", obs.g1(n_k)),
+                        ("density_mean", mean), ("density_squared_mean", squared),
+                        ("g2", obs.g2(mean, squared))):
+        ref = g[name]
+        assert np.linalg.norm(value - ref) <= 1e-12 * np.linalg.norm(ref), name
