@@ -129,6 +129,10 @@ int pg_set_noise(pg_solver* s, const uint64_t* seeds, const double* gamma,
  * chunks of up to 64 steps into CUDA graphs. */
 int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const double* stage_scales,
                    int use_graphs);
+/* Build, without launching anything, the CUDA graphs an n_steps pg_rk4_advance uses (for
+ * either buffer parity), so that the first such advance replays them instead of capturing (no
+ * counterpart in the reference, which captures on first use; rk4_cuda_solver.py:3564-3602). */
+int pg_rk4_prepare(pg_solver* s, int32_t n_steps);
 
 /* Override the RK4 launch geometry (the autotuner's knobs): tile_w useful columns per
  * block (tile_w >= nx selects one full-width block per row strip) and strip_h output
@@ -147,6 +151,8 @@ int pg_rk4_get_geometry(pg_solver* s, int32_t* tile_w, int32_t* strip_h);
  * the second reservoir half step (ordering 1), with counter step = start_step + k. */
 int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t n_steps,
                      const double* half_scales, int use_graphs);
+/* The same for pg_split_advance of the ordering (see pg_rk4_prepare). */
+int pg_split_prepare(pg_solver* s, int32_t ordering, int32_t n_steps);
 /* Whether the state buffer holds psi(x, y) (0) or its unnormalised spectrum (1). */
 int pg_set_state_kind(pg_solver* s, int32_t spectral);
 int pg_get_state_kind(pg_solver* s, int32_t* spectral);
@@ -259,6 +265,16 @@ int pg_rk4_get_kernel(pg_solver* s, int32_t* kind);
  * the failure path can be exercised (PG_ERR_INVALID for other values).  Changing it drops the
  * captured CUDA graphs. */
 int pg_set_wait_limit(pg_solver* s, int32_t polls);
+
+/* CUDA graph capture failures (rk4_cuda_solver.py:3591-3602 restores the pre-chunk state and
+ * re-runs the chunk with plain launches when a capture fails).  Here a capture only records, so
+ * nothing of a chunk has run when its capture or instantiation fails: pg_rk4_advance and
+ * pg_split_advance run that chunk as plain launches from the same state and count it in
+ * pg_graph_fallbacks.  pg_test_fail_next_graph is a test hook: the next graph this solver
+ * builds fails at capture (1) or instantiation (2) as a failing CUDA call would (0 clears it);
+ * it drops the solver's cached graphs. */
+int pg_test_fail_next_graph(pg_solver* s, int32_t what);
+int64_t pg_graph_fallbacks(pg_solver* s);
 
 /* Number of kernel launches the last advance call issued (graph nodes included). */
 int64_t pg_last_launch_count(pg_solver* s);

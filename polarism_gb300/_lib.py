@@ -65,9 +65,11 @@ SIGNATURES = {
     "pg_set_potential": (C.c_int, [_vp, _vp, C.c_int]),
     "pg_set_noise": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _f64]),
     "pg_rk4_advance": (C.c_int, [_vp, _i64, _i32, _vp, C.c_int]),
+    "pg_rk4_prepare": (C.c_int, [_vp, _i32]),
     "pg_rk4_set_geometry": (C.c_int, [_vp, _i32, _i32]),
     "pg_rk4_get_geometry": (C.c_int, [_vp, C.POINTER(_i32), C.POINTER(_i32)]),
     "pg_split_advance": (C.c_int, [_vp, _i32, _i64, _i32, _vp, C.c_int]),
+    "pg_split_prepare": (C.c_int, [_vp, _i32, _i32]),
     "pg_set_state_kind": (C.c_int, [_vp, _i32]),
     "pg_get_state_kind": (C.c_int, [_vp, C.POINTER(_i32)]),
     "pg_ifrk_advance": (C.c_int, [_vp, _i32, _i64, _i32, _vp]),
@@ -89,6 +91,8 @@ SIGNATURES = {
     "pg_rk4_set_kernel": (C.c_int, [_vp, _i32]),
     "pg_rk4_get_kernel": (C.c_int, [_vp, C.POINTER(_i32)]),
     "pg_set_wait_limit": (C.c_int, [_vp, _i32]),
+    "pg_test_fail_next_graph": (C.c_int, [_vp, _i32]),
+    "pg_graph_fallbacks": (_i64, [_vp]),
     "pg_last_launch_count": (_i64, [_vp]),
     "pg_philox_words": (C.c_int, [_vp, _u64, _vp, _i64]),
     "pg_wigner_normals": (C.c_int, [_vp, _u64, _i32, _vp, _i64]),

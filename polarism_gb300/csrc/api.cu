@@ -253,12 +253,15 @@ int graph_for(pg_solver* s, int len, int parity, cudaGraphExec_t* out) {
     *out = it->second;
     return PG_OK;
   }
+  const int forced = s->graph_failure;  // test hook: fail as the real call would
+  s->graph_failure = 0;
   cudaGraph_t graph = nullptr;
   PG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t launch_err = cudaSuccess;
   for (int k = 0; k < len && launch_err == cudaSuccess; ++k)
     launch_err = launch_step(s, (parity + k) & 1, k);
   cudaError_t end_err = cudaStreamEndCapture(s->stream, &graph);
+  if (forced == 1 && end_err == cudaSuccess) end_err = cudaErrorStreamCaptureInvalidated;
   if (launch_err != cudaSuccess || end_err != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
     pg::set_error(std::string("graph capture failed: ") +
@@ -266,7 +269,7 @@ int graph_for(pg_solver* s, int len, int parity, cudaGraphExec_t* out) {
     return PG_ERR_CUDA;
   }
   cudaGraphExec_t exec = nullptr;
-  cudaError_t inst = cudaGraphInstantiate(&exec, graph, 0);
+  cudaError_t inst = forced == 2 ? cudaErrorInvalidValue : cudaGraphInstantiate(&exec, graph, 0);
   cudaGraphDestroy(graph);
   if (inst != cudaSuccess) {
     pg::set_error(std::string("graph instantiate failed: ") + cudaGetErrorString(inst));
@@ -511,6 +514,38 @@ int pg_set_wait_limit(pg_solver* s, int32_t polls) {
   return PG_OK;
 }
 
+int pg_test_fail_next_graph(pg_solver* s, int32_t what) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_test_fail_next_graph: null solver");
+  PG_CHECK(what >= 0 && what <= 2, PG_ERR_INVALID,
+           "pg_test_fail_next_graph: 0 (none), 1 (capture) or 2 (instantiation)");
+  s->graph_failure = what;
+  free_graphs(s);  // the next chunk must capture anew
+  return PG_OK;
+}
+
+int64_t pg_graph_fallbacks(pg_solver* s) { return s ? s->graph_fallbacks : -1; }
+
+int pg_rk4_prepare(pg_solver* s, int32_t n_steps) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_rk4_prepare: null solver");
+  PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_rk4_prepare: negative step count");
+  // The chunks pg_rk4_advance would cut n_steps into (graphs of even length up to kChunk; a
+  // chunk keeps the buffer parity), for either starting parity.
+  int done = 0;
+  while (done < n_steps) {
+    int len = std::min(kChunk, n_steps - done);
+    if (len >= 2 && (len & 1)) len -= 1;
+    if (len >= 2) {
+      for (int parity = 0; parity < 2; ++parity) {
+        cudaGraphExec_t exec = nullptr;
+        const int rc = graph_for(s, len, parity, &exec);
+        if (rc != PG_OK) return rc;
+      }
+    }
+    done += len;
+  }
+  return PG_OK;
+}
+
 int pg_rk4_get_kernel(pg_solver* s, int32_t* kind) {
   PG_CHECK(s && kind, PG_ERR_INVALID, "pg_rk4_get_kernel: null argument");
   *kind = !use_wide(s) ? 1 : s->rk4_kernel == 3 ? 3 : 2;
@@ -618,10 +653,16 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
                                     3 * s->pump_terms,
                                     start_step + done);
     if (rc != PG_OK) return rc;
-    if (graph) {
-      cudaGraphExec_t exec = nullptr;
-      rc = graph_for(s, len, s->cur, &exec);
-      if (rc != PG_OK) return rc;
+    cudaGraphExec_t exec = nullptr;
+    // A chunk whose graph cannot be captured or instantiated runs as plain launches: capture
+    // only records (nothing of the chunk has run), so the state buffers are as before it, the
+    // role of the reference's pre-chunk copy and restore (rk4_cuda_solver.py:3591-3602).
+    if (graph && graph_for(s, len, s->cur, &exec) != PG_OK) {
+      cudaGetLastError();
+      ++s->graph_fallbacks;
+      exec = nullptr;
+    }
+    if (exec != nullptr) {
       PG_CUDA(cudaGraphLaunch(exec, s->stream));
       s->cur = (s->cur + len) & 1;
     } else {

@@ -66,7 +66,7 @@ int setup_tables(pg_solver* s) {
   // Separable propagators exp(-i hbar k^2 tau / 2m) = (1 + dx[j]) (1 + dy[i]), stored as the
   // differences d = exp(-i theta) - 1 = (-2 sin^2(theta / 2), -sin theta), which keep their
   // relative precision at small theta (a rounded exp(-i theta) there has |f| > 1: its cosine
-  // rounds to 1).  The power-of-two scale of each table is applied apart (row_scale).
+  // rounds to 1).  The power-of-two scale of each table is applied apart (RowPassArgs::scale).
   const size_t per = static_cast<size_t>(nx + ny);
   std::vector<T> prop(static_cast<size_t>(PROP_COUNT) * m * per * 2);
   for (int table = 0; table < PROP_COUNT; ++table) {
@@ -264,6 +264,53 @@ cudaError_t chunk_launches(pg_solver* s, const PassPlan& p, int ordering, int le
   return e;
 }
 
+// The graph of one chunk of `len` steps of the ordering, captured and instantiated on first
+// use (test hook: graph_failure makes the capture (1) or instantiation (2) fail).
+template <typename T>
+int split_graph_for(pg_solver* s, const PassPlan& p, int ordering, int len, cudaGraphExec_t* out) {
+  auto key = std::make_tuple(ordering, len, 0);
+  auto it = s->split_graphs.find(key);
+  if (it != s->split_graphs.end()) {
+    *out = it->second;
+    return PG_OK;
+  }
+  const int forced = s->graph_failure;
+  s->graph_failure = 0;
+  cudaGraph_t graph = nullptr;
+  PG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t le = chunk_launches<T>(s, p, ordering, len);
+  cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
+  if (forced == 1 && ee == cudaSuccess) ee = cudaErrorStreamCaptureInvalidated;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t ie = cudaSuccess;
+  if (le == cudaSuccess && ee == cudaSuccess)
+    ie = forced == 2 ? cudaErrorInvalidValue : cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (le != cudaSuccess || ee != cudaSuccess || ie != cudaSuccess) {
+    set_error(std::string("split-step graph capture failed: ") +
+              cudaGetErrorString(le != cudaSuccess ? le : ee != cudaSuccess ? ee : ie));
+    return PG_ERR_CUDA;
+  }
+  s->split_graphs[key] = exec;
+  *out = exec;
+  return PG_OK;
+}
+
+template <typename T>
+int split_prepare_t(pg_solver* s, int ordering, int n_steps) {
+  const PassPlan p = plan(s);
+  for (int done = 0; done < n_steps;) {
+    const int len = std::min(kChunk, n_steps - done);
+    cudaGraphExec_t exec = nullptr;
+    if (len >= 2) {
+      const int rc = split_graph_for<T>(s, p, ordering, len, &exec);
+      if (rc != PG_OK) return rc;
+    }
+    done += len;
+  }
+  return PG_OK;
+}
+
 template <typename T>
 int split_advance_t(pg_solver* s, int ordering, int64_t start_step, int n_steps,
                     const double* scales, int use_graphs) {
@@ -292,31 +339,15 @@ int split_advance_t(pg_solver* s, int ordering, int64_t start_step, int n_steps,
     int rc = stage_coefficients(s, scales + static_cast<size_t>(done) * 2 * s->pump_terms * m, len,
                                 2 * s->pump_terms, start_step + done);
     if (rc != PG_OK) return rc;
-    if (use_graphs && len >= 2) {
-      auto key = std::make_tuple(ordering, len, 0);
-      auto it = s->split_graphs.find(key);
-      cudaGraphExec_t exec = nullptr;
-      if (it == s->split_graphs.end()) {
-        cudaGraph_t graph = nullptr;
-        PG_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t le = chunk_launches<T>(s, p, ordering, len);
-        cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
-        if (le != cudaSuccess || ee != cudaSuccess) {
-          if (graph) cudaGraphDestroy(graph);
-          set_error(std::string("split-step graph capture failed: ") +
-                    cudaGetErrorString(le != cudaSuccess ? le : ee));
-          return PG_ERR_CUDA;
-        }
-        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ie != cudaSuccess) {
-          set_error(std::string("split-step graph instantiate failed: ") + cudaGetErrorString(ie));
-          return PG_ERR_CUDA;
-        }
-        s->split_graphs[key] = exec;
-      } else {
-        exec = it->second;
-      }
+    cudaGraphExec_t exec = nullptr;
+    if (use_graphs && len >= 2 && split_graph_for<T>(s, p, ordering, len, &exec) != PG_OK) {
+      // A failed capture or instantiation has run nothing of the chunk (capture only records):
+      // the chunk runs as plain launches (see pg_rk4_advance).
+      cudaGetLastError();
+      ++s->graph_fallbacks;
+      exec = nullptr;
+    }
+    if (exec != nullptr) {
       PG_CUDA(cudaGraphLaunch(exec, s->stream));
     } else {
       PG_CUDA(chunk_launches<T>(s, p, ordering, len));
@@ -375,6 +406,18 @@ int pg_split_advance(pg_solver* s, int32_t ordering, int64_t start_step, int32_t
   return s->cfg.precision == PG_DOUBLE
              ? pg::split_advance_t<double>(s, ordering, start_step, n_steps, half_scales, use_graphs)
              : pg::split_advance_t<float>(s, ordering, start_step, n_steps, half_scales, use_graphs);
+}
+
+int pg_split_prepare(pg_solver* s, int32_t ordering, int32_t n_steps) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_split_prepare: null solver");
+  PG_CHECK(ordering == 0 || ordering == 1, PG_ERR_INVALID, "pg_split_prepare: ordering must be 0 or 1");
+  PG_CHECK(n_steps >= 0, PG_ERR_INVALID, "pg_split_prepare: negative step count");
+  PG_CHECK(s->comps == 1 && s->res_comps == 1, PG_ERR_UNSUPPORTED,
+           "pg_split_prepare: two-component fields run on the IFRK path");
+  int rc = pg::ensure_split(s);
+  if (rc != PG_OK) return rc;
+  return s->cfg.precision == PG_DOUBLE ? pg::split_prepare_t<double>(s, ordering, n_steps)
+                                       : pg::split_prepare_t<float>(s, ordering, n_steps);
 }
 
 int pg_set_state_kind(pg_solver* s, int32_t spectral) {

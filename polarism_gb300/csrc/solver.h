@@ -69,6 +69,11 @@ struct pg_solver {
   void* ifrk = nullptr;       // IFRK stage buffers (created on first use)
   void* accum = nullptr;      // FP64 observable sums (created on first use)
   long long last_launches = 0;
+  // Graph capture failures: graph_failure (a test hook) makes the next capture (1) or
+  // instantiation (2) fail as a failing CUDA call would; graph_fallbacks counts the chunks
+  // that ran as plain launches after a capture or instantiation failed.
+  int graph_failure = 0;
+  long long graph_fallbacks = 0;
 };
 
 

@@ -227,6 +227,15 @@ class RK4Engine:
         with four sites a thread (rows of 512 or 1024 sites)."""
         _lib.check(self.lib.pg_rk4_set_kernel(self.handle, int(kind)), "pg_rk4_set_kernel")
 
+    def fail_next_graph(self, what):
+        """Test hook: the next CUDA graph fails at capture (1) or instantiation (2)."""
+        _lib.check(self.lib.pg_test_fail_next_graph(self.handle, int(what)), "pg_test_fail_next_graph")
+
+    @property
+    def graph_fallbacks(self) -> int:
+        """Chunks that ran as plain launches because their graph could not be built."""
+        return int(self.lib.pg_graph_fallbacks(self.handle))
+
     def set_wait_limit(self, polls):
         """100000 (the default: the polls each mbarrier wait of the TMA-fed kernels makes before it
         gives up) or 0: the kernels withhold each block's first row copy, so that a wait runs
@@ -250,6 +259,15 @@ class RK4Engine:
         shape = tuple(int(v) for v in lead) + ((self.pump_terms,) if self.pump_terms > 1 else ()) \
             + (self.members,)
         return np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64), shape))
+
+    def prepare(self, n_steps):
+        """Build the CUDA graphs an ``advance`` of ``n_steps`` uses, launching nothing."""
+        _lib.check(self.lib.pg_rk4_prepare(self.handle, int(n_steps)), "pg_rk4_prepare")
+
+    def split_prepare(self, ordering, n_steps):
+        """Build the CUDA graphs a ``split_advance`` of ``n_steps`` uses, launching nothing."""
+        _lib.check(self.lib.pg_split_prepare(self.handle, int(ordering), int(n_steps)),
+                   "pg_split_prepare")
 
     def advance(self, start_step, n_steps, stage_scales, use_graphs=True):
         """``stage_scales``: array (n_steps, 3, [L,] members) of pump coefficients."""

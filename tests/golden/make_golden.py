@@ -414,7 +414,7 @@ def accumulator_case(out, name="accumulators", samples=6):
     from polarism.simulation_controller import SimulationController
 
     cfg = Config()
-    cfg.grid.nx, cfg.grid.ny, cfg.grid.lx, cfg.grid.ly = 16, 12, 20.0, 9.0
+    cfg.grid.nx, cfg.grid.ny, cfg.grid.lx, cfg.grid.ly = 16, 8, 20.0, 6.0
     cfg.reservoir.reservoir_type = "single"
     cfg.potential.potential_type = "zero"
     cfg.laser.mode = "single"
