@@ -95,6 +95,13 @@ int setup_tables(pg_solver* s) {
   PG_CUDA(cudaMemcpy(s->tw_y, twy.data(), twy.size() * sizeof(T), cudaMemcpyHostToDevice));
   PG_CUDA(cudaMemcpy(s->prop, prop.data(), prop.size() * sizeof(T), cudaMemcpyHostToDevice));
   PG_CUDA(configure_split_kernels<T>(200 * 1024));
+  if (sizeof(T) == 4 && (split_fast_row(nx, ny) || split_fast_col(nx, ny))) {
+    std::vector<float> tw4(4 * 1024);
+    split_fast_twiddles(tw4.data());
+    PG_CUDA(cudaMalloc(&s->tw4, tw4.size() * sizeof(float)));
+    PG_CUDA(cudaMemcpy(s->tw4, tw4.data(), tw4.size() * sizeof(float), cudaMemcpyHostToDevice));
+    PG_CUDA(configure_split_fast());
+  }
   return PG_OK;
 }
 
@@ -220,6 +227,10 @@ cudaError_t row_launch(pg_solver* s, const PassPlan& p, int forward, int table, 
                 (static_cast<size_t>(table < 0 ? 0 : table) * s->cfg.members * per) * 2;
   const T* py = px + static_cast<size_t>(s->cfg.nx) * 2;
   // Member m's factors start at px + m * (nx + ny) complex values (py follows its px).
+  if (sizeof(T) == 4 && s->tw4 != nullptr && split_fast_row(s->cfg.nx, s->cfg.ny))
+    return launch_row_fast(static_cast<float*>(s->psi[s->cur]), static_cast<const float*>(s->tw4),
+                           reinterpret_cast<const float*>(px), reinterpret_cast<const float*>(py),
+                           a, s->cfg.members, s->stream);
   return launch_row_pass<T>(static_cast<T*>(s->psi[s->cur]), static_cast<const T*>(s->tw_x), px,
                             py, a, s->cfg.members, s->stream);
 }
@@ -233,6 +244,12 @@ cudaError_t col_launch(pg_solver* s, const PassPlan& p, int inverse, int op, int
   a.op = op;
   a.scale_offset = scale_offset;
   a.step_offset = step_offset;
+  if (sizeof(T) == 4 && s->tw4 != nullptr && split_fast_col(s->cfg.nx, s->cfg.ny))
+    return launch_col_fast(static_cast<float*>(s->psi[s->cur]), static_cast<float*>(s->res[s->cur]),
+                           static_cast<const float*>(s->pump), static_cast<const float*>(s->potential),
+                           static_cast<const float*>(s->tw4),
+                           static_cast<const SplitConst<float>*>(s->split_consts),
+                           static_cast<const float*>(s->scales), s->step_base, a, s->stream);
   return launch_col_pass<T>(static_cast<T*>(s->psi[s->cur]), static_cast<T*>(s->res[s->cur]),
                             static_cast<const T*>(s->pump), static_cast<const T*>(s->potential),
                             static_cast<const T*>(s->tw_y),
@@ -373,6 +390,8 @@ int split_release(pg_solver* s) {
   s->split_graphs.clear();
   cudaFree(s->tw_x);
   cudaFree(s->tw_y);
+  cudaFree(s->tw4);
+  s->tw4 = nullptr;
   cudaFree(s->prop);
   cudaFree(s->split_consts);
   s->tw_x = s->tw_y = s->prop = s->split_consts = nullptr;

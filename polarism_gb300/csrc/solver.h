@@ -64,6 +64,7 @@ struct pg_solver {
   void* tw_x = nullptr;       // exp(-2 pi i k / nx), k < nx
   void* tw_y = nullptr;
   void* prop = nullptr;       // [table][member][nx + ny] propagator factors
+  void* tw4 = nullptr;        // FP32 1024-point four-step factors W_1024^{n2 k1} (split_fast.cu)
   void* split_consts = nullptr;
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> split_graphs;  // (ordering, len, parity)
   void* ifrk = nullptr;       // IFRK stage buffers (created on first use)

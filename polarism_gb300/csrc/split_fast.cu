@@ -1,0 +1,278 @@
+// Split-step passes for FP32 rows and columns of 1024 sites: register-resident four-step FFTs.
+//
+// A 1024-point transform is 1024 = 32 x 32 (n = n2 + 32 n1, k = k1 + 32 k2):
+//   X[k1 + 32 k2] = sum_n2 W_32^{n2 k2} W_1024^{n2 k1} sum_n1 x[n2 + 32 n1] W_32^{n1 k1}.
+// A thread holds the 32 values x[n2 + 32 n1] of its n2 (n1 = register index), does the inner
+// 32-point DFT in registers, multiplies by W_1024^{n2 k1}, exchanges once through shared
+// memory so that it holds the 32 values of one k1, and does the outer 32-point DFT: it ends
+// with X[k1 + 32 k2] (k2 = register index), the same layout it started from, so the kinetic
+// factor and the local step apply in place.  One exchange per transform replaces the generic
+// kernel's five barrier-separated radix-4 passes through shared memory (split.cu).
+//
+// Rows: a warp per row (lane = n2), the exchange within the warp.  Columns: a block per panel
+// of eight columns (thread = (column, n2)), the exchange across the block, and between the
+// inverse and forward transforms the local step (split_local.cuh) runs over the panel in
+// shared memory as a plain loop, so its code exists once.
+//
+// Precision: every twiddle that is not +-1 or +-i is applied as a rounded value plus its
+// remainder (the 32-point constants and the table W_1024^{n2 k1}), as the generic FP32 passes
+// do: rounded factors alone carry a per-step amplitude bias that drifts the norm over long runs.
+#include <cmath>
+
+#include "split_local.cuh"
+
+namespace pg {
+namespace {
+
+constexpr int kN = 1024;
+constexpr int kRowsPerWarp = 4;             // rows a warp transforms in turn (row pass)
+constexpr int kRowWarps = 8;                // warps a block (row pass)
+constexpr int kPanel = 8;                   // columns a block (column pass)
+constexpr int kXStride = 33;                // padded row of the 32 x 32 exchange
+constexpr int kPanelStride = 32 * 33 + 4;   // one column's exchange block (elements = 4 mod 16)
+
+// W_32^e = exp(-2 pi i e / 32) = c - i s for e = 1..15 (not 8) as {c, s} rounded to FP32 and
+// the remainders {c - c_fp32, s - s_fp32}, from the double-precision cos and sin; e is a
+// constant once the DFT loops are unrolled, so the switch folds to immediates.
+__device__ __forceinline__ float4 w32(int e) {
+  switch (e) {
+    case 1: return make_float4(0.9807852506637573f, 0.19509032368659973f, 2.9739473106360492e-08f, -1.6704715388726754e-09f);
+    case 2: return make_float4(0.9238795042037964f, 0.3826834261417389f, 2.830748968563057e-08f, 6.2233507236442165e-09f);
+    case 3: return make_float4(0.8314695954322815f, 0.5555702447891235f, 1.687026340846387e-08f, -1.1769521357507529e-08f);
+    case 4: return make_float4(0.7071067690849304f, 0.7071067690849304f, 1.2101617485882343e-08f, 1.2101617485882343e-08f);
+    case 5: return make_float4(0.5555702447891235f, 0.8314695954322815f, -1.1769521357507529e-08f, 1.687026340846387e-08f);
+    case 6: return make_float4(0.3826834261417389f, 0.9238795042037964f, 6.2233507236442165e-09f, 2.830748968563057e-08f);
+    case 7: return make_float4(0.19509032368659973f, 0.9807852506637573f, -1.670471427850373e-09f, 2.9739473106360492e-08f);
+    case 9: return make_float4(-0.19509032368659973f, 0.9807852506637573f, 1.6704715388726754e-09f, 2.9739473106360492e-08f);
+    case 10: return make_float4(-0.3826834261417389f, 0.9238795042037964f, -6.2233507236442165e-09f, 2.830748968563057e-08f);
+    case 11: return make_float4(-0.5555702447891235f, 0.8314695954322815f, 1.1769521357507529e-08f, 1.687026340846387e-08f);
+    case 12: return make_float4(-0.7071067690849304f, 0.7071067690849304f, -1.2101617485882343e-08f, 1.2101617485882343e-08f);
+    case 13: return make_float4(-0.8314695954322815f, 0.5555702447891235f, -1.687026340846387e-08f, -1.1769521357507529e-08f);
+    case 14: return make_float4(-0.9238795042037964f, 0.3826834261417389f, -2.830748968563057e-08f, 6.223351167733426e-09f);
+    case 15: return make_float4(-0.9807852506637573f, 0.19509032368659973f, -2.9739473106360492e-08f, -1.6704710947834656e-09f);
+    default: return make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+__host__ __device__ constexpr int brev5(int i) {
+  return ((i & 1) << 4) | ((i & 2) << 2) | (i & 4) | ((i & 8) >> 2) | ((i & 16) >> 4);
+}
+
+// x * W_32^e (forward) or x * conj(W_32^e) (inverse); e is a constant once unrolled.
+template <bool INV>
+__device__ __forceinline__ float2 w32mul(float2 x, int e) {
+  if (e == 0) return x;
+  if (e == 8) return INV ? make_float2(-x.y, x.x) : make_float2(x.y, -x.x);
+  const float4 w = w32(e);
+  const float ch = w.x, sh = w.y, cl = w.z, sl = w.w;
+  // forward: (x.x c + x.y s) + i (x.y c - x.x s); inverse: (x.x c - x.y s) + i (x.y c + x.x s)
+  const float ys = INV ? -x.y : x.y;
+  const float xs = INV ? x.x : -x.x;
+  const float re = fmaf(x.x, ch, fmaf(ys, sh, fmaf(x.x, cl, ys * sl)));
+  const float im = fmaf(x.y, ch, fmaf(xs, sh, fmaf(x.y, cl, xs * sl)));
+  return make_float2(re, im);
+}
+
+// In-register 32-point DFT (radix 2, decimation in time; the bit-reversed read is a renaming).
+template <bool INV>
+__device__ __forceinline__ void dft32(float2 (&v)[32]) {
+  float2 a[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) a[i] = v[brev5(i)];
+#pragma unroll
+  for (int s = 1; s <= 5; ++s) {
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {  // the 16 butterflies of stage s (span m = 2^s)
+      const int h = 1 << (s - 1);
+      const int j = b & (h - 1);
+      const int lo = ((b >> (s - 1)) << s) + j;
+      const float2 u = a[lo];
+      const float2 t = w32mul<INV>(a[lo + h], j << (5 - s));
+      a[lo] = make_float2(u.x + t.x, u.y + t.y);
+      a[lo + h] = make_float2(u.x - t.x, u.y - t.y);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = a[i];
+}
+
+// Inner DFT and the W_1024^{n2 k1} factors (tw4[k1][n2]: rounded value and remainder).
+template <bool INV>
+__device__ __forceinline__ void four_step_first(float2 (&v)[32], int n2, const float4* tw4) {
+  dft32<INV>(v);
+#pragma unroll
+  for (int k1 = 1; k1 < 32; ++k1) {
+    const float4 w = tw4[k1 * 32 + n2];
+    v[k1] = INV ? cmulc2f(v[k1], make_float2(w.x, w.y), make_float2(w.z, w.w))
+                : cmul2f(v[k1], make_float2(w.x, w.y), make_float2(w.z, w.w));
+  }
+}
+
+// A 1024-point transform of a row held by a warp (lane = n2, buf: 32 x kXStride values).
+template <bool INV>
+__device__ __forceinline__ void fft1024_warp(float2 (&v)[32], int lane, float2* buf,
+                                             const float4* tw4) {
+  four_step_first<INV>(v, lane, tw4);
+#pragma unroll
+  for (int k1 = 0; k1 < 32; ++k1) buf[k1 * kXStride + lane] = v[k1];
+  __syncwarp();
+#pragma unroll
+  for (int n2 = 0; n2 < 32; ++n2) v[n2] = buf[lane * kXStride + n2];
+  __syncwarp();
+  dft32<INV>(v);
+}
+
+// ------------------------------------------------------------------ row pass
+__global__ void __launch_bounds__(kRowWarps * 32, 2)
+    row_fast_kernel(float2* __restrict__ data, const float4* __restrict__ tw4_g,
+                    const float2* __restrict__ px, const float2* __restrict__ py,
+                    const RowPassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* tw4 = reinterpret_cast<float4*>(smem_raw);                     // [32][32]
+  float2* xb = reinterpret_cast<float2*>(tw4 + kN);                      // [warps][32][33]
+  for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int member = blockIdx.z;
+  float2* buf = xb + warp * 32 * kXStride;
+  const float2* pxm = px + static_cast<long long>(member) * a.table_stride;
+  const float2* pym = py + static_cast<long long>(member) * a.table_stride;
+  const float scale = static_cast<float>(a.scale);
+  const long long plane = static_cast<long long>(kN) * a.ny;
+  for (int q = 0; q < kRowsPerWarp; ++q) {
+    const int row = (blockIdx.x * kRowWarps + warp) * kRowsPerWarp + q;
+    float2* d = data + member * plane + static_cast<long long>(row) * kN;
+    float2 v[32];
+#pragma unroll
+    for (int t = 0; t < 32; ++t) v[t] = d[lane + 32 * t];
+    if (a.forward) fft1024_warp<false>(v, lane, buf, tw4);
+    if (a.multiply) {
+      // psi (1 + dx) (1 + dy) scale, the factor differences stored (see split.cu)
+      const float2 dy = pym[row];
+#pragma unroll
+      for (int r = 0; r < 32; ++r) {
+        const float2 dx = pxm[lane + 32 * r];
+        const float2 dxy = cmul(dx, dy);
+        const float2 f1 = make_float2(dx.x + dy.x + dxy.x, dx.y + dy.y + dxy.y);
+        const float2 vf = cmul(v[r], f1);
+        v[r] = make_float2((v[r].x + vf.x) * scale, (v[r].y + vf.y) * scale);
+      }
+    }
+    if (a.inverse) fft1024_warp<true>(v, lane, buf, tw4);
+#pragma unroll
+    for (int t = 0; t < 32; ++t) d[lane + 32 * t] = v[t];
+  }
+}
+
+// ------------------------------------------------------------------ column pass
+// A 1024-point transform of the block's eight columns (thread = (column c, n2 = p)); pan is
+// the panel's exchange buffer ([c][k1][n2], columns kPanelStride apart).
+template <bool INV>
+__device__ __forceinline__ void fft1024_panel(float2 (&v)[32], int p, int c, float2* pan,
+                                              const float4* tw4) {
+  four_step_first<INV>(v, p, tw4);
+  __syncthreads();  // every earlier read of pan is done
+#pragma unroll
+  for (int k1 = 0; k1 < 32; ++k1) pan[c * kPanelStride + k1 * kXStride + p] = v[k1];
+  __syncthreads();
+#pragma unroll
+  for (int n2 = 0; n2 < 32; ++n2) v[n2] = pan[c * kPanelStride + p * kXStride + n2];
+  dft32<INV>(v);
+}
+
+__global__ void __launch_bounds__(kPanel * 32, 2)
+    col_fast_kernel(float2* __restrict__ data, float* __restrict__ res, const float* __restrict__ pump,
+                    const float* __restrict__ potential, const float4* __restrict__ tw4_g,
+                    const SplitConst<float>* __restrict__ consts, const float* __restrict__ scales,
+                    const unsigned long long* __restrict__ step_base, const ColPassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* tw4 = reinterpret_cast<float4*>(smem_raw);  // [32][32]
+  float2* pan = reinterpret_cast<float2*>(tw4 + kN);  // exchange, or [row][c] for the local step
+  for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = lane & (kPanel - 1);
+  const int p = warp * 4 + (lane >> 3);  // n2: 0..31
+  const int member = blockIdx.z;
+  const int x0 = blockIdx.x * kPanel;
+  const long long plane = static_cast<long long>(a.nx) * kN;
+  float2* d = data + member * plane + x0 + c;
+  float2 v[32];
+#pragma unroll
+  for (int t = 0; t < 32; ++t) v[t] = d[static_cast<long long>(p + 32 * t) * a.nx];
+  if (a.inverse) fft1024_panel<true>(v, p, c, pan, tw4);
+  if (a.op != SPLIT_OP_NONE) {
+    // Through shared memory in site order, so that the local step is one loop.
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 32; ++t) pan[(p + 32 * t) * kPanel + c] = v[t];
+    __syncthreads();
+    const LocalStep<float> local(a, member, res, pump, potential, consts, scales, step_base);
+#pragma unroll 2
+    for (int e = threadIdx.x; e < kPanel * kN; e += blockDim.x) {
+      const int row = e / kPanel, col = e % kPanel;
+      float2 x = pan[e];
+      local.apply(x, static_cast<long long>(row) * a.nx + x0 + col);
+      pan[e] = x;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 32; ++t) v[t] = pan[(p + 32 * t) * kPanel + c];
+  }
+  if (a.forward) fft1024_panel<false>(v, p, c, pan, tw4);
+#pragma unroll
+  for (int t = 0; t < 32; ++t) d[static_cast<long long>(p + 32 * t) * a.nx] = v[t];
+}
+
+size_t row_fast_smem() { return kN * sizeof(float4) + kRowWarps * 32 * kXStride * sizeof(float2); }
+size_t col_fast_smem() { return kN * sizeof(float4) + kPanel * kPanelStride * sizeof(float2); }
+
+}  // namespace
+
+bool split_fast_row(int nx, int ny) { return nx == kN && ny % (kRowWarps * kRowsPerWarp) == 0; }
+bool split_fast_col(int nx, int ny) { return ny == kN && nx % kPanel == 0; }
+
+void split_fast_twiddles(float* out) {
+  // tw4[k1][n2] = W_1024^{n2 k1}: rounded value and remainder, from double precision.
+  const double pi = 3.141592653589793238462643383279502884;
+  for (int k1 = 0; k1 < 32; ++k1)
+    for (int n2 = 0; n2 < 32; ++n2) {
+      const double ang = -2.0 * pi * static_cast<double>((n2 * k1) % kN) / kN;
+      const double cr = std::cos(ang), ci = std::sin(ang);
+      float* o = out + 4 * (k1 * 32 + n2);
+      o[0] = static_cast<float>(cr);
+      o[1] = static_cast<float>(ci);
+      o[2] = static_cast<float>(cr - static_cast<double>(o[0]));
+      o[3] = static_cast<float>(ci - static_cast<double>(o[1]));
+    }
+}
+
+cudaError_t configure_split_fast() {
+  cudaError_t e = cudaFuncSetAttribute(row_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(row_fast_smem()));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(col_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(col_fast_smem()));
+}
+
+cudaError_t launch_row_fast(float* data, const float* tw4, const float* px, const float* py,
+                            const RowPassArgs& a, int members, cudaStream_t stream) {
+  const dim3 grid(a.ny / (kRowWarps * kRowsPerWarp), 1, members);
+  row_fast_kernel<<<grid, kRowWarps * 32, row_fast_smem(), stream>>>(
+      reinterpret_cast<float2*>(data), reinterpret_cast<const float4*>(tw4),
+      reinterpret_cast<const float2*>(px), reinterpret_cast<const float2*>(py), a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_col_fast(float* data, float* res, const float* pump, const float* potential,
+                            const float* tw4, const SplitConst<float>* consts, const float* scales,
+                            const unsigned long long* step_base, const ColPassArgs& a,
+                            cudaStream_t stream) {
+  const dim3 grid(a.nx / kPanel, 1, a.members);
+  col_fast_kernel<<<grid, kPanel * 32, col_fast_smem(), stream>>>(
+      reinterpret_cast<float2*>(data), res, pump, potential, reinterpret_cast<const float4*>(tw4),
+      consts, scales, step_base, a);
+  return cudaGetLastError();
+}
+
+}  // namespace pg

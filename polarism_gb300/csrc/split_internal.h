@@ -77,6 +77,20 @@ cudaError_t launch_col_pass(T* data, T* res, const T* pump, const T* potential, 
 template <typename T>
 cudaError_t configure_split_kernels(size_t max_smem);
 
+// Register-resident four-step passes for FP32 rows / columns of 1024 sites (split_fast.cu):
+// whether they apply, their W_1024^{n2 k1} table (1024 float4: rounded value, remainder),
+// attribute set-up and launches (arguments as launch_row_pass / launch_col_pass).
+bool split_fast_row(int nx, int ny);
+bool split_fast_col(int nx, int ny);
+void split_fast_twiddles(float* out);
+cudaError_t configure_split_fast();
+cudaError_t launch_row_fast(float* data, const float* tw4, const float* px, const float* py,
+                            const RowPassArgs& a, int members, cudaStream_t stream);
+cudaError_t launch_col_fast(float* data, float* res, const float* pump, const float* potential,
+                            const float* tw4, const SplitConst<float>* consts, const float* scales,
+                            const unsigned long long* step_base, const ColPassArgs& a,
+                            cudaStream_t stream);
+
 // Complex values one thread stages per FFT pass: blocks need N * C <= this * threads.
 int split_max_vals(bool is_double);
 
