@@ -208,12 +208,39 @@ __global__ void __launch_bounds__(kPanel * 32, 2)
     for (int t = 0; t < 32; ++t) pan[(p + 32 * t) * kPanel + c] = v[t];
     __syncthreads();
     const LocalStep<float> local(a, member, res, pump, potential, consts, scales, step_base);
+    if (local.single()) {
+      const int nx = a.nx;
+      switch (a.op * 2 + (a.noise ? 1 : 0)) {
+#define PG_SPLIT_SINGLE(OP, NOISE)                                                      \
+  case OP * 2 + NOISE:                                                                  \
+    _Pragma("unroll 4") for (int e = threadIdx.x; e < kPanel * kN; e += blockDim.x) {   \
+      float2 x = pan[e];                                                                \
+      local.apply_single<OP, NOISE>(x, (e / kPanel) * nx + x0 + e % kPanel);            \
+      pan[e] = x;                                                                       \
+    }                                                                                   \
+    break;
+        PG_SPLIT_SINGLE(SPLIT_OP_KOUTER, 1)
+        PG_SPLIT_SINGLE(SPLIT_OP_KOUTER, 0)
+        PG_SPLIT_SINGLE(SPLIT_OP_NONLINEAR, 1)
+        PG_SPLIT_SINGLE(SPLIT_OP_NONLINEAR, 0)
+        PG_SPLIT_SINGLE(SPLIT_OP_RES_START, 1)
+        PG_SPLIT_SINGLE(SPLIT_OP_RES_START, 0)
+        PG_SPLIT_SINGLE(SPLIT_OP_RES_END, 1)
+        PG_SPLIT_SINGLE(SPLIT_OP_RES_END, 0)
+        PG_SPLIT_SINGLE(SPLIT_OP_RES_END_START, 1)
+        PG_SPLIT_SINGLE(SPLIT_OP_RES_END_START, 0)
+#undef PG_SPLIT_SINGLE
+        default:
+          break;
+      }
+    } else {
 #pragma unroll 2
-    for (int e = threadIdx.x; e < kPanel * kN; e += blockDim.x) {
-      const int row = e / kPanel, col = e % kPanel;
-      float2 x = pan[e];
-      local.apply(x, static_cast<long long>(row) * a.nx + x0 + col);
-      pan[e] = x;
+      for (int e = threadIdx.x; e < kPanel * kN; e += blockDim.x) {
+        const int row = e / kPanel, col = e % kPanel;
+        float2 x = pan[e];
+        local.apply(x, static_cast<long long>(row) * a.nx + x0 + col);
+        pan[e] = x;
+      }
     }
     __syncthreads();
 #pragma unroll

@@ -124,7 +124,10 @@ template <typename T>
 struct LocalStep {
   using C2 = typename C2T<T>::type;
   SplitConst<T> k;
-  const ColPassArgs* a;
+  // The launch's settings, copied (a pointer to the kernel's parameter would move it to local
+  // memory and make every read a local load).
+  int op, reservoir, noise, pot_kind;
+  long long pump_term_stride;
   int m_count, L;
   const T* c0;
   const T* c1;
@@ -140,7 +143,11 @@ struct LocalStep {
   __device__ __forceinline__ LocalStep(const ColPassArgs& args, int member, T* res, const T* pump,
                                        const T* potential, const SplitConst<T>* consts,
                                        const T* scales, const unsigned long long* step_base) {
-    a = &args;
+    op = args.op;
+    reservoir = args.reservoir;
+    noise = args.noise;
+    pot_kind = args.potential;
+    pump_term_stride = args.pump_term_stride;
     k = consts[member];
     m_count = args.members;
     // Coefficients [k][sample][term][member]; the term axis exists only with several lasers.
@@ -169,18 +176,52 @@ struct LocalStep {
   __device__ __forceinline__ void res_half(T& n, T& n2, T rho, T pump_value) const {
     if (two) {
       reservoir_half2(n, n2, rho, pump_value, h, quadratic, k);
-    } else if (a->reservoir) {
+    } else if (reservoir) {
       n = reservoir_half(n, rho, pump_value, h, k);
     }
   }
 
+  // Whether apply_single covers this launch: one reservoir field, one laser and no potential
+  // (the common case, without the general code's branches).
+  __device__ __forceinline__ bool single() const {
+    return reservoir && !two && L == 1 && vm == nullptr;
+  }
+
+  // apply() for that case with the operation known at compile time: the same operations, in
+  // the same order (32-bit site offsets: a member holds fewer than 2^31 sites).
+  template <int OP, bool NOISE>
+  __device__ __forceinline__ void apply_single(C2& v, int o) const {
+    T n = rm[o];
+    const T P = pm[o];
+    if (OP == SPLIT_OP_KOUTER) {
+      n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
+      nonlinear(v.x, v.y, n, T(0), false, T(0), T(0), dt, k);
+      n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s1, P), h, k);
+    } else if (OP == SPLIT_OP_RES_START || OP == SPLIT_OP_RES_END) {
+      n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
+    } else if (OP == SPLIT_OP_RES_END_START) {
+      const T rho = v.x * v.x + v.y * v.y;
+      n = reservoir_half(n, rho, mul_rn_t(s0, P), h, k);
+      n = reservoir_half(n, rho, mul_rn_t(s1, P), h, k);
+    } else if (OP == SPLIT_OP_NONLINEAR) {
+      nonlinear(v.x, v.y, n, T(0), false, T(0), T(0), dt, k);
+    }
+    if (NOISE && (OP == SPLIT_OP_KOUTER || OP == SPLIT_OP_NONLINEAR)) {
+      const uint32_t cell[1] = {static_cast<uint32_t>(o)};
+      Words4 w[1];
+      philox_cells(cell, prefix, w);
+      WignerDraw<T>::apply(w[0], k.noise_a + k.noise_b * n, v.x, v.y);
+    }
+    if (OP != SPLIT_OP_NONLINEAR) rm[o] = n;
+  }
+
   __device__ __forceinline__ void apply(C2& v, long long o) const {
-    T n = (a->reservoir || two) ? rm[o] : T(0);
+    T n = (reservoir || two) ? rm[o] : T(0);
     T n2 = two ? rm2[o] : T(0);
     T Pa, Pb;  // pump at the first and the second coefficient sample
     if (L > 1) {
-      Pa = pump_terms_value(pm, a->pump_term_stride, c0, m_count, L, o);
-      Pb = pump_terms_value(pm, a->pump_term_stride, c1, m_count, L, o);
+      Pa = pump_terms_value(pm, pump_term_stride, c0, m_count, L, o);
+      Pb = pump_terms_value(pm, pump_term_stride, c1, m_count, L, o);
     } else {
       const T P = pm[o];
       Pa = mul_rn_t(s0, P);
@@ -188,16 +229,16 @@ struct LocalStep {
     }
     T vre = T(0), vim = T(0);
     if (vm) {
-      vre = a->potential == 2 ? vm[2 * o] : vm[o];
-      vim = a->potential == 2 ? vm[2 * o + 1] : T(0);
+      vre = pot_kind == 2 ? vm[2 * o] : vm[o];
+      vim = pot_kind == 2 ? vm[2 * o + 1] : T(0);
     }
     bool add_noise = false;
-    switch (a->op) {
+    switch (op) {
       case SPLIT_OP_KOUTER:
         res_half(n, n2, v.x * v.x + v.y * v.y, Pa);
         nonlinear(v.x, v.y, n, n2, two, vre, vim, dt, k);
         res_half(n, n2, v.x * v.x + v.y * v.y, Pb);
-        add_noise = a->noise != 0;
+        add_noise = noise != 0;
         break;
       case SPLIT_OP_RES_START:
         res_half(n, n2, v.x * v.x + v.y * v.y, Pa);
@@ -210,7 +251,7 @@ struct LocalStep {
       }
       case SPLIT_OP_NONLINEAR:
         nonlinear(v.x, v.y, n, n2, two, vre, vim, dt, k);
-        add_noise = a->noise != 0;
+        add_noise = noise != 0;
         break;
       case SPLIT_OP_RES_END:
         res_half(n, n2, v.x * v.x + v.y * v.y, Pa);
@@ -224,7 +265,7 @@ struct LocalStep {
       philox_cells(cell, prefix, w);
       WignerDraw<T>::apply(w[0], k.noise_a + k.noise_b * n, v.x, v.y);
     }
-    if (a->reservoir || two) rm[o] = n;
+    if (reservoir || two) rm[o] = n;
     if (two) rm2[o] = n2;
   }
 };
