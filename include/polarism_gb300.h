@@ -276,6 +276,13 @@ int pg_set_wait_limit(pg_solver* s, int32_t polls);
 int pg_test_fail_next_graph(pg_solver* s, int32_t what);
 int64_t pg_graph_fallbacks(pg_solver* s);
 
+/* Host waits the library has made for this solver: host_syncs counts every wait for the
+ * solver's stream to drain (each synchronising entry point: state and input copies, results,
+ * set-up), throttle_waits the advance calls that found their pinned staging slot still in
+ * use (the host had queued four chunks ahead of the device) and waited for it.  An advance
+ * and a pg_steady_update make no host wait of the first kind. */
+int pg_sync_counts(pg_solver* s, int64_t* host_syncs, int64_t* throttle_waits);
+
 /* Number of kernel launches the last advance call issued (graph nodes included). */
 int64_t pg_last_launch_count(pg_solver* s);
 
@@ -341,6 +348,19 @@ int64_t pg_sweep_last_launch_count(pg_sweep* w);
 int pg_sweep_synchronize(pg_sweep* w);
 /* Per-member steady-state comparison with the previous call, as pg_steady_check. */
 int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, double* norms);
+/* The device steady-state monitor for the sweep, as pg_steady_reset / _update / _poll /
+ * _results for a solver (each member's norm uses its own cell area dx * dy): no host wait
+ * from reset to results, and with halt_when_all_stopped every sweep launch after the check
+ * that finds every member stopped returns at once.  A run uses either these or
+ * pg_sweep_steady_check. */
+int pg_sweep_steady_reset(pg_sweep* w);
+int pg_sweep_steady_update(pg_sweep* w, int64_t step, int32_t record, double rtol,
+                           int32_t halt_when_all_stopped);
+int pg_sweep_steady_poll(pg_sweep* w, int32_t* stopped, int64_t* updates_done);
+int pg_sweep_steady_results(pg_sweep* w, double* rel_density, double* rel_norm, double* norms,
+                            int64_t* stop_steps, int64_t* halt_step);
+/* Host waits of the sweep handle, as pg_sync_counts. */
+int pg_sweep_sync_counts(pg_sweep* w, int64_t* host_syncs, int64_t* throttle_waits);
 
 /* Learned warm start (no counterpart in the reference: Polarism has no learned component).
  * Kernels of a Fourier neural operator trained on solver-made steady states.  All run

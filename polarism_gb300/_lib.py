@@ -93,6 +93,7 @@ SIGNATURES = {
     "pg_set_wait_limit": (C.c_int, [_vp, _i32]),
     "pg_test_fail_next_graph": (C.c_int, [_vp, _i32]),
     "pg_graph_fallbacks": (_i64, [_vp]),
+    "pg_sync_counts": (C.c_int, [_vp, C.POINTER(_i64), C.POINTER(_i64)]),
     "pg_last_launch_count": (_i64, [_vp]),
     "pg_philox_words": (C.c_int, [_vp, _u64, _vp, _i64]),
     "pg_wigner_normals": (C.c_int, [_vp, _u64, _i32, _vp, _i64]),
@@ -117,6 +118,11 @@ SIGNATURES = {
     "pg_sweep_last_launch_count": (_i64, [_vp]),
     "pg_sweep_synchronize": (C.c_int, [_vp]),
     "pg_sweep_steady_check": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pg_sweep_steady_reset": (C.c_int, [_vp]),
+    "pg_sweep_steady_update": (C.c_int, [_vp, _i64, _i32, _f64, _i32]),
+    "pg_sweep_steady_poll": (C.c_int, [_vp, C.POINTER(_i32), C.POINTER(_i64)]),
+    "pg_sweep_steady_results": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.POINTER(_i64)]),
+    "pg_sweep_sync_counts": (C.c_int, [_vp, C.POINTER(_i64), C.POINTER(_i64)]),
     "pg_gemm_bf16": (C.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _i32,
                                C.c_float, C.c_float, _i32, _i64, _i64, _i64, _vp]),
     "pg_gemm_bf16_2d": (C.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _i32,

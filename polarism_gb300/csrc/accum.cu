@@ -9,13 +9,12 @@
 //   steady-state comparison of simulation_controller.py:710-734 (relative density and norm
 //   changes against the previous check), reduced in FP64 through per-block partial sums.
 // * The device-resident steady-state monitor (pg_steady_update / _poll / _results): the
-//   comparison, the per-member stop decision and the first stop step of
-//   simulation_controller.py:698-734 are made by a one-block kernel after the partial sums, so
-//   the chunk loop of simulation_controller.py:1063-1130 needs no host round trip per check.
-//   The kernel publishes (update index, members stopped) in one 64-bit word of mapped host
-//   memory that the host reads without waiting, and, when asked, sets the solver's halt word
-//   once every member has stopped: RK4 launches queued after that return at once, so the run
-//   ends on the step of the deciding check as the reference's loop does.
+//   partial sums here, then the decision of steady_monitor.cu (comparison, per-member stop
+//   decision and first stop step of simulation_controller.py:698-734), so the chunk loop of
+//   simulation_controller.py:1063-1130 needs no host round trip per check.  Once every member
+//   has stopped the solver's halt word is set: RK4 and split-step launches queued after that
+//   return at once, so the run ends on the step of the deciding check as the reference's
+//   loop does.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -25,6 +24,7 @@
 #include "ifrk_internal.h"
 #include "pg_internal.h"
 #include "solver.h"
+#include "steady_monitor.h"
 
 namespace pg {
 namespace {
@@ -145,74 +145,17 @@ __global__ void steady_partials_kernel(const typename C2T<T>::type* __restrict__
   }
 }
 
-// Per-member decision of one steady-state check from the partial sums (one block): relative
-// density and norm changes, the stop criterion of simulation_controller.py:728-729 and the
-// first stop step (_record_stops, :698-708).  results = [rel_density | rel_norm | norm].
-__global__ void steady_decide_kernel(const double* __restrict__ partials, int blocks, int members,
-                                     double cell, int have_old, int record, double rtol,
-                                     long long step, int halt_when_all, double* __restrict__ norm_old,
-                                     long long* __restrict__ stop_step, double* __restrict__ results,
-                                     int* __restrict__ halt, long long* __restrict__ halt_step,
-                                     unsigned long long* __restrict__ host_word,
-                                     unsigned int update_index) {
-  __shared__ int stopped;
-  if (halt != nullptr && __ldcg(halt) != 0) return;  // already halted: nothing has changed
-  if (threadIdx.x == 0) stopped = 0;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
-  for (int m = warp; m < members; m += warps) {
-    double v[3] = {0.0, 0.0, 0.0};
-    for (int b = lane; b < blocks; b += 32)
-      for (int q = 0; q < 3; ++q) v[q] += partials[(static_cast<long long>(m) * blocks + b) * 3 + q];
-    for (int q = 0; q < 3; ++q)
-      for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
-    if (lane == 0) {
-      const double norm = v[2] * cell;
-      double rd = INFINITY, rn = INFINITY;
-      if (have_old) {
-        rd = sqrt(v[0]) / fmax(sqrt(v[1]), 1e-30);
-        rn = fabs(norm - norm_old[m]) / fmax(norm_old[m], 1e-30);
-        const bool reached = norm < 1e-30 || (rn < rtol && rd < rtol);
-        if (record && reached && stop_step[m] < 0) stop_step[m] = step;
-      }
-      results[m] = rd;
-      results[members + m] = rn;
-      results[2 * members + m] = norm;
-      norm_old[m] = norm;
-      if (stop_step[m] >= 0) atomicAdd(&stopped, 1);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (halt_when_all && stopped == members && halt != nullptr) {
-      *halt = 1;
-      *halt_step = step;
-    }
-    *reinterpret_cast<volatile unsigned long long*>(host_word) =
-        (static_cast<unsigned long long>(update_index) << 32) | static_cast<unsigned int>(stopped);
-    __threadfence_system();
-  }
-}
-
 struct AccumBuffers {
   double* sum_rho = nullptr;
   double* sum_rho2 = nullptr;
   double* sum_k = nullptr;
   void* half = nullptr;      // scratch spectrum for the momentum distribution
   void* rho_old = nullptr;   // density at the previous steady-state check
-  bool have_old = false;
   double* partials = nullptr;
   int partial_blocks = 0;    // per member
   double* out = nullptr;     // device results (members)
   long long samples_rho = 0, samples_k = 0;
-  // Device steady-state monitor.
-  double* norm_old = nullptr;        // device, members
-  long long* stop_step = nullptr;    // device, members (-1: not stopped)
-  double* results = nullptr;         // device, 3 * members
-  long long* halt_step = nullptr;    // device
-  unsigned long long* host_word = nullptr;  // mapped host memory: (update index << 32) | stopped
-  unsigned long long* dev_word = nullptr;   // its device alias
-  unsigned int updates = 0;          // checks enqueued since the last reset
+  SteadyMonitor mon;                 // device steady-state monitor (its have_old: rho_old holds a check)
 };
 
 constexpr int kReduceThreads = 256;
@@ -256,11 +199,7 @@ void accum_release(pg_solver* s) {
   cudaFree(a->rho_old);
   cudaFree(a->partials);
   cudaFree(a->out);
-  cudaFree(a->norm_old);
-  cudaFree(a->stop_step);
-  cudaFree(a->results);
-  cudaFree(a->halt_step);
-  if (a->host_word) cudaFreeHost(a->host_word);
+  steady_monitor_free(a->mon);
   delete a;
   s->accum = nullptr;
 }
@@ -376,7 +315,7 @@ int pg_accumulator_sums(pg_solver* s, int32_t kind, double* out, int64_t* sample
   double* src = kind == 0 ? a.sum_rho : kind == 1 ? a.sum_rho2 : kind == 2 ? a.sum_k : nullptr;
   PG_CHECK(src, PG_ERR_INVALID, "pg_accumulator_sums: kind 0 sum rho, 1 sum rho^2, 2 sum |psi_k|^2");
   PG_CUDA(cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   *samples = kind == 2 ? a.samples_k : a.samples_rho;
   return PG_OK;
 }
@@ -398,7 +337,7 @@ int pg_accumulator_load(pg_solver* s, int32_t kind, const double* sums, int64_t 
   }
   if (!*dst) PG_CUDA(cudaMalloc(dst, bytes));
   PG_CUDA(cudaMemcpyAsync(*dst, sums, bytes, cudaMemcpyHostToDevice, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   if (kind == 2)
     a.samples_k = samples;
   else
@@ -410,23 +349,23 @@ int pg_steady_export(pg_solver* s, void* density, double* norms, int64_t* stop_s
                      int32_t* have_reference) {
   PG_CHECK(s && have_reference, PG_ERR_INVALID, "pg_steady_export: null argument");
   *have_reference = 0;
-  if (!s->accum || !pg::acc(s).norm_old) {
+  if (!s->accum || !pg::acc(s).mon.norm_old) {
     if (stop_steps)
       for (int m = 0; m < s->cfg.members; ++m) stop_steps[m] = -1;
     return PG_OK;
   }
   pg::AccumBuffers& a = pg::acc(s);
   const int m = s->cfg.members;
-  PG_CUDA(cudaStreamSynchronize(s->stream));
-  if (a.have_old) {
+  PG_CUDA(pg::stream_sync(s));
+  if (a.mon.have_old) {
     if (density)
       PG_CUDA(cudaMemcpy(density, a.rho_old, static_cast<size_t>(s->sites) * s->real_size,
                          cudaMemcpyDeviceToHost));
-    if (norms) PG_CUDA(cudaMemcpy(norms, a.norm_old, sizeof(double) * m, cudaMemcpyDeviceToHost));
+    if (norms) PG_CUDA(cudaMemcpy(norms, a.mon.norm_old, sizeof(double) * m, cudaMemcpyDeviceToHost));
     *have_reference = 1;
   }
   if (stop_steps)
-    PG_CUDA(cudaMemcpy(stop_steps, a.stop_step, sizeof(long long) * m, cudaMemcpyDeviceToHost));
+    PG_CUDA(cudaMemcpy(stop_steps, a.mon.stop_step, sizeof(long long) * m, cudaMemcpyDeviceToHost));
   return PG_OK;
 }
 
@@ -439,14 +378,15 @@ int pg_steady_import(pg_solver* s, const void* density, const double* norms,
   if (rc != PG_OK) return rc;
   pg::AccumBuffers& a = pg::acc(s);
   const int m = s->cfg.members;
+  if (have_reference || stop_steps) ++s->host_syncs;  // blocking copies
   if (have_reference) {
     PG_CUDA(cudaMemcpy(a.rho_old, density, static_cast<size_t>(s->sites) * s->real_size,
                        cudaMemcpyHostToDevice));
-    PG_CUDA(cudaMemcpy(a.norm_old, norms, sizeof(double) * m, cudaMemcpyHostToDevice));
-    a.have_old = true;
+    PG_CUDA(cudaMemcpy(a.mon.norm_old, norms, sizeof(double) * m, cudaMemcpyHostToDevice));
+    a.mon.have_old = true;
   }
   if (stop_steps)
-    PG_CUDA(cudaMemcpy(a.stop_step, stop_steps, sizeof(long long) * m, cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpy(a.mon.stop_step, stop_steps, sizeof(long long) * m, cudaMemcpyHostToDevice));
   return PG_OK;
 }
 
@@ -459,8 +399,8 @@ int pg_accumulator_reset(pg_solver* s) {
   if (a.sum_rho2) PG_CUDA(cudaMemsetAsync(a.sum_rho2, 0, bytes, s->stream));
   if (a.sum_k) PG_CUDA(cudaMemsetAsync(a.sum_k, 0, bytes, s->stream));
   a.samples_rho = a.samples_k = 0;
-  a.have_old = false;
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  a.mon.have_old = false;
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -479,7 +419,7 @@ int pg_norms(pg_solver* s, double* out) {
                                    a.partials, a.partial_blocks, a.out, s->stream);
   PG_CUDA(e);
   PG_CUDA(cudaMemcpyAsync(out, a.out, sizeof(double) * s->cfg.members, cudaMemcpyDeviceToHost, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -488,25 +428,10 @@ int pg_steady_reset(pg_solver* s) {
   int rc = pg::ensure_accum(s);
   if (rc != PG_OK) return rc;
   pg::AccumBuffers& a = pg::acc(s);
-  const int m = s->cfg.members;
-  if (!a.norm_old) {
-    PG_CUDA(cudaMalloc(&a.norm_old, sizeof(double) * m));
-    PG_CUDA(cudaMalloc(&a.stop_step, sizeof(long long) * m));
-    PG_CUDA(cudaMalloc(&a.results, sizeof(double) * 3 * m));
-    PG_CUDA(cudaMalloc(&a.halt_step, sizeof(long long)));
-    PG_CUDA(cudaHostAlloc(&a.host_word, sizeof(unsigned long long), cudaHostAllocMapped));
-    PG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&a.dev_word), a.host_word, 0));
-  }
+  PG_CUDA(pg::steady_monitor_alloc(a.mon, s->cfg.members));
   if (!a.rho_old) PG_CUDA(cudaMalloc(&a.rho_old, static_cast<size_t>(s->sites) * s->real_size));
-  PG_CUDA(cudaStreamSynchronize(s->stream));  // no check of an earlier run is still in flight
-  PG_CUDA(cudaMemsetAsync(a.norm_old, 0, sizeof(double) * m, s->stream));
-  PG_CUDA(cudaMemsetAsync(a.stop_step, 0xff, sizeof(long long) * m, s->stream));  // -1
-  PG_CUDA(cudaMemsetAsync(a.halt_step, 0xff, sizeof(long long), s->stream));
-  PG_CUDA(cudaMemsetAsync(s->halt, 0, sizeof(int), s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
-  *reinterpret_cast<volatile unsigned long long*>(a.host_word) = 0ull;
-  a.have_old = false;
-  a.updates = 0;
+  // Stream ordered, without a host wait (steady_monitor_reset).
+  PG_CUDA(pg::steady_monitor_reset(a.mon, s->halt, s->stream));
   return PG_OK;
 }
 
@@ -518,7 +443,7 @@ int pg_steady_update(pg_solver* s, int64_t step, int32_t record, double rtol,
   int rc = pg::ensure_accum(s);
   if (rc != PG_OK) return rc;
   pg::AccumBuffers& a = pg::acc(s);
-  if (!a.norm_old) {
+  if (!a.mon.norm_old) {
     rc = pg_steady_reset(s);
     if (rc != PG_OK) return rc;
   }
@@ -527,53 +452,42 @@ int pg_steady_update(pg_solver* s, int64_t step, int32_t record, double rtol,
   if (s->cfg.precision == PG_DOUBLE)
     pg::steady_partials_kernel<double><<<dim3(blocks, m), 256, 0, s->stream>>>(
         static_cast<const double2*>(s->psi[s->cur]), static_cast<double*>(a.rho_old), s->plane,
-        s->comps, a.have_old ? 1 : 0, a.partials, s->halt);
+        s->comps, a.mon.have_old ? 1 : 0, a.partials, s->halt);
   else
     pg::steady_partials_kernel<float><<<dim3(blocks, m), 256, 0, s->stream>>>(
         static_cast<const float2*>(s->psi[s->cur]), static_cast<float*>(a.rho_old), s->plane,
-        s->comps, a.have_old ? 1 : 0, a.partials, s->halt);
+        s->comps, a.mon.have_old ? 1 : 0, a.partials, s->halt);
   PG_CUDA(cudaGetLastError());
-  a.updates += 1;
-  pg::steady_decide_kernel<<<1, 256, 0, s->stream>>>(
-      a.partials, blocks, m, s->cfg.dx * s->cfg.dy, a.have_old ? 1 : 0, record ? 1 : 0, rtol,
-      static_cast<long long>(step), halt_when_all_stopped ? 1 : 0, a.norm_old, a.stop_step,
-      a.results, s->halt, a.halt_step, a.dev_word, a.updates);
-  PG_CUDA(cudaGetLastError());
-  a.have_old = true;
+  PG_CUDA(pg::steady_monitor_decide(a.mon, a.partials, blocks, nullptr, s->cfg.dx * s->cfg.dy,
+                                    record ? 1 : 0, rtol, static_cast<long long>(step), s->flips,
+                                    halt_when_all_stopped ? 1 : 0, s->halt, s->stream));
   return PG_OK;
 }
 
 int pg_steady_poll(pg_solver* s, int32_t* stopped, int64_t* updates_done) {
   PG_CHECK(s && stopped && updates_done, PG_ERR_INVALID, "pg_steady_poll: null argument");
-  if (!s->accum || !pg::acc(s).host_word) {
+  if (!s->accum) {
     *stopped = 0;
     *updates_done = 0;
     return PG_OK;
   }
-  const unsigned long long w = *reinterpret_cast<volatile unsigned long long*>(pg::acc(s).host_word);
-  *stopped = static_cast<int32_t>(w & 0xffffffffull);
-  *updates_done = static_cast<int64_t>(w >> 32);
+  pg::steady_monitor_poll(pg::acc(s).mon, stopped, updates_done);
   return PG_OK;
 }
 
 int pg_steady_results(pg_solver* s, double* rel_density, double* rel_norm, double* norms,
                       int64_t* stop_steps, int64_t* halt_step) {
   PG_CHECK(s, PG_ERR_INVALID, "pg_steady_results: null solver");
-  PG_CHECK(s->accum && pg::acc(s).norm_old, PG_ERR_INVALID,
+  PG_CHECK(s->accum && pg::acc(s).mon.norm_old, PG_ERR_INVALID,
            "pg_steady_results: no steady-state check has been made");
   pg::AccumBuffers& a = pg::acc(s);
   const int m = s->cfg.members;
   std::vector<double> res(static_cast<size_t>(3) * m);
   std::vector<long long> stops(m);
-  long long hs = -1;
+  long long hs[2] = {-1, -1};  // step and flips of the halting check
   int halted = 0;
-  PG_CUDA(cudaMemcpyAsync(res.data(), a.results, res.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                          s->stream));
-  PG_CUDA(cudaMemcpyAsync(stops.data(), a.stop_step, stops.size() * sizeof(long long),
-                          cudaMemcpyDeviceToHost, s->stream));
-  PG_CUDA(cudaMemcpyAsync(&halted, s->halt, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-  PG_CUDA(cudaMemcpyAsync(&hs, a.halt_step, sizeof(long long), cudaMemcpyDeviceToHost, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::steady_monitor_fetch(a.mon, s->halt, res.data(), stops.data(), &halted, hs, s->stream));
+  PG_CUDA(pg::stream_sync(s));
   for (int mm = 0; mm < m; ++mm) {
     if (rel_density) rel_density[mm] = res[mm];
     if (rel_norm) rel_norm[mm] = res[m + mm];
@@ -583,13 +497,15 @@ int pg_steady_results(pg_solver* s, double* rel_density, double* rel_norm, doubl
   if (halted) {
     // RK4 launches after the halt returned without writing, yet the host swapped the
     // ping-pong buffers for each of them: the state of the halt step is under the parity it
-    // had then.  Clear the halt so that the solver steps again.
-    s->cur ^= static_cast<int>((s->parity_step - hs) & 1);
-    s->parity_step = hs;
+    // had then (split steps, in place, swap nothing).  Clear the halt so that the solver
+    // steps again.
+    s->cur ^= static_cast<int>((s->flips - hs[1]) & 1);
+    s->flips = hs[1];
+    s->parity_step = hs[0];
     PG_CUDA(cudaMemsetAsync(s->halt, 0, sizeof(int), s->stream));
-    PG_CUDA(cudaStreamSynchronize(s->stream));
+    PG_CUDA(pg::stream_sync(s));
   }
-  if (halt_step) *halt_step = halted ? hs : -1;
+  if (halt_step) *halt_step = halted ? hs[0] : -1;
   return PG_OK;
 }
 

@@ -73,6 +73,7 @@ namespace pg {
 int stage_coefficients(pg_solver* s, const double* coeffs, int len, int per_step, int64_t step) {
   pg_solver::Slot& slot = s->staging[s->next_slot];
   s->next_slot = (s->next_slot + 1) % kStagingSlots;
+  if (cudaEventQuery(slot.done) == cudaErrorNotReady) ++s->throttle_waits;
   PG_CUDA(cudaEventSynchronize(slot.done));
   const int m = s->cfg.members;
   const size_t count = static_cast<size_t>(len) * per_step * m;
@@ -151,7 +152,7 @@ int upload_consts(pg_solver* s) {
     PG_CUDA(cudaMemcpyAsync(s->consts, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice,
                             s->stream));
   }
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -426,7 +427,7 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
 }
 
 void pg_destroy(pg_solver* s) {
-  if (s && s->stream) cudaStreamSynchronize(s->stream);
+  if (s && s->stream) pg::stream_sync(s);
   release(s);
 }
 
@@ -437,10 +438,10 @@ namespace {
 int check_device_flag(pg_solver* s) {
   int flag = 0;
   PG_CUDA(cudaMemcpyAsync(&flag, s->err_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   if (flag) {
     cudaMemsetAsync(s->err_flag, 0, sizeof(int), s->stream);
-    cudaStreamSynchronize(s->stream);
+    pg::stream_sync(s);
     pg::set_error("a bounded device wait timed out; results of the last advance are invalid");
     return PG_ERR_TIMEOUT;
   }
@@ -450,7 +451,7 @@ int check_device_flag(pg_solver* s) {
 
 int pg_synchronize(pg_solver* s) {
   PG_CHECK(s, PG_ERR_INVALID, "pg_synchronize: null solver");
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return check_device_flag(s);
 }
 
@@ -465,7 +466,7 @@ int pg_set_state(pg_solver* s, const void* psi, const void* res, int on_device) 
   if (s->cfg.reservoir != PG_RES_NONE)
     PG_CUDA(cudaMemcpyAsync(s->res[s->cur], res, static_cast<size_t>(s->res_values) * s->real_size,
                             kind, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -477,7 +478,7 @@ int pg_get_state(pg_solver* s, void* psi, void* res, int on_device) {
   if (res && s->cfg.reservoir != PG_RES_NONE)
     PG_CUDA(cudaMemcpyAsync(res, s->res[s->cur], static_cast<size_t>(s->res_values) * s->real_size,
                             kind, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return check_device_flag(s);
 }
 
@@ -508,7 +509,7 @@ int pg_set_wait_limit(pg_solver* s, int32_t polls) {
   PG_CHECK(polls == 0 || polls == pg::kWaitPolls, PG_ERR_INVALID,
            "pg_set_wait_limit: polls must be 0 (the give-up setting: every wait gives up at once) "
            "or 100000 (the kernels' compiled bound)");
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   s->wait_limit = polls;
   free_graphs(s);  // captured launches carry the old limit
   return PG_OK;
@@ -524,6 +525,13 @@ int pg_test_fail_next_graph(pg_solver* s, int32_t what) {
 }
 
 int64_t pg_graph_fallbacks(pg_solver* s) { return s ? s->graph_fallbacks : -1; }
+
+int pg_sync_counts(pg_solver* s, int64_t* host_syncs, int64_t* throttle_waits) {
+  PG_CHECK(s && host_syncs && throttle_waits, PG_ERR_INVALID, "pg_sync_counts: null argument");
+  *host_syncs = s->host_syncs;
+  *throttle_waits = s->throttle_waits;
+  return PG_OK;
+}
 
 int pg_rk4_prepare(pg_solver* s, int32_t n_steps) {
   PG_CHECK(s, PG_ERR_INVALID, "pg_rk4_prepare: null solver");
@@ -564,7 +572,7 @@ int pg_set_pump(pg_solver* s, const void* envelope, int on_device) {
   const size_t bytes = static_cast<size_t>(s->pump_term_stride) * s->pump_terms * s->real_size;
   PG_CUDA(cudaMemcpyAsync(s->pump, envelope, bytes,
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -576,7 +584,7 @@ int pg_set_potential(pg_solver* s, const void* potential, int on_device) {
                        s->real_size * (s->cfg.potential == PG_POT_COMPLEX ? 2 : 1);
   PG_CUDA(cudaMemcpyAsync(s->potential, potential, bytes,
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -665,10 +673,12 @@ int pg_rk4_advance(pg_solver* s, int64_t start_step, int32_t n_steps, const doub
     if (exec != nullptr) {
       PG_CUDA(cudaGraphLaunch(exec, s->stream));
       s->cur = (s->cur + len) & 1;
+      s->flips += len;
     } else {
       for (int k = 0; k < len; ++k) {
         PG_CUDA(launch_step(s, s->cur, k));
         s->cur ^= 1;
+        ++s->flips;
       }
     }
     s->last_launches += len;

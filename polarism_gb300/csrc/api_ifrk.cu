@@ -129,14 +129,16 @@ int ensure_ifrk(pg_solver* s) {
       host[m] = SpinorConst{p.hbar / (2.0 * p.m_eff), 0.5 * p.zeeman, p.te_tm, 1.0 / p.hbar};
     }
     PG_CUDA(cudaMalloc(&b->spin, host.size() * sizeof(SpinorConst)));
-    PG_CUDA(cudaMemcpy(b->spin, host.data(), host.size() * sizeof(SpinorConst), cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpyAsync(b->spin, host.data(), host.size() * sizeof(SpinorConst),
+                            cudaMemcpyHostToDevice, s->stream));
+    PG_CUDA(pg::stream_sync(s));
     if (c.precision == PG_SINGLE) {
       PG_CUDA(cudaMalloc(&b->spin_modes, sizeof(float) * kSpinModeFields * static_cast<size_t>(s->plane) *
                                              c.members));
       PG_CUDA(launch_spin_mode_table(b->spin_modes, b->spin, c.nx, c.ny, c.members,
                                      2.0 * kPi2 / (static_cast<double>(c.nx) * c.dx),
                                      2.0 * kPi2 / (static_cast<double>(c.ny) * c.dy), s->stream));
-      PG_CUDA(cudaStreamSynchronize(s->stream));
+      PG_CUDA(pg::stream_sync(s));
     }
   }
   const size_t esize = s->real_size;
@@ -184,7 +186,7 @@ int upload_tables(pg_solver* s, const std::vector<double>& taus) {
   }
   PG_CUDA(cudaMemcpyAsync(b.tables, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice,
                           s->stream));
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -443,7 +445,7 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
     const size_t count = static_cast<size_t>(panels) * s->cfg.members;
     PG_CUDA(cudaMemcpyAsync(b.host_partials.data(), b.partials, count * sizeof(double),
                             cudaMemcpyDeviceToHost, s->stream));
-    PG_CUDA(cudaStreamSynchronize(s->stream));
+    PG_CUDA(pg::stream_sync(s));
     // Values per member entering the RMS: every field component and reservoir plane.
     const double sites = static_cast<double>(s->plane) * (s->comps + s->res_fields * s->res_comps);
     double err = 0.0;

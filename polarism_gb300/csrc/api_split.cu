@@ -91,17 +91,23 @@ int setup_tables(pg_solver* s) {
   PG_CUDA(cudaMalloc(&s->tw_y, twy.size() * sizeof(T)));
   PG_CUDA(cudaMalloc(&s->prop, prop.size() * sizeof(T)));
   PG_CUDA(cudaMalloc(&s->split_consts, static_cast<size_t>(m) * sizeof(SplitConst<T>)));
-  PG_CUDA(cudaMemcpy(s->tw_x, twx.data(), twx.size() * sizeof(T), cudaMemcpyHostToDevice));
-  PG_CUDA(cudaMemcpy(s->tw_y, twy.data(), twy.size() * sizeof(T), cudaMemcpyHostToDevice));
-  PG_CUDA(cudaMemcpy(s->prop, prop.data(), prop.size() * sizeof(T), cudaMemcpyHostToDevice));
+  PG_CUDA(cudaMemcpyAsync(s->tw_x, twx.data(), twx.size() * sizeof(T), cudaMemcpyHostToDevice,
+                          s->stream));
+  PG_CUDA(cudaMemcpyAsync(s->tw_y, twy.data(), twy.size() * sizeof(T), cudaMemcpyHostToDevice,
+                          s->stream));
+  PG_CUDA(cudaMemcpyAsync(s->prop, prop.data(), prop.size() * sizeof(T), cudaMemcpyHostToDevice,
+                          s->stream));
   PG_CUDA(configure_split_kernels<T>(200 * 1024));
   if (sizeof(T) == 4 && (split_fast_row(nx, ny) || split_fast_col(nx, ny))) {
     std::vector<float> tw4(4 * 1024);
     split_fast_twiddles(tw4.data());
     PG_CUDA(cudaMalloc(&s->tw4, tw4.size() * sizeof(float)));
-    PG_CUDA(cudaMemcpy(s->tw4, tw4.data(), tw4.size() * sizeof(float), cudaMemcpyHostToDevice));
+    PG_CUDA(cudaMemcpyAsync(s->tw4, tw4.data(), tw4.size() * sizeof(float), cudaMemcpyHostToDevice,
+                            s->stream));
     PG_CUDA(configure_split_fast());
+    PG_CUDA(pg::stream_sync(s));  // the host tables go out of scope
   }
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -136,7 +142,9 @@ int upload_split_consts(pg_solver* s) {
       k.seed = 0ull;
     }
   }
-  PG_CUDA(cudaMemcpy(s->split_consts, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice));
+  PG_CUDA(cudaMemcpyAsync(s->split_consts, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice,
+                          s->stream));
+  PG_CUDA(pg::stream_sync(s));
   return PG_OK;
 }
 
@@ -183,6 +191,7 @@ PassPlan plan(const pg_solver* s) {
   int threads = block_threads(static_cast<long long>(c.ny / rows) * c.members, rows * c.nx);
   r.threads = threads;
   r.table_stride = c.nx + c.ny;
+  r.halt = s->halt;
   ColPassArgs& k = p.col;
   k.nx = c.nx;
   k.ny = c.ny;
@@ -209,6 +218,7 @@ PassPlan plan(const pg_solver* s) {
   k.pot_stride = c.potential_per_member ? s->plane : 0;
   k.dt_d = c.dt;
   k.dt_f = static_cast<float>(c.dt);
+  k.halt = s->halt;
   return p;
 }
 

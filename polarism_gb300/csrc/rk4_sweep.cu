@@ -31,6 +31,7 @@
 #include "philox.cuh"
 #include "pg_internal.h"
 #include "rk4_site.cuh"
+#include "steady_monitor.h"
 #include "tma.cuh"
 
 namespace pg {
@@ -66,7 +67,9 @@ __global__ void __launch_bounds__(LANES / 2, (LANES >= 1024 ? 1 : 2))
                      const SweepMember* __restrict__ members, const SweepItem* __restrict__ items,
                      const int n_items, const int n_members, const float* __restrict__ scales,
                      const unsigned long long* __restrict__ step_base, const int step_offset,
-                     const float dt, const int wait_limit, int* __restrict__ err_flag) {
+                     const float dt, const int wait_limit, int* __restrict__ err_flag,
+                     const int* __restrict__ halt) {
+  if (halt != nullptr && __ldcg(halt) != 0) return;  // steady-state monitor halted the sweep
   constexpr int HALF = LANES / 2;
   // One block per SM (1024 lanes): a split arrive/wait barrier lets its warps drift apart
   // by up to a row, which measured faster; with two blocks per SM the blocks already
@@ -357,8 +360,10 @@ int blocks_per_sm(bool noise) {
 // sum rho_old^2, sum rho; rho_old <- rho (polarism/simulation_controller.py:710-734).
 __global__ void sweep_steady_partials_kernel(const float2* __restrict__ psi, float* __restrict__ rho_old,
                                              const SweepMember* __restrict__ members, int have_old,
-                                             double* __restrict__ partials) {
+                                             double* __restrict__ partials,
+                                             const int* __restrict__ halt) {
   __shared__ double red[3][32];
+  if (halt != nullptr && __ldcg(halt) != 0) return;  // the state no longer advances
   const SweepMember mem = members[blockIdx.y];
   const long long sites = static_cast<long long>(mem.nx) * mem.ny;
   double d2 = 0.0, o2 = 0.0, n = 0.0;
@@ -440,12 +445,28 @@ struct pg_sweep {
   double* partials = nullptr;
   bool have_old = false;
   std::vector<double> norm_old;
+  // Device steady-state monitor (pg_sweep_steady_update): decisions, halt word (every sweep
+  // launch returns at once while it is set), per-member cell areas, and the buffer swaps so
+  // far (the parity of the halting check's state).
+  pg::SteadyMonitor mon;
+  int* halt = nullptr;
+  double* cells = nullptr;
+  long long flips = 0;
+  // Host waits (pg_sweep_sync_counts), as the solver handle counts them.
+  long long host_syncs = 0;
+  long long throttle_waits = 0;
 };
 
 namespace {
 
 using pg::SweepItem;
 using pg::SweepMember;
+
+// Wait for everything queued on the sweep's stream (counted in host_syncs).
+cudaError_t sweep_sync(pg_sweep* w) {
+  ++w->host_syncs;
+  return cudaStreamSynchronize(w->stream);
+}
 
 bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
@@ -480,6 +501,9 @@ void sweep_release(pg_sweep* w) {
   cudaFree(w->err_flag);
   cudaFree(w->rho_old);
   cudaFree(w->partials);
+  pg::steady_monitor_free(w->mon);
+  cudaFree(w->halt);
+  cudaFree(w->cells);
   if (w->t_begin) cudaEventDestroy(w->t_begin);
   if (w->t_end) cudaEventDestroy(w->t_end);
   if (w->stream) cudaStreamDestroy(w->stream);
@@ -514,7 +538,7 @@ int upload_sweep_consts(pg_sweep* w) {
   }
   PG_CUDA(cudaMemcpyAsync(w->consts, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice,
                           w->stream));
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   return PG_OK;
 }
 
@@ -561,7 +585,7 @@ int build_items(pg_sweep* w, int lanes, int strip_rows) {
   if (!items.empty())
     PG_CUDA(cudaMemcpyAsync(w->ditems, items.data(), items.size() * sizeof(SweepItem),
                             cudaMemcpyHostToDevice, w->stream));
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   w->n_items = static_cast<int>(items.size());
   const long long resident = static_cast<long long>(lanes_blocks_per_sm(lanes, true)) * w->sm_count;
   w->blocks = static_cast<int>(std::max<long long>(1, std::min<long long>(resident, w->n_items)));
@@ -629,7 +653,7 @@ cudaError_t launch_sweep_step(pg_sweep* w, int from, int step_offset) {
       reinterpret_cast<const float2*>(w->psi[from]), w->res[from], w->pump,                    \
       reinterpret_cast<float2*>(w->psi[to]), w->res[to], w->consts, w->dmembers, w->ditems,     \
       w->n_items, w->members, w->scales, w->step_base, step_offset, dt, w->wait_limit,           \
-      w->err_flag)
+      w->err_flag, w->halt)
   if (w->lanes == 1024) {
     if (w->noise) PG_SWEEP_LAUNCH(1024, true); else PG_SWEEP_LAUNCH(1024, false);
   } else {
@@ -673,6 +697,7 @@ int sweep_graph_for(pg_sweep* w, int len, int parity, cudaGraphExec_t* out) {
 int stage_sweep_coefficients(pg_sweep* w, const double* coeffs, int len, int64_t step) {
   pg_sweep::Slot& slot = w->staging[w->next_slot];
   w->next_slot = (w->next_slot + 1) % pg::kSweepSlots;
+  if (cudaEventQuery(slot.done) == cudaErrorNotReady) ++w->throttle_waits;
   PG_CUDA(cudaEventSynchronize(slot.done));
   const size_t count = static_cast<size_t>(len) * 3 * w->members;
   float* h = static_cast<float*>(slot.host);
@@ -690,10 +715,10 @@ int stage_sweep_coefficients(pg_sweep* w, const double* coeffs, int len, int64_t
 int sweep_check_flag(pg_sweep* w) {
   int flag = 0;
   PG_CUDA(cudaMemcpyAsync(&flag, w->err_flag, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   if (flag) {
     cudaMemsetAsync(w->err_flag, 0, sizeof(int), w->stream);
-    cudaStreamSynchronize(w->stream);
+    sweep_sync(w);
     pg::set_error("a bounded device wait timed out; results of the last advance are invalid");
     return PG_ERR_TIMEOUT;
   }
@@ -766,6 +791,14 @@ int pg_sweep_create(int32_t members, const pg_sweep_grid* grids, const pg_physic
   cudaMemsetAsync(w->step_base, 0, sizeof(unsigned long long), w->stream);
   if ((e = cudaMalloc(&w->err_flag, sizeof(int))) != cudaSuccess) return fail(e, "error flag");
   cudaMemsetAsync(w->err_flag, 0, sizeof(int), w->stream);
+  if ((e = cudaMalloc(&w->halt, sizeof(int))) != cudaSuccess) return fail(e, "halt word");
+  cudaMemsetAsync(w->halt, 0, sizeof(int), w->stream);
+  std::vector<double> cells(members);
+  for (int m = 0; m < members; ++m) cells[m] = grids[m].dx * grids[m].dy;
+  if ((e = cudaMalloc(&w->cells, members * sizeof(double))) != cudaSuccess) return fail(e, "cells");
+  if ((e = cudaMemcpyAsync(w->cells, cells.data(), members * sizeof(double), cudaMemcpyHostToDevice,
+                           w->stream)) != cudaSuccess)
+    return fail(e, "cells upload");
   if ((e = pg::configure_lanes<512>()) != cudaSuccess) return fail(e, "kernel attributes");
   if ((e = pg::configure_lanes<1024>()) != cudaSuccess) return fail(e, "kernel attributes");
   const size_t staging_bytes = static_cast<size_t>(pg::kSweepChunk) * 3 * members * 4 + 64;
@@ -812,7 +845,7 @@ int pg_sweep_set_state(pg_sweep* w, const void* psi, const void* res, int on_dev
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   PG_CUDA(cudaMemcpyAsync(w->psi[w->cur], psi, static_cast<size_t>(w->sites) * 8, kind, w->stream));
   PG_CUDA(cudaMemcpyAsync(w->res[w->cur], res, static_cast<size_t>(w->sites) * 4, kind, w->stream));
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   return PG_OK;
 }
 
@@ -822,7 +855,7 @@ int pg_sweep_get_state(pg_sweep* w, void* psi, void* res, int on_device) {
   PG_CUDA(cudaMemcpyAsync(psi, w->psi[w->cur], static_cast<size_t>(w->sites) * 8, kind, w->stream));
   if (res)
     PG_CUDA(cudaMemcpyAsync(res, w->res[w->cur], static_cast<size_t>(w->sites) * 4, kind, w->stream));
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   return sweep_check_flag(w);
 }
 
@@ -837,7 +870,7 @@ int pg_sweep_set_pump(pg_sweep* w, const void* envelope, int on_device) {
   PG_CHECK(w && envelope, PG_ERR_INVALID, "pg_sweep_set_pump: null argument");
   PG_CUDA(cudaMemcpyAsync(w->pump, envelope, static_cast<size_t>(w->sites) * 4,
                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, w->stream));
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   return PG_OK;
 }
 
@@ -863,7 +896,7 @@ int pg_sweep_set_tiling(pg_sweep* w, int32_t lanes, int32_t strip_rows) {
   PG_CHECK(w, PG_ERR_INVALID, "pg_sweep_set_tiling: null sweep");
   int rc = check_tiling(w, lanes, strip_rows);
   if (rc != PG_OK) return rc;
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   return build_items(w, lanes, strip_rows);
 }
 
@@ -872,7 +905,7 @@ int pg_sweep_set_wait_limit(pg_sweep* w, int32_t polls) {
   PG_CHECK(polls == 0 || polls == pg::kWaitPolls, PG_ERR_INVALID,
            "pg_sweep_set_wait_limit: polls must be 0 (the give-up setting: every wait gives up at "
            "once) or 100000 (the kernel's compiled bound)");
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   w->wait_limit = polls;
   sweep_free_graphs(w);  // captured launches carry the old setting
   return PG_OK;
@@ -891,7 +924,7 @@ int pg_sweep_get_tiling(pg_sweep* w, int32_t* lanes, int32_t* strip_rows, int32_
 
 int pg_sweep_set_active(pg_sweep* w, const uint8_t* active) {
   PG_CHECK(w, PG_ERR_INVALID, "pg_sweep_set_active: null sweep");
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   for (int m = 0; m < w->members; ++m) w->active[m] = active ? (active[m] ? 1 : 0) : 1;
   // An inactive member keeps its state: copy it into the other parity buffer now, since
   // the ping-pong buffers of active members swap every step and the state of an
@@ -931,6 +964,7 @@ int pg_sweep_advance(pg_sweep* w, int64_t start_step, int32_t n_steps, const dou
       for (int k = 0; k < len; ++k) PG_CUDA(launch_sweep_step(w, (w->cur + k) & 1, k));
     }
     w->cur = (w->cur + len) & 1;
+    w->flips += len;
     w->last_launches += w->n_items ? len : 0;
     done += len;
   }
@@ -951,7 +985,7 @@ int64_t pg_sweep_last_launch_count(pg_sweep* w) { return w ? w->last_launches : 
 
 int pg_sweep_synchronize(pg_sweep* w) {
   PG_CHECK(w, PG_ERR_INVALID, "pg_sweep_synchronize: null sweep");
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   return sweep_check_flag(w);
 }
 
@@ -963,12 +997,12 @@ int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, do
     PG_CUDA(cudaMalloc(&w->partials, static_cast<size_t>(m) * pg::kSteadyBlocks * 3 * sizeof(double)));
   pg::sweep_steady_partials_kernel<<<dim3(pg::kSteadyBlocks, m), 256, 0, w->stream>>>(
       reinterpret_cast<const float2*>(w->psi[w->cur]), w->rho_old, w->dmembers, w->have_old ? 1 : 0,
-      w->partials);
+      w->partials, nullptr);
   PG_CUDA(cudaGetLastError());
   std::vector<double> host(static_cast<size_t>(3) * pg::kSteadyBlocks * m);
   PG_CUDA(cudaMemcpyAsync(host.data(), w->partials, host.size() * sizeof(double),
                           cudaMemcpyDeviceToHost, w->stream));
-  PG_CUDA(cudaStreamSynchronize(w->stream));
+  PG_CUDA(sweep_sync(w));
   if (w->norm_old.size() != static_cast<size_t>(m)) w->norm_old.assign(m, 0.0);
   for (int mm = 0; mm < m; ++mm) {
     double d2 = 0, o2 = 0, n = 0;
@@ -990,6 +1024,79 @@ int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, do
   }
   w->have_old = true;
   return sweep_check_flag(w);
+}
+
+int pg_sweep_steady_reset(pg_sweep* w) {
+  PG_CHECK(w, PG_ERR_INVALID, "pg_sweep_steady_reset: null sweep");
+  const int m = w->members;
+  if (!w->rho_old) PG_CUDA(cudaMalloc(&w->rho_old, static_cast<size_t>(w->sites) * 4));
+  if (!w->partials)
+    PG_CUDA(cudaMalloc(&w->partials, static_cast<size_t>(m) * pg::kSteadyBlocks * 3 * sizeof(double)));
+  PG_CUDA(pg::steady_monitor_alloc(w->mon, m));
+  PG_CUDA(pg::steady_monitor_reset(w->mon, w->halt, w->stream));
+  w->have_old = false;
+  return PG_OK;
+}
+
+int pg_sweep_steady_update(pg_sweep* w, int64_t step, int32_t record, double rtol,
+                           int32_t halt_when_all_stopped) {
+  PG_CHECK(w, PG_ERR_INVALID, "pg_sweep_steady_update: null sweep");
+  PG_CHECK(rtol >= 0.0, PG_ERR_INVALID, "pg_sweep_steady_update: negative rtol");
+  if (!w->mon.norm_old) {
+    const int rc = pg_sweep_steady_reset(w);
+    if (rc != PG_OK) return rc;
+  }
+  pg::sweep_steady_partials_kernel<<<dim3(pg::kSteadyBlocks, w->members), 256, 0, w->stream>>>(
+      reinterpret_cast<const float2*>(w->psi[w->cur]), w->rho_old, w->dmembers,
+      w->mon.have_old ? 1 : 0, w->partials, w->halt);
+  PG_CUDA(cudaGetLastError());
+  PG_CUDA(pg::steady_monitor_decide(w->mon, w->partials, pg::kSteadyBlocks, w->cells, 0.0,
+                                    record ? 1 : 0, rtol, static_cast<long long>(step), w->flips,
+                                    halt_when_all_stopped ? 1 : 0, w->halt, w->stream));
+  return PG_OK;
+}
+
+int pg_sweep_steady_poll(pg_sweep* w, int32_t* stopped, int64_t* updates_done) {
+  PG_CHECK(w && stopped && updates_done, PG_ERR_INVALID, "pg_sweep_steady_poll: null argument");
+  pg::steady_monitor_poll(w->mon, stopped, updates_done);
+  return PG_OK;
+}
+
+int pg_sweep_steady_results(pg_sweep* w, double* rel_density, double* rel_norm, double* norms,
+                            int64_t* stop_steps, int64_t* halt_step) {
+  PG_CHECK(w, PG_ERR_INVALID, "pg_sweep_steady_results: null sweep");
+  PG_CHECK(w->mon.norm_old, PG_ERR_INVALID, "pg_sweep_steady_results: no steady-state check has been made");
+  const int m = w->members;
+  std::vector<double> res(static_cast<size_t>(3) * m);
+  std::vector<long long> stops(m);
+  long long hs[2] = {-1, -1};  // step and buffer swaps of the halting check
+  int halted = 0;
+  PG_CUDA(pg::steady_monitor_fetch(w->mon, w->halt, res.data(), stops.data(), &halted, hs, w->stream));
+  PG_CUDA(sweep_sync(w));
+  for (int mm = 0; mm < m; ++mm) {
+    if (rel_density) rel_density[mm] = res[mm];
+    if (rel_norm) rel_norm[mm] = res[m + mm];
+    if (norms) norms[mm] = res[2 * m + mm];
+    if (stop_steps) stop_steps[mm] = stops[mm];
+  }
+  if (halted) {
+    // Sweep launches after the halt returned without writing while the host swapped the
+    // buffers for each: the halting check's state is under the parity it had then.  Clear
+    // the halt so that the sweep steps again.
+    w->cur ^= static_cast<int>((w->flips - hs[1]) & 1);
+    w->flips = hs[1];
+    PG_CUDA(cudaMemsetAsync(w->halt, 0, sizeof(int), w->stream));
+    PG_CUDA(sweep_sync(w));
+  }
+  if (halt_step) *halt_step = halted ? hs[0] : -1;
+  return sweep_check_flag(w);
+}
+
+int pg_sweep_sync_counts(pg_sweep* w, int64_t* host_syncs, int64_t* throttle_waits) {
+  PG_CHECK(w && host_syncs && throttle_waits, PG_ERR_INVALID, "pg_sweep_sync_counts: null argument");
+  *host_syncs = w->host_syncs;
+  *throttle_waits = w->throttle_waits;
+  return PG_OK;
 }
 
 }  // extern "C"

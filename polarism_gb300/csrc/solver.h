@@ -50,10 +50,12 @@ struct pg_solver {
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (length, parity) -> graph
   int* err_flag = nullptr;   // set by kernels whose bounded waits gave up
   int wait_limit = 100000;   // 0: bounded waits give up at once (pg_set_wait_limit)
-  // Device halt word of the steady-state monitor: once it is set every RK4 launch returns
-  // at once, so steps queued after the last member stopped leave the state as it was.
+  // Device halt word of the steady-state monitor: once it is set every RK4 and split-step
+  // launch returns at once, so steps queued after the last member stopped leave the state
+  // as it was.
   int* halt = nullptr;
   long long parity_step = 0;  // absolute step whose state sits under `cur` after pg_rk4_advance
+  long long flips = 0;        // swaps of `cur` by RK4 steps so far (split steps work in place)
   int rk4_kernel = 0;        // 0 auto, 1 tiled streaming kernel, 2 full-width kernel,
                              // 3 full-width kernel with four sites a thread
   int wide_blocks = 0;       // persistent grid of the full-width kernel
@@ -75,7 +77,20 @@ struct pg_solver {
   // that ran as plain launches after a capture or instantiation failed.
   int graph_failure = 0;
   long long graph_fallbacks = 0;
+  // Host waits (pg_sync_counts): host_syncs counts every wait of the library for the
+  // solver's stream to drain, throttle_waits the staging-ring waits that found the slot's
+  // earlier copy still queued (the host had run kStagingSlots chunks ahead of the device).
+  long long host_syncs = 0;
+  long long throttle_waits = 0;
 };
+
+namespace pg {
+// Wait for everything queued on the solver's stream (counted in host_syncs).
+inline cudaError_t stream_sync(pg_solver* s) {
+  ++s->host_syncs;
+  return cudaStreamSynchronize(s->stream);
+}
+}  // namespace pg
 
 
 namespace pg {

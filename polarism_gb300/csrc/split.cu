@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(1024) row_pass_kernel(typename C2T<T>::type* _
                                                         const RowPassArgs a) {
   using C2 = typename C2T<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.halt != nullptr && __ldcg(a.halt) != 0) return;  // steady-state monitor halted the run
   constexpr bool COMP = sizeof(T) == 4;  // FP32: twiddles as rounded value + remainder
   C2* tws = reinterpret_cast<C2*>(smem_raw);
   C2* buf = tws + (COMP ? 2 : 1) * a.nx;
@@ -90,6 +91,7 @@ __global__ void __launch_bounds__(1024) col_pass_kernel(typename C2T<T>::type* _
                                                         const ColPassArgs a) {
   using C2 = typename C2T<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.halt != nullptr && __ldcg(a.halt) != 0) return;  // steady-state monitor halted the run
   constexpr bool COMP = sizeof(T) == 4;  // FP32: twiddles as rounded value + remainder
   C2* tws = reinterpret_cast<C2*>(smem_raw);
   C2* buf = tws + (COMP ? 2 : 1) * a.ny;

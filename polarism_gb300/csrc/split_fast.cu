@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(kRowWarps * 32, 2)
                     const float2* __restrict__ px, const float2* __restrict__ py,
                     const RowPassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.halt != nullptr && __ldcg(a.halt) != 0) return;  // steady-state monitor halted the run
   float4* tw4 = reinterpret_cast<float4*>(smem_raw);                     // [32][32]
   float2* xb = reinterpret_cast<float2*>(tw4 + kN);                      // [warps][32][33]
   for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];
@@ -186,6 +187,7 @@ __global__ void __launch_bounds__(kPanel * 32, 2)
                     const SplitConst<float>* __restrict__ consts, const float* __restrict__ scales,
                     const unsigned long long* __restrict__ step_base, const ColPassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (a.halt != nullptr && __ldcg(a.halt) != 0) return;  // steady-state monitor halted the run
   float4* tw4 = reinterpret_cast<float4*>(smem_raw);  // [32][32]
   float2* pan = reinterpret_cast<float2*>(tw4 + kN);  // exchange, or [row][c] for the local step
   for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];

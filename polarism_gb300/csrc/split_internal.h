@@ -34,6 +34,7 @@ struct RowPassArgs {
   int forward, inverse, multiply;
   int table_stride;     // complex values between consecutive members' propagator factors
   double scale;         // power-of-two factor of the kick: psi (1 + d) * scale
+  const int* halt;      // steady-state monitor's halt word: when set the pass returns at once
 };
 
 struct ColPassArgs {
@@ -54,6 +55,7 @@ struct ColPassArgs {
   int step_offset;      // noise step = step_base[0] + step_offset
   double dt_d;
   float dt_f;
+  const int* halt;      // as RowPassArgs::halt
   // dt in the working precision is read through dt_of<T>().
   template <typename T>
   __host__ __device__ T dt_of() const;

@@ -236,6 +236,13 @@ class RK4Engine:
         """Chunks that ran as plain launches because their graph could not be built."""
         return int(self.lib.pg_graph_fallbacks(self.handle))
 
+    def sync_counts(self):
+        """(host_syncs, throttle_waits): the library's waits for this solver's stream to drain,
+        and the advance calls that waited for a staging slot still in use."""
+        h, w = C.c_int64(), C.c_int64()
+        _lib.check(self.lib.pg_sync_counts(self.handle, C.byref(h), C.byref(w)), "pg_sync_counts")
+        return int(h.value), int(w.value)
+
     def set_wait_limit(self, polls):
         """100000 (the default: the polls each mbarrier wait of the TMA-fed kernels makes before it
         gives up) or 0: the kernels withhold each block's first row copy, so that a wait runs

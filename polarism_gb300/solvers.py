@@ -214,20 +214,23 @@ class _GB300Solver(AbstractSolver):
         self._upload_inputs(engine, model, envelopes, potential)
         return engine, members, [c for _, c in terms]
 
-    def _upload_state(self, engine, model, array):
+    def _reservoir_array(self, engine, model, device):
+        """The reservoir fields in the engine's layout: the single field itself, the two
+        fields of the double reservoirs stacked as (2, B, Cr, ny, nx), None without one."""
         res_state = model.reservoir.get_state()
-        device = _is_device(array)
         if self._reservoir_type == "single":
-            res0 = res_state[0]
-        elif self._reservoir_type in ("double", "quadratic-double"):  # (2, B, Cr, ny, nx)
+            return res_state[0]
+        if self._reservoir_type in ("double", "quadratic-double"):
             if device:
                 import torch
 
-                res0 = torch.stack(list(res_state))
-            else:
-                res0 = np.stack([np.asarray(f, dtype=engine.real) for f in res_state])
-        else:
-            res0 = None
+                return torch.stack(list(res_state))
+            return np.stack([np.asarray(f, dtype=engine.real) for f in res_state])
+        return None
+
+    def _upload_state(self, engine, model, array):
+        device = _is_device(array)
+        res0 = self._reservoir_array(engine, model, device)
         if res0 is not None:
             engine.set_state(array if device else np.ascontiguousarray(array, dtype=engine.complex),
                              res0 if device else np.ascontiguousarray(res0, dtype=engine.real))
@@ -246,6 +249,11 @@ class _GB300Solver(AbstractSolver):
         return engine.get_state()
 
     def _finish(self, model, state, res, n_steps):
+        self._hand_back(model, res)
+        state.step += n_steps
+        state.t = state.t0 + state.step * self._dt
+
+    def _hand_back(self, model, res):
         # Every kernel leaves n_R clamped at zero at the end of a step, as the reservoir's
         # set_state would.  When the result went in place into the reservoir's own host array
         # (inplace_host), handing it back through set_state would only repeat that clamp over
@@ -257,8 +265,57 @@ class _GB300Solver(AbstractSolver):
             model.reservoir.set_state((res,))
         elif self._reservoir_type in ("double", "quadratic-double"):
             model.reservoir.set_state((res[0], res[1]))
+
+    # ------------------------------------------------------------------ resident state
+    #: Keep the state in device memory between ``advance`` calls (switched on by
+    #: :class:`polarism_gb300.run_loop.DeviceSteadyMonitor`).  The state's field and the
+    #: reservoir's arrays then keep their contents from before the first resident chunk until
+    #: :meth:`flush` copies the device state back, so that a chunk waits for nothing: the
+    #: steps and the steady-state checks are queued behind one another on the solver's
+    #: stream.  ``state.step`` and ``state.t`` advance as usual.
+    resident = False
+    #: Whether the class can keep its state resident (a real-space state between calls).
+    supports_resident = False
+    _held = None    # (field, reservoir arrays) that the device state stands for
+    _stale = False  # the device state is newer than those arrays
+
+    def _holds(self, model, state, field):
+        """The device state stands for the arrays the state and the reservoir hold now:
+        nothing has replaced them since the last resident chunk or flush."""
+        if not self.resident or self._held is None or self._engine is None:
+            return False
+        held_field, held_res = self._held
+        current = tuple(model.reservoir.get_state())
+        return (held_field is field and len(held_res) == len(current)
+                and all(a is b for a, b in zip(held_res, current)))
+
+    def _keep(self, model, state, field, n_steps):
+        """Bookkeeping of a resident chunk: no copy back, the step and time advance."""
+        self._held = (field, tuple(model.reservoir.get_state()))
+        self._stale = True
         state.step += n_steps
         state.t = state.t0 + state.step * self._dt
+
+    def flush(self, model, state):
+        """Copy a resident device state back into ``state`` and the reservoir (one host
+        wait); the device keeps it, so the next resident chunk uploads nothing."""
+        if not self._stale:
+            return
+        engine = self._engine
+        field = state.field
+        device = _is_device(field)
+        res_in = self._reservoir_array(engine, model, device)
+        psi, res = self._download_state(engine, field, res_in, device)
+        state.field = psi
+        self._hand_back(model, res)
+        self._stale = False
+        self._held = (state.field, tuple(model.reservoir.get_state()))
+
+    def release_resident(self, model, state):
+        """Flush and leave resident mode."""
+        self.flush(model, state)
+        self.resident = False
+        self._held = None
 
     @property
     def engine(self):
@@ -269,6 +326,7 @@ class RK4CudaSolver(_GB300Solver):
     """Fused whole-step RK4 on GB300 with in-kernel Philox Wigner noise (``rk4-cuda``)."""
 
     name = "rk4-cuda"
+    supports_resident = True
     reservoir_types = ("single", "none", "double", "quadratic-double")
     capabilities = SolverCapabilities(
         components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
@@ -291,10 +349,14 @@ class RK4CudaSolver(_GB300Solver):
         field = state.field
         self.batch_physics.check(field, 1)
         engine, members, coefficient = self._prepare(model, state)
-        device, res_in = self._upload_state(engine, model, field)
+        if not self._holds(model, state, field):
+            device, res_in = self._upload_state(engine, model, field)
         scales = self.stage_scales(coefficient, state.t0, state.step, n_steps, members)
         engine.advance(state.step, n_steps, scales,
                        use_graphs=bool(getattr(self.config.solver, "cuda_graphs", True)))
+        if self.resident:
+            self._keep(model, state, field, n_steps)
+            return
         psi, res = self._download_state(engine, field, res_in, device)
         state.field = psi
         self._finish(model, state, res, n_steps)
@@ -309,6 +371,7 @@ class SplitStepFFTSolver(_GB300Solver):
 
     name = "split-step-fft"
     ordering = 0
+    supports_resident = True
     reservoir_types = ("single", "none", "double", "quadratic-double")
     capabilities = SolverCapabilities(
         components=frozenset({1}), ndim=frozenset({2}), grid_types=frozenset({"periodic"}),
@@ -333,11 +396,15 @@ class SplitStepFFTSolver(_GB300Solver):
         field = state.field  # materialises psi from a cached spectrum if needed
         self.batch_physics.check(field, 1)
         engine, members, coefficient = self._prepare(model, state)
-        device, res_in = self._upload_state(engine, model, field)
+        if not self._holds(model, state, field):
+            device, res_in = self._upload_state(engine, model, field)
         engine.set_state_kind(False)
         scales = self.half_scales(coefficient, state.t0, state.step, n_steps, members)
         engine.split_advance(self.ordering, state.step, n_steps, scales,
                              use_graphs=bool(getattr(self.config.solver, "cuda_graphs", True)))
+        if self.resident:
+            self._keep(model, state, field, n_steps)
+            return
         psi, res = self._download_state(engine, field, res_in, device)
         state.field = psi
         self._finish(model, state, res, n_steps)
@@ -352,6 +419,7 @@ class SplitStepFFTCudaSolver(SplitStepFFTSolver):
 
     name = "split-step-fft-cuda"
     ordering = 1
+    supports_resident = False  # leaves a spectrum, which the steady check cannot read
 
     def advance(self, model, state, n_steps: int) -> None:
         if n_steps <= 0:

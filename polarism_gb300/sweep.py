@@ -190,6 +190,40 @@ class SweepEngine:
                    "pg_sweep_steady_check")
         return tuple(out)
 
+    # -- device-resident steady-state monitor (as RK4Engine's) ---------------------------
+    def steady_reset(self):
+        _lib.check(self._lib.pg_sweep_steady_reset(self._h), "pg_sweep_steady_reset")
+
+    def steady_update(self, step, record=True, rtol=1e-6, halt=False):
+        """Enqueue one steady-state check (no wait)."""
+        _lib.check(self._lib.pg_sweep_steady_update(self._h, int(step), int(bool(record)),
+                                                    float(rtol), int(bool(halt))),
+                   "pg_sweep_steady_update")
+
+    def steady_poll(self):
+        """(members stopped, checks finished since the reset), read without waiting."""
+        stopped, done = C.c_int32(), C.c_int64()
+        _lib.check(self._lib.pg_sweep_steady_poll(self._h, C.byref(stopped), C.byref(done)),
+                   "pg_sweep_steady_poll")
+        return int(stopped.value), int(done.value)
+
+    def steady_results(self):
+        """Waits; returns (rel_density, rel_norm, norms, stop_steps, halt_step or None)."""
+        out = [np.empty(self.members, dtype=np.float64) for _ in range(3)]
+        stops = np.empty(self.members, dtype=np.int64)
+        halt = C.c_int64()
+        _lib.check(self._lib.pg_sweep_steady_results(self._h, *[o.ctypes.data for o in out],
+                                                     stops.ctypes.data, C.byref(halt)),
+                   "pg_sweep_steady_results")
+        return (*out, stops, None if halt.value < 0 else int(halt.value))
+
+    def sync_counts(self):
+        """(host_syncs, throttle_waits) of the sweep handle (see RK4Engine.sync_counts)."""
+        h, w = C.c_int64(), C.c_int64()
+        _lib.check(self._lib.pg_sweep_sync_counts(self._h, C.byref(h), C.byref(w)),
+                   "pg_sweep_sync_counts")
+        return int(h.value), int(w.value)
+
 
 # --------------------------------------------------------------------------- autotuner
 def tiling_candidates(grids):
@@ -303,6 +337,9 @@ class SweepResult:
     t: float
     wall_time: float
     tiling: dict = field(default_factory=dict)
+    # Host waits of the sweep handle from the first chunk until the run first waited for the
+    # device monitor's decisions (or to the end of the loop): 0 with the device monitor.
+    loop_syncs: int = -1
 
 
 def _member_inputs(cfg):
@@ -323,7 +360,7 @@ def _member_inputs(cfg):
 
 def run_sweep(member_cfgs, *, total_time=None, check_every=None, rtol=None, min_time=None,
               steady_state=None, autotune=True, freeze_stopped=False, use_graphs=True,
-              chunk_steps=None, initial=None):
+              chunk_steps=None, initial=None, device_monitor=True):
     """Advance every member config (host-mirror ``Config`` objects that may differ in grid,
     pump, physics and seed; one ``dt``) with one persistent launch per RK4 step.
 
@@ -331,6 +368,14 @@ def run_sweep(member_cfgs, *, total_time=None, check_every=None, rtol=None, min_
     ``solver.total_time``.  ``freeze_stopped`` leaves members out of the launch once they
     have a stop time (the reference keeps stepping them until every member has stopped);
     ``initial`` optionally gives per-member ``(psi, n_R)`` starting fields.
+
+    With ``device_monitor`` (the default) the steady-state checks are queued on the device
+    behind the chunks (``pg_sweep_steady_update``): the host reads the monitor's progress word
+    without waiting, and the check that finds every member stopped halts the sweep, so the run
+    ends on that check's step with no host wait per chunk.  With ``freeze_stopped`` the host
+    freezes members when the progress word shows new stops (one wait each time); they keep
+    stepping until then, so a frozen member's final state can be a few chunks past its stop
+    step.  ``device_monitor=False`` reads every check back and decides on the host.
     """
     cfgs = list(member_cfgs)
     first = cfgs[0]
@@ -375,8 +420,24 @@ def run_sweep(member_cfgs, *, total_time=None, check_every=None, rtol=None, min_
         chunk = int(chunk_steps or (interval if interval else min(n_total, 4096)) or 1)
         stop_times = np.full(engine.members, np.nan)
         active = np.ones(engine.members, dtype=bool)
+        monitor = bool(interval and device_monitor)
+        frozen = 0
         step = 0
         wall0 = time.perf_counter()
+        if monitor:
+            engine.steady_reset()
+        syncs0 = engine.sync_counts()[0]
+        loop_syncs = []
+
+        def settle():
+            """Wait for the queued checks; record their stops; the step the state is at."""
+            if not loop_syncs:
+                loop_syncs.append(engine.sync_counts()[0] - syncs0)
+            *_, stops, halt_step = engine.steady_results()
+            new = (stops >= 0) & np.isnan(stop_times)
+            stop_times[new] = stops[new] * dt
+            return new, halt_step
+
         while step < n_total and not (steady and np.isfinite(stop_times).all()):
             end = min(n_total, step + chunk)
             if interval:
@@ -389,7 +450,18 @@ def run_sweep(member_cfgs, *, total_time=None, check_every=None, rtol=None, min_
                     scales[k, s] = [coef(tt) for coef in coefficients]
             engine.advance(step, n, scales, use_graphs=use_graphs)
             step = end
-            if interval and step % interval == 0:
+            if monitor and step % interval == 0:
+                engine.steady_update(step, record=step * dt >= min_time, rtol=rtol, halt=True)
+                stopped, _ = engine.steady_poll()
+                if stopped == engine.members or (freeze_stopped and stopped > frozen):
+                    new, halt_step = settle()
+                    if halt_step is not None:
+                        step = halt_step
+                    elif freeze_stopped and new.any():
+                        active &= ~new
+                        engine.set_active(active)
+                    frozen = int(np.isfinite(stop_times).sum())
+            elif interval and step % interval == 0:
                 rel_d, rel_n, norms = engine.steady_check()
                 reached = (norms < 1e-30) | ((rel_n < rtol) & (rel_d < rtol))
                 if step * dt >= min_time:
@@ -398,12 +470,16 @@ def run_sweep(member_cfgs, *, total_time=None, check_every=None, rtol=None, min_
                     if freeze_stopped and newly.any():
                         active &= ~newly
                         engine.set_active(active)
+        if monitor and not np.isfinite(stop_times).all():
+            settle()  # the run reached total_time: the stops of the checks still queued
+        if not loop_syncs:
+            loop_syncs.append(engine.sync_counts()[0] - syncs0)
         engine.synchronize()
         wall = time.perf_counter() - wall0
         psi, res = engine.get_state()
         return SweepResult(psi=[p.copy() for p in psi], reservoir=[r.copy() for r in res],
                            stop_times=stop_times, steps=step, t=step * dt, wall_time=wall,
-                           tiling=tiling or engine.tiling)
+                           tiling=tiling or engine.tiling, loop_syncs=loop_syncs[0])
     finally:
         engine.close()
 

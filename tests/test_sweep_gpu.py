@@ -223,3 +223,55 @@ def test_run_sweep_records_stop_times_like_the_controller(cuda_lib, tmp_path, mo
     sweep = Sweep(cfg, {"grid.nx": [128, 64], "grid.ny": [128, 64], "noise.seed": [1, 2]}, mode="zip")
     sweep.run(autotune=False, freeze_stopped=True)
     assert np.all(np.isnan(sweep.stop_times)) and sweep.result.steps == 200
+
+
+def _relaxing_members():
+    """Uneven members relaxing to the fixed point of a near-uniform pump at three strengths
+    (they stop at different checks), with a smooth initial field and reservoir."""
+    from polarism_gb300 import host
+
+    cfgs, initial = [], []
+    for (nx, ny), p0 in zip([(64, 64), (128, 64), (64, 128)], (4.0, 8.0, 16.0)):
+        c = host.Config()
+        c.grid.nx, c.grid.ny, c.grid.lx, c.grid.ly = nx, ny, float(nx), float(ny)
+        c.physics.gamma_R = 0.5
+        c.solver.precision = "single"
+        c.solver.dt = 0.05
+        c.solver.total_time = 200.0
+        c.stop.steady_state = True
+        c.stop.check_every = 1.0
+        c.stop.rtol = 5e-3
+        c.laser.P0, c.laser.sigma_space = p0, 1e4
+        c.noise.enabled = False
+        cfgs.append(c)
+        x = np.arange(nx) - nx / 2
+        row = (1.0 + 0.02 * np.cos(2 * np.pi * x / nx)).astype(np.complex64)
+        initial.append((np.ascontiguousarray(np.broadcast_to(row, (ny, nx))),
+                        np.full((ny, nx), 4.0, np.float32)))
+    return cfgs, initial
+
+
+def test_run_sweep_device_monitor_matches_host_decisions_without_waits(cuda_lib, tmp_path,
+                                                                        monkeypatch):
+    """The sweep's steady-state checks decided on the device stop every member on the same
+    check as checks read back to the host, end on the same step with the same state, and make
+    no host wait while the chunks and checks are queued (the sweep handle's own counter)."""
+    from polarism_gb300.sweep import run_sweep
+
+    monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path))
+    cfgs, initial = _relaxing_members()
+    host_run = run_sweep(cfgs, autotune=False, initial=initial, device_monitor=False)
+    dev_run = run_sweep(cfgs, autotune=False, initial=initial, device_monitor=True)
+    assert np.isfinite(host_run.stop_times).all() and host_run.steps < 4000
+    assert len(set(host_run.stop_times.tolist())) == 3
+    np.testing.assert_array_equal(dev_run.stop_times, host_run.stop_times)
+    assert dev_run.steps == host_run.steps
+    for a, b in zip(dev_run.psi + dev_run.reservoir, host_run.psi + host_run.reservoir):
+        assert np.array_equal(a, b)
+    assert dev_run.loop_syncs == 0
+    assert host_run.loop_syncs >= host_run.steps // 20  # a wait at every check
+
+    # Freezing members as their stops show: the same stop times, no wait per chunk.
+    frozen = run_sweep(cfgs, autotune=False, initial=initial, freeze_stopped=True)
+    np.testing.assert_array_equal(frozen.stop_times, host_run.stop_times)
+    assert frozen.steps == host_run.steps and frozen.loop_syncs == 0
