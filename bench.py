@@ -722,7 +722,9 @@ def run_sweep_bench(args):
             "wall_s": res.wall_time, "t_end_ps": res.t, "steps": res.steps,
             "stopped": int(np.isfinite(res.stop_times).sum()), "members": len(cfgs),
             "stop_time_ps_median": float(np.nanmedian(res.stop_times)) if np.isfinite(res.stop_times).any() else None,
-            "freeze_stopped": bool(args.freeze_stopped), "rtol": 1e-6, "check_every_ps": 10.0}
+            "freeze_stopped": bool(args.freeze_stopped), "rtol": 1e-6, "check_every_ps": 10.0,
+            "host_waits_before_first_decision": res.loop_syncs,
+            "stop_times_ps": [None if not np.isfinite(v) else float(v) for v in res.stop_times]}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -821,11 +823,56 @@ def run_spinor_bench(args):
         "trials_rejected": ctl.rejected, "observable_samples": samples,
         "final_norm": float(norms[0]), "clocks": clocks,
     }
+    line["observables"] = spinor_observables(eng, grid, samples, args.observables_out)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = spinor_cpu_baseline(cfg, grid, model, state)
     eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def spinor_observables(eng, grid, samples, out_path=None):
+    """The run's FP64 accumulators finalised into Polarism's observables (momentum
+    distribution n(k), g1(r), <n>, g2) per circular component, summarised; with ``out_path``
+    the full arrays are written there (npz)."""
+    from polarism_gb300 import observables as ob
+
+    if samples == 0:
+        return None
+    sum_rho, s_rho = eng.accumulator_sums("rho")
+    sum_rho2, _ = eng.accumulator_sums("rho2")
+    sum_k, s_k = eng.accumulator_sums("k")
+    cell, cells = grid.dx * grid.dy, grid.nx * grid.ny
+    n_k = ob.momentum_distribution(sum_k, s_k, cell, cells)[0]   # (2, ny, nx), centred
+    g1 = ob.g1(n_k)
+    mean, sq = ob.density_moments(sum_rho, sum_rho2, s_rho)
+    g2 = ob.g2(mean, sq)[0]
+    mean = mean[0]
+    kx = np.fft.fftshift(2 * np.pi * np.fft.fftfreq(grid.nx, grid.dx))
+    ky = np.fft.fftshift(2 * np.pi * np.fft.fftfreq(grid.ny, grid.dy))
+    x = (np.arange(grid.nx) - grid.nx // 2) * grid.dx
+    y = (np.arange(grid.ny) - grid.ny // 2) * grid.dy
+    r = np.hypot(x[None, :], y[:, None])
+    out = {"samples": int(samples), "components": []}
+    for c, name in enumerate(("psi_plus", "psi_minus")):
+        peak = np.unravel_index(int(np.argmax(n_k[c])), n_k[c].shape)
+        core = mean[c] > 0.1 * mean[c].max()
+        g1_r = {f"{d:g}um": float(np.mean(np.abs(g1[c][(r >= d - 0.5 * grid.dx) & (r < d + 0.5 * grid.dx)])))
+                for d in (2.0, 5.0, 10.0, 20.0, 40.0)}
+        out["components"].append({
+            "component": name,
+            "particles": float(mean[c].sum() * cell),
+            "n_k_peak": float(n_k[c][peak]), "k_peak_per_um": [float(kx[peak[1]]), float(ky[peak[0]])],
+            "n_k_total": float(n_k[c].sum()),
+            "g1_abs_ring_mean": g1_r,
+            "g2_condensate_mean": float(np.mean(g2[c][core])) if core.any() else None,
+            "g2_at_density_max": float(g2[c].reshape(-1)[int(np.argmax(mean[c]))]),
+        })
+    if out_path:
+        np.savez_compressed(out_path, n_k=n_k, g1=g1, mean_density=mean, g2=g2, kx=kx, ky=ky,
+                            samples=samples)
+        out["arrays"] = str(out_path)
+    return out
 
 
 def spinor_cpu_baseline(cfg, grid, model, state, trials=2):
@@ -937,6 +984,8 @@ def main():
                     help="rk4: the 1024^2 fused-step benchmark; sweep: the uneven-size sweep; "
                          "spinor: the adaptive two-component IFRK run")
     ap.add_argument("--spinor-time", type=float, default=500.0)
+    ap.add_argument("--observables-out", default=None,
+                    help="spinor workload: write n(k), g1, <n> and g2 to this npz file")
     ap.add_argument("--fno-n", type=int, default=256)
     ap.add_argument("--fno-train", type=int, default=2000)
     ap.add_argument("--fno-test", type=int, default=200)

@@ -471,7 +471,11 @@ def run_sweep(member_cfgs, *, total_time=None, check_every=None, rtol=None, min_
                         active &= ~newly
                         engine.set_active(active)
         if monitor and not np.isfinite(stop_times).all():
-            settle()  # the run reached total_time: the stops of the checks still queued
+            # The run reached total_time: the stops of the checks still queued, and the step of
+            # the state when one of them halted the sweep.
+            _, halt_step = settle()
+            if halt_step is not None:
+                step = halt_step
         if not loop_syncs:
             loop_syncs.append(engine.sync_counts()[0] - syncs0)
         engine.synchronize()
