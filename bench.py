@@ -729,6 +729,95 @@ def run_sweep_bench(args):
         print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- IFRK leg
+# Classical RK4 in Butcher form (the tableau pg_ifrk_advance runs as "rk4").
+IFRK4_A = ((), (0.5,), (0.0, 0.5), (0.0, 0.0, 1.0))
+IFRK4_B = (1 / 6, 1 / 3, 1 / 3, 1 / 6)
+
+
+def ifrk_bytes_per_site(A, b, complex_bytes=8, real_bytes=4):
+    """Bytes per site and step that the Lawson IFRK pass structure of ``csrc/api_ifrk.cu``
+    reads and writes in DRAM (scalar field, single reservoir, one laser, no potential).  W is
+    the y-transformed field the passes hand on; stage i's row pass reads W, stores the stage's
+    transformed row (psi0_hat at stage 0, f_hat_{i-1} after), reads psi0_hat (i > 0) and every
+    earlier f_hat_j with a_ij != 0 except the one it has just formed, writes W; its column pass
+    reads W, n_0, the pump envelope and dn_j for a_ij != 0, writes dn_i and W.  The final row
+    pass combines psi0_hat and the f_hat_j with b_j != 0; the final column pass reads dn_j,
+    writes n_1, psi_1 and W.  The Lawson tables (nx + ny values per factor) stay in cache."""
+    c, r = complex_bytes, real_bytes
+    s = len(b)
+    total = 0
+    for i in range(s):
+        row = 3 * c + (c if i > 0 else 0) + c * sum(1 for j in range(i - 1) if A[i][j] != 0.0)
+        col = 2 * c + r + r + r * sum(1 for j in range(i) if A[i][j] != 0.0) + r
+        total += row + col
+    final_row = 4 * c + c * sum(1 for j in range(s - 1) if b[j] != 0.0)
+    final_col = 3 * c + r + r * sum(1 for j in range(s) if b[j] != 0.0) + r
+    return total + final_row + final_col
+
+
+def run_ifrk_bench(args):
+    """Fixed-step Lawson IFRK4 (ifrk4-fft-cuda) throughput at 1024^2: members x 1024^2 FP32,
+    single reservoir, Wigner noise on, site-updates/s against the HBM roofline at the pass
+    structure's bytes per site (ifrk_bytes_per_site)."""
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from polarism_gb300 import build as _build
+
+    _build.build()
+    from polarism_gb300.engine import TABLEAU_NODES, MemberPhysics, RK4Engine
+
+    members = args.members
+    w = workload(members, first=rank_members(rank, world, members)[0])
+    eng = RK4Engine(NX, NY, members, w["dx"], w["dy"], DT, MemberPhysics(**PHYSICS), "single",
+                    pump_per_member=True)
+    eng.set_pump(w["env"])
+    eng.set_noise(w["seeds"], PHYSICS["gamma_C"], PHYSICS["R"], 1.0, DT / (4 * w["dx"] * w["dy"]))
+    eng.set_state(w["psi"], w["n"])
+    stream = torch.cuda.ExternalStream(eng.stream)
+    stages = len(TABLEAU_NODES["rk4"])
+    scales = np.full((args.warmup + args.steps, stages, members), P0)
+    eng.ifrk_advance("rk4", 0, args.warmup, scales[:args.warmup])
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    eng.ifrk_advance("rk4", args.warmup, args.steps, scales[args.warmup:])
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = eng.last_launch_count
+    elapsed_ms = start.elapsed_time(stop)
+    eng.close()
+    sites = members * NX * NY
+    value = sites * args.steps / (elapsed_ms / 1e3)
+    bytes_per_site = ifrk_bytes_per_site(IFRK4_A, IFRK4_B)
+    achieved = bytes_per_site * sites / (elapsed_ms / 1e3 / args.steps) / 1e9
+    peak, peak_kind = measured_peak()
+    line = {
+        "metric": f"IFRK4 site-updates/s at {NX}^2 (fixed step)", "value": value,
+        "unit": "site-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"ifrk4-fft-cuda (Lawson RK4, fixed dt=5e-4), {NX}^2 periodic, "
+                               f"lx=ly={LX:g}, single reservoir, Wigner noise on, complex64",
+                   "members": members, "grid": [NY, NX],
+                   "l2": "inputs larger than L2 (%.0f MB state vs 129 MB L2)" % (sites * 16 / 1e6)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_site": bytes_per_site},
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------------------------- spinor leg
 SPINOR_N = 512
 SPINOR_L = 128.0          # um: dx = 0.25 um, the ring (r = 30, w = 4) well inside the box
@@ -980,7 +1069,8 @@ def main():
                          "sites a thread (wide4), the tiled kernel, or the engine's choice")
     ap.add_argument("--split-ordering", choices=["kouter", "cpu"], default="kouter",
                     help="split workload: K-outer (split-step-fft-cuda) or CPU ordering")
-    ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno"], default="rk4",
+    ap.add_argument("--workload", choices=["rk4", "split", "sweep", "spinor", "fno", "ifrk"],
+                    default="rk4",
                     help="rk4: the 1024^2 fused-step benchmark; sweep: the uneven-size sweep; "
                          "spinor: the adaptive two-component IFRK run")
     ap.add_argument("--spinor-time", type=float, default=500.0)
@@ -1020,6 +1110,9 @@ def main():
         return
     if args.workload == "fno":
         run_fno_bench(args)
+        return
+    if args.workload == "ifrk":
+        run_ifrk_bench(args)
         return
     if args.workload == "sweep":
         if args.members == 32 and "--members" not in sys.argv:
