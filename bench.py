@@ -134,6 +134,12 @@ class ClockSampler:
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        # nvidia-smi's start-up can hold the GPU for a while (seconds have been seen on a
+        # GB300 machine): wait for its first sample so that this happens before the timed region.
+        deadline = time.perf_counter() + 10.0
+        while not self.lines and self.proc.poll() is None and time.perf_counter() < deadline:
+            time.sleep(0.02)
+        time.sleep(0.1)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -371,7 +377,6 @@ def run_ours(args):
     barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    time.sleep(0.3)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     start.record(stream)
@@ -511,7 +516,6 @@ def run_split_bench(args):
     barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    time.sleep(0.3)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     start.record(stream)
@@ -668,7 +672,6 @@ def run_sweep_bench(args):
     eng.synchronize()
     sampler = ClockSampler(local)
     sampler.start()
-    time.sleep(0.3)
     eng.advance(args.warmup, args.steps, scales[args.warmup:])
     elapsed_ms = max_over_ranks(eng.last_time_ms(), world, "cuda")
     clocks = sampler.stop()
@@ -783,7 +786,6 @@ def run_ifrk_bench(args):
     torch.cuda.synchronize()
     sampler = ClockSampler(local)
     sampler.start()
-    time.sleep(0.3)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     start.record(stream)

@@ -96,6 +96,14 @@ __device__ __forceinline__ void dft32(float2 (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = a[i];
 }
 
+// conj of the 32 values: an inverse transform is the forward transform of the conjugate,
+// conjugated, so each kernel carries one copy of the transform's code (an instruction-cache
+// working set half as large; the kernels were stalled on instruction fetch).
+__device__ __forceinline__ void conj32(float2 (&v)[32]) {
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i].y = -v[i].y;
+}
+
 // Inner DFT and the W_1024^{n2 k1} factors (tw4[k1][n2]: rounded value and remainder).
 template <bool INV>
 __device__ __forceinline__ void four_step_first(float2 (&v)[32], int n2, const float4* tw4) {
@@ -108,18 +116,18 @@ __device__ __forceinline__ void four_step_first(float2 (&v)[32], int n2, const f
   }
 }
 
-// A 1024-point transform of a row held by a warp (lane = n2, buf: 32 x kXStride values).
-template <bool INV>
+// A forward 1024-point transform of a row held by a warp (lane = n2, buf: 32 x kXStride
+// values).
 __device__ __forceinline__ void fft1024_warp(float2 (&v)[32], int lane, float2* buf,
                                              const float4* tw4) {
-  four_step_first<INV>(v, lane, tw4);
+  four_step_first<false>(v, lane, tw4);
 #pragma unroll
   for (int k1 = 0; k1 < 32; ++k1) buf[k1 * kXStride + lane] = v[k1];
   __syncwarp();
 #pragma unroll
   for (int n2 = 0; n2 < 32; ++n2) v[n2] = buf[lane * kXStride + n2];
   __syncwarp();
-  dft32<INV>(v);
+  dft32<false>(v);
 }
 
 // ------------------------------------------------------------------ row pass
@@ -140,45 +148,52 @@ __global__ void __launch_bounds__(kRowWarps * 32, 2)
   const float2* pym = py + static_cast<long long>(member) * a.table_stride;
   const float scale = static_cast<float>(a.scale);
   const long long plane = static_cast<long long>(kN) * a.ny;
+#pragma unroll 1
   for (int q = 0; q < kRowsPerWarp; ++q) {
     const int row = (blockIdx.x * kRowWarps + warp) * kRowsPerWarp + q;
     float2* d = data + member * plane + static_cast<long long>(row) * kN;
     float2 v[32];
 #pragma unroll
     for (int t = 0; t < 32; ++t) v[t] = d[lane + 32 * t];
-    if (a.forward) fft1024_warp<false>(v, lane, buf, tw4);
-    if (a.multiply) {
-      // psi (1 + dx) (1 + dy) scale, the factor differences stored (see split.cu)
-      const float2 dy = pym[row];
+    // Phase 0: forward transform and kick; phase 1: the inverse transform (conj32).
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ++ph) {
+      if (ph == 0 ? a.forward : a.inverse) {
+        if (ph == 1) conj32(v);
+        fft1024_warp(v, lane, buf, tw4);
+        if (ph == 1) conj32(v);
+      }
+      if (ph == 0 && a.multiply) {
+        // psi (1 + dx) (1 + dy) scale, the factor differences stored (see split.cu)
+        const float2 dy = pym[row];
 #pragma unroll
-      for (int r = 0; r < 32; ++r) {
-        const float2 dx = pxm[lane + 32 * r];
-        const float2 dxy = cmul(dx, dy);
-        const float2 f1 = make_float2(dx.x + dy.x + dxy.x, dx.y + dy.y + dxy.y);
-        const float2 vf = cmul(v[r], f1);
-        v[r] = make_float2((v[r].x + vf.x) * scale, (v[r].y + vf.y) * scale);
+        for (int r = 0; r < 32; ++r) {
+          const float2 dx = pxm[lane + 32 * r];
+          const float2 dxy = cmul(dx, dy);
+          const float2 f1 = make_float2(dx.x + dy.x + dxy.x, dx.y + dy.y + dxy.y);
+          const float2 vf = cmul(v[r], f1);
+          v[r] = make_float2((v[r].x + vf.x) * scale, (v[r].y + vf.y) * scale);
+        }
       }
     }
-    if (a.inverse) fft1024_warp<true>(v, lane, buf, tw4);
 #pragma unroll
     for (int t = 0; t < 32; ++t) d[lane + 32 * t] = v[t];
   }
 }
 
 // ------------------------------------------------------------------ column pass
-// A 1024-point transform of the block's eight columns (thread = (column c, n2 = p)); pan is
-// the panel's exchange buffer ([c][k1][n2], columns kPanelStride apart).
-template <bool INV>
+// A forward 1024-point transform of the block's eight columns (thread = (column c, n2 = p));
+// pan is the panel's exchange buffer ([c][k1][n2], columns kPanelStride apart).
 __device__ __forceinline__ void fft1024_panel(float2 (&v)[32], int p, int c, float2* pan,
                                               const float4* tw4) {
-  four_step_first<INV>(v, p, tw4);
+  four_step_first<false>(v, p, tw4);
   __syncthreads();  // every earlier read of pan is done
 #pragma unroll
   for (int k1 = 0; k1 < 32; ++k1) pan[c * kPanelStride + k1 * kXStride + p] = v[k1];
   __syncthreads();
 #pragma unroll
   for (int n2 = 0; n2 < 32; ++n2) v[n2] = pan[c * kPanelStride + p * kXStride + n2];
-  dft32<INV>(v);
+  dft32<false>(v);
 }
 
 __global__ void __launch_bounds__(kPanel * 32, 2)
@@ -202,8 +217,16 @@ __global__ void __launch_bounds__(kPanel * 32, 2)
   float2 v[32];
 #pragma unroll
   for (int t = 0; t < 32; ++t) v[t] = d[static_cast<long long>(p + 32 * t) * a.nx];
-  if (a.inverse) fft1024_panel<true>(v, p, c, pan, tw4);
-  if (a.op != SPLIT_OP_NONE) {
+  // Phase 0: the inverse transform (conj32 around the forward one) and the local step;
+  // phase 1: the forward transform.
+#pragma unroll 1
+  for (int ph = 0; ph < 2; ++ph) {
+    if (ph == 0 ? a.inverse : a.forward) {
+      if (ph == 0) conj32(v);
+      fft1024_panel(v, p, c, pan, tw4);
+      if (ph == 0) conj32(v);
+    }
+    if (ph == 1 || a.op == SPLIT_OP_NONE) continue;
     // Through shared memory in site order, so that the local step is one loop.
     __syncthreads();
 #pragma unroll
@@ -248,7 +271,6 @@ __global__ void __launch_bounds__(kPanel * 32, 2)
 #pragma unroll
     for (int t = 0; t < 32; ++t) v[t] = pan[(p + 32 * t) * kPanel + c];
   }
-  if (a.forward) fft1024_panel<false>(v, p, c, pan, tw4);
 #pragma unroll
   for (int t = 0; t < 32; ++t) d[static_cast<long long>(p + 32 * t) * a.nx] = v[t];
 }
