@@ -186,19 +186,22 @@ def run_uniform(cfgs, initial=None, total_time=None):
     interval = int(round(c0.stop.check_every / dt))
     rtol = float(c0.stop.rtol)
     m = len(cfgs)
-    lasers = [host.make_laser(c.laser, grid.X, grid.Y, "single") for c in cfgs]
-    env = np.stack([l._spatial_envelope for l in lasers])[:, None].astype(np.float32)
+    precision = getattr(c0.solver, "precision", "single")
+    real = np.float64 if precision == "double" else np.float32
+    cplx = np.complex128 if precision == "double" else np.complex64
+    lasers = [host.make_laser(c.laser, grid.X, grid.Y, precision) for c in cfgs]
+    env = np.stack([l._spatial_envelope for l in lasers])[:, None].astype(real)
     eng = Engine(grid.nx, grid.ny, m, grid.dx, grid.dy, dt,
-                 [MemberPhysics.from_object(c.physics) for c in cfgs], "single", pump_per_member=True)
+                 [MemberPhysics.from_object(c.physics) for c in cfgs], precision, pump_per_member=True)
     try:
         eng.set_pump(env)
         if initial is None:
             psi0 = np.stack([host.make_initial_psi(grid.shape, c.noise.initial_amplitude, c.noise.seed,
-                                                   np.complex64, np.float32) for c in cfgs])[:, None]
-            n0 = np.zeros((m, 1) + grid.shape, np.float32)
+                                                   cplx, real) for c in cfgs])[:, None]
+            n0 = np.zeros((m, 1) + grid.shape, real)
         else:
-            psi0 = np.ascontiguousarray(np.asarray(initial[0], np.complex64).reshape(m, 1, *grid.shape))
-            n0 = np.ascontiguousarray(np.asarray(initial[1], np.float32).reshape(m, 1, *grid.shape))
+            psi0 = np.ascontiguousarray(np.asarray(initial[0], cplx).reshape(m, 1, *grid.shape))
+            n0 = np.ascontiguousarray(np.asarray(initial[1], real).reshape(m, 1, *grid.shape))
         eng.set_state(psi0, n0)
         p0 = np.asarray([c.laser.P0 for c in cfgs])
         n_total = int(round(total / dt))
