@@ -1004,8 +1004,11 @@ def run_fno_bench(args):
     from polarism_gb300 import warmstart as ws
 
     n = args.fno_n
-    train_cfgs = ws.pump_members(args.fno_train, seed=11, n=n, total_time=args.fno_time, dt=args.fno_dt)
-    test_cfgs = ws.pump_members(args.fno_test, seed=12, n=n, total_time=args.fno_time, dt=args.fno_dt)
+    kinds = tuple(args.fno_kinds.split(","))
+    train_cfgs = ws.pump_members(args.fno_train, seed=11, n=n, total_time=args.fno_time, dt=args.fno_dt,
+                                 kinds=kinds, precision=args.fno_precision)
+    test_cfgs = ws.pump_members(args.fno_test, seed=12, n=n, total_time=args.fno_time, dt=args.fno_dt,
+                                kinds=kinds, precision=args.fno_precision)
     t0 = time.perf_counter()
     data = ws.run_uniform(train_cfgs)
     gen_s = time.perf_counter() - t0
@@ -1026,22 +1029,33 @@ def run_fno_bench(args):
     plain = ws.run_uniform(test_cfgs)
     ev = ws.evaluate(model, test_cfgs, plain)
     valid = np.isfinite(ev.plain_time) & (plain.final_norms > 1e-6)
+    test_kinds = [c.laser.profile["type"] for c in test_cfgs]
+    train_kinds = [c.laser.profile["type"] for c in train_cfgs]
+    by_kind = {k: {"train": train_kinds.count(k), "train_steady": int(sum(1 for c, q in zip(train_kinds, keep) if c == k and q)),
+                   "test": test_kinds.count(k), "test_plain_steady": int(sum(1 for c, q in zip(test_kinds, valid) if c == k and q)),
+                   "accepted": int(sum(1 for c, q, v in zip(test_kinds, ev.accepted, valid) if c == k and q and v))}
+               for k in kinds}
     line = {
         "metric": "sweep time-to-steady-state, plain start / warm start (config 5)",
         "value": ev.speedup_time, "unit": "x (simulated time)", "n_gpus": world,
-        "higher_is_better": True, "dtype": "f32 solver, bf16 network with f32 accumulate",
+        "higher_is_better": True,
+        "dtype": f"{'f64' if args.fno_precision == 'double' else 'f32'} solver, bf16 network with f32 accumulate",
         "data": "synthetic (solver-generated steady states)",
         "config": {"workload": f"{n}^2, lx=ly=128 um, dt={args.fno_dt} ps, pumps gaussian/ring/square lattice, "
                                "P0 in [1,3] P_th, rtol 1e-6 per 10 ps, FNO width "
                                f"{args.fno_width} modes {args.fno_modes} 4 layers",
                    "train_members": len(train_cfgs), "train_steady": int(keep.sum()),
                    "test_members": len(test_cfgs), "test_plain_steady": int(valid.sum()),
-                   "epochs": args.fno_epochs, "batch": args.fno_batch},
+                   "epochs": args.fno_epochs, "batch": args.fno_batch,
+                   "solver_precision": args.fno_precision, "reservoir_closure": True,
+                   "by_kind": by_kind},
         "speedup_wall": ev.speedup_wall, "plain_wall_s": ev.plain_wall, "warm_wall_s": ev.warm_wall,
         "accepted": int(ev.accepted[valid].sum()),
         "plain_time_ps_mean": float(np.mean(ev.plain_time[valid])) if valid.any() else None,
         "warm_cost_ps_mean": float(np.mean(ev.cost_time[valid])) if valid.any() else None,
         "density_error_median": float(np.median(ev.density_error[valid])) if valid.any() else None,
+        "plain_time_ps": [float(v) for v in ev.plain_time[valid]],
+        "warm_time_ps": [float(v) for v in ev.warm_time[valid]],
         "train_loss_first_last": [losses[0], float(np.mean(losses[-10:]))],
         "data_generation_s": gen_s, "training_s": train_s,
     }
@@ -1089,6 +1103,9 @@ def main():
     ap.add_argument("--fno-width", type=int, default=32)
     ap.add_argument("--fno-modes", type=int, default=16)
     ap.add_argument("--fno-targets", choices=["steady", "final"], default="steady")
+    ap.add_argument("--fno-precision", choices=["single", "double"], default="double",
+                    help="precision of the runs that make and judge steady states")
+    ap.add_argument("--fno-kinds", default="gaussian,ring,lattice")
     ap.add_argument("--steady-time", type=float, default=0.0,
                     help="sweep workload: also run to steady state (up to this many ps)")
     ap.add_argument("--freeze-stopped", action="store_true")

@@ -1,10 +1,13 @@
-"""The learned warm start end to end on a small case (64^2, Gaussian pumps): solver-made
-targets, FNO training on the GPU kernels, prediction and the judged warm-start run.
+"""The learned warm start end to end on a small case (64^2, Gaussian pumps at 2-3 x threshold):
+solver-made steady states, FNO training on the GPU kernels, and the judged comparison of
+time to the steady-state criterion of ``SimulationController._check_steady_state``
+(``polarism/simulation_controller.py:710-734``, rtol 1e-6 per 10 ps) from the plain noise start
+and from the warm start, a warm result accepted only at steady density within 1e-3 (relative
+L2) of the plain result, a rejected member charged both runs.
 
-What the trained network gains over the method without it is measured where it is
-deterministic: the warm-start state is much closer to the solver's late-time state than the
-plain noise start is (density relative L2), and the warm-started solver run ends near the
-plain run's late-time density.
+The runs step in FP64: in FP32 the rounding of every step keeps the slowest condensate modes
+moving by about the criterion itself, and most members never meet it (2 of 16 in 12000 ps,
+against 16 of 16 within 3760 ps in FP64, on this family of pumps).
 """
 from __future__ import annotations
 
@@ -14,44 +17,42 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _members(count, seed):
+def _members(count, seed, total_time=6000.0):
     from polarism_gb300 import warmstart as ws
 
-    cfgs = ws.pump_members(count, seed, n=64, length=64.0, dt=0.02, total_time=1200.0,
+    cfgs = ws.pump_members(count, seed, n=64, length=64.0, dt=0.02, total_time=total_time,
                            kinds=("gaussian",))
     rng = np.random.default_rng(seed)
     p_th = ws.threshold(cfgs[0].physics)
     for c in cfgs:
         c.laser.profile = {"type": "gaussian", "sigma": float(rng.uniform(10.0, 14.0))}
         c.laser.P0 = float(rng.uniform(2.0, 3.0) * p_th)
-        c.stop.rtol = 0.0  # run every member to the total time
     return cfgs
 
 
-def test_warm_start_beats_the_noise_start(cuda_lib):
+def test_warm_start_reaches_the_criterion_sooner_at_equal_steady_density(cuda_lib):
     from polarism_gb300 import warmstart as ws
 
-    train = _members(48, seed=3)
-    test = _members(8, seed=4)
+    train, test = _members(48, seed=3), _members(8, seed=4)
+    assert all(c.solver.precision == "double" for c in train + test)
     data = ws.run_uniform(train)
-    ref = ws.run_uniform(test)
-    a, y = ws.features(train), ws.targets(list(data.psi), list(data.reservoir))
-    model = ws.WarmStart(64, width=16, modes=8, layers=4, hidden=32, seed=0)
-    losses = model.fit(a, y, epochs=60, batch=8, lr=3e-3)
-    assert np.mean(losses[-6:]) < 0.5 * np.mean(losses[:6])  # last epoch vs first
-    psi, n_r = model.predict(ws.features(test))
-    warm_err = np.array([ws.density_error(psi[i], ref.psi[i]) for i in range(len(test))])
-    from polarism_gb300 import host
+    keep = np.isfinite(data.stop_times) & (data.final_norms > 1e-6)
+    assert keep.sum() >= 40  # the plain solver makes the training targets
+    a = ws.features([c for c, k in zip(train, keep) if k])
+    y = ws.targets(list(data.psi[keep]), list(data.reservoir[keep]))
+    model = ws.WarmStart(64, width=32, modes=16, layers=4, hidden=64, seed=0)
+    losses = model.fit(a, y, epochs=150, batch=8, lr=3e-3)
+    assert np.mean(losses[-5:]) < 1e-2 * np.mean(losses[:5])
 
-    noise = [host.make_initial_psi((64, 64), 1e-3, c.noise.seed, np.complex64, np.float32) for c in test]
-    plain_err = np.array([ws.density_error(noise[i], ref.psi[i]) for i in range(len(test))])
-    lasing = ref.final_norms > 1e-3 * ref.final_norms.max()
-    print("lasing", lasing, "prediction error", np.round(warm_err, 3), "noise-start error",
-          np.round(plain_err, 3))
-    assert lasing.sum() >= 4
-    assert np.median(warm_err[lasing]) < 0.5 and np.all(plain_err[lasing] > 0.99)
-    # The judged warm-start run ends near the plain run's late-time density.
-    warm = ws.run_uniform(test, initial=(psi, n_r))
-    final_err = np.array([ws.density_error(warm.psi[i], ref.psi[i]) for i in range(len(test))])
-    print("after the warm-started run", np.round(final_err, 4))
-    assert np.median(final_err[lasing]) < 0.5
+    plain = ws.run_uniform(test)
+    valid = np.isfinite(plain.stop_times) & (plain.final_norms > 1e-6)
+    assert valid.all()  # every held-out member lases and meets the criterion from noise
+    ev = ws.evaluate(model, test, plain)
+    print("plain stop (ps)", plain.stop_times.tolist(), "warm stop (ps)", ev.warm_time.tolist(),
+          "density error", np.round(ev.density_error, 6).tolist(), "accepted", ev.accepted.tolist(),
+          "time ratio", round(ev.speedup_time, 3))
+    assert ev.accepted.sum() >= 6
+    acc = ev.accepted
+    assert np.all(ev.warm_time[acc] < ev.plain_time[acc])
+    assert np.all(ev.density_error[acc] <= 1e-3)
+    assert ev.speedup_time >= 2.5

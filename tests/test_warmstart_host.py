@@ -18,7 +18,29 @@ def test_pump_members_are_seeded_and_within_the_configured_ranges():
         assert 1.0 * p_th <= c.laser.P0 <= 3.0 * p_th
         assert c.laser.profile["type"] in ("gaussian", "ring", "lattice")
         assert c.physics.kinetic_relaxation_eta == 0.02 and c.noise.stochastic == "none"
+        assert c.solver.precision == "double"
     assert len({c.noise.seed for c in a}) == len(a)
+
+
+def test_reservoir_closure_is_the_stationary_reservoir_of_the_condensate():
+    """n_R from psi makes dn_R/dt = P - (gamma_R + R |psi|^2) n_R vanish (single reservoir,
+    polarism/reservoir/single_reservoir.py) and is P / gamma_R where psi = 0."""
+    from polarism_gb300 import host
+    from polarism_gb300 import warmstart as ws
+
+    cfgs = ws.pump_members(3, seed=4, n=16, length=16.0)
+    rng = np.random.default_rng(1)
+    psi = rng.standard_normal((3, 16, 16)) + 1j * rng.standard_normal((3, 16, 16))
+    psi[2] = 0
+    n_r = ws.reservoir_closure(cfgs, psi)
+    grid = host.PeriodicGrid(cfgs[0].grid)
+    for m, c in enumerate(cfgs):
+        pump = host.make_laser(c.laser, grid.X, grid.Y, "double")._spatial_envelope * c.laser.P0
+        ph = c.physics
+        rate = pump - (ph.gamma_R + ph.R * np.abs(psi[m]) ** 2) * n_r[m]
+        assert np.max(np.abs(rate)) <= 1e-15 * np.max(pump)
+    assert np.allclose(n_r[2], host.make_laser(cfgs[2].laser, grid.X, grid.Y, "double")._spatial_envelope
+                       * cfgs[2].laser.P0 / cfgs[2].physics.gamma_R, rtol=1e-15)
 
 
 def test_features_targets_and_phase_convention():
