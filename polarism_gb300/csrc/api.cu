@@ -172,11 +172,16 @@ pg::RK4Features features(const pg_solver* s) {
   return f;
 }
 
+// The full-width kernel takes one laser, or two on rows of at most 1024 sites (their
+// envelopes stream as extra ring rows; wider rows' bands have no room for them).
+bool wide_lasers_ok(int terms, int nx) { return terms == 1 || (terms == 2 && nx <= 1024); }
+
 bool use_wide(const pg_solver* s) {
   const pg::RK4Features f = features(s);
-  // FP32, single reservoir and one laser; a potential or kinetic relaxation selects the
-  // full-width kernel's general variant.
-  const bool eligible = s->cfg.precision == PG_SINGLE && f.reservoir == 1 && f.pump_terms == 1 &&
+  // FP32, single reservoir, one laser (two on rows up to 1024 sites); a potential, kinetic
+  // relaxation or a second laser selects the full-width kernel's general variant.
+  const bool eligible = s->cfg.precision == PG_SINGLE && f.reservoir == 1 &&
+                        wide_lasers_ok(f.pump_terms, s->cfg.nx) &&
                         pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny);
   if (s->rk4_kernel == 1) return false;
   return eligible;
@@ -202,6 +207,8 @@ cudaError_t launch_step(pg_solver* s, int from, int step_offset) {
     w.members = s->cfg.members;
     w.blocks = s->wide_blocks;
     w.pump_stride = s->cfg.pump_per_member ? s->plane : 0;
+    w.pump_terms = f.pump_terms;
+    w.pump_term_stride = s->pump_term_stride;
     w.halt = s->halt;
     w.pot = static_cast<const float*>(s->potential);
     w.pot_stride = s->cfg.potential_per_member ? s->plane : 0;
@@ -404,7 +411,8 @@ int pg_create(const pg_config* cfg, const pg_physics* physics, pg_solver** out) 
   cudaMemsetAsync(s->halt, 0, sizeof(int), s->stream);
   if (cfg->precision == PG_SINGLE && pg::wide_rk4_supported(cfg->nx, cfg->ny)) {
     if ((e = pg::configure_wide_rk4()) != cudaSuccess) return fail(e, "wide kernel attributes");
-    s->wide_blocks = pg::wide_rk4_grid(cfg->nx, cfg->ny, cfg->members, s->sm_count);
+    s->wide_blocks = pg::wide_rk4_grid(cfg->nx, cfg->ny, cfg->members, s->sm_count,
+                                       s->pump_terms == 2 && cfg->nx <= 1024 ? 2 : 1);
     if (pg::quad_rk4_supported(cfg->nx, cfg->ny)) {
       if ((e = pg::configure_quad_rk4()) != cudaSuccess) return fail(e, "quad kernel attributes");
       s->quad_blocks = pg::quad_rk4_grid(cfg->nx, cfg->ny, cfg->members, s->sm_count);
@@ -493,11 +501,13 @@ int pg_rk4_set_kernel(pg_solver* s, int32_t kind) {
              "potential");
   if (kind >= 2) {
     const pg::RK4Features f = features(s);
-    PG_CHECK(s->cfg.precision == PG_SINGLE && f.reservoir == 1 && f.pump_terms == 1 &&
+    PG_CHECK(s->cfg.precision == PG_SINGLE && f.reservoir == 1 &&
+                 wide_lasers_ok(f.pump_terms, s->cfg.nx) && (kind == 2 || f.pump_terms == 1) &&
                  pg::wide_rk4_supported(s->cfg.nx, s->cfg.ny),
              PG_ERR_UNSUPPORTED,
              "pg_rk4_set_kernel: the full-width kernel needs FP32, a single reservoir, one laser "
-             "and nx in {128, 256, 512, 1024} or a multiple of 1024 up to 16384");
+             "(two on rows of at most 1024 sites) and nx in {128, 256, 512, 1024} or a multiple "
+             "of 1024 up to 16384");
   }
   s->rk4_kernel = kind;
   free_graphs(s);

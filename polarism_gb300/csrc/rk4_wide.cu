@@ -62,7 +62,10 @@ constexpr int kInbox = 2 * 2 * 3;
 constexpr int kFailWords = 2;
 constexpr uint32_t kEdgeBytes = 3 * 8;  // one iteration's delivery: three stage values
 
-template <int NX, bool NOISE, bool GENERAL, bool BAND, bool CLUSTER = false>
+// TERMS: separable lasers whose envelopes stream beside psi and n_R (one ring row each); the
+// pump of a stage is sum_l c_l E_l with products and partial sums rounded apart, as the tiled
+// kernel forms it.  Several lasers run on rows of at most 1024 sites.
+template <int NX, bool NOISE, bool GENERAL, bool BAND, bool CLUSTER = false, int TERMS = 1>
 __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 1024 ? 1 : 1024 / NX))
     rk4_wide_kernel(const float2* __restrict__ psi_in, const float* __restrict__ n_in,
                     const float* __restrict__ pump, float2* __restrict__ psi_out,
@@ -74,6 +77,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
   constexpr int ACTIVE = WideShape<NX, BAND, CLUSTER>::ACTIVE;
   constexpr int HALF = WideShape<NX, BAND, CLUSTER>::THREADS;  // exchange-buffer stride
   constexpr bool HALO = BAND || CLUSTER;  // shared-memory rows carry the band's halo
+  static_assert(TERMS == 1 || !HALO, "several lasers run on rows of at most 1024 sites");
   // One block per SM (1024-site rows): a split arrive/wait barrier lets its warps drift
   // apart by up to a row, which measured faster; with several blocks per SM the blocks
   // already interleave and a block-wide barrier is cheaper.
@@ -82,11 +86,11 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float2* ring_psi = reinterpret_cast<float2*>(smem_raw);          // [kRing][W]
   float* ring_n = reinterpret_cast<float*>(ring_psi + kRing * W);  // [kRing][W]
-  float* ring_p = ring_n + kRing * W;                              // [kRing][W]
+  float* ring_p = ring_n + kRing * W;                              // [kRing][TERMS][W]
   // Exchange: each thread's first (xa) and second (xb) column of the three stage inputs,
   // [parity][stage][thread]; two 8-byte stores a stage keep the values in the register pairs
   // the packed arithmetic produced them in.
-  float2* xa = reinterpret_cast<float2*>(ring_p + kRing * W);  // [2][3][HALF]
+  float2* xa = reinterpret_cast<float2*>(ring_p + kRing * TERMS * W);  // [2][3][HALF]
   float2* xb = xa + 6 * HALF;                                  // [2][3][HALF]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(xb + 6 * HALF);  // [kBars]
   const uint32_t xbar = smem_u32(&mbar[kRing]);
@@ -128,7 +132,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
   const uint32_t left_rank = CLUSTER ? static_cast<uint32_t>((rank + bands - 1) % bands) : 0u;
   const uint32_t right_rank = CLUSTER ? static_cast<uint32_t>((rank + 1) % bands) : 0u;
   const long long plane = static_cast<long long>(gnx) * ny;
-  constexpr uint32_t kRowBytes = W * 16u;
+  constexpr uint32_t kRowBytes = W * (12u + 4u * TERMS);
 
   if (t == 0) {
     for (int s = 0; s < kRing; ++s) mbar_init(smem_u32(&mbar[s]), 1);
@@ -189,9 +193,18 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
     const RhsConst<float> kk = consts[member];
     const WideConst k = wide_const(kk);
     const uint32_t key0 = static_cast<uint32_t>(kk.seed), key1 = static_cast<uint32_t>(kk.seed >> 32);
-    const float s0 = scales[(step_offset * 3 + 0) * g.members + member];
-    const float s1 = scales[(step_offset * 3 + 1) * g.members + member];
-    const float s2 = scales[(step_offset * 3 + 2) * g.members + member];
+    // Coefficient sample q of laser l: scales[[step][q][l][member]].  With one laser the
+    // stage multiplies s_q by the envelope; with several, pump_pair forms sum_l c_ql E_l and
+    // the stage's factor is 1 (a multiply by 1 rounds nothing).
+    float cs[3][TERMS];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+#pragma unroll
+      for (int l = 0; l < TERMS; ++l)
+        cs[q][l] = scales[(static_cast<long long>(step_offset * 3 + q) * TERMS + l) * g.members + member];
+    const float s0 = TERMS == 1 ? cs[0][0] : 1.f;
+    const float s1 = TERMS == 1 ? cs[1][0] : 1.f;
+    const float s2 = TERMS == 1 ? cs[2][0] : 1.f;
     const unsigned long long noise_step = NOISE ? step_base[0] + step_offset : 0ull;
     const PhiloxCellPrefix prefix =
         philox_cell_prefix(static_cast<uint32_t>(noise_step), static_cast<uint32_t>(noise_step >> 32),
@@ -241,6 +254,21 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
       return pair_rhs(ca, cb, L, R, upa, upb, dna, dnb, n2, __fmul2_rn(make_float2(s, s), P), k,
                       da, db);
     };
+    // The pump envelope pair of ring slot `slot` (one laser), or the stage pump of coefficient
+    // sample q (several).
+    auto pump_pair = [&](int slot, int q) -> float2 {
+      const float* base = ring_p + slot * TERMS * W + col0;
+      const float2 e0 = *reinterpret_cast<const float2*>(base);
+      if (TERMS == 1) return e0;
+      float2 v = make_float2(__fmul_rn(cs[q][0], e0.x), __fmul_rn(cs[q][0], e0.y));
+#pragma unroll
+      for (int l = 1; l < TERMS; ++l) {
+        const float2 e = *reinterpret_cast<const float2*>(base + l * W);
+        v = make_float2(__fadd_rn(v.x, __fmul_rn(cs[q][l], e.x)),
+                        __fadd_rn(v.y, __fmul_rn(cs[q][l], e.y)));
+      }
+      return v;
+    };
     float2* out_psi_m = psi_out + member * plane + gcol0w;
     float* out_n_m = n_out + member * plane + gcol0w;
     int row_first = (ya - 4) % ny;
@@ -257,7 +285,10 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
       if (!HALO) {
         bulk_g2s(smem_u32(ring_psi + slot * W), psi_m + ro, NX * 8u, bar);
         bulk_g2s(smem_u32(ring_n + slot * W), n_m + ro, NX * 4u, bar);
-        bulk_g2s(smem_u32(ring_p + slot * W), p_m + ro, NX * 4u, bar);
+#pragma unroll
+        for (int l = 0; l < TERMS; ++l)
+          bulk_g2s(smem_u32(ring_p + (slot * TERMS + l) * W), p_m + l * g.pump_term_stride + ro,
+                   NX * 4u, bar);
       } else {
         // Columns [gc0, gc0 + W) of the periodic row: one copy, or two where the band wraps
         // (the first band starts at gnx - 4, the last one ends past gnx).  Every piece is a
@@ -335,7 +366,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         const float2 up0 = make_float2(u4.x, u4.y), up1 = make_float2(u4.z, u4.w);
         const float2 dn0 = make_float2(d4.x, d4.y), dn1 = make_float2(d4.z, d4.w);
         const float2 n1v = *reinterpret_cast<const float2*>(ring_n + slot1 * W + col0);
-        const float2 P1 = *reinterpret_cast<const float2*>(ring_p + slot1 * W + col0);
+        const float2 P1 = pump_pair(slot1, 0);
         // Rows of the four stages (general variant only: the potential is read per stage).
         int srow[4] = {0, 0, 0, 0};
         if (GENERAL) {
@@ -383,7 +414,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         {
           float2 lt2, rt2;
           xchg((j + 1) & 1, 0, lt2, rt2);
-          const float2 P2 = *reinterpret_cast<const float2*>(ring_p + slot2 * W + col0);
+          const float2 P2 = pump_pair(slot2, 1);
           const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot2 * W + col0);
           const Pair c = q1[jb];
           float2 da, db, va, vb;
@@ -399,7 +430,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         {
           float2 lt3, rt3;
           xchg((j + 1) & 1, 1, lt3, rt3);
-          const float2 P3 = *reinterpret_cast<const float2*>(ring_p + slot3 * W + col0);
+          const float2 P3 = pump_pair(slot3, 1);
           const float2 n0 = *reinterpret_cast<const float2*>(ring_n + slot3 * W + col0);
           const float4 p4 = *reinterpret_cast<const float4*>(ring_psi + slot3 * W + col0);
           const Pair c = q2[jc];
@@ -416,7 +447,7 @@ __global__ void __launch_bounds__(WideShape<NX, BAND, CLUSTER>::THREADS, (NX >= 
         {
           float2 lt4, rt4;
           xchg((j + 1) & 1, 2, lt4, rt4);
-          const float2 P4 = *reinterpret_cast<const float2*>(ring_p + slot4 * W + col0);
+          const float2 P4 = pump_pair(slot4, 2);
           const Pair c = q3[jd];
           float2 da, db, va, vb;
           pot_at(srow[3], va, vb);
@@ -500,10 +531,10 @@ namespace {
 // limit is 8); wider rows as independent bands.
 bool use_cluster(int nx) { return nx > 1024 && nx % 1024 == 0 && nx / 1024 <= 8; }
 
-template <int NX, bool BAND, bool CLUSTER>
+template <int NX, bool BAND, bool CLUSTER, int TERMS = 1>
 size_t smem_for() {
   using S = WideShape<NX, BAND, CLUSTER>;
-  return static_cast<size_t>(kRing) * S::W * 16 + static_cast<size_t>(6) * S::THREADS * 16 +
+  return static_cast<size_t>(kRing) * S::W * (12 + 4 * TERMS) + static_cast<size_t>(6) * S::THREADS * 16 +
          kBars * sizeof(uint64_t) + kInbox * sizeof(float2) + kFailWords * sizeof(int);
 }
 
@@ -524,12 +555,28 @@ cudaError_t configure_shape() {
   return e;
 }
 
+// Two lasers (the general variant, rows of at most 1024 sites).
+template <int NX>
+cudaError_t configure_two_lasers() {
+  const int smem = static_cast<int>(smem_for<NX, false, false, 2>());
+  cudaError_t e = cudaFuncSetAttribute(rk4_wide_kernel<NX, true, true, false, false, 2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(rk4_wide_kernel<NX, false, true, false, false, 2>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
+}
+
 template <int NX, bool BAND>
-int blocks_shape(bool noise) {
+int blocks_shape(bool noise, int terms = 1) {
   int blocks = 0;
   const int threads = WideShape<NX, BAND>::THREADS;
   cudaError_t e =
-      noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      terms == 2 && !BAND
+          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &blocks, rk4_wide_kernel<NX, true, true, false, false, 2>, threads,
+                smem_for<NX, false, false, 2>())
+      : noise ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                   &blocks, rk4_wide_kernel<NX, true, false, BAND>, threads, smem_for<NX, BAND, false>())
             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                   &blocks, rk4_wide_kernel<NX, false, false, BAND>, threads, smem_for<NX, BAND, false>());
@@ -574,6 +621,17 @@ cudaError_t launch_shape(const float* psi_in, const float* n_in, const float* pu
   const float2* pin = reinterpret_cast<const float2*>(psi_in);
   float2* pout = reinterpret_cast<float2*>(psi_out);
   const bool general = wide_general(g);
+  if (!BAND && g.pump_terms == 2) {
+    const size_t smem2 = smem_for<NX, false, false, 2>();
+    if (noise)
+      rk4_wide_kernel<NX, true, true, false, false, 2><<<g.blocks, threads, smem2, stream>>>(
+          pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+    else
+      rk4_wide_kernel<NX, false, true, false, false, 2><<<g.blocks, threads, smem2, stream>>>(
+          pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
+    return cudaGetLastError();
+  }
+  if (g.pump_terms != 1) return cudaErrorInvalidValue;
   if (noise && general) {
     rk4_wide_kernel<NX, true, true, BAND><<<g.blocks, threads, smem, stream>>>(
         pin, n_in, pump, pout, n_out, consts, scales, step_base, step_offset, dt, g, err_flag);
@@ -647,10 +705,14 @@ cudaError_t configure_wide_rk4() {
   if (e == cudaSuccess) e = configure_shape<1024, false, false>();
   if (e == cudaSuccess) e = configure_shape<1024, true, false>();
   if (e == cudaSuccess) e = configure_shape<1024, false, true>();
+  if (e == cudaSuccess) e = configure_two_lasers<128>();
+  if (e == cudaSuccess) e = configure_two_lasers<256>();
+  if (e == cudaSuccess) e = configure_two_lasers<512>();
+  if (e == cudaSuccess) e = configure_two_lasers<1024>();
   return e;
 }
 
-int wide_rk4_grid(int nx, int ny, int members, int sm_count) {
+int wide_rk4_grid(int nx, int ny, int members, int sm_count, int terms) {
   if (use_cluster(nx)) {
     // Whole clusters, as many as fit at once, and at least 16 rows a cluster.
     const int size = nx / 1024;
@@ -661,10 +723,10 @@ int wide_rk4_grid(int nx, int ny, int members, int sm_count) {
   }
   int per_sm = 1;
   switch (nx) {
-    case 128: per_sm = blocks_shape<128, false>(true); break;
-    case 256: per_sm = blocks_shape<256, false>(true); break;
-    case 512: per_sm = blocks_shape<512, false>(true); break;
-    case 1024: per_sm = blocks_shape<1024, false>(true); break;
+    case 128: per_sm = blocks_shape<128, false>(true, terms); break;
+    case 256: per_sm = blocks_shape<256, false>(true, terms); break;
+    case 512: per_sm = blocks_shape<512, false>(true, terms); break;
+    case 1024: per_sm = blocks_shape<1024, false>(true, terms); break;
     default: per_sm = blocks_shape<1024, true>(true); break;
   }
   // Rows wider than 1024 sites (BAND) are separate 1024-site bands, each its own row stream.
@@ -693,6 +755,7 @@ cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float*
       return launch_shape<1024, false>(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
                                        step_offset, dt, noise, g, err_flag, stream);
     default:
+      if (g.pump_terms != 1) return cudaErrorInvalidValue;
       if (use_cluster(g.nx))
         return launch_cluster(psi_in, n_in, pump, psi_out, n_out, consts, scales, step_base,
                               step_offset, dt, noise, g, err_flag, stream);

@@ -10,6 +10,8 @@ struct WideGeom {
   int nx, ny, members;
   int blocks;              // persistent grid size
   long long pump_stride;   // 0: shared envelope; nx*ny: one per member
+  int pump_terms = 1;      // separable lasers: 1, or 2 on rows of at most 1024 sites
+  long long pump_term_stride = 0;  // reals between consecutive lasers' envelopes
   const int* halt = nullptr;  // when non-null and set, the launch returns at once
   // General variant: potential (0 none, 1 real, 2 complex; shared or per member) and the
   // kinetic-relaxation term.
@@ -27,7 +29,7 @@ size_t wide_rk4_smem(int nx);
 cudaError_t configure_wide_rk4();
 // Grid of the full-width kernel for this shape: persistent blocks (or, for rows of 2048 to
 // 8192 sites, whole clusters of nx / 1024 CTAs), at least 16 rows of work each.
-int wide_rk4_grid(int nx, int ny, int members, int sm_count);
+int wide_rk4_grid(int nx, int ny, int members, int sm_count, int terms = 1);
 cudaError_t launch_rk4_wide(const float* psi_in, const float* n_in, const float* pump,
                             float* psi_out, float* n_out, const RhsConst<float>* consts,
                             const float* scales, const unsigned long long* step_base,

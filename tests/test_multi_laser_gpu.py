@@ -192,3 +192,46 @@ def test_drop_in_solvers_with_a_pulse_train_and_a_cw_spot(cuda_lib, method):
         psi_o, f_o = st.real_space(), st.fields
     assert rel_l2(state.field, psi_o) < 1e-10
     assert rel_l2(model.reservoir.get_state()[0], f_o[0]) < 1e-10
+
+
+@pytest.mark.parametrize("nx,ny,members", [(256, 24, 2), (1024, 12, 2)])
+def test_two_lasers_on_the_full_width_kernel(cuda_lib, nx, ny, members):
+    """Two lasers streamed as extra ring rows of the full-width kernel (kind 2): against the
+    tiled kernel (1e-5) and the FP64 oracle (1e-4), per-member envelopes, time-dependent
+    coefficients at every half step, Wigner noise on."""
+    from polarism_gb300.engine import MemberPhysics, RK4Engine
+
+    rng = np.random.default_rng(nx + 3 * ny)
+    p = dict(hbar=0.6582119514, m_eff=0.284, g_C=0.001, g_R=0.002, g_I=0.0, R=0.02,
+             gamma_C=0.083, gamma_R=0.005)
+    dx, dy, dt, steps = 0.45, 0.55, 1e-3, 9
+    psi0 = 0.05 * (rng.standard_normal((members, 1, ny, nx))
+                   + 1j * rng.standard_normal((members, 1, ny, nx)))
+    res0 = np.abs(rng.standard_normal((members, 1, ny, nx))) * 0.02
+    env = np.abs(rng.standard_normal((2, members, 1, ny, nx)))  # [laser][member]
+    seeds = [21 + m for m in range(members)]
+    samples = 0.02 + 0.01 * rng.random((2 * steps + 1, 2, members))  # [half step][laser][member]
+    scales = np.stack([samples[2 * k:2 * k + 3] for k in range(steps)])  # (steps, 3, 2, members)
+    outs = {}
+    for kernel in (1, 2):
+        eng = RK4Engine(nx, ny, members, dx, dy, dt, MemberPhysics(**p), "single",
+                        pump_per_member=True, pump_terms=2)
+        eng.set_kernel(kernel)
+        assert eng.kernel() == kernel
+        eng.set_pump(env.astype(np.float32))
+        eng.set_noise(seeds, p["gamma_C"], p["R"], 1.0, dt / (4 * dx * dy))
+        eng.set_state(psi0.astype(np.complex64), res0.astype(np.float32))
+        eng.advance(0, steps, scales)
+        outs[kernel] = eng.get_state()
+        eng.close()
+    assert rel_l2(outs[2][0], outs[1][0]) < 1e-5 and rel_l2(outs[2][1], outs[1][1]) < 1e-5
+    nz = gpe.Noise(seeds, [p["gamma_C"]] * members, [p["R"]] * members, [1.0] * members, dt,
+                   dx * dy, "double", normals_precision="single")
+
+    def pump_at(t):  # sum over the lasers at the half-step sample of time t
+        c = samples[int(round(2 * t / dt))]  # (2, members)
+        return sum(c[l][:, None, None, None] * env[l] for l in range(2))
+
+    psi_o, fields = gpe.rk4_advance(psi0.copy(), (res0.copy(),), pump_at, 0.0, p, dx, dy, dt, 0,
+                                    steps, noise=nz)
+    assert rel_l2(outs[2][0], psi_o) < 1e-4 and rel_l2(outs[2][1], fields[0]) < 1e-4
