@@ -1016,6 +1016,8 @@ def run_fno_bench(args):
     # --fno-targets final every member's final state is a target (short profiling runs).
     lasing = data.final_norms > 1e-6
     keep = np.ones_like(lasing) if args.fno_targets == "final" else np.isfinite(data.stop_times) & lasing
+    print(f"training runs: {len(train_cfgs)} members, {int(lasing.sum())} lasing, {int(keep.sum())} "
+          f"reached the criterion, {gen_s:.1f} s", file=sys.stderr, flush=True)
     if not keep.any():
         raise SystemExit("no training targets: no member reached a lasing steady state")
     a = ws.features([c for c, k in zip(train_cfgs, keep) if k])
@@ -1023,9 +1025,11 @@ def run_fno_bench(args):
     model = ws.WarmStart(n, width=args.fno_width, modes=args.fno_modes)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    losses = model.fit(a, y, epochs=args.fno_epochs, batch=args.fno_batch, lr=args.fno_lr)
+    losses = model.fit(a, y, epochs=args.fno_epochs, batch=min(args.fno_batch, len(a)), lr=args.fno_lr)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t1
+    print(f"training: {len(a)} states, {args.fno_epochs} epochs, {time.perf_counter() - t1:.1f} s, loss "
+          f"{losses[0]:.3e} -> {np.mean(losses[-10:]):.3e}", file=sys.stderr, flush=True)
     plain = ws.run_uniform(test_cfgs)
     ev = ws.evaluate(model, test_cfgs, plain)
     valid = np.isfinite(ev.plain_time) & (plain.final_norms > 1e-6)
