@@ -245,8 +245,9 @@ int pg_field_norms_noalloc(const void* psi, int32_t precision, int32_t members,
 
 /* Choose the RK4 kernel: 0 automatic, 1 the tiled streaming kernel (any size, FP32/FP64,
  * potential and relaxation terms), 2 the full-width FP32 kernel (nx in {128, 256, 512, 1024},
- * or a multiple of 1024 up to 16384 in 1024-site bands; single reservoir, one laser; real or
- * complex potential and kinetic relaxation in its general variant), 3 the full-width kernel
+ * or a multiple of 1024 up to 16384 in 1024-site bands; single reservoir, one laser, or two on
+ * rows of at most 1024 sites; real or complex potential and kinetic relaxation in its general
+ * variant), 3 the full-width kernel
  * with four sites a thread (rows of 512 or 1024 sites, no potential or relaxation; bitwise the
  * same results as 2).  pg_rk4_get_kernel reports the one in use (1, 2 or 3). */
 int pg_rk4_set_kernel(pg_solver* s, int32_t kind);
