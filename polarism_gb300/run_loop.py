@@ -202,13 +202,27 @@ class DeviceSteadyMonitor:
                 self.settle()
 
     # ------------------------------------------------------------------ settling
-    def flush(self):
-        """Copy the device state back into the controller's state and reservoir."""
+    def _collect(self):
+        """Wait for the queued checks and copy their first stop steps into the controller's
+        stop times (where it has none yet).  Returns the halting check's step, or None."""
         ctl = self.controller
-        if not self._settled and self._started:
-            stopped, _ = self.solver.engine.steady_poll()
-            if stopped == self.solver.engine.members:
-                self.settle()
+        engine = self.solver.engine
+        _, _, _, stops, halt_step = engine.steady_results()
+        new = (stops >= 0) & np.isnan(ctl.stop_times)
+        ctl.stop_times[new] = ctl.state.t0 + stops[new] * float(ctl.cfg.solver.dt)
+        return halt_step
+
+    def flush(self):
+        """Before anything else of the controller reads the state: the device's stop
+        decisions so far go into ``stop_times`` (an event that records stops must see them
+        first, as it would after the reference's own checks), and the device state is copied
+        back into the controller's state and reservoir.  If a check has halted the run, this
+        settles it."""
+        ctl = self.controller
+        if self._started and not self._settled:
+            halt_step = self._collect()
+            if halt_step is not None:
+                self._settle_halted_or_final(halt_step)
                 return
         self.solver.flush(ctl.model, ctl.state)
 
@@ -219,17 +233,16 @@ class DeviceSteadyMonitor:
             if not self._started:
                 self.solver.flush(self.controller.model, self.controller.state)
             return
+        self._settle_halted_or_final(self._collect())
+
+    def _settle_halted_or_final(self, halt_step):
         ctl = self.controller
         state = ctl.state
         engine = self.solver.engine
-        dt = float(ctl.cfg.solver.dt)
-        _, _, _, stops, halt_step = engine.steady_results()
         self.settles += 1
-        new = (stops >= 0) & np.isnan(ctl.stop_times)
-        ctl.stop_times[new] = state.t0 + stops[new] * dt
         if halt_step is not None:
             state.step = int(halt_step)
-            state.t = state.t0 + state.step * dt
+            state.t = state.t0 + state.step * float(ctl.cfg.solver.dt)
             ctl._steady_last_step = state.step
             self._halted = True
         self.solver.flush(ctl.model, state)

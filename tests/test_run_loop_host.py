@@ -237,3 +237,42 @@ def test_device_monitor_refuses_a_solver_that_leaves_a_spectrum(monitored):
     ctl = _controller("split-step-fft-cuda")
     with pytest.raises(ValueError, match="cannot keep its state"):
         DeviceSteadyMonitor(ctl)
+
+
+def test_device_monitor_copies_the_state_back_for_accumulators_and_events(monitored):
+    """The controller's other readers of the state -- a scheduled accumulator (g2, every
+    0.02 ps from 0.04 ps) and an event callback (every 0.04 ps) -- see the same states with the
+    monitor installed as without it, and the event's stop decision still ends the run."""
+    from polarism_gb300.run_loop import run_with_device_monitor
+
+    def setup(ctl, seen):
+        def event(view):
+            seen.append((view.step, np.array(view.density)))
+            return view.step >= 120  # every member "stops" by event at step 120
+        ctl.add_event(event, 0.04)
+
+    runs = {}
+    for mode in ("host", "device"):
+        ctl = _controller("rk4-cuda", steps=300, rtol=1e-9)  # the steady check never stops anyone
+        ctl.cfg.result.accumulators = {"g2": {"start": 0.04, "every": 0.02}}
+        from polarism.results.accumulators import G2Accumulator
+
+        ctl._accumulators = {"g2": G2Accumulator(ctl, start=0.04, every=0.02)}
+        seen = []
+        setup(ctl, seen)
+        if mode == "host":
+            ctl.run()
+        else:
+            run_with_device_monitor(ctl)
+        runs[mode] = (ctl, seen)
+    (h, h_seen), (d, d_seen) = runs["host"], runs["device"]
+    assert [s for s, _ in d_seen] == [s for s, _ in h_seen] and h_seen[-1][0] == 120
+    for (_, a), (_, b) in zip(d_seen, h_seen):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(d.stop_times, h.stop_times)
+    assert d.state.step == h.state.step == 120
+    np.testing.assert_array_equal(np.array(d.state.field), np.array(h.state.field))
+    ah, ad = h._accumulators["g2"], d._accumulators["g2"]
+    assert ad.samples == ah.samples > 0
+    for x, y in zip(ad.results(), ah.results()):
+        np.testing.assert_array_equal(np.asarray(x.value), np.asarray(y.value))
