@@ -251,17 +251,62 @@ def reservoir_closure(cfgs, psi):
     return out
 
 
+def amplitude_balance(cfgs, psi, lo=0.25, hi=4.0, iters=60):
+    """psi rescaled so that the condensate neither gains nor loses particles with the reservoir
+    of :func:`reservoir_closure`: at a steady state of polarism/model.py:89-127,
+    dN/dt = sum (R n_R - gamma_C) |psi|^2 + eta (hbar / m) sum n_R Re(psi* lap psi) = 0 (the
+    Hamiltonian part conserves N).  With psi -> sqrt(s) psi and n_R = P / (gamma_R + R s |psi|^2)
+    this is sum n_R(s) w - gamma_C sum |psi|^2 = 0, w = R |psi|^2 + eta (hbar / m)
+    Re(psi* lap psi) (the solver's five-point Laplacian), solved for s by bisection in log s.
+    The total population is the slowest thing for a start to get right (it relaxes through the
+    reservoir), so a start with the right shape but the wrong amount converges slowly.
+    Members without a root in [lo, hi] keep their psi."""
+    grid = host.PeriodicGrid(cfgs[0].grid)
+    dx, dy = grid.dx, grid.dy
+    out = []
+    for c, p in zip(cfgs, psi):
+        p = np.asarray(p, np.complex128)
+        ph = c.physics
+        pump = host.make_laser(c.laser, grid.X, grid.Y, "double")._spatial_envelope * c.laser.P0
+        rho = np.abs(p) ** 2
+        lap = ((np.roll(p, 1, 1) + np.roll(p, -1, 1) - 2 * p) / dx ** 2
+               + (np.roll(p, 1, 0) + np.roll(p, -1, 0) - 2 * p) / dy ** 2)
+        eta = float(getattr(ph, "kinetic_relaxation_eta", 0.0) or 0.0)
+        w = ph.R * rho + eta * (ph.hbar / ph.m_eff) * np.real(np.conj(p) * lap)
+        loss = ph.gamma_C * rho.sum()
+
+        def g(s):
+            return np.sum(pump * w / (ph.gamma_R + ph.R * s * rho)) - loss
+
+        a, b = np.log(lo), np.log(hi)
+        ga, gb = g(lo), g(hi)
+        if loss <= 0 or not (ga > 0 > gb):
+            out.append(p)
+            continue
+        for _ in range(iters):
+            mid = 0.5 * (a + b)
+            if g(np.exp(mid)) > 0:
+                a = mid
+            else:
+                b = mid
+        out.append(p * np.sqrt(np.exp(0.5 * (a + b))))
+    return np.stack(out)
+
+
 def density_error(psi_a, psi_b):
     ra, rb = np.abs(psi_a) ** 2, np.abs(psi_b) ** 2
     return float(np.sqrt(np.sum((ra - rb) ** 2)) / max(np.sqrt(np.sum(rb ** 2)), 1e-30))
 
 
-def evaluate(ws, cfgs, plain, density_tol=1e-3, closure=True):
+def evaluate(ws, cfgs, plain, density_tol=1e-3, closure=True, balance=False):
     """Warm-start the members of ``cfgs`` (whose plain-start result is ``plain``, from
     :func:`run_uniform`) and compare.  Only members whose plain run reached a lasing steady
     state enter the ratios (decayed members have no condensate to predict).  ``closure``: the
-    warm n_R is :func:`reservoir_closure` of the predicted psi instead of the network's n_R."""
+    warm n_R is :func:`reservoir_closure` of the predicted psi instead of the network's n_R;
+    ``balance``: psi is first rescaled by :func:`amplitude_balance`."""
     psi, n_r = ws.predict(features(cfgs))
+    if balance:
+        psi = amplitude_balance(cfgs, psi)
     if closure:
         n_r = reservoir_closure(cfgs, psi)
     warm = run_uniform(cfgs, initial=(psi, n_r))

@@ -98,3 +98,21 @@ def test_evaluate_accounting(monkeypatch):
     share = (50.0 + 60.0) / (40.0 + 50.0 + 60.0)
     assert np.isclose(ev.warm_wall, 2.0 + share * 8.0)
     assert np.isclose(ev.speedup_wall, 8.0 / (2.0 + share * 8.0))
+
+
+def test_amplitude_balance_restores_the_uniform_steady_population():
+    """A uniform condensate under a uniform pump is stationary when R n_R = gamma_C with
+    n_R = P / (gamma_R + R |psi|^2), i.e. |psi|^2 = P / gamma_C - gamma_R / R; the balance
+    rescales any uniform psi to that density (the Laplacian term vanishes)."""
+    from polarism_gb300 import warmstart as ws
+
+    cfgs = ws.pump_members(2, seed=6, n=16, length=16.0)
+    for c in cfgs:
+        c.laser.profile = {"type": "gaussian", "sigma": 1e9}  # uniform to double precision
+    ph = cfgs[0].physics
+    psi = np.full((2, 16, 16), 0.3 + 0.4j)
+    out = ws.amplitude_balance(cfgs, psi)
+    for m, c in enumerate(cfgs):
+        expect = c.laser.P0 / ph.gamma_C - ph.gamma_R / ph.R
+        assert np.allclose(np.abs(out[m]) ** 2, expect, rtol=1e-12)
+        assert np.allclose(np.angle(out[m]), np.angle(psi[m]))
