@@ -1052,6 +1052,7 @@ def run_fno_bench(args):
                    "test_members": len(test_cfgs), "test_plain_steady": int(valid.sum()),
                    "epochs": args.fno_epochs, "batch": args.fno_batch,
                    "solver_precision": args.fno_precision, "reservoir_closure": True,
+                   "amplitude_balance": True,
                    "by_kind": by_kind},
         "speedup_wall": ev.speedup_wall, "plain_wall_s": ev.plain_wall, "warm_wall_s": ev.warm_wall,
         "accepted": int(ev.accepted[valid].sum()),

@@ -13,8 +13,9 @@ Pipeline (none of it replaces reference code; Polarism has no learned component)
    ``(P(x)/P_th, x, y)`` to the steady ``(Re psi, Im psi, n_R)``, with psi's global phase fixed
    (the phase at the density maximum set to zero: steady states are stationary only up to a
    global phase rotation).
-4. :func:`evaluate` starts held-out members from the prediction -- psi from the network, n_R
-   from psi through the reservoir's own steady-state relation (:func:`reservoir_closure`) --
+4. :func:`evaluate` starts held-out members from the prediction -- psi from the network,
+   rescaled to the particle balance of a steady state (:func:`amplitude_balance`), n_R from psi
+   through the reservoir's own steady-state relation (:func:`reservoir_closure`) --
    runs the same solver to the same criterion and accepts a warm result only when it reached
    the criterion (the stationarity residual) and its steady density is within ``density_tol``
    (relative L2) of the plain-start result; otherwise the member falls back to the plain start
@@ -298,7 +299,7 @@ def density_error(psi_a, psi_b):
     return float(np.sqrt(np.sum((ra - rb) ** 2)) / max(np.sqrt(np.sum(rb ** 2)), 1e-30))
 
 
-def evaluate(ws, cfgs, plain, density_tol=1e-3, closure=True, balance=False):
+def evaluate(ws, cfgs, plain, density_tol=1e-3, closure=True, balance=True):
     """Warm-start the members of ``cfgs`` (whose plain-start result is ``plain``, from
     :func:`run_uniform`) and compare.  Only members whose plain run reached a lasing steady
     state enter the ratios (decayed members have no condensate to predict).  ``closure``: the
