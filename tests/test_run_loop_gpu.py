@@ -153,7 +153,6 @@ def test_host_decided_loop_waits_every_chunk(cuda_lib):
     """The same loop without the monitor: the drop-in copies the state in and out around every
     chunk, each a host wait the counter sees."""
     ctl = _controller("rk4-cuda", "single")
-    ctl.solver.pipeline_groups = 1  # one device solver, whose waits the counter reports
     counts = {}
     ctl.after_first_advance = lambda: counts.setdefault("start", ctl.solver.engine.sync_counts())
     ctl.run()
