@@ -449,8 +449,6 @@ def run_e2e(args, w, members, torch):
     model.reservoir.nR = pinned_n
     solver = RK4CudaSolver(cfg, grid, model)
     solver.inplace_host = True  # results land in the same pinned arrays every call
-    if args.e2e_groups is not None:
-        solver.pipeline_groups = args.e2e_groups
     chunk = 64
     solver.advance(model, state, chunk)  # warm-up: uploads pump/noise, captures graphs
 
@@ -1081,8 +1079,6 @@ def main():
     ap.add_argument("--members", type=int, default=32)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-calls", type=int, default=8)
-    ap.add_argument("--e2e-groups", type=int, default=None,
-                    help="member groups of the drop-in's host-array path (default: the solver's)")
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=1024,
