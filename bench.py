@@ -464,11 +464,8 @@ def run_e2e(args, w, members, torch):
             "h2d_bytes_per_step": per_call / chunk, "d2h_bytes_per_step": per_call / chunk,
             "h2d_bytes_per_call": per_call, "d2h_bytes_per_call": per_call,
             "step": f"{calls} RK4CudaSolver.advance calls of {chunk} RK4 steps each on pinned "
-                    "host state (bytes per step = bytes per call / steps per call); the members "
-                    f"step in {min(solver.pipeline_groups, members)} groups on their own streams, "
-                    "one group's copies overlapping the others' steps",
-            "calls": calls, "steps_per_call": chunk,
-            "member_groups": min(solver.pipeline_groups, members)}
+                    "host state (bytes per step = bytes per call / steps per call)",
+            "calls": calls, "steps_per_call": chunk}
 
 
 # ----------------------------------------------------------------------------- split-step leg
