@@ -69,9 +69,9 @@ class _GB300Solver(AbstractSolver):
         self._dt = float(config.solver.dt)
         self._engine = None
         self._engine_key = None
-        self._groups = None       # [(engine, (a, b))] of the pipelined host-array path
-        self._groups_key = None
-        self._pool = None
+        self._pump_key = None
+        self._noise_key = None
+        self._potential_key = None
         _lib.load()
 
     # ------------------------------------------------------------------ helpers
@@ -107,6 +107,7 @@ class _GB300Solver(AbstractSolver):
                                      reservoir_components=self._res_components,
                                      pump_terms=pump_terms)
             self._engine_key = key
+            self._pump_key = self._noise_key = self._potential_key = None
         return self._engine
 
     @staticmethod
@@ -122,24 +123,10 @@ class _GB300Solver(AbstractSolver):
                              "(envelope x coefficient(t) per laser)")
         return list(terms)
 
-    @staticmethod
-    def _member_slice(array, span):
-        """Members [a, b) of a per-member array (leading axis of length `total`, when several);
-        a shared array as it is."""
-        if span is None:
-            return array
-        a, b, total = span
-        return array[a:b] if total > 1 and np.ndim(array) >= 1 and np.shape(array)[0] == total \
-            else array
-
-    def _upload_inputs(self, engine, model, envelopes, potential, span=None):
-        """Pump envelopes, potential and noise parameters into `engine` when they changed
-        (by identity; the keys live on the engine).  `span` = (a, b, total): the engine steps
-        members [a, b) of `total`."""
-        keys = engine.__dict__.setdefault("_input_keys", {})
-        envs = [self._member_slice(np.asarray(_host(e)), span) for e in envelopes]
-        key = tuple((id(e), h.shape) for e, h in zip(envelopes, envs)) + (span,)
-        if keys.get("pump") != key:
+    def _upload_inputs(self, engine, model, envelopes, potential):
+        envs = [_host(e) for e in envelopes]
+        key = tuple((id(e), h.shape) for e, h in zip(envelopes, envs))
+        if self._pump_key != key:
             if len(envs) == 1:
                 env = np.ascontiguousarray(envs[0], dtype=engine.real)
             else:
@@ -151,25 +138,22 @@ class _GB300Solver(AbstractSolver):
                                                           else (engine.ny, engine.nx)), shape)
                     for h in envs]), dtype=engine.real)
             engine.set_pump(env)
-            keys["pump"] = key
+            self._pump_key = key
         if engine.potential_kind != _lib.PG_POT_NONE:
-            pkey = (id(potential), span)
-            if keys.get("potential") != pkey:
-                engine.set_potential(np.ascontiguousarray(self._member_slice(_host(potential), span)))
-                keys["potential"] = pkey
+            pkey = id(potential)
+            if self._potential_key != pkey:
+                engine.set_potential(np.ascontiguousarray(_host(potential)))
+                self._potential_key = pkey
         noise = model.noise
         active = bool(noise is not None and getattr(noise, "active", True))
-        nkey = (id(noise), active, span)
-        if keys.get("noise") != nkey:
+        nkey = (id(noise), active)
+        if self._noise_key != nkey:
             if active:
-                def part(v):
-                    v = np.asarray(v).reshape(-1)
-                    return v if span is None or v.size != span[2] else v[span[0]:span[1]]
-                engine.set_noise(part(noise.seeds), part(noise.gamma), part(noise.scattering),
-                                 part(noise.strength), noise.dt / (4.0 * noise.volume))
+                engine.set_noise(noise.seeds, noise.gamma, noise.scattering, noise.strength,
+                                 noise.dt / (4.0 * noise.volume))
             else:
                 engine.set_noise(None)
-            keys["noise"] = nkey
+            self._noise_key = nkey
 
     @staticmethod
     def _coefficient_row(coefficients, time, members):
@@ -354,106 +338,16 @@ class RK4CudaSolver(_GB300Solver):
         description="GB300 fused RK4 (one sm_103a kernel per step, stage-coupled reservoir, "
                     "Philox Wigner noise in registers).")
 
-    #: Host arrays of several members step in up to this many member groups, each on its own
-    #: device solver (its own stream) driven from its own host thread, so that one group's
-    #: host <-> device copies overlap the other groups' steps.  Members are independent, so
-    #: the results are bitwise those of one solver; 0 or 1 keeps one solver.
-    pipeline_groups = 4
-
     def __init__(self, config, grid, model):
         super().__init__(config, grid, model)
         if getattr(config.solver, "laplacian", "five-point") != "five-point":
             raise ValueError("rk4-cuda (GB300) implements the five-point Laplacian")
-
-    def _pipelined(self, field):
-        return (not self.resident and int(self.pipeline_groups or 0) > 1 and not _is_device(field)
-                and self._reservoir_type in ("single", "none") and int(field.shape[0]) >= 2)
-
-    def _ensure_groups(self, model, members, pump_envs, potential):
-        """One engine per member group (sizes differ by at most one member)."""
-        g = min(int(self.pipeline_groups), members)
-        edges = [round(i * members / g) for i in range(g + 1)]
-        bounds = [(a, b) for a, b in zip(edges[:-1], edges[1:]) if b > a]
-        pump_per_member = any(np.ndim(e) == 4 and e.shape[0] > 1 for e in pump_envs)
-        pot_kind, pot_per_member = _lib.PG_POT_NONE, False
-        if potential is not None and np.ndim(potential) > 0 and np.any(potential != 0):
-            pot_kind = _lib.PG_POT_COMPLEX if np.iscomplexobj(potential) else _lib.PG_POT_REAL
-            pot_per_member = np.ndim(potential) == 4 and potential.shape[0] > 1
-        key = (members, tuple(bounds), pump_per_member, pot_kind, pot_per_member, len(pump_envs))
-        if self._groups is None or self._groups_key != key:
-            self._close_groups()
-            physics = self._physics_list(members, model)
-            g = self._grid
-            self._groups = [
-                (RK4Engine(g.nx, g.ny, b - a, g.dx, g.dy, self._dt, physics[a:b], self._precision,
-                           reservoir=self._reservoir_type, potential=pot_kind,
-                           pump_per_member=pump_per_member and b - a > 1,
-                           potential_per_member=pot_per_member and b - a > 1,
-                           components=self._components, reservoir_components=self._res_components,
-                           pump_terms=len(pump_envs)), (a, b))
-                for a, b in bounds]
-            self._groups_key = key
-        return self._groups
-
-    def _close_groups(self):
-        for engine, _ in self._groups or []:
-            engine.close()
-        self._groups = None
-
-    def _advance_groups(self, model, state, field, n_steps):
-        """The host-array path over member groups (see pipeline_groups)."""
-        from concurrent.futures import ThreadPoolExecutor
-
-        members = int(field.shape[0])
-        terms = self._pump_terms(model.pump)
-        envelopes = [e for e, _ in terms]
-        coefficient = [c for _, c in terms]
-        potential = getattr(model, "potential", None)
-        groups = self._ensure_groups(model, members, [np.asarray(_host(e)) for e in envelopes],
-                                     None if potential is None else _host(potential))
-        for engine, (a, b) in groups:
-            self._upload_inputs(engine, model, envelopes, potential, (a, b, members))
-        real = groups[0][0].real
-        cplx = groups[0][0].complex
-        scales = self.stage_scales(coefficient, state.t0, state.step, n_steps, members)
-        res_in = model.reservoir.get_state()[0] if self._reservoir_type == "single" else None
-        psi_in = np.ascontiguousarray(field, dtype=cplx)
-        res_arr = None if res_in is None else np.ascontiguousarray(res_in, dtype=real)
-        inplace = (self.inplace_host and self._writable(field, cplx)
-                   and (res_in is None or self._writable(res_in, real)))
-        psi_out = field if inplace else np.empty_like(psi_in)
-        res_out = None if res_arr is None else (res_in if inplace else np.empty_like(res_arr))
-        use_graphs = bool(getattr(self.config.solver, "cuda_graphs", True))
-
-        def run(i):
-            engine, (a, b) = groups[i]
-            if res_arr is None:
-                engine.set_state(psi_in[a:b])
-            else:
-                engine.set_state(psi_in[a:b], res_arr[a:b])
-            engine.advance(state.step, n_steps, np.ascontiguousarray(scales[..., a:b]),
-                           use_graphs=use_graphs)
-            engine.get_state(psi_out[a:b], None if res_out is None else res_out[a:b])
-
-        if self._pool is None or self._pool._max_workers < len(groups):
-            self._pool = ThreadPoolExecutor(max_workers=len(groups))
-        list(self._pool.map(run, range(len(groups))))
-        state.field = psi_out
-        self._finish(model, state, res_out, n_steps)
 
     def advance(self, model, state, n_steps: int) -> None:
         if n_steps <= 0:
             return
         field = state.field
         self.batch_physics.check(field, 1)
-        # One path's device solvers at a time (each holds the whole state's memory).
-        if self._pipelined(field):
-            if self._engine is not None:
-                self._engine.close()
-                self._engine, self._engine_key, self._held = None, None, None
-            self._advance_groups(model, state, field, n_steps)
-            return
-        self._close_groups()
         engine, members, coefficient = self._prepare(model, state)
         if not self._holds(model, state, field):
             device, res_in = self._upload_state(engine, model, field)

@@ -170,28 +170,3 @@ def test_in_place_host_results_match_default_path(cuda_lib, solver_name):
         outs.append((state.field.copy(), model.reservoir.get_state()[0].copy()))
     assert np.array_equal(outs[0][0], outs[1][0])
     assert np.array_equal(outs[0][1], outs[1][1])
-
-
-@pytest.mark.parametrize("precision", ["single", "double"])
-def test_member_groups_give_the_one_solver_result_bitwise(cuda_lib, precision):
-    """Host arrays of five members: stepped in four member groups on their own solvers and
-    streams from host threads (the copies of one group overlapping another's steps), the
-    result is bitwise that of one solver, over two advance calls (step and time carried)."""
-    from polarism_gb300 import solvers
-    from polarism_gb300.host import build_simulation
-
-    cfg = _config(precision)
-    members = _members(cfg, 5)
-    outs = []
-    for groups in (1, 4):
-        grid, model, state = build_simulation(cfg, members)
-        solver = solvers.RK4CudaSolver(cfg, grid, model)
-        solver.pipeline_groups = groups
-        for n in (7, 6):
-            solver.advance(model, state, n)
-        assert (solver._groups is not None) == (groups > 1)
-        outs.append((np.array(state.field), np.array(model.reservoir.get_state()[0]), state.step,
-                     state.t))
-    assert np.array_equal(outs[0][0].view(np.uint8), outs[1][0].view(np.uint8))
-    assert np.array_equal(outs[0][1].view(np.uint8), outs[1][1].view(np.uint8))
-    assert outs[0][2:] == outs[1][2:] == (13, outs[0][3])
