@@ -305,6 +305,19 @@ void set_taus(IfrkRowArgs& r, const StepTables& st) {
   }
 }
 
+// A row pass: the register-resident four-step form for FP32 one-component rows of 1024 sites,
+// the generic Stockham pass otherwise.
+template <typename T>
+cudaError_t ifrk_row(pg_solver* s, const T* in, T* save, T* out, const T* tables,
+                     const IfrkRowArgs& a, const T* tw) {
+  if constexpr (sizeof(T) == 4) {
+    if (s->tw4 != nullptr && ifrk_fast_row(a))
+      return launch_ifrk_row_fast(in, save, out, tables, static_cast<const float*>(s->tw4), a,
+                                  s->stream);
+  }
+  return launch_ifrk_row<T>(in, save, out, tables, a, tw, s->stream);
+}
+
 template <typename T>
 int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& st, double h,
              int scale_base, int step_offset, bool noise, bool adaptive, double rtol, double atol,
@@ -349,7 +362,7 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
     }
     T* save = static_cast<T*>(i == 0 ? b.psi0_hat : b.fhat[i - 1]);
     set_taus(r, st);
-    PG_CUDA(launch_ifrk_row<T>(W, save, W, tables, r, tw_x, s->stream));
+    PG_CUDA(ifrk_row<T>(s, W, save, W, tables, r, tw_x));
     IfrkColArgs a = p.col;
     a.mode = 0;
     a.inverse = 1;
@@ -386,8 +399,7 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
       ++r.terms;
     }
     set_taus(r, st);
-    PG_CUDA(launch_ifrk_row<T>(W, static_cast<T*>(b.fhat[tb.stages - 1]), W, tables, r, tw_x,
-                               s->stream));
+    PG_CUDA(ifrk_row<T>(s, W, static_cast<T*>(b.fhat[tb.stages - 1]), W, tables, r, tw_x));
     IfrkColArgs a = p.col;
     a.mode = 1;
     a.inverse = 1;
@@ -421,7 +433,8 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
       ++r.terms;
     }
     set_taus(r, st);
-    PG_CUDA(launch_ifrk_row<T>(nullptr, nullptr, static_cast<T*>(b.ehat), tables, r, tw_x, s->stream));
+    PG_CUDA(ifrk_row<T>(s, static_cast<const T*>(nullptr), static_cast<T*>(nullptr),
+                        static_cast<T*>(b.ehat), tables, r, tw_x));
     IfrkColArgs a = p.col;
     a.mode = 2;
     a.inverse = 1;

@@ -19,6 +19,7 @@
 // do: rounded factors alone carry a per-step amplitude bias that drifts the norm over long runs.
 #include <cmath>
 
+#include "ifrk_internal.h"
 #include "split_local.cuh"
 
 namespace pg {
@@ -181,6 +182,83 @@ __global__ void __launch_bounds__(kRowWarps * 32, 2)
   }
 }
 
+// ------------------------------------------------------------------ IFRK row pass
+// ifrk_row_kernel (ifrk.cu) for FP32 rows of 1024 sites of a one-component field: the row's
+// forward transform, the stage spectrum saved, the Lawson combination
+// sum_t coef_t Ex_t[kx] Ey_t[ky] src_t (src_t: this row's spectrum, or a stored one), the
+// inverse transform; a warp per row, as row_fast_kernel.
+__global__ void __launch_bounds__(kRowWarps * 32, 2)
+    ifrk_row_fast_kernel(const float2* __restrict__ in, float2* __restrict__ save,
+                         float2* __restrict__ out, const float2* __restrict__ tables,
+                         const float4* __restrict__ tw4_g, const IfrkRowArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* tw4 = reinterpret_cast<float4*>(smem_raw);                     // [32][32]
+  float2* xb = reinterpret_cast<float2*>(tw4 + kN);                      // [warps][32][33]
+  for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int member = blockIdx.z;
+  float2* buf = xb + warp * 32 * kXStride;
+  const long long table_stride = static_cast<long long>(a.members) * (kN + a.ny);
+#pragma unroll 1
+  for (int q = 0; q < kRowsPerWarp; ++q) {
+    const int row = (blockIdx.x * kRowWarps + warp) * kRowsPerWarp + q;
+    const long long moff = member * a.member_stride + static_cast<long long>(row) * kN;
+    float2 v[32];
+#pragma unroll
+    for (int t = 0; t < 32; ++t) v[t] = in ? in[moff + lane + 32 * t] : make_float2(0.f, 0.f);
+    // Phase 0: forward transform, save, combination; phase 1: the inverse transform (conj32).
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ++ph) {
+      if (ph == 0 ? a.forward : a.inverse) {
+        if (ph == 1) conj32(v);
+        fft1024_warp(v, lane, buf, tw4);
+        if (ph == 1) conj32(v);
+      }
+      if (ph == 1) continue;
+      if (save) {
+#pragma unroll
+        for (int r = 0; r < 32; ++r) save[moff + lane + 32 * r] = v[r];
+      }
+      // The term on this row's own spectrum (src null; at most one) first, in place, then the
+      // stored spectra, a term at a time so that the row stays the only array in registers.
+      int own = -1;
+      for (int s = 0; s < a.terms; ++s)
+        if (a.src[s] == nullptr) own = s;
+      const float2* tabs = tables + static_cast<long long>(member) * (kN + a.ny);
+      if (own >= 0) {
+        const float2* tab = tabs + a.table[own] * table_stride;
+        const float2 ey = tab[kN + row];
+        const float c = static_cast<float>(a.coef[own]);
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+          const float2 ev = cmul(cmul(tab[lane + 32 * r], ey), v[r]);
+          v[r] = make_float2(c * ev.x, c * ev.y);
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < 32; ++r) v[r] = make_float2(0.f, 0.f);
+      }
+#pragma unroll 1
+      for (int s = 0; s < a.terms; ++s) {
+        if (s == own) continue;
+        const float2* tab = tabs + a.table[s] * table_stride;
+        const float2* src = static_cast<const float2*>(a.src[s]) + moff;
+        const float2 ey = tab[kN + row];
+        const float c = static_cast<float>(a.coef[s]);
+#pragma unroll
+        for (int r = 0; r < 32; ++r) {
+          const float2 ev = cmul(cmul(tab[lane + 32 * r], ey), src[lane + 32 * r]);
+          v[r].x += c * ev.x;
+          v[r].y += c * ev.y;
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 32; ++t) out[moff + lane + 32 * t] = v[t];
+  }
+}
+
 // ------------------------------------------------------------------ column pass
 // A forward 1024-point transform of the block's eight columns (thread = (column c, n2 = p));
 // pan is the panel's exchange buffer ([c][k1][n2], columns kPanelStride apart).
@@ -302,6 +380,9 @@ cudaError_t configure_split_fast() {
   cudaError_t e = cudaFuncSetAttribute(row_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(row_fast_smem()));
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(ifrk_row_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(row_fast_smem()));
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(col_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(col_fast_smem()));
 }
@@ -312,6 +393,20 @@ cudaError_t launch_row_fast(float* data, const float* tw4, const float* px, cons
   row_fast_kernel<<<grid, kRowWarps * 32, row_fast_smem(), stream>>>(
       reinterpret_cast<float2*>(data), reinterpret_cast<const float4*>(tw4),
       reinterpret_cast<const float2*>(px), reinterpret_cast<const float2*>(py), a);
+  return cudaGetLastError();
+}
+
+bool ifrk_fast_row(const IfrkRowArgs& a) {
+  return a.comps == 1 && !a.spinor && a.nx == kN && a.ny % (kRowWarps * kRowsPerWarp) == 0;
+}
+
+cudaError_t launch_ifrk_row_fast(const float* in, float* save, float* out, const float* tables,
+                                 const float* tw4, const IfrkRowArgs& a, cudaStream_t stream) {
+  const dim3 grid(a.ny / (kRowWarps * kRowsPerWarp), 1, a.members);
+  ifrk_row_fast_kernel<<<grid, kRowWarps * 32, row_fast_smem(), stream>>>(
+      reinterpret_cast<const float2*>(in), reinterpret_cast<float2*>(save),
+      reinterpret_cast<float2*>(out), reinterpret_cast<const float2*>(tables),
+      reinterpret_cast<const float4*>(tw4), a);
   return cudaGetLastError();
 }
 

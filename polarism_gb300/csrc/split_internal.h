@@ -93,6 +93,13 @@ cudaError_t launch_col_fast(float* data, float* res, const float* pump, const fl
                             const unsigned long long* step_base, const ColPassArgs& a,
                             cudaStream_t stream);
 
+// The IFRK row pass on the same transforms (FP32, one component, rows of 1024 sites): whether
+// it applies and its launch (arguments as launch_ifrk_row; tw4 as above).
+struct IfrkRowArgs;
+bool ifrk_fast_row(const IfrkRowArgs& a);
+cudaError_t launch_ifrk_row_fast(const float* in, float* save, float* out, const float* tables,
+                                 const float* tw4, const IfrkRowArgs& a, cudaStream_t stream);
+
 // Complex values one thread stages per FFT pass: blocks need N * C <= this * threads.
 int split_max_vals(bool is_double);
 

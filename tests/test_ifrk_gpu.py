@@ -70,11 +70,13 @@ def test_ifrk4_matches_reference_trajectory(cuda_lib, precision, tol):
 
 @pytest.mark.parametrize("tableau", ["rk4", "dp5"])
 @pytest.mark.parametrize("precision,tol", [("double", 1e-10), ("single", 1e-4)])
-def test_fixed_step_with_noise_and_members(cuda_lib, tableau, precision, tol):
-    """Fixed-step IFRK with the Wigner increment after each step, three members."""
+@pytest.mark.parametrize("ny,nx", [(16, 32), (32, 1024)])
+def test_fixed_step_with_noise_and_members(cuda_lib, tableau, precision, tol, ny, nx):
+    """Fixed-step IFRK with the Wigner increment after each step, three members; FP32 rows of
+    1024 sites run the register-resident four-step row pass."""
     from polarism_gb300.engine import TABLEAU_NODES, Engine, MemberPhysics
 
-    ny, nx, members = 16, 32, 3
+    members = 3
     dx, dy, dt = 1.1, 0.9, 0.01
     rng = np.random.default_rng(21)
     psi0 = 0.1 * (rng.standard_normal((members, 1, ny, nx)) + 1j * rng.standard_normal((members, 1, ny, nx)))
@@ -107,6 +109,29 @@ def test_fixed_step_with_noise_and_members(cuda_lib, tableau, precision, tol):
             state.psi, state.psi_k = field, None
         assert rel_l2(psi[m], state.psi[0]) < tol, m
         assert rel_l2(res[m], state.fields[0][0]) < tol, m
+
+
+def test_dp5_trial_error_norm_on_the_1024_row_pass(cuda_lib):
+    """The adaptive trial's error estimate (a row pass over stored stage spectra only) on FP32
+    rows of 1024 sites against the FP64 engine's: the error norm within 1e-3 and, away from
+    the threshold, the same accept decision."""
+    from polarism_gb300.engine import Engine, MemberPhysics
+
+    ny, nx, dx, dy = 32, 1024, 0.4, 0.4
+    rng = np.random.default_rng(8)
+    psi0 = 0.2 * (rng.standard_normal((1, 1, ny, nx)) + 1j * rng.standard_normal((1, 1, ny, nx)))
+    res0 = np.abs(rng.standard_normal((1, 1, ny, nx))) * 0.05
+    env = np.exp(-0.5 * (((np.arange(nx) - nx / 2) * dx) ** 2)[None, :] / 400.0)
+    errs = {}
+    for precision in ("double", "single"):
+        eng = Engine(nx, ny, 1, dx, dy, 0.01, MemberPhysics(**P), precision)
+        eng.set_pump(np.broadcast_to(env, (ny, nx)).astype(eng.real))
+        eng.set_state(psi0.astype(eng.complex), res0.astype(eng.real))
+        errs[precision] = eng.ifrk_trial(0.02, np.full((7, 1), 0.2), 1e-6, 1e-8)
+        eng.close()
+    assert abs(errs["single"][0] - errs["double"][0]) <= 1e-3 * errs["double"][0]
+    if abs(errs["double"][0] - 1.0) > 1e-2:
+        assert errs["single"][1] == errs["double"][1]
 
 
 def test_dp5_adaptive_matches_reference_run(cuda_lib):
