@@ -276,3 +276,28 @@ def test_device_monitor_copies_the_state_back_for_accumulators_and_events(monito
     assert ad.samples == ah.samples > 0
     for x, y in zip(ad.results(), ah.results()):
         np.testing.assert_array_equal(np.asarray(x.value), np.asarray(y.value))
+
+
+def test_device_monitor_continues_a_run_from_the_controllers_steady_reference(monitored):
+    """A second run() that continues the first (total_time raised): the monitor starts from the
+    density and stop times the controller kept, as the reference's own check continues from
+    _steady_density, so both ways stop every member on the same steps."""
+    from polarism_gb300.run_loop import DeviceSteadyMonitor
+
+    results = {}
+    for mode in ("host", "device"):
+        ctl = _controller("rk4-cuda", steps=60, rtol=0.18)
+        monitor = DeviceSteadyMonitor(ctl).install() if mode == "device" else None
+        ctl.run()                                  # 60 steps: the zero member stops at 0.1 ps
+        first = ctl.stop_times.copy()
+        ctl.cfg.solver.total_time = 2e-3 * 400
+        ctl.run()                                  # continues from step 60
+        results[mode] = (first, ctl.stop_times.copy(), ctl.state.step, np.array(ctl.state.field))
+        if monitor is not None:
+            monitor.uninstall()
+    (h1, h2, hs, hf), (d1, d2, ds, df) = results["host"], results["device"]
+    np.testing.assert_array_equal(d1, h1)
+    assert np.isfinite(h1).sum() == 1 and np.isfinite(h2).all()
+    np.testing.assert_array_equal(d2, h2)
+    assert ds == hs < 400
+    np.testing.assert_array_equal(df, hf)
