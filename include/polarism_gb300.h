@@ -181,6 +181,10 @@ int pg_ifrk_trial(pg_solver* s, int32_t tableau, double h, const double* stage_s
 int pg_accumulate(pg_solver* s, int32_t kinds);
 int pg_accumulator_sums(pg_solver* s, int32_t kind, double* out, int64_t* samples);
 int pg_accumulator_reset(pg_solver* s);
+/* Zero the observable sums and their sample counts, stream ordered (no host wait; the
+ * steady-state monitor is left alone).  Samples queued while the solver's halt word is set
+ * (after the steady-state check that stopped every member) add nothing. */
+int pg_accumulator_zero(pg_solver* s);
 /* Restore one accumulator (kind as pg_accumulator_sums) and its sample count, as
  * Accumulator.load_state_dict does on a checkpoint resume (polarism/results/accumulators.py:
  * 83-87,117-119,155-158). */

@@ -77,6 +77,7 @@ SIGNATURES = {
     "pg_accumulate": (C.c_int, [_vp, _i32]),
     "pg_accumulator_sums": (C.c_int, [_vp, _i32, _vp, C.POINTER(_i64)]),
     "pg_accumulator_reset": (C.c_int, [_vp]),
+    "pg_accumulator_zero": (C.c_int, [_vp]),
     "pg_norms": (C.c_int, [_vp, _vp]),
     "pg_steady_check": (C.c_int, [_vp, _vp, _vp, _vp]),
     "pg_steady_update": (C.c_int, [_vp, C.c_int64, C.c_int32, C.c_double, C.c_int32]),

@@ -32,7 +32,8 @@ namespace {
 template <typename T>
 __global__ void density_moments_kernel(const typename C2T<T>::type* __restrict__ psi,
                                        double* __restrict__ sum_rho, double* __restrict__ sum_rho2,
-                                       long long n) {
+                                       long long n, const int* __restrict__ halt) {
+  if (halt != nullptr && __ldcg(halt) != 0) return;  // a sample after the run halted: none
   for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
        e += static_cast<long long>(gridDim.x) * blockDim.x) {
     const auto v = psi[e];
@@ -49,9 +50,10 @@ __global__ void __launch_bounds__(1024) spectrum_power_row_kernel(const typename
                                                                   const typename C2T<T>::type* __restrict__ tw,
                                                                   double* __restrict__ sum_k, int nx,
                                                                   int ny, int log2nx, int rows,
-                                                                  int log2rows) {
+                                                                  int log2rows, const int* __restrict__ halt) {
   using C2 = typename C2T<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (halt != nullptr && __ldcg(halt) != 0) return;  // a sample after the run halted: none
   C2* tws = reinterpret_cast<C2*>(smem_raw);
   C2* buf = tws + nx;
   const int member = blockIdx.z;
@@ -231,10 +233,10 @@ int pg_accumulate(pg_solver* s, int32_t kinds) {
     const int blocks = static_cast<int>(std::min<long long>(4096, (values + 255) / 256));
     if (dbl)
       pg::density_moments_kernel<double><<<blocks, 256, 0, s->stream>>>(
-          static_cast<const double2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, values);
+          static_cast<const double2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, values, s->halt);
     else
       pg::density_moments_kernel<float><<<blocks, 256, 0, s->stream>>>(
-          static_cast<const float2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, values);
+          static_cast<const float2*>(s->psi[s->cur]), a.sum_rho, a.sum_rho2, values, s->halt);
     PG_CUDA(cudaGetLastError());
     a.samples_rho += 1;
   }
@@ -293,13 +295,13 @@ int pg_accumulate(pg_solver* s, int32_t kinds) {
                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
       pg::spectrum_power_row_kernel<double><<<dim3(ny / rows, 1, planes), threads, smem, s->stream>>>(
           static_cast<const double2*>(a.half), static_cast<const double2*>(s->tw_x), a.sum_k, nx, ny,
-          ilog2(nx), rows, ilog2(rows));
+          ilog2(nx), rows, ilog2(rows), s->halt);
     } else {
       cudaFuncSetAttribute(pg::spectrum_power_row_kernel<float>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
       pg::spectrum_power_row_kernel<float><<<dim3(ny / rows, 1, planes), threads, smem, s->stream>>>(
           static_cast<const float2*>(a.half), static_cast<const float2*>(s->tw_x), a.sum_k, nx, ny,
-          ilog2(nx), rows, ilog2(rows));
+          ilog2(nx), rows, ilog2(rows), s->halt);
     }
     PG_CUDA(cudaGetLastError());
     a.samples_k += 1;
@@ -387,6 +389,18 @@ int pg_steady_import(pg_solver* s, const void* density, const double* norms,
   }
   if (stop_steps)
     PG_CUDA(cudaMemcpy(a.mon.stop_step, stop_steps, sizeof(long long) * m, cudaMemcpyHostToDevice));
+  return PG_OK;
+}
+
+int pg_accumulator_zero(pg_solver* s) {
+  PG_CHECK(s, PG_ERR_INVALID, "pg_accumulator_zero: null solver");
+  if (!s->accum) return PG_OK;
+  pg::AccumBuffers& a = pg::acc(s);
+  const size_t bytes = static_cast<size_t>(s->field_values) * sizeof(double);
+  if (a.sum_rho) PG_CUDA(cudaMemsetAsync(a.sum_rho, 0, bytes, s->stream));
+  if (a.sum_rho2) PG_CUDA(cudaMemsetAsync(a.sum_rho2, 0, bytes, s->stream));
+  if (a.sum_k) PG_CUDA(cudaMemsetAsync(a.sum_k, 0, bytes, s->stream));
+  a.samples_rho = a.samples_k = 0;
   return PG_OK;
 }
 

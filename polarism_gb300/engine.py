@@ -327,6 +327,10 @@ class RK4Engine:
     def accumulator_reset(self):
         _lib.check(self.lib.pg_accumulator_reset(self.handle), "pg_accumulator_reset")
 
+    def accumulator_zero(self):
+        """Zero the sums without a host wait and without touching the steady-state monitor."""
+        _lib.check(self.lib.pg_accumulator_zero(self.handle), "pg_accumulator_zero")
+
     def accumulator_load(self, kind, sums, samples):
         """Restore one accumulator (kind "rho", "rho2" or "k") and its sample count."""
         index = {"rho": 0, "rho2": 1, "k": 2}[kind]

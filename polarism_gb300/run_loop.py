@@ -21,8 +21,11 @@ steps do:
   it, the monitor waits once, fills ``controller.stop_times``, and puts the state of the
   deciding check back into the controller's state with that check's ``step`` and ``t``: the
   loop then ends where the reference's ends;
+* the controller's ``g2`` and ``momentum-distribution`` accumulators sum on the device
+  (``pg_accumulate``, FP64, queued behind the chunk like the checks; samples queued after the
+  halting check add nothing) and receive the sums and sample counts when the run settles;
 * whatever else of the controller reads the state (result recording, event views, checkpoints,
-  accumulator updates) first copies the device state back.
+  other accumulators) first copies the device state back.
 
 A run that ends before every member has stopped settles at its last step, before ``run``
 prints and stores the stop times.  A run ended by a signal settles when ``run`` returns.
@@ -50,6 +53,10 @@ class DeviceSteadyMonitor:
 
     #: Controller methods that read the state and therefore copy the device state back first.
     READERS = ("_record_results", "_event_view", "save_checkpoint")
+    #: Accumulators (``polarism/results/accumulators.py``) whose sums the library forms on the
+    #: device: name -> the sums they hold.
+    DEVICE_ACCUMULATORS = {"g2": ("sum_density", "sum_density_squared"),
+                           "momentum-distribution": ("sum_k",)}
 
     def __init__(self, controller, poll_every: int = 1):
         solver = controller.solver
@@ -70,6 +77,9 @@ class DeviceSteadyMonitor:
         self._n_steps = 0
         self._interval = 0
         self._accumulator_updates = []
+        self._device_accumulators = {}   # name -> accumulator summed on the device
+        self._samples = {}               # name -> [(step, t)] of the samples queued this run
+        self._zeroed = False
 
     # ------------------------------------------------------------------ installation
     def install(self):
@@ -153,11 +163,21 @@ class DeviceSteadyMonitor:
         self._settled = False
         self._halted = False
         self.checks = 0
-        # Accumulators read the state after the advances they follow.
+        # Accumulators read the state after the advances they follow: g2 and the momentum
+        # distribution (one of each) sum on the device, the others see the copied-back state.
+        self._device_accumulators = {}
+        self._samples = {}
+        self._zeroed = False
         for accumulator in getattr(ctl, "_accumulators", {}).values():
             update = accumulator.update
             self._accumulator_updates.append((accumulator, "update" in vars(accumulator), update))
-            accumulator.update = self._flushing(update)
+            name = getattr(accumulator, "name", "")
+            if name in self.DEVICE_ACCUMULATORS and name not in self._device_accumulators:
+                self._device_accumulators[name] = accumulator
+                self._samples[name] = []
+                accumulator.update = self._device_update(name, update)
+            else:
+                accumulator.update = self._flushing(update)
 
     def _end(self):
         for accumulator, had, update in self._accumulator_updates:
@@ -166,6 +186,43 @@ class DeviceSteadyMonitor:
             else:
                 del accumulator.update
         self._accumulator_updates.clear()
+
+    def _device_update(self, name, host_update):
+        """An accumulator sample queued on the device (before any chunk there is no device
+        state yet: that sample is taken on the host, as the reference takes it)."""
+        def update(state, t):
+            engine = self.solver.engine
+            if engine is None or not self.solver._stale and self.solver._held is None:
+                return host_update(state, t)
+            if not self._zeroed:
+                engine.accumulator_zero()
+                self._zeroed = True
+            engine.accumulate(density=name == "g2", momentum=name == "momentum-distribution")
+            self._samples[name].append((int(state.step), t))
+        return update
+
+    def _finish_accumulators(self, halt_step):
+        """Add the device sums and the samples taken up to the halting check (all, without a
+        halt) to each device-summed accumulator (one wait)."""
+        if not self._zeroed:
+            return
+        engine = self.solver.engine
+        kinds = {"sum_density": "rho", "sum_density_squared": "rho2", "sum_k": "k"}
+        for name, accumulator in self._device_accumulators.items():
+            taken = [(s, t) for s, t in self._samples[name] if halt_step is None or s <= halt_step]
+            if not taken:
+                continue
+            values = dict(accumulator.state_dict())
+            for key in self.DEVICE_ACCUMULATORS[name]:
+                sums, _ = engine.accumulator_sums(kinds[key])
+                host = _to_host(values[key])
+                values[key] = host + sums.reshape(np.shape(host))
+            if not values["samples"]:
+                values["t_first"] = taken[0][1]
+            values["samples"] = int(values["samples"]) + len(taken)
+            values["t_last"] = taken[-1][1]
+            accumulator.load_state_dict(values)
+        self._zeroed = False
 
     # ------------------------------------------------------------------ the check
     def _start(self, engine):
@@ -231,6 +288,7 @@ class DeviceSteadyMonitor:
         the state back to the deciding check."""
         if self._settled or not self._started:
             if not self._started:
+                self._finish_accumulators(None)
                 self.solver.flush(self.controller.model, self.controller.state)
             return
         self._settle_halted_or_final(self._collect())
@@ -240,6 +298,7 @@ class DeviceSteadyMonitor:
         state = ctl.state
         engine = self.solver.engine
         self.settles += 1
+        self._finish_accumulators(halt_step)
         if halt_step is not None:
             state.step = int(halt_step)
             state.t = state.t0 + state.step * float(ctl.cfg.solver.dt)

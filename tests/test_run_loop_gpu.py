@@ -31,8 +31,10 @@ class LoopController:
     ``solver``, ``stop_times``, the ``_steady_*`` attributes, ``_check_steady_state`` and
     ``run``.  ``after_first_advance`` is called once, after the first chunk."""
 
-    def __init__(self, cfg, grid, model, state, solver):
+    def __init__(self, cfg, grid, model, state, solver, accumulate_every=0):
         self.cfg, self.grid, self.model, self.state, self.solver = cfg, grid, model, state, solver
+        self.accumulate_every = accumulate_every  # steps between g2 samples (0: none)
+        self._accumulators = {"g2": G2Sums(state)} if accumulate_every else {}
         self.stop_times = np.full(state.batch_size, np.nan)
         self._steady_density = None
         self._steady_norm = None
@@ -62,18 +64,54 @@ class LoopController:
         interval = round(self.cfg.stop.check_every / dt)
         step = self.state.step
         first = True
+        every = self.accumulate_every
         while step < n_steps and not np.isfinite(self.stop_times).all():
             end = min(n_steps, (step // interval + 1) * interval)
+            if every:
+                end = min(end, (step // every + 1) * every)
             self.solver.advance(self.model, self.state, end - step)
             if first and self.after_first_advance is not None:
                 self.after_first_advance()
             first = False
             step = self.state.step
+            if every and step % every == 0:
+                self._accumulators["g2"].update(self.state, self.state.t)
             if step % interval == 0 and self._steady_last_step != step:
                 self._check_steady_state()
 
 
-def _controller(method, precision):
+class G2Sums:
+    """The reference's G2Accumulator sums (``polarism/results/accumulators.py:134-160``):
+    per-site FP64 sums of |psi|^2 and |psi|^4 with the sample count and times."""
+
+    name = "g2"
+
+    def __init__(self, state):
+        self.sum_density = np.zeros(state.psi.shape)
+        self.sum_density_squared = np.zeros(state.psi.shape)
+        self.samples, self.t_first, self.t_last = 0, None, None
+
+    def update(self, state, t):
+        re, im = state.psi.real.astype(np.float64), state.psi.imag.astype(np.float64)
+        density = re * re + im * im
+        self.sum_density += density
+        self.sum_density_squared += density * density
+        if self.samples == 0:
+            self.t_first = t
+        self.t_last = t
+        self.samples += 1
+
+    def state_dict(self):
+        return {"samples": self.samples, "t_first": self.t_first, "t_last": self.t_last,
+                "sum_density": self.sum_density, "sum_density_squared": self.sum_density_squared}
+
+    def load_state_dict(self, values):
+        self.samples, self.t_first, self.t_last = values["samples"], values["t_first"], values["t_last"]
+        self.sum_density = np.asarray(values["sum_density"], dtype=np.float64)
+        self.sum_density_squared = np.asarray(values["sum_density_squared"], dtype=np.float64)
+
+
+def _controller(method, precision, accumulate_every=0):
     from polarism_gb300 import solvers
     from polarism_gb300.host import Config, build_simulation
 
@@ -102,7 +140,7 @@ def _controller(method, precision):
     model.reservoir.set_state((np.full_like(n0, 4.0),))
     cls = {"rk4-cuda": solvers.RK4CudaSolver, "split-step-fft": solvers.SplitStepFFTSolver}[method]
     solver = cls(cfg, grid, model)
-    return LoopController(cfg, grid, model, state, solver)
+    return LoopController(cfg, grid, model, state, solver, accumulate_every)
 
 
 @pytest.mark.parametrize("precision", ["single", "double"])
@@ -159,3 +197,35 @@ def test_host_decided_loop_waits_every_chunk(cuda_lib):
     chunks = ctl.state.step // INTERVAL
     syncs = ctl.solver.engine.sync_counts()[0] - counts["start"][0]
     assert syncs >= 2 * (chunks - 1)
+
+
+@pytest.mark.parametrize("precision", ["single", "double"])
+def test_device_accumulator_in_the_run_loop(cuda_lib, precision):
+    """A g2 accumulator sampled every 50 steps: summed on the device under the monitor (no host
+    wait while chunks, checks and samples are queued; samples after the halting check add
+    nothing), it ends with the host loop's sample count, times and bitwise-equal sums."""
+    from polarism_gb300.run_loop import DeviceSteadyMonitor
+
+    host = _controller("rk4-cuda", precision, accumulate_every=50)
+    host.run()
+    dev = _controller("rk4-cuda", precision, accumulate_every=50)
+    monitor = DeviceSteadyMonitor(dev).install()
+    counts = {}
+    dev.after_first_advance = lambda: counts.setdefault("start", dev.solver.engine.sync_counts())
+    settle = monitor.settle
+
+    def settle_counted():
+        counts.setdefault("settle", dev.solver.engine.sync_counts())
+        settle()
+
+    monitor.settle = settle_counted
+    dev.run()
+    assert counts["settle"][0] == counts["start"][0]
+    np.testing.assert_array_equal(dev.stop_times, host.stop_times)
+    assert dev.state.step == host.state.step
+    h, d = host._accumulators["g2"].state_dict(), dev._accumulators["g2"].state_dict()
+    assert (d["samples"], d["t_first"], d["t_last"]) == (h["samples"], h["t_first"], h["t_last"])
+    assert h["samples"] >= 10
+    assert np.array_equal(d["sum_density"], h["sum_density"])
+    assert np.array_equal(d["sum_density_squared"], h["sum_density_squared"])
+    monitor.uninstall()

@@ -22,7 +22,7 @@ import pytest
 from tests.test_reference_driver_host import RecordingEngine, reference  # noqa: F401
 
 SYNCING = ("set_state", "get_state", "steady_results", "steady_export", "steady_import",
-           "steady_reset", "synchronize")
+           "steady_reset", "synchronize", "accumulator_sums")
 
 
 class MonitoringEngine(RecordingEngine):
@@ -121,6 +121,26 @@ class MonitoringEngine(RecordingEngine):
         halt = self.halt_step
         self.halted = False
         return rd, rn, nm, self.stop_step.copy(), halt
+
+    # FP64 observable sums (pg_accumulate, pg_accumulator_zero, pg_accumulator_sums) --------
+    def accumulator_zero(self):
+        shape = (self.members, 1, self.ny, self.nx)
+        self.sums = {"rho": np.zeros(shape), "rho2": np.zeros(shape), "k": np.zeros(shape)}
+
+    def accumulate(self, density=True, momentum=False):
+        if self.halted:  # the accumulation kernels return at once after the halt
+            return
+        if density:
+            rho = self.psi.real.astype(np.float64) ** 2 + self.psi.imag.astype(np.float64) ** 2
+            self.sums["rho"] += rho
+            self.sums["rho2"] += rho * rho
+        if momentum:
+            fk = np.fft.fftn(self.psi, axes=(-2, -1))
+            self.sums["k"] += fk.real.astype(np.float64) ** 2 + fk.imag.astype(np.float64) ** 2
+
+    def accumulator_sums(self, kind):
+        self._sync("accumulator_sums")
+        return self.sums[kind].copy(), 0
 
     def steady_export(self):
         self._sync("steady_export")
@@ -301,3 +321,35 @@ def test_device_monitor_continues_a_run_from_the_controllers_steady_reference(mo
     np.testing.assert_array_equal(d2, h2)
     assert ds == hs < 400
     np.testing.assert_array_equal(df, hf)
+
+
+def test_device_accumulators_match_the_reference_accumulators(monitored):
+    """g2 (from t = 0: its first sample is taken on the host before any chunk) and the
+    momentum distribution summed on the device under the monitor, with the steady-state stop
+    halting the run (and, in the lagging case, samples queued past the halt): the same sample
+    counts, first and last times and sums as the reference's own accumulators."""
+    from polarism.results.accumulators import G2Accumulator, MomentumDistribution
+
+    from polarism_gb300.run_loop import run_with_device_monitor
+
+    out = {}
+    for mode in ("host", "device"):
+        ctl = _controller("rk4-cuda", rtol=0.18)
+        ctl._accumulators = {"g2": G2Accumulator(ctl, start=0.0, every=0.02),
+                             "momentum-distribution": MomentumDistribution(ctl, start=0.04,
+                                                                           every=0.04)}
+        if mode == "host":
+            ctl.run()
+        else:
+            monitor = run_with_device_monitor(ctl)
+            assert set(monitor._device_accumulators) == {"g2", "momentum-distribution"}
+        out[mode] = ctl
+    h, d = out["host"], out["device"]
+    assert d.state.step == h.state.step < 400
+    for name in ("g2", "momentum-distribution"):
+        sh, sd = h._accumulators[name].state_dict(), d._accumulators[name].state_dict()
+        assert (sd["samples"], sd["t_first"], sd["t_last"]) == (sh["samples"], sh["t_first"],
+                                                                  sh["t_last"]), name
+        for key in sh:
+            if key.startswith("sum"):
+                np.testing.assert_allclose(sd[key], sh[key], rtol=1e-12, atol=0)
