@@ -38,9 +38,11 @@ __global__ void density_moments_kernel(const typename C2T<T>::type* __restrict__
        e += static_cast<long long>(gridDim.x) * blockDim.x) {
     const auto v = psi[e];
     const double re = static_cast<double>(v.x), im = static_cast<double>(v.y);
-    const double rho = re * re + im * im;
-    sum_rho[e] += rho;
-    sum_rho2[e] += rho * rho;
+    // Rounded as the reference's NumPy sums are: each product and each sum on its own (no
+    // fused multiply-add), so FP64 sums of an FP32 or FP64 field are bitwise the reference's.
+    const double rho = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+    sum_rho[e] = __dadd_rn(sum_rho[e], rho);
+    sum_rho2[e] = __dadd_rn(sum_rho2[e], __dmul_rn(rho, rho));
   }
 }
 
@@ -65,7 +67,7 @@ __global__ void __launch_bounds__(1024) spectrum_power_row_kernel(const typename
   smem_fft<T, false, false>(buf, tws, log2nx, log2rows, 1, nx);
   for (int e = threadIdx.x; e < count; e += blockDim.x) {
     const double re = static_cast<double>(buf[e].x), im = static_cast<double>(buf[e].y);
-    sum_k[off + e] += re * re + im * im;
+    sum_k[off + e] = __dadd_rn(sum_k[off + e], __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
   }
 }
 
