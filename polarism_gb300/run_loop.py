@@ -79,6 +79,7 @@ class DeviceSteadyMonitor:
         self._accumulator_updates = []
         self._device_accumulators = {}   # name -> accumulator summed on the device
         self._samples = {}               # name -> [(step, t)] of the samples queued this run
+        self._before = {}                # name -> (samples, t_first, t_last) before them
         self._zeroed = False
 
     # ------------------------------------------------------------------ installation
@@ -167,25 +168,41 @@ class DeviceSteadyMonitor:
         # distribution (one of each) sum on the device, the others see the copied-back state.
         self._device_accumulators = {}
         self._samples = {}
+        self._before = {}
         self._zeroed = False
         for accumulator in getattr(ctl, "_accumulators", {}).values():
             update = accumulator.update
-            self._accumulator_updates.append((accumulator, "update" in vars(accumulator), update))
+            self._accumulator_updates.append((accumulator, "update", "update" in vars(accumulator),
+                                              update))
             name = getattr(accumulator, "name", "")
             if name in self.DEVICE_ACCUMULATORS and name not in self._device_accumulators:
                 self._device_accumulators[name] = accumulator
                 self._samples[name] = []
                 accumulator.update = self._device_update(name, update)
+                # The controller asks for results when the loop ends (its sample counts are
+                # kept current): the device sums come in first.
+                results = getattr(accumulator, "results", None)
+                if results is not None:
+                    self._accumulator_updates.append((accumulator, "results",
+                                                      "results" in vars(accumulator), results))
+                    accumulator.results = self._settled_first(results)
             else:
                 accumulator.update = self._flushing(update)
 
     def _end(self):
-        for accumulator, had, update in self._accumulator_updates:
+        for accumulator, attr, had, method in reversed(self._accumulator_updates):
             if had:
-                accumulator.update = update
+                setattr(accumulator, attr, method)
             else:
-                del accumulator.update
+                delattr(accumulator, attr)
         self._accumulator_updates.clear()
+
+    def _settled_first(self, method):
+        @functools.wraps(method)
+        def wrapper(*args, **kwargs):
+            self.settle()
+            return method(*args, **kwargs)
+        return wrapper
 
     def _device_update(self, name, host_update):
         """An accumulator sample queued on the device (before any chunk there is no device
@@ -197,8 +214,16 @@ class DeviceSteadyMonitor:
             if not self._zeroed:
                 engine.accumulator_zero()
                 self._zeroed = True
+            accumulator = self._device_accumulators[name]
+            if not self._samples[name]:
+                self._before[name] = (accumulator.samples, accumulator.t_first, accumulator.t_last)
             engine.accumulate(density=name == "g2", momentum=name == "momentum-distribution")
             self._samples[name].append((int(state.step), t))
+            # The sample count and times as the accumulator's own update keeps them.
+            if accumulator.samples == 0:
+                accumulator.t_first = t
+            accumulator.t_last = t
+            accumulator.samples += 1
         return update
 
     def _finish_accumulators(self, halt_step):
@@ -209,19 +234,20 @@ class DeviceSteadyMonitor:
         engine = self.solver.engine
         kinds = {"sum_density": "rho", "sum_density_squared": "rho2", "sum_k": "k"}
         for name, accumulator in self._device_accumulators.items():
-            taken = [(s, t) for s, t in self._samples[name] if halt_step is None or s <= halt_step]
-            if not taken:
+            if not self._samples[name]:
                 continue
+            taken = [(s, t) for s, t in self._samples[name] if halt_step is None or s <= halt_step]
+            samples, t_first, t_last = self._before[name]
             values = dict(accumulator.state_dict())
             for key in self.DEVICE_ACCUMULATORS[name]:
                 sums, _ = engine.accumulator_sums(kinds[key])
                 host = _to_host(values[key])
                 values[key] = host + sums.reshape(np.shape(host))
-            if not values["samples"]:
-                values["t_first"] = taken[0][1]
-            values["samples"] = int(values["samples"]) + len(taken)
-            values["t_last"] = taken[-1][1]
+            values["samples"] = int(samples) + len(taken)
+            values["t_first"] = t_first if samples else (taken[0][1] if taken else None)
+            values["t_last"] = taken[-1][1] if taken else t_last
             accumulator.load_state_dict(values)
+            self._samples[name] = []
         self._zeroed = False
 
     # ------------------------------------------------------------------ the check

@@ -296,6 +296,12 @@ def test_device_monitor_copies_the_state_back_for_accumulators_and_events(monito
     assert ad.samples == ah.samples > 0
     for x, y in zip(ad.results(), ah.results()):
         np.testing.assert_array_equal(np.asarray(x.value), np.asarray(y.value))
+    # The results the controller gathered inside run() (its loop ended on the event, before
+    # any settle of the monitor's) already hold the device sums.
+    assert set(d.accumulated) == set(h.accumulated) and h.accumulated
+    for key in h.accumulated:
+        np.testing.assert_array_equal(np.asarray(d.accumulated[key].value),
+                                      np.asarray(h.accumulated[key].value))
 
 
 def test_device_monitor_continues_a_run_from_the_controllers_steady_reference(monitored):
@@ -353,3 +359,7 @@ def test_device_accumulators_match_the_reference_accumulators(monitored):
         for key in sh:
             if key.startswith("sum"):
                 np.testing.assert_allclose(sd[key], sh[key], rtol=1e-12, atol=0)
+    assert set(d.accumulated) == set(h.accumulated) and h.accumulated
+    for key in h.accumulated:
+        np.testing.assert_allclose(np.asarray(d.accumulated[key].value),
+                                   np.asarray(h.accumulated[key].value), rtol=1e-12, atol=1e-300)
