@@ -182,7 +182,8 @@ int pg_accumulate(pg_solver* s, int32_t kinds);
 int pg_accumulator_sums(pg_solver* s, int32_t kind, double* out, int64_t* samples);
 int pg_accumulator_reset(pg_solver* s);
 /* Zero the observable sums and their sample counts, stream ordered (no host wait; the
- * steady-state monitor is left alone).  Samples queued while the solver's halt word is set
+ * steady-state monitor is left alone): a fresh MomentumDistribution / G2Accumulator
+ * (polarism/results/accumulators.py:95-172) for a run whose samples are queued on the device.  Samples queued while the solver's halt word is set
  * (after the steady-state check that stopped every member) add nothing. */
 int pg_accumulator_zero(pg_solver* s);
 /* Restore one accumulator (kind as pg_accumulator_sums) and its sample count, as
@@ -281,7 +282,8 @@ int pg_set_wait_limit(pg_solver* s, int32_t polls);
 int pg_test_fail_next_graph(pg_solver* s, int32_t what);
 int64_t pg_graph_fallbacks(pg_solver* s);
 
-/* Host waits the library has made for this solver: host_syncs counts every wait for the
+/* No counterpart in the reference (whose NumPy/CuPy loop waits whenever it reads a value).
+ * Host waits the library has made for this solver: host_syncs counts every wait for the
  * solver's stream to drain (each synchronising entry point: state and input copies, results,
  * set-up), throttle_waits the advance calls that found their pinned staging slot still in
  * use (the host had queued four chunks ahead of the device) and waited for it.  An advance
@@ -357,7 +359,9 @@ int pg_sweep_steady_check(pg_sweep* w, double* rel_density, double* rel_norm, do
  * _results for a solver (each member's norm uses its own cell area dx * dy): no host wait
  * from reset to results, and with halt_when_all_stopped every sweep launch after the check
  * that finds every member stopped returns at once.  A run uses either these or
- * pg_sweep_steady_check. */
+ * pg_sweep_steady_check.  Replaces the per-group steady-state stop of Sweep.run
+ * (polarism/sweep.py:98-324 running SimulationController.run, simulation_controller.py:698-734,
+ * 1063-1130). */
 int pg_sweep_steady_reset(pg_sweep* w);
 int pg_sweep_steady_update(pg_sweep* w, int64_t step, int32_t record, double rtol,
                            int32_t halt_when_all_stopped);
