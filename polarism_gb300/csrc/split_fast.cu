@@ -20,7 +20,6 @@
 #include <cmath>
 
 #include "ifrk_internal.h"
-#include "ifrk_local.cuh"
 #include "split_local.cuh"
 
 namespace pg {
@@ -354,80 +353,6 @@ __global__ void __launch_bounds__(kPanel * 32, 2)
   for (int t = 0; t < 32; ++t) d[static_cast<long long>(p + 32 * t) * a.nx] = v[t];
 }
 
-// ------------------------------------------------------------------ IFRK column pass
-// ifrk_col_kernel (ifrk.cu) for FP32 columns of 1024 sites of a one-component field: an
-// eight-column panel, the inverse transform, the per-site step (IfrkLocal) through shared
-// memory in site order, the forward transform; mode 2 reduces the error norm per panel.
-__global__ void __launch_bounds__(kPanel * 32, 2)
-    ifrk_col_fast_kernel(float2* __restrict__ psi, const float* __restrict__ n0,
-                         float* __restrict__ dn_out, float* __restrict__ n_out,
-                         float2* __restrict__ psi_start, float2* __restrict__ psi_new,
-                         const float* __restrict__ pump, const float* __restrict__ potential,
-                         const float4* __restrict__ tw4_g, const SplitConst<float>* __restrict__ consts,
-                         const float* __restrict__ scales,
-                         const unsigned long long* __restrict__ step_base,
-                         double* __restrict__ partials, const IfrkColArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double red[32];
-  float4* tw4 = reinterpret_cast<float4*>(smem_raw);  // [32][32]
-  float2* pan = reinterpret_cast<float2*>(tw4 + kN);  // exchange, or [row][c] for the site step
-  for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int c = lane & (kPanel - 1);
-  const int p = warp * 4 + (lane >> 3);  // n2: 0..31
-  const int member = blockIdx.z;
-  const int x0 = blockIdx.x * kPanel;
-  const long long plane = static_cast<long long>(a.nx) * kN;
-  float2* d = psi + member * plane + x0 + c;
-  float2 v[32];
-#pragma unroll
-  for (int t = 0; t < 32; ++t) v[t] = d[static_cast<long long>(p + 32 * t) * a.nx];
-  double local = 0.0;
-  // Phase 0: the inverse transform (conj32 around the forward one) and the site step;
-  // phase 1: the forward transform.
-#pragma unroll 1
-  for (int ph = 0; ph < 2; ++ph) {
-    if (ph == 0 ? a.inverse : a.forward) {
-      if (ph == 0) conj32(v);
-      fft1024_panel(v, p, c, pan, tw4);
-      if (ph == 0) conj32(v);
-    }
-    if (ph == 1 || a.mode == 3) continue;
-    __syncthreads();
-#pragma unroll
-    for (int t = 0; t < 32; ++t) pan[(p + 32 * t) * kPanel + c] = v[t];
-    __syncthreads();
-    const IfrkLocal<float> step(a, member, n0, dn_out, n_out, psi_start, psi_new, pump, potential,
-                                consts, scales, step_base);
-#pragma unroll 2
-    for (int e = threadIdx.x; e < kPanel * kN; e += blockDim.x) {
-      float2 vv[2] = {pan[e], make_float2(0.f, 0.f)};
-      step.site(vv, static_cast<long long>(e / kPanel) * a.nx + x0 + e % kPanel, local);
-      pan[e] = vv[0];
-    }
-    __syncthreads();
-    if (a.mode == 2) break;
-#pragma unroll
-    for (int t = 0; t < 32; ++t) v[t] = pan[(p + 32 * t) * kPanel + c];
-  }
-  if (a.mode == 2) {
-    // Block reduction of the FP64 partial sums; one value per (member, panel).
-    for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
-    if (lane == 0) red[warp] = local;
-    __syncthreads();
-    if (warp == 0) {
-      double s = lane < (static_cast<int>(blockDim.x) >> 5) ? red[lane] : 0.0;
-      for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-      if (lane == 0) partials[member * gridDim.x + blockIdx.x] = s;
-    }
-    return;
-  }
-  if (a.mode == 1 && !a.forward) return;
-#pragma unroll
-  for (int t = 0; t < 32; ++t) d[static_cast<long long>(p + 32 * t) * a.nx] = v[t];
-}
-
 size_t row_fast_smem() { return kN * sizeof(float4) + kRowWarps * 32 * kXStride * sizeof(float2); }
 size_t col_fast_smem() { return kN * sizeof(float4) + kPanel * kPanelStride * sizeof(float2); }
 
@@ -458,9 +383,6 @@ cudaError_t configure_split_fast() {
   e = cudaFuncSetAttribute(ifrk_row_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(row_fast_smem()));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(ifrk_col_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(col_fast_smem()));
-  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(col_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(col_fast_smem()));
 }
@@ -485,25 +407,6 @@ cudaError_t launch_ifrk_row_fast(const float* in, float* save, float* out, const
       reinterpret_cast<const float2*>(in), reinterpret_cast<float2*>(save),
       reinterpret_cast<float2*>(out), reinterpret_cast<const float2*>(tables),
       reinterpret_cast<const float4*>(tw4), a);
-  return cudaGetLastError();
-}
-
-bool ifrk_fast_col(const IfrkColArgs& a) {
-  return a.comps == 1 && a.ny == kN && a.nx % kPanel == 0 && a.cols == kPanel;
-}
-
-cudaError_t launch_ifrk_col_fast(float* psi, const float* n0, float* dn_out, float* n_out,
-                                 const float* psi_start, const float* psi_new, const float* pump,
-                                 const float* potential, const float* tw4,
-                                 const SplitConst<float>* consts, const float* scales,
-                                 const unsigned long long* step_base, double* partials,
-                                 const IfrkColArgs& a, cudaStream_t stream) {
-  const dim3 grid(a.nx / kPanel, 1, a.members);
-  ifrk_col_fast_kernel<<<grid, kPanel * 32, col_fast_smem(), stream>>>(
-      reinterpret_cast<float2*>(psi), n0, dn_out, n_out,
-      reinterpret_cast<float2*>(const_cast<float*>(psi_start)),
-      reinterpret_cast<float2*>(const_cast<float*>(psi_new)), pump, potential,
-      reinterpret_cast<const float4*>(tw4), consts, scales, step_base, partials, a);
   return cudaGetLastError();
 }
 
