@@ -181,18 +181,18 @@ struct LocalStep {
     }
   }
 
-  // Whether apply_single covers this launch: one reservoir field, one laser and no potential
+  // Whether step_single covers this launch: one reservoir field, one laser and no potential
   // (the common case, without the general code's branches).
   __device__ __forceinline__ bool single() const {
     return reservoir && !two && L == 1 && vm == nullptr;
   }
 
-  // apply() for that case with the operation known at compile time: the same operations, in
-  // the same order (32-bit site offsets: a member holds fewer than 2^31 sites).
+  // apply() for that case with the operation known at compile time, on values already
+  // loaded: the reservoir n and the envelope P at site o (32-bit site offsets: a member holds
+  // fewer than 2^31 sites).  The same operations, in the same order; returns the new n, which
+  // the caller stores unless OP is SPLIT_OP_NONLINEAR.
   template <int OP, bool NOISE>
-  __device__ __forceinline__ void apply_single(C2& v, int o) const {
-    T n = rm[o];
-    const T P = pm[o];
+  __device__ __forceinline__ T step_single(C2& v, T n, T P, int o) const {
     if (OP == SPLIT_OP_KOUTER) {
       n = reservoir_half(n, v.x * v.x + v.y * v.y, mul_rn_t(s0, P), h, k);
       nonlinear(v.x, v.y, n, T(0), false, T(0), T(0), dt, k);
@@ -212,7 +212,7 @@ struct LocalStep {
       philox_cells(cell, prefix, w);
       WignerDraw<T>::apply(w[0], k.noise_a + k.noise_b * n, v.x, v.y);
     }
-    if (OP != SPLIT_OP_NONLINEAR) rm[o] = n;
+    return n;
   }
 
   __device__ __forceinline__ void apply(C2& v, long long o) const {
