@@ -318,6 +318,26 @@ cudaError_t ifrk_row(pg_solver* s, const T* in, T* save, T* out, const T* tables
   return launch_ifrk_row<T>(in, save, out, tables, a, tw, s->stream);
 }
 
+// A column pass: the register-resident form for FP32 one-component columns of 1024 sites
+// (the forward-only pass, and stages and step ends with one single reservoir and one laser),
+// the generic Stockham pass otherwise.
+template <typename T>
+cudaError_t ifrk_col(pg_solver* s, T* psi, const T* n0, T* dn_out, T* n_out, const T* psi_start,
+                     const T* psi_new, const T* tw, const SplitConst<T>* consts, const T* scales,
+                     const IfrkColArgs& a) {
+  if constexpr (sizeof(T) == 4) {
+    if (s->tw4 != nullptr && ifrk_fast_col(a))
+      return launch_ifrk_col_fast(psi, n0, dn_out, n_out, psi_start, psi_new,
+                                  static_cast<const float*>(s->pump),
+                                  static_cast<const float*>(s->potential),
+                                  static_cast<const float*>(s->tw4), consts, scales, s->step_base,
+                                  a, s->stream);
+  }
+  return launch_ifrk_col<T>(psi, n0, dn_out, n_out, psi_start, psi_new,
+                            static_cast<const T*>(s->pump), static_cast<const T*>(s->potential), tw,
+                            consts, scales, s->step_base, nullptr, a, s->stream);
+}
+
 template <typename T>
 int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& st, double h,
              int scale_base, int step_offset, bool noise, bool adaptive, double rtol, double atol,
@@ -337,9 +357,7 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
     a.mode = 3;
     a.inverse = 0;
     a.forward = 1;
-    PG_CUDA(launch_ifrk_col<T>(W, n0, nullptr, nullptr, nullptr, nullptr,
-                               static_cast<const T*>(s->pump), static_cast<const T*>(s->potential),
-                               tw_y, consts, nullptr, s->step_base, nullptr, a, s->stream));
+    PG_CUDA(ifrk_col<T>(s, W, n0, nullptr, nullptr, nullptr, nullptr, tw_y, consts, nullptr, a));
     b.w_valid = true;
     s->last_launches += 1;
   }
@@ -375,10 +393,9 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
       ++a.terms;
     }
     a.scale_index = scale_base + i;
-    PG_CUDA(launch_ifrk_col<T>(W, n0, static_cast<T*>(b.dn[i]), nullptr,
-                               adaptive && i == 0 ? static_cast<T*>(b.psi_start) : nullptr, nullptr,
-                               static_cast<const T*>(s->pump), static_cast<const T*>(s->potential),
-                               tw_y, consts, scales, s->step_base, nullptr, a, s->stream));
+    PG_CUDA(ifrk_col<T>(s, W, n0, static_cast<T*>(b.dn[i]), nullptr,
+                        adaptive && i == 0 ? static_cast<T*>(b.psi_start) : nullptr, nullptr, tw_y,
+                        consts, scales, a));
     s->last_launches += 2;
   }
   // Final combination.
@@ -413,10 +430,8 @@ int run_step(pg_solver* s, const Plan& p, const Tableau& tb, const StepTables& s
       a.coef[a.terms] = h * tb.b[j];
       ++a.terms;
     }
-    PG_CUDA(launch_ifrk_col<T>(W, n0, nullptr, static_cast<T*>(b.n_new), nullptr,
-                               static_cast<T*>(b.psi_new), static_cast<const T*>(s->pump),
-                               static_cast<const T*>(s->potential), tw_y, consts, scales,
-                               s->step_base, nullptr, a, s->stream));
+    PG_CUDA(ifrk_col<T>(s, W, n0, nullptr, static_cast<T*>(b.n_new), nullptr,
+                        static_cast<T*>(b.psi_new), tw_y, consts, scales, a));
     s->last_launches += 2;
   }
   if (adaptive) {

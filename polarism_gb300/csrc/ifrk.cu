@@ -12,6 +12,7 @@
 
 #include "fft.cuh"
 #include "ifrk_internal.h"
+#include "ifrk_sites.cuh"
 #include "philox.cuh"
 #include "pg_internal.h"
 
@@ -242,111 +243,6 @@ __device__ __forceinline__ T scaled_square(T mag, T scale) {
   return mag == T(0) ? T(0) : T(INFINITY);
 }
 
-__device__ __forceinline__ float mul_rn_i(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double mul_rn_i(double a, double b) { return __dmul_rn(a, b); }
-
-// The site step of a stage (MODE 0) or step-end (MODE 1) column pass for the common
-// configuration: one field component, one single reservoir, one pump term.  Each thread takes
-// U sites of the panel at a time and issues every global load of the batch (reservoir, the
-// TERMS stage derivatives, pump, potential) before it forms the first result, so U sites'
-// loads are in flight where the generic loop in ifrk_col_kernel has one site's; the generic
-// loop also indexes its per-field arrays at run time, which puts them in local memory.  The
-// arithmetic is the generic loop's, expression for expression and in the same order.
-// Tableau rows of up to five terms have a form here (Lawson RK4 and Dormand-Prince 5).
-template <typename T, int MODE, int TERMS>
-__device__ __forceinline__ void ifrk_sites_single(typename C2T<T>::type* buf, const IfrkColArgs& a,
-                                                  const SplitConst<T>& k, int x0, long long mbase,
-                                                  const T* __restrict__ n0, T* __restrict__ dn_out,
-                                                  T* __restrict__ n_out,
-                                                  typename C2T<T>::type* __restrict__ psi_start,
-                                                  typename C2T<T>::type* __restrict__ psi_new,
-                                                  const T* __restrict__ pm, const T* __restrict__ vm,
-                                                  T s0, const PhiloxCellPrefix& prefix) {
-  using C2 = typename C2T<T>::type;
-  // The largest batches that stay within the 64 registers of 1024-thread blocks without
-  // spilling (the step end also holds U Philox states).
-  constexpr int U = MODE == 0 ? (sizeof(T) == 4 ? 3 : 2) : (sizeof(T) == 4 ? 2 : 1);
-  const int C = a.cols, lc = a.log2cols;
-  const int count = C * a.ny;
-  const T* dn[TERMS > 0 ? TERMS : 1];
-  T cf[TERMS > 0 ? TERMS : 1];
-#pragma unroll
-  for (int j = 0; j < TERMS; ++j) {
-    dn[j] = static_cast<const T*>(a.dn[j]) + mbase;
-    cf[j] = static_cast<T>(a.coef[j]);
-  }
-  const T* nm = n0 + mbase;
-  const int stride = U * static_cast<int>(blockDim.x);
-  for (int e0 = threadIdx.x; e0 < count; e0 += stride) {
-    int o[U], bi[U];
-    bool ok[U];
-    C2 v[U];
-    T nv[U], acc[U], pp[U], vre[U], vim[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int e = e0 + u * static_cast<int>(blockDim.x);
-      ok[u] = e < count;
-      const int ee = ok[u] ? e : e0;  // a site of the panel: loads stay in bounds
-      const int c = ee & (C - 1), i = ee >> lc;
-      o[u] = i * a.nx + x0 + c;
-      bi[u] = i * C + c;
-      v[u] = buf[bi[u]];
-      nv[u] = nm[o[u]];
-      acc[u] = T(0);
-      if (MODE == 0) {
-        pp[u] = pm[o[u]];
-        vre[u] = T(0);
-        vim[u] = T(0);
-        if (vm) {
-          vre[u] = a.potential == 2 ? vm[2 * static_cast<long long>(o[u])] : vm[o[u]];
-          vim[u] = a.potential == 2 ? vm[2 * static_cast<long long>(o[u]) + 1] : T(0);
-        }
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < TERMS; ++j)
-#pragma unroll
-      for (int u = 0; u < U; ++u) acc[u] += cf[j] * dn[j][o[u]];
-    if (MODE == 0) {
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (!ok[u]) continue;
-        const T nval = nv[u] + acc[u];
-        const C2 x = v[u];
-        const T rho = x.x * x.x + x.y * x.y;
-        if (psi_start) psi_start[mbase + o[u]] = x;
-        const T eff = vre[u] + k.g_C * rho + k.g_R * nval;
-        const T e_over = eff * k.inv_hbar;
-        const T g = T(0.5) * (k.R * nval - k.gamma_C) + vim[u] * k.inv_hbar;
-        buf[bi[u]] = C2{g * x.x + e_over * x.y, g * x.y - e_over * x.x};
-        const T P = mul_rn_i(s0, pp[u]);
-        dn_out[mbase + o[u]] = P - (k.gamma_R + k.R * rho) * nval;
-      }
-    } else {
-      Words4 w[U];
-      if (a.noise) {
-        uint32_t cell[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) cell[u] = static_cast<uint32_t>(o[u]);
-        philox_cells(cell, prefix, w);
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (!ok[u]) continue;
-        T nval = nv[u] + acc[u];
-        nval = nval > T(0) ? nval : T(0);
-        n_out[mbase + o[u]] = nval;
-        C2 x = v[u];
-        if (a.noise) {
-          WignerDraw<T>::apply(w[u], k.noise_a + k.noise_b * nval, x.x, x.y);
-          buf[bi[u]] = x;
-        }
-        psi_new[mbase + o[u]] = x;
-      }
-    }
-  }
-}
-
 // Column pass over a panel of `cols` columns of every component of one member.  Reservoir
 // planes are laid out [field][member][reservoir component][y][x]; with one reservoir
 // component per field component each component feeds its own reservoirs with its own
@@ -411,35 +307,16 @@ __global__ void __launch_bounds__(1024) ifrk_col_kernel(typename C2T<T>::type* _
     const int NQ = F * Cr;
     const long long qstride = static_cast<long long>(Cr) * plane;      // reservoir member stride
     const long long fstride = static_cast<long long>(a.members) * qstride;  // field stride
-    bool done = false;
-    if (F == 1 && Cr == 1 && comps == 1 && a.mode != 2 && !(L > 1 && cs) &&
-        plane <= 0x7fffffffLL) {
-      done = true;
-      const long long mb = static_cast<long long>(member) * plane;
-      switch (a.mode * 8 + a.terms) {
-#define PG_IFRK_SINGLE(MODE, TERMS)                                                              \
-  case MODE * 8 + TERMS:                                                                         \
-    ifrk_sites_single<T, MODE, TERMS>(buf, a, k, x0, mb, n0, dn_out, n_out, psi_start, psi_new, \
-                                      pm, vm, s0, prefix[0]);                                    \
-    break;
-        PG_IFRK_SINGLE(0, 0)
-        PG_IFRK_SINGLE(0, 1)
-        PG_IFRK_SINGLE(0, 2)
-        PG_IFRK_SINGLE(0, 3)
-        PG_IFRK_SINGLE(0, 4)
-        PG_IFRK_SINGLE(0, 5)
-        PG_IFRK_SINGLE(1, 1)
-        PG_IFRK_SINGLE(1, 2)
-        PG_IFRK_SINGLE(1, 3)
-        PG_IFRK_SINGLE(1, 4)
-        PG_IFRK_SINGLE(1, 5)
-#undef PG_IFRK_SINGLE
-        default:
-          done = false;
-      }
-    }
-    // Every other configuration (and tableau rows with more terms): a site at a time.
-    if (!done)
+    // The common configuration in batches of sites a thread (ifrk_sites.cuh): three at a stage
+    // and two at the step end (FP64: two and one) are the most that stay within the 64
+    // registers of 1024-thread blocks without spilling.
+    const bool batched = ifrk_sites_batched(a) && plane <= 0x7fffffffLL;
+    if (batched)
+      ifrk_sites_run<T, sizeof(T) == 4 ? 3 : 2, sizeof(T) == 4 ? 2 : 1>(
+          buf, C, a.log2cols, a.ny, a, k, x0, static_cast<long long>(member) * plane, n0, dn_out,
+          n_out, psi_start, psi_new, pm, vm, s0, prefix[0]);
+    // Every other configuration: a site at a time.
+    if (!batched)
     for (int e = threadIdx.x; e < count; e += blockDim.x) {
       const int c = e & (C - 1), i = e >> a.log2cols;
       const long long o = static_cast<long long>(i) * a.nx + x0 + c;

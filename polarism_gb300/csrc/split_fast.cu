@@ -20,6 +20,7 @@
 #include <cmath>
 
 #include "ifrk_internal.h"
+#include "ifrk_sites.cuh"
 #include "split_local.cuh"
 
 namespace pg {
@@ -386,6 +387,77 @@ __global__ void __launch_bounds__(kPanel * 32, 2)
   for (int t = 0; t < 32; ++t) d[static_cast<long long>(p + 32 * t) * a.nx] = v[t];
 }
 
+// ------------------------------------------------------------------ IFRK column pass
+// ifrk_col_kernel (ifrk.cu) for FP32 columns of 1024 sites of a one-component field: the
+// forward-only pass that forms W (mode 3, any reservoir), and the stage and step-end passes
+// (modes 0 and 1) for one single reservoir and one laser (ifrk_sites_batched).  An eight-column
+// panel, the inverse transform, the site step over the panel in shared memory in site order
+// (ifrk_sites.cuh, kIfrkBatch sites a thread at a stage, kIfrkEndBatch at the step end), the
+// forward transform.  The error norm (mode 2) stays on the generic pass.
+constexpr int kIfrkBatch = 8;     // 4 / 2 measured 4 % slower
+constexpr int kIfrkEndBatch = 4;
+__global__ void __launch_bounds__(kPanel * 32, 2)
+    ifrk_col_fast_kernel(float2* __restrict__ psi, const float* __restrict__ n0,
+                         float* __restrict__ dn_out, float* __restrict__ n_out,
+                         float2* __restrict__ psi_start, float2* __restrict__ psi_new,
+                         const float* __restrict__ pump, const float* __restrict__ potential,
+                         const float4* __restrict__ tw4_g,
+                         const SplitConst<float>* __restrict__ consts,
+                         const float* __restrict__ scales,
+                         const unsigned long long* __restrict__ step_base, const IfrkColArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float4* tw4 = reinterpret_cast<float4*>(smem_raw);  // [32][32]
+  float2* pan = reinterpret_cast<float2*>(tw4 + kN);  // exchange, or [row][c] for the site step
+  for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = lane & (kPanel - 1);
+  const int p = warp * 4 + (lane >> 3);  // n2: 0..31
+  const int member = blockIdx.z;
+  const int x0 = blockIdx.x * kPanel;
+  const long long plane = static_cast<long long>(a.nx) * kN;
+  float2* d = psi + member * plane + x0 + c;
+  float2 v[32];
+#pragma unroll
+  for (int t = 0; t < 32; ++t) v[t] = d[static_cast<long long>(p + 32 * t) * a.nx];
+  // Phase 0: the inverse transform (conj32 around the forward one) and the site step;
+  // phase 1: the forward transform (one copy of the transform's code).
+#pragma unroll 1
+  for (int ph = 0; ph < 2; ++ph) {
+    if (ph == 0 ? a.inverse : a.forward) {
+      if (ph == 0) conj32(v);
+      fft1024_panel(v, p, c, pan, tw4);
+      if (ph == 0) conj32(v);
+    }
+    if (ph == 1 || a.mode == 3) continue;
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 32; ++t) pan[(p + 32 * t) * kPanel + c] = v[t];
+    __syncthreads();
+    {
+      const SplitConst<float> k = consts[member];
+      const float s0 = scales ? scales[static_cast<long long>(a.scale_index) * a.members + member]
+                              : 0.f;
+      const float* pm = pump + member * a.pump_stride;
+      const float* vm =
+          potential ? potential + member * a.pot_stride * (a.potential == 2 ? 2 : 1) : nullptr;
+      const unsigned long long step = a.noise ? step_base[0] + a.step_offset : 0ull;
+      const PhiloxCellPrefix prefix = philox_cell_prefix(
+          static_cast<uint32_t>(step), static_cast<uint32_t>(step >> 32), 1u,
+          static_cast<uint32_t>(k.seed), static_cast<uint32_t>(k.seed >> 32));
+      ifrk_sites_run<float, kIfrkBatch, kIfrkEndBatch>(pan, kPanel, 3, kN, a, k, x0,
+                                                       member * plane, n0, dn_out, n_out,
+                                                       psi_start, psi_new, pm, vm, s0, prefix);
+    }
+    __syncthreads();
+    if (a.mode == 1 && !a.forward) return;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) v[t] = pan[(p + 32 * t) * kPanel + c];
+  }
+#pragma unroll
+  for (int t = 0; t < 32; ++t) d[static_cast<long long>(p + 32 * t) * a.nx] = v[t];
+}
+
 size_t row_fast_smem() { return kN * sizeof(float4) + kRowWarps * 32 * kXStride * sizeof(float2); }
 size_t col_fast_smem() { return kN * sizeof(float4) + kPanel * kPanelStride * sizeof(float2); }
 
@@ -416,6 +488,9 @@ cudaError_t configure_split_fast() {
   e = cudaFuncSetAttribute(ifrk_row_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(row_fast_smem()));
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(ifrk_col_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(col_fast_smem()));
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(col_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               static_cast<int>(col_fast_smem()));
 }
@@ -440,6 +515,27 @@ cudaError_t launch_ifrk_row_fast(const float* in, float* save, float* out, const
       reinterpret_cast<const float2*>(in), reinterpret_cast<float2*>(save),
       reinterpret_cast<float2*>(out), reinterpret_cast<const float2*>(tables),
       reinterpret_cast<const float4*>(tw4), a);
+  return cudaGetLastError();
+}
+
+bool ifrk_fast_col(const IfrkColArgs& a) {
+  return a.comps == 1 && a.ny == kN && a.nx % kPanel == 0 &&
+         static_cast<long long>(a.nx) * kN <= 0x7fffffffLL &&
+         (a.mode == 3 || ifrk_sites_batched(a));
+}
+
+cudaError_t launch_ifrk_col_fast(float* psi, const float* n0, float* dn_out, float* n_out,
+                                 const float* psi_start, const float* psi_new, const float* pump,
+                                 const float* potential, const float* tw4,
+                                 const SplitConst<float>* consts, const float* scales,
+                                 const unsigned long long* step_base, const IfrkColArgs& a,
+                                 cudaStream_t stream) {
+  const dim3 grid(a.nx / kPanel, 1, a.members);
+  ifrk_col_fast_kernel<<<grid, kPanel * 32, col_fast_smem(), stream>>>(
+      reinterpret_cast<float2*>(psi), n0, dn_out, n_out,
+      reinterpret_cast<float2*>(const_cast<float*>(psi_start)),
+      reinterpret_cast<float2*>(const_cast<float*>(psi_new)), pump, potential,
+      reinterpret_cast<const float4*>(tw4), consts, scales, step_base, a);
   return cudaGetLastError();
 }
 

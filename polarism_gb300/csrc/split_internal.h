@@ -96,7 +96,17 @@ cudaError_t launch_col_fast(float* data, float* res, const float* pump, const fl
 // The IFRK row pass on the same transforms (FP32, one component, rows of 1024 sites): whether
 // it applies and its launch (arguments as launch_ifrk_row; tw4 as above).
 struct IfrkRowArgs;
+struct IfrkColArgs;
 bool ifrk_fast_row(const IfrkRowArgs& a);
+// The IFRK column pass likewise (one component, columns of 1024 sites, eight-column panels):
+// the forward-only pass, and stages and step ends with one single reservoir and one laser.
+bool ifrk_fast_col(const IfrkColArgs& a);
+cudaError_t launch_ifrk_col_fast(float* psi, const float* n0, float* dn_out, float* n_out,
+                                 const float* psi_start, const float* psi_new, const float* pump,
+                                 const float* potential, const float* tw4,
+                                 const SplitConst<float>* consts, const float* scales,
+                                 const unsigned long long* step_base, const IfrkColArgs& a,
+                                 cudaStream_t stream);
 cudaError_t launch_ifrk_row_fast(const float* in, float* save, float* out, const float* tables,
                                  const float* tw4, const IfrkRowArgs& a, cudaStream_t stream);
 
