@@ -70,10 +70,11 @@ def test_ifrk4_matches_reference_trajectory(cuda_lib, precision, tol):
 
 @pytest.mark.parametrize("tableau", ["rk4", "dp5"])
 @pytest.mark.parametrize("precision,tol", [("double", 1e-10), ("single", 1e-4)])
-@pytest.mark.parametrize("ny,nx", [(16, 32), (32, 1024)])
+@pytest.mark.parametrize("ny,nx", [(16, 32), (32, 1024), (1024, 32)])
 def test_fixed_step_with_noise_and_members(cuda_lib, tableau, precision, tol, ny, nx):
     """Fixed-step IFRK with the Wigner increment after each step, three members; FP32 rows of
-    1024 sites run the register-resident four-step row pass."""
+    1024 sites run the register-resident four-step row pass, FP32 columns of 1024 sites the
+    register-resident column pass with the batched site step (stages and step end)."""
     from polarism_gb300.engine import TABLEAU_NODES, Engine, MemberPhysics
 
     members = 3
@@ -111,17 +112,59 @@ def test_fixed_step_with_noise_and_members(cuda_lib, tableau, precision, tol, ny
         assert rel_l2(res[m], state.fields[0][0]) < tol, m
 
 
-def test_dp5_trial_error_norm_on_the_1024_row_pass(cuda_lib):
-    """The adaptive trial's error estimate (a row pass over stored stage spectra only) on FP32
-    rows of 1024 sites against the FP64 engine's: the error norm within 1e-2 and, away from
-    the threshold, the same accept decision."""
+@pytest.mark.parametrize("tableau", ["rk4", "dp5"])
+def test_fast_column_pass_with_complex_potential(cuda_lib, tableau):
+    """FP32 columns of 1024 sites with a complex potential, two members: the batched site step
+    of the register-resident column pass reads V_re and V_im per site."""
+    from polarism_gb300 import _lib
+    from polarism_gb300.engine import TABLEAU_NODES, Engine, MemberPhysics
+
+    members, ny, nx = 2, 1024, 16
+    dx, dy, dt = 0.8, 0.5, 0.01
+    rng = np.random.default_rng(34)
+    psi0 = 0.1 * (rng.standard_normal((members, 1, ny, nx)) + 1j * rng.standard_normal((members, 1, ny, nx)))
+    res0 = np.abs(rng.standard_normal((members, 1, ny, nx))) * 0.05
+    y = (np.arange(ny) - ny / 2) * dy
+    env = np.broadcast_to(np.exp(-0.5 * y[:, None] ** 2 / 900.0), (ny, nx))
+    pot = (0.02 * np.cos(2 * np.pi * y / 64.0)[:, None] + 0.005j * np.sin(2 * np.pi * y / 96.0)[:, None]
+           + np.zeros((1, nx)))
+    phys = [MemberPhysics(**dict(P, R=0.02 + 0.01 * m)) for m in range(members)]
+    eng = Engine(nx, ny, members, dx, dy, dt, phys, "single", potential=_lib.PG_POT_COMPLEX)
+    eng.set_pump(env.astype(eng.real))
+    eng.set_potential(pot.astype(eng.complex))
+    eng.set_state(psi0.astype(eng.complex), res0.astype(eng.real))
+    steps = 5
+    coeff = lambda t: 0.3 * (1.0 + 0.2 * np.cos(7 * t))  # noqa: E731
+    nodes = TABLEAU_NODES[tableau]
+    scales = np.asarray([[[coeff(k * dt + c * dt)] * members for c in nodes] for k in range(steps)])
+    eng.ifrk_advance(tableau, 0, steps, scales)
+    psi, res = eng.get_state()
+    eng.close()
+    tab = gpe.RK4_TABLEAU if tableau == "rk4" else gpe.DP5_TABLEAU
+    k2 = _k2(nx, ny, dx, dy)
+    for m in range(members):
+        pm = dict(P, R=phys[m].R)
+        state = gpe.IFRKState(psi=psi0[m:m + 1].copy(), fields=(res0[m:m + 1].copy(),))
+        for k in range(steps):
+            gpe.ifrk_step(state, dt, tab, lambda t: env * coeff(t), pot, pm, k2, dx, dy)
+        assert rel_l2(psi[m], state.real_space()[0]) < 1e-4, m
+        assert rel_l2(res[m], state.fields[0][0]) < 1e-4, m
+
+
+@pytest.mark.parametrize("ny,nx", [(32, 1024), (1024, 32)])
+def test_dp5_trial_error_norm_on_the_1024_site_passes(cuda_lib, ny, nx):
+    """The adaptive trial's error estimate on FP32 rows (a row pass over stored stage spectra
+    only) or columns (stages and step end on the register-resident column pass, the error norm
+    on the generic one) of 1024 sites against the FP64 engine's: the error norm within 1e-2
+    and, away from the threshold, the same accept decision."""
     from polarism_gb300.engine import Engine, MemberPhysics
 
-    ny, nx, dx, dy = 32, 1024, 0.4, 0.4
+    dx, dy = 0.4, 0.4
     rng = np.random.default_rng(8)
     psi0 = 0.2 * (rng.standard_normal((1, 1, ny, nx)) + 1j * rng.standard_normal((1, 1, ny, nx)))
     res0 = np.abs(rng.standard_normal((1, 1, ny, nx))) * 0.05
-    env = np.exp(-0.5 * (((np.arange(nx) - nx / 2) * dx) ** 2)[None, :] / 400.0)
+    env = np.exp(-0.5 * (((np.arange(nx) - nx / 2) * dx) ** 2)[None, :] / 400.0
+                 - 0.5 * (((np.arange(ny) - ny / 2) * dy) ** 2)[:, None] / 400.0)
     errs = {}
     for precision in ("double", "single"):
         eng = Engine(nx, ny, 1, dx, dy, 0.01, MemberPhysics(**P), precision)
