@@ -99,6 +99,26 @@ def test_split_matches_oracle(cuda_lib, precision, tol, ordering):
     assert rel_l2(res, f_o[0]) < tol
 
 
+@pytest.mark.parametrize("potential", [False, True])
+@pytest.mark.parametrize("ordering", ["cpu", "kouter"])
+@pytest.mark.parametrize("ny,nx", [(1024, 16), (16, 1024)])
+def test_split_1024_site_passes_match_oracle(cuda_lib, ny, nx, ordering, potential):
+    """FP32 rows and columns of 1024 sites run the register-resident four-step passes; the
+    column pass's local step runs in batches of sites (one reservoir, one laser, no potential)
+    or a site at a time (with a potential).  Against the FP64 oracle at 1e-4."""
+    c = _case(nx=nx, ny=ny, seed=11, potential=potential)
+    steps = 6
+    eng = _engine(c, "single")
+    eng.split_advance(0 if ordering == "cpu" else 1, 0, steps, _half_scales(c["dt"], 0, steps))
+    psi, res = eng.get_state()
+    eng.close()
+    if ordering == "kouter":
+        psi = np.fft.ifft2(psi.astype(np.complex128), axes=(-2, -1))
+    psi_o, f_o = _oracle(c, ordering, steps, "single")
+    assert rel_l2(psi, psi_o) < 1e-4
+    assert rel_l2(res, f_o[0]) < 1e-4
+
+
 def test_split_cpu_ordering_matches_reference_output(cuda_lib):
     """The reference's own split-step-fft trajectory (FP64, Wigner on, 32x16)."""
     from polarism_gb300.engine import Engine, MemberPhysics
