@@ -193,10 +193,9 @@ __global__ void __launch_bounds__(kRowWarps * 32, 2)
                          float2* __restrict__ out, const float2* __restrict__ tables,
                          const float4* __restrict__ tw4_g, const IfrkRowArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float4* tw4 = reinterpret_cast<float4*>(smem_raw);                     // [32][32]
-  float2* xb = reinterpret_cast<float2*>(tw4 + kN);                      // [warps][32][33]
-  for (int i = threadIdx.x; i < kN; i += blockDim.x) tw4[i] = tw4_g[i];
-  __syncthreads();
+  // The twiddle table through L1, as in the IFRK column pass (no block barrier either).
+  const float4* tw4 = tw4_g;                                             // [32][32]
+  float2* xb = reinterpret_cast<float2*>(smem_raw);                      // [warps][32][33]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int member = blockIdx.z;
   float2* buf = xb + warp * 32 * kXStride;
@@ -462,6 +461,7 @@ __global__ void __launch_bounds__(kPanel * 32, 2)
 size_t row_fast_smem() { return kN * sizeof(float4) + kRowWarps * 32 * kXStride * sizeof(float2); }
 size_t col_fast_smem() { return kN * sizeof(float4) + kPanel * kPanelStride * sizeof(float2); }
 size_t ifrk_col_fast_smem() { return kPanel * kPanelStride * sizeof(float2); }
+size_t ifrk_row_fast_smem() { return kRowWarps * 32 * kXStride * sizeof(float2); }
 
 }  // namespace
 
@@ -488,7 +488,7 @@ cudaError_t configure_split_fast() {
                                        static_cast<int>(row_fast_smem()));
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(ifrk_row_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(row_fast_smem()));
+                           static_cast<int>(ifrk_row_fast_smem()));
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(ifrk_col_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(ifrk_col_fast_smem()));
@@ -513,7 +513,7 @@ bool ifrk_fast_row(const IfrkRowArgs& a) {
 cudaError_t launch_ifrk_row_fast(const float* in, float* save, float* out, const float* tables,
                                  const float* tw4, const IfrkRowArgs& a, cudaStream_t stream) {
   const dim3 grid(a.ny / (kRowWarps * kRowsPerWarp), 1, a.members);
-  ifrk_row_fast_kernel<<<grid, kRowWarps * 32, row_fast_smem(), stream>>>(
+  ifrk_row_fast_kernel<<<grid, kRowWarps * 32, ifrk_row_fast_smem(), stream>>>(
       reinterpret_cast<const float2*>(in), reinterpret_cast<float2*>(save),
       reinterpret_cast<float2*>(out), reinterpret_cast<const float2*>(tables),
       reinterpret_cast<const float4*>(tw4), a);
